@@ -1,0 +1,502 @@
+"""Python face of the library, mirroring the reference's ``_C_flare`` module
+(src/ace_binding.cpp:26-221) for the prediction path.
+
+Classes and the methods the hot path uses keep the reference's names and
+argument meaning; the work runs in libflare_pp_gb300.so on the GPU.
+"""
+import numpy as np
+
+from . import _lib
+from ._lib import check, f64, i32, lib, ptr, FPP_PREC_FP64, FPP_PREC_MIXED
+
+PRECISIONS = {"fp64": FPP_PREC_FP64, "mixed": FPP_PREC_MIXED}
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class _Handle:
+    _destroy = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and self._destroy:
+            try:
+                getattr(lib(), self._destroy)(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+# --------------------------------------------------------------------------
+class Structure(_Handle):
+    """Periodic structure with a GPU neighbor list.
+
+    Structure(cell, species, positions[, cutoff, descriptor_calculators]),
+    src/flare_pp/structure.h:92-97.  Neighbor attributes are copied from the
+    device on first access.
+    """
+    _destroy = "fpp_structure_destroy"
+
+    def __init__(self, cell, species, positions, cutoff=None,
+                 descriptor_calculators=(), stream=None):
+        self.cell = f64(cell).reshape(3, 3)
+        self.species = [int(s) for s in np.asarray(species).reshape(-1)]
+        self.positions = f64(positions).reshape(-1, 3)
+        self.noa = len(self.species)
+        self.energy = np.zeros(0)
+        self.forces = np.zeros(0)
+        self.stresses = np.zeros(0)
+        self.mean_efs = np.zeros(0)
+        self.variance_efs = np.zeros(0)
+        self.descriptors = []
+        self.descriptor_calculators = list(descriptor_calculators)
+        self._h = None
+        self._nb = None
+        self.cutoff = None
+        if cutoff is not None:
+            self.cutoff = float(cutoff)
+            h = _lib.ctypes.c_void_p()
+            sp = i32(self.species)
+            check(lib().fpp_structure_create(
+                ptr(self.cell), ptr(sp), ptr(self.positions), self.noa,
+                self.cutoff, _stream(stream), _lib.ctypes.byref(h)))
+            self._h = h.value
+            self.compute_descriptors()
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("structure has no neighbor list (no cutoff given)")
+        return self._h
+
+    def set_positions(self, positions, stream=None):
+        """New positions (same cell and species); rebuilds the neighbor list."""
+        if hasattr(positions, "data_ptr"):   # a CUDA tensor of float64
+            check(lib().fpp_structure_set_positions(
+                self.handle, positions.data_ptr(), 1, _stream(stream)))
+            self.positions = None
+        else:
+            self.positions = f64(positions).reshape(-1, 3)
+            check(lib().fpp_structure_set_positions(
+                self.handle, ptr(self.positions), 0, _stream(stream)))
+        self._nb = None
+
+    def compute_descriptors(self):
+        self.descriptors = [d.compute_struc(self)
+                            for d in self.descriptor_calculators]
+
+    # neighbor attributes (structure.h:12-49) ---------------------------
+    def _neighbors(self):
+        if self._nb is None:
+            noa = _lib.ctypes.c_int32()
+            nn = _lib.ctypes.c_int64()
+            sw = _lib.ctypes.c_int32()
+            vol = _lib.ctypes.c_double()
+            check(lib().fpp_structure_info(self.handle, _lib.ctypes.byref(noa),
+                                           _lib.ctypes.byref(nn),
+                                           _lib.ctypes.byref(sw),
+                                           _lib.ctypes.byref(vol)))
+            n, np_ = noa.value, nn.value
+            cnt = np.zeros(n, np.int32)
+            cum = np.zeros(n + 1, np.int32)
+            idx = np.zeros(np_, np.int32)
+            nsp = np.zeros(np_, np.int32)
+            rel = np.zeros((np_, 4))
+            wp = np.zeros((n, 3))
+            check(lib().fpp_structure_get_neighbors(
+                self.handle, ptr(cnt), ptr(cum), ptr(idx), ptr(nsp), ptr(rel),
+                ptr(wp)))
+            self._nb = dict(neighbor_count=cnt, cumulative_neighbor_count=cum,
+                            structure_indices=idx, neighbor_species=nsp,
+                            relative_positions=rel, wrapped_positions=wp,
+                            n_neighbors=np_, sweep=sw.value, volume=vol.value)
+        return self._nb
+
+    neighbor_count = property(lambda self: self._neighbors()["neighbor_count"])
+    cumulative_neighbor_count = property(
+        lambda self: self._neighbors()["cumulative_neighbor_count"])
+    structure_indices = property(lambda self: self._neighbors()["structure_indices"])
+    neighbor_species = property(lambda self: self._neighbors()["neighbor_species"])
+    relative_positions = property(lambda self: self._neighbors()["relative_positions"])
+    wrapped_positions = property(lambda self: self._neighbors()["wrapped_positions"])
+    n_neighbors = property(lambda self: self._neighbors()["n_neighbors"])
+    sweep = property(lambda self: self._neighbors()["sweep"])
+
+    @property
+    def volume(self):
+        return abs(float(np.linalg.det(self.cell)))
+
+
+# --------------------------------------------------------------------------
+class DescriptorValues:
+    """Per-species descriptor blocks of one structure (descriptor.h:31-57)."""
+
+    def __init__(self):
+        self.n_descriptors = 0
+        self.n_types = 0
+        self.n_atoms = 0
+        self.volume = 0.0
+        self.descriptors = []
+        self.descriptor_force_dervs = []
+        self.neighbor_coordinates = []
+        self.descriptor_norms = []
+        self.descriptor_force_dots = []
+        self.cutoff_values = []
+        self.cutoff_dervs = []
+        self.neighbor_counts = []
+        self.cumulative_neighbor_counts = []
+        self.atom_indices = []
+        self.neighbor_indices = []
+        self.n_clusters = 0
+        self.n_clusters_by_type = []
+        self.cumulative_type_count = [0]
+        self.n_neighbors_by_type = []
+        self.structure = None
+
+
+class ClusterDescriptor:
+    """Sparse-set rows grouped by type (descriptor.h:61-90)."""
+
+    def __init__(self, structure=None, clusters=None):
+        self.descriptors = []
+        self.descriptor_norms = []
+        self.cutoff_values = []
+        self.n_clusters_by_type = []
+        self.cumulative_type_count = []
+        self.n_descriptors = 0
+        self.n_types = 0
+        self.n_clusters = 0
+        if structure is not None:
+            if clusters is None:
+                self.add_all_clusters(structure)
+            else:
+                self.add_clusters_by_type(structure, clusters)
+
+    def initialize_cluster(self, n_types, n_descriptors):
+        """descriptor.cpp:68-85."""
+        if self.n_clusters != 0:
+            return
+        self.n_types = n_types
+        self.n_descriptors = n_descriptors
+        self.descriptors = [np.zeros((0, n_descriptors)) for _ in range(n_types)]
+        self.descriptor_norms = [np.zeros(0) for _ in range(n_types)]
+        self.cutoff_values = [np.zeros(0) for _ in range(n_types)]
+        self.n_clusters_by_type = [0] * n_types
+        self.cumulative_type_count = [0] * n_types
+
+    def add_clusters_by_type(self, dv, clusters):
+        """descriptor.cpp:104-140."""
+        self.initialize_cluster(dv.n_types, dv.n_descriptors)
+        for s in range(self.n_types):
+            idx = np.asarray(clusters[s], dtype=np.int64)
+            self.descriptors[s] = np.vstack([self.descriptors[s],
+                                             dv.descriptors[s][idx]])
+            self.descriptor_norms[s] = np.concatenate(
+                [self.descriptor_norms[s], dv.descriptor_norms[s][idx]])
+            self.cutoff_values[s] = np.concatenate(
+                [self.cutoff_values[s], dv.cutoff_values[s][idx]])
+        for s in range(self.n_types):
+            self.n_clusters_by_type[s] += len(clusters[s])
+            self.n_clusters += len(clusters[s])
+            if s > 0:
+                self.cumulative_type_count[s] = (
+                    self.cumulative_type_count[s - 1] + self.n_clusters_by_type[s - 1])
+
+    def add_all_clusters(self, dv):
+        self.add_clusters_by_type(
+            dv, [list(range(dv.n_clusters_by_type[s])) for s in range(dv.n_types)])
+
+
+# --------------------------------------------------------------------------
+class B2(_Handle):
+    """B2 power spectrum (b2.h:34-46).  compute_struc runs on the GPU in FP64
+    and, like the reference, returns the stored force derivatives."""
+    _destroy = "fpp_b2_destroy"
+
+    def __init__(self, radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
+                 descriptor_settings, cutoffs=None):
+        self.radial_basis = radial_basis
+        self.cutoff_function = cutoff_function
+        self.radial_hyps = list(map(float, radial_hyps))
+        self.cutoff_hyps = list(map(float, cutoff_hyps))
+        self.descriptor_settings = [int(v) for v in descriptor_settings]
+        ns = self.descriptor_settings[0]
+        if cutoffs is None:
+            cutoffs = np.full((ns, ns), self.radial_hyps[1])
+        self.cutoffs = f64(cutoffs).reshape(ns, ns)
+        self.store_dervs = True
+        rh = f64(self.radial_hyps)
+        ch = f64(self.cutoff_hyps) if self.cutoff_hyps else f64([0.0])
+        ds = i32(self.descriptor_settings)
+        h = _lib.ctypes.c_void_p()
+        check(lib().fpp_b2_create(radial_basis.encode(), cutoff_function.encode(),
+                                  ptr(rh), len(rh), ptr(ch), len(self.cutoff_hyps),
+                                  ptr(ds), ptr(self.cutoffs), _lib.ctypes.byref(h)))
+        self._h = h.value
+        n = _lib.ctypes.c_int32()
+        check(lib().fpp_b2_n_descriptors(self._h, _lib.ctypes.byref(n)))
+        self.n_descriptors = n.value
+
+    def compute_struc(self, structure, stream=None):
+        """B2::compute_struc (b2.cpp:76-179) -> DescriptorValues."""
+        st = _stream(stream)
+        noa, nd, ns = structure.noa, self.n_descriptors, self.descriptor_settings[0]
+        desc = np.zeros((noa, nd))
+        norms = np.zeros(noa)
+        npairs = _lib.ctypes.c_int64()
+        check(lib().fpp_b2_pair_count(self._h, structure.handle,
+                                      _lib.ctypes.byref(npairs), st))
+        np_ = npairs.value
+        cnt = np.zeros(noa, np.int32)
+        nidx = np.zeros(np_, np.int32)
+        ncoord = np.zeros((np_, 3))
+        dervs = np.zeros((3 * np_, nd)) if self.store_dervs else None
+        dots = np.zeros(3 * np_) if self.store_dervs else None
+        check(lib().fpp_b2_compute(self._h, structure.handle, ptr(desc), ptr(norms),
+                                   ptr(cnt), ptr(nidx), ptr(ncoord), ptr(dervs),
+                                   ptr(dots), st))
+        cum = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+        sp = np.asarray(structure.species)
+        dv = DescriptorValues()
+        dv.n_descriptors, dv.n_types, dv.n_atoms = nd, ns, noa
+        dv.volume = structure.volume
+        dv.cumulative_type_count = [0]
+        for s in range(ns):
+            atoms = np.nonzero(sp == s)[0]
+            nn = cnt[atoms].astype(np.int64)
+            dv.n_clusters_by_type.append(len(atoms))
+            dv.cumulative_type_count.append(dv.cumulative_type_count[s] + len(atoms))
+            dv.n_clusters += len(atoms)
+            dv.n_neighbors_by_type.append(int(nn.sum()))
+            dv.descriptors.append(desc[atoms])
+            dv.descriptor_norms.append(norms[atoms])
+            dv.cutoff_values.append(np.ones(len(atoms)))
+            dv.cutoff_dervs.append(np.zeros(3 * int(nn.sum())))
+            dv.neighbor_counts.append(nn)
+            dv.cumulative_neighbor_counts.append(
+                np.concatenate([[0], np.cumsum(nn)[:-1]]).astype(np.int64)
+                if len(atoms) else np.zeros(0, np.int64))
+            dv.atom_indices.append(atoms)
+            rows = (np.concatenate([np.arange(cum[a], cum[a + 1]) for a in atoms])
+                    if len(atoms) else np.zeros(0, np.int64)).astype(np.int64)
+            dv.neighbor_indices.append(nidx[rows].astype(np.int64))
+            dv.neighbor_coordinates.append(ncoord[rows])
+            if self.store_dervs:
+                frows = (3 * rows[:, None] + np.arange(3)[None]).ravel()
+                dv.descriptor_force_dervs.append(dervs[frows])
+                dv.descriptor_force_dots.append(dots[frows])
+            else:
+                dv.descriptor_force_dervs.append(None)
+                dv.descriptor_force_dots.append(None)
+        dv.structure = structure
+        dv.descriptor_calculator = self
+        return dv
+
+
+# --------------------------------------------------------------------------
+class NormalizedDotProduct:
+    """k = sigma^2 (d.p / |d||p|)^power (normalized_dot_product.h:11-73)."""
+
+    def __init__(self, sigma, power):
+        self.sigma = float(sigma)
+        self.power = float(power)
+        self.kernel_hyperparameters = np.array([self.sigma])
+
+    def _model(self, b2, envs, alpha=None):
+        return _Model(b2, self.sigma, self.power, envs, alpha)
+
+    def envs_struc(self, envs, struc, hyps=None, stream=None):
+        """envs_struc (normalized_dot_product.cpp:115-210), FP64 on the GPU;
+        ``struc`` is the DescriptorValues of a Structure built here."""
+        sigma = self.sigma if hyps is None else float(hyps[0])
+        m = _Model(struc.descriptor_calculator, sigma, self.power, envs)
+        n_out = 1 + 3 * struc.n_atoms + 6
+        K = np.zeros((envs.n_clusters, n_out))
+        check(lib().fpp_envs_struc(m.handle, struc.structure.handle, ptr(K),
+                                   _stream(stream)))
+        return K
+
+    def envs_envs(self, envs1, envs2, hyps=None):
+        """envs_envs (normalized_dot_product.cpp:27-87)."""
+        sig2 = (self.sigma if hyps is None else float(hyps[0])) ** 2
+        K = np.zeros((envs1.n_clusters, envs2.n_clusters))
+        for s in range(envs1.n_types):
+            d1, d2 = envs1.descriptors[s], envs2.descriptors[s]
+            n1, n2 = envs1.descriptor_norms[s], envs2.descriptor_norms[s]
+            if len(n1) == 0 or len(n2) == 0:
+                continue
+            ok1, ok2 = n1 >= 1e-8, n2 >= 1e-8
+            h1 = np.where(ok1[:, None], d1 / np.where(ok1, n1, 1)[:, None], 0)
+            h2 = np.where(ok2[:, None], d2 / np.where(ok2, n2, 1)[:, None], 0)
+            v = sig2 * (h1 @ h2.T) ** self.power
+            v = np.where(ok1[:, None] & ok2[None, :], v, 0.0)
+            c1, c2 = envs1.cumulative_type_count[s], envs2.cumulative_type_count[s]
+            K[c1:c1 + len(n1), c2:c2 + len(n2)] += v
+        return K
+
+
+class _Model(_Handle):
+    """Device model: sparse set + weights (+ R_inv, mapped beta)."""
+    _destroy = "fpp_model_destroy"
+
+    def __init__(self, b2, sigma, power, envs, alpha=None, R_inv=None):
+        h = _lib.ctypes.c_void_p()
+        check(lib().fpp_model_create(b2._h, float(sigma), float(power),
+                                     _lib.ctypes.byref(h)))
+        self._h = h.value
+        self.b2 = b2
+        self.n_species = b2.descriptor_settings[0]
+        self.n_descriptors = b2.n_descriptors
+        n_tot = envs.n_clusters
+        alpha = np.zeros(n_tot) if alpha is None else f64(alpha)
+        for s in range(envs.n_types):
+            D = f64(envs.descriptors[s])
+            nrm = f64(envs.descriptor_norms[s])
+            off = envs.cumulative_type_count[s]
+            a = f64(alpha[off:off + len(nrm)])
+            check(lib().fpp_model_set_sparse(self._h, s, len(nrm), ptr(D), ptr(nrm),
+                                             ptr(a)))
+        if R_inv is not None:
+            R = f64(R_inv)
+            check(lib().fpp_model_set_R_inv(self._h, R.shape[0], ptr(R)))
+        self.beta_power = 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def compute_beta(self, power, stream=None):
+        """compute_map_coeff_pow1/2 -> packed beta, (n_species, beta_size)."""
+        nd, ns = self.n_descriptors, self.n_species
+        size = nd if power == 1 else nd * (nd + 1) // 2
+        out = np.zeros((ns, size))
+        check(lib().fpp_model_compute_beta(self._h, ptr(out), _stream(stream)))
+        return out
+
+    def set_beta(self, power, beta_packed):
+        b = f64(beta_packed)
+        check(lib().fpp_model_set_beta(self._h, int(power), ptr(b)))
+
+
+# --------------------------------------------------------------------------
+class SparseGP:
+    """Prediction side of SparseGP (sparse_gp.h:12-112) for one
+    NormalizedDotProduct kernel over one B2 descriptor."""
+
+    def __init__(self, kernels, energy_noise, force_noise, stress_noise):
+        self.kernels = list(kernels)
+        if len(self.kernels) != 1:
+            raise NotImplementedError("one kernel per model")
+        self.energy_noise = energy_noise
+        self.force_noise = force_noise
+        self.stress_noise = stress_noise
+        self.sparse_descriptors = []
+        self.alpha = None
+        self.R_inv = None
+        self.Sigma = None
+        self._model = None
+        self._mapped = False
+
+    def set_model(self, b2, sparse_descriptors, alpha, R_inv=None):
+        """Load a trained model: the sparse ClusterDescriptor, alpha and
+        optionally R_inv (the outputs of update_matrices_QR)."""
+        self.b2 = b2
+        self.sparse_descriptors = [sparse_descriptors]
+        self.alpha = f64(alpha)
+        self.R_inv = None if R_inv is None else f64(R_inv)
+        k = self.kernels[0]
+        self._model = _Model(b2, k.sigma, k.power, sparse_descriptors, self.alpha,
+                             self.R_inv)
+        self._mapped = False
+
+    def _ensure_mapped(self, stream=None):
+        if not self._mapped:
+            self.mapping_coefficients = self._model.compute_beta(
+                self.kernels[0].power, stream)
+            self._mapped = True
+
+    def predict_mean(self, structure, stream=None):
+        """sparse_gp.cpp:612-628 -> structure.mean_efs."""
+        out = np.zeros(1 + 3 * structure.noa + 6)
+        check(lib().fpp_predict(self._model.handle, structure.handle, ptr(out), None,
+                                _stream(stream)))
+        structure.mean_efs = out
+
+    def predict_SOR(self, structure, stream=None):
+        """sparse_gp.cpp:630-649 -> structure.mean_efs, structure.variance_efs."""
+        if self.R_inv is None:
+            raise ValueError("predict_SOR needs R_inv")
+        out = np.zeros(1 + 3 * structure.noa + 6)
+        var = np.zeros_like(out)
+        check(lib().fpp_predict(self._model.handle, structure.handle, ptr(out),
+                                ptr(var), _stream(stream)))
+        structure.mean_efs = out
+        structure.variance_efs = var
+
+    def predict_mapped(self, structure, precision="mixed", stream=None,
+                       atom_energies=False):
+        """Energy, forces and stress through the mapped coefficients (the pair
+        style's evaluation) on the periodic structure."""
+        self._ensure_mapped(stream)
+        e = np.zeros(1)
+        f = np.zeros((structure.noa, 3))
+        s = np.zeros(6)
+        ae = np.zeros(structure.noa) if atom_energies else None
+        check(lib().fpp_predict_mapped(self._model.handle, structure.handle,
+                                       PRECISIONS[precision], ptr(e), ptr(f), ptr(s),
+                                       ptr(ae), 0, _stream(stream)))
+        return (e[0], f, s, ae) if atom_energies else (e[0], f, s)
+
+
+class PairFLARE:
+    """Mapped-beta pair style (lammps_plugins/pair_flare.h:20-50): reads the
+    potential file and computes energy, forces and virial on LAMMPS-shaped
+    arrays (full neighbor list, 1-based types, ghost atoms)."""
+
+    def __init__(self, filename=None, model=None, b2=None):
+        if filename is not None:
+            self.read_file(filename)
+        elif model is not None:
+            self.model = model
+        self.precision = "fp64"
+
+    def read_file(self, filename):
+        """pair_flare.cpp:263-396."""
+        from .potential import read_potential
+        pot = read_potential(filename)
+        self.pot = pot
+        ns, N, lmax = pot["n_species"], pot["n_max"], pot["l_max"]
+        cut = pot["cutoffs"].reshape(ns, ns)
+        self.cutoff = float(cut.max())
+        b2 = B2(pot["radial"], pot["cutoff_function"], [0.0, self.cutoff], [],
+                [ns, N, lmax], cut)
+        envs = ClusterDescriptor()
+        envs.initialize_cluster(ns, b2.n_descriptors)
+        self.b2 = b2
+        self.model = _Model(b2, 1.0, pot["power"], envs)
+        self.model.set_beta(pot["power"], pot["beta"])
+
+    def compute(self, x, type_, ilist, numneigh, neighbors, nlocal=None,
+                precision=None, eatom=False, stream=None):
+        """PairFLARE::compute (pair_flare.cpp:68-184).  Returns
+        (f, eng_vdwl, virial[, eatom])."""
+        x = f64(x).reshape(-1, 3)
+        t = i32(type_)
+        il = i32(ilist)
+        nn = i32(numneigh)
+        nb = i32(neighbors)
+        nall = len(x)
+        nlocal = len(il) if nlocal is None else int(nlocal)
+        f = np.zeros((nall, 3))
+        e = np.zeros(1)
+        v = np.zeros(6)
+        ea = np.zeros(nall) if eatom else None
+        prec = PRECISIONS[precision or self.precision]
+        check(lib().fpp_pair_compute(self.model.handle, nlocal, nall, ptr(x), ptr(t),
+                                     len(il), ptr(il), ptr(nn), ptr(nb), prec, ptr(f),
+                                     ptr(e), ptr(v), ptr(ea), _stream(stream)))
+        return (f, e[0], v, ea) if eatom else (f, e[0], v)

@@ -1,0 +1,610 @@
+// B2 descriptor forward pass and its adjoint (forces and virial without the
+// stored descriptor_force_dervs tensor).
+//
+// Forward (one warp per atom), src/flare_pp/descriptors/b2.cpp:244-399 and
+// :181-242:
+//   c[(s N + n) H + lm] = sum_j g_n(r_ij) Y_lm(r_ij)   over neighbors of species s
+//                          with r_ij <= cutoffs[s_i][s_j]
+//   p[(n1, n2 >= n1, l)] = sum_m c[n1, lm] c[n2, lm],  |p| in FP64
+// The neighbor bases are computed one neighbor per lane and staged in shared
+// memory; each lane then owns one (l, m) column and accumulates all radial
+// channels in registers (compensated in FP32).
+//
+// Adjoint (one warp per atom), lammps_plugins/lammps_descriptor.cpp:250-304 and
+// pair_flare.cpp:141-175:
+//   w = dE/dp, u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]
+//   f_ij = dE/dr_ij = sum_{n, lm} u[s_j N + n, lm] d(g_n Y_lm)/dr_ij
+// with the bases recomputed per pair.  Forces are then gathered per atom from
+// f_ij and the reverse pair's f_ji, so the result is deterministic.
+#include <cuda_fp16.h>
+
+#include "basis.cuh"
+#include "b2_kernels.h"
+#include "common.cuh"
+
+namespace fpp {
+
+int upload_harmonic_tables(cudaStream_t stream) {
+  HarmonicTables t;
+  const double pi = 3.14159265358979323846;
+  for (int l = 0; l <= kMaxL; l++)
+    for (int m = 0; m <= kMaxL; m++) {
+      double v = 0;
+      if (m <= l) {
+        double f = 1;
+        for (int k = l - m + 1; k <= l + m; k++) f *= k;  // (l+m)!/(l-m)!
+        v = sqrt((2 * l + 1) / (4 * pi) / f);
+        if (m > 0) v *= sqrt(2.0);
+      }
+      t.norm[l * (kMaxL + 1) + m] = v;
+    }
+  for (int m = 0; m <= kMaxL; m++) {
+    double d = 1;
+    for (int k = 1; k < 2 * m; k += 2) d *= k;
+    t.dfact[m] = d;
+  }
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_harm, &t, sizeof(t), 0,
+                                          cudaMemcpyHostToDevice, stream);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+// Running sum; compensated (Neumaier) when T is float.
+template <typename T> struct Acc {
+  T s = T(0), c = T(0);
+  __device__ __forceinline__ void add(T x) {
+    if (sizeof(T) == 4) {
+      T t = s + x;
+      if (fabs(s) >= fabs(x))
+        c += (s - t) + x;
+      else
+        c += (x - t) + s;
+      s = t;
+    } else {
+      s += x;
+    }
+  }
+};
+
+// x^2 + y^2 + z^2 of a pair vector, rounded as the host computes it.
+__device__ __forceinline__ double rsq_exact(const dvec4 &r) {
+  return dadd(dadd(dmul(r.y, r.y), dmul(r.z, r.z)), dmul(r.w, r.w));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Forward.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_b2_forward(B2Args a, const int *__restrict__ offset,
+             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
+             const int *__restrict__ nbr_s, const int *__restrict__ species,
+             const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
+             T *__restrict__ c_out, T *__restrict__ p_out,
+             double *__restrict__ norm_out, double *__restrict__ phat64,
+             __half *__restrict__ phat_hi, __half *__restrict__ phat_lo, int ldp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int atom = blockIdx.x * nwarps + warp;
+  const int N = a.N, H = a.H, NS = a.n_species, W = a.window;
+  const int WS = W + 1;  // padded stride (conflict-free lane columns)
+  const int sb = NS * N * H;
+  // per-warp carve-out
+  const size_t per_warp = a.smem_per_warp;
+  unsigned char *base = smem_raw + per_warp * warp;
+  T *g_s = reinterpret_cast<T *>(base);           // [N][WS]
+  T *y_s = g_s + N * WS;                          // [H][WS]
+  T *c_s = y_s + H * WS;                          // [sb]
+  T *cc_s = c_s + sb;                             // [sb] compensation
+  int *sp_s = reinterpret_cast<int *>(cc_s + sb); // [W]
+  if (atom >= a.noa) return;
+
+  for (int k = lane; k < sb; k += 32) {
+    c_s[k] = T(0);
+    cc_s[k] = T(0);
+  }
+  const int si = species[atom];
+  const int beg = offset[atom], end = offset[atom + 1];
+  __syncwarp();
+  for (int w0 = beg; w0 < end; w0 += W) {
+    const int cnt = min(W, end - w0);
+    // stage bases, one neighbor per lane
+    for (int b = lane; b < cnt; b += 32) {
+      const int p = w0 + b;
+      const int sj = nbr_s[p];
+      const dvec4 rd = rel[p];
+      const double rcut = a.cutoffs[si * NS + sj];
+      const bool keep = a.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+      T r, x, y, z;
+      if (sizeof(T) == 8) {
+        r = T(rd.x);
+        x = T(rd.y);
+        y = T(rd.z);
+        z = T(rd.w);
+      } else {
+        const float4 rf = rel32[p];
+        x = T(rf.x);
+        y = T(rf.y);
+        z = T(rf.z);
+        r = T(rf.w);
+      }
+      sp_s[b] = keep ? sj : -1;
+      radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, g_s + b, nullptr, WS);
+      real_harmonics<T>(x, y, z, a.lmax, y_s + b, nullptr, WS);
+    }
+    __syncwarp();
+    // accumulate: lane owns column lm, registers hold the N radial channels
+    for (int s = 0; s < NS; s++) {
+      for (int lm0 = 0; lm0 < H; lm0 += 32) {
+        const int lm = lm0 + lane;
+        const bool act = lm < H;
+        const int lmc = act ? lm : 0;
+        Acc<T> acc[kMaxN];
+#pragma unroll
+        for (int n = 0; n < kMaxN; n++)
+          if (n < N) {
+            acc[n].s = c_s[(s * N + n) * H + lmc];
+            acc[n].c = cc_s[(s * N + n) * H + lmc];
+          }
+        for (int b = 0; b < cnt; b++) {
+          if (sp_s[b] != s) continue;
+          const T yv = y_s[lmc * WS + b];
+#pragma unroll
+          for (int n = 0; n < kMaxN; n++)
+            if (n < N) acc[n].add(g_s[n * WS + b] * yv);
+        }
+        if (act) {
+#pragma unroll
+          for (int n = 0; n < kMaxN; n++)
+            if (n < N) {
+              c_s[(s * N + n) * H + lm] = acc[n].s;
+              cc_s[(s * N + n) * H + lm] = acc[n].c;
+            }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // fold the compensation and publish c
+  for (int k = lane; k < sb; k += 32) {
+    T v = c_s[k] + cc_s[k];
+    c_s[k] = v;
+    c_out[(size_t)atom * sb + k] = v;
+  }
+  __syncwarp();
+  // B2 contraction: p[d] with d = q (lmax+1) + l, pair q = (n1, n2 >= n1)
+  const int L1 = a.lmax + 1;
+  const int nd = a.n_d;
+  double nsq = 0.0;
+  for (int d = lane; d < nd; d += 32) {
+    const int q = d / L1, l = d - q * L1;
+    const int pr = pair_tab[q];
+    const int n1 = pr & 0xffff, n2 = pr >> 16;
+    const T *c1 = c_s + n1 * H + l * l, *c2 = c_s + n2 * H + l * l;
+    T v = T(0);
+    for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
+    nsq += double(v) * double(v);
+    if (p_out) p_out[(size_t)atom * nd + d] = v;
+  }
+  nsq = warp_sum(nsq);
+  const double nrm = sqrt(nsq);
+  if (lane == 0) norm_out[atom] = nrm;
+  const int row = row_of_atom[atom];
+  const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+  for (int d = lane; d < nd; d += 32) {
+    const int q = d / L1, l = d - q * L1;
+    const int pr = pair_tab[q];
+    const int n1 = pr & 0xffff, n2 = pr >> 16;
+    const T *c1 = c_s + n1 * H + l * l, *c2 = c_s + n2 * H + l * l;
+    T v = T(0);
+    for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
+    if (phat64) phat64[(size_t)row * ldp + d] = double(v) * inv;
+    if (phat_hi) {
+      const float x = float(double(v) * inv) * 16384.0f;
+      const __half h = __float2half_rn(x);
+      const float rem = (x - __half2float(h)) * 2048.0f;
+      phat_hi[(size_t)row * ldp + d] = h;
+      phat_lo[(size_t)row * ldp + d] = __float2half_rn(rem);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_b2_adjoint(B2Args a, AdjArgs g, const int *__restrict__ offset,
+             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
+             const int *__restrict__ nbr_s, const int *__restrict__ species,
+             const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
+             const T *__restrict__ c_in, const double *__restrict__ norm_in,
+             double *__restrict__ atom_e, T *__restrict__ pair_f) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int atom = blockIdx.x * nwarps + warp;
+  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
+  const int sb = NS * N * H;
+  const int L1 = a.lmax + 1;
+  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
+  T *w_s = reinterpret_cast<T *>(base);  // [nd]
+  T *c_s = w_s + nd;                     // [sb]
+  T *u_s = c_s + sb;                     // [sb]
+  T *bas = u_s + sb;                     // [(2N + 4H)][33]
+  if (atom >= a.noa) return;
+  const int si = species[atom];
+  const int row = row_of_atom[atom];
+  const double nrm = norm_in[atom];
+
+  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
+
+  // ---- w = dE/dp and the atom energy ----
+  bool empty;
+  double e = 0.0;
+  if (g.mode == kWFromV2 || g.mode == kWFromV1) {
+    empty = g.mode == kWFromV2 ? (nrm * nrm < g.empty_thresh)
+                               : (nrm * nrm < g.empty_thresh);
+    // phat reconstructed from the contraction operands
+    double dot = 0.0;
+    for (int d = lane; d < nd; d += 32) {
+      double ph, v;
+      if (g.phat64) {
+        ph = g.phat64[(size_t)row * g.ldp + d];
+      } else {
+        ph = (double(__half2float(g.phat_hi[(size_t)row * g.ldp + d])) +
+              double(__half2float(g.phat_lo[(size_t)row * g.ldp + d])) * (1.0 / 2048.0)) *
+             (1.0 / 16384.0);
+      }
+      if (g.mode == kWFromV2)
+        v = g.V64 ? g.V64[(size_t)row * g.ldv + d] : double(g.V32[(size_t)row * g.ldv + d]);
+      else
+        v = g.beta1[(size_t)si * nd + d];
+      dot += ph * v;
+    }
+    dot = warp_sum(dot);
+    e = empty ? 0.0 : dot;
+    const double inv = empty ? 0.0 : 1.0 / nrm;
+    for (int d = lane; d < nd; d += 32) {
+      double ph, v;
+      if (g.phat64) {
+        ph = g.phat64[(size_t)row * g.ldp + d];
+      } else {
+        ph = (double(__half2float(g.phat_hi[(size_t)row * g.ldp + d])) +
+              double(__half2float(g.phat_lo[(size_t)row * g.ldp + d])) * (1.0 / 2048.0)) *
+             (1.0 / 16384.0);
+      }
+      if (g.mode == kWFromV2) {
+        v = g.V64 ? g.V64[(size_t)row * g.ldv + d] : double(g.V32[(size_t)row * g.ldv + d]);
+        w_s[d] = T(2.0 * (v - e * ph) * inv);
+      } else {
+        v = g.beta1[(size_t)si * nd + d];
+        w_s[d] = T((v - e * ph) * inv);
+      }
+    }
+  } else {  // kWGiven: dE/dp supplied per atom (kernel form)
+    empty = false;
+    for (int d = lane; d < nd; d += 32) w_s[d] = T(g.w_given[(size_t)row * g.ldp + d]);
+    e = g.e_given ? g.e_given[row] : 0.0;
+  }
+  if (lane == 0) atom_e[atom] = e;
+  __syncwarp();
+
+  // ---- u = dE/dc ----
+  for (int lm0 = 0; lm0 < H; lm0 += 32) {
+    const int lm = lm0 + lane;
+    if (lm < H) {
+      int l = 0;
+      while ((l + 1) * (l + 1) <= lm) l++;
+      for (int n1 = 0; n1 < NS * N; n1++) {
+        T acc = T(0);
+        const int nr = NS * N;
+        for (int n2 = 0; n2 < nr; n2++) {
+          const int lo = min(n1, n2), hi = max(n1, n2);
+          const int q = lo * nr - (lo * (lo - 1)) / 2 + (hi - lo);
+          T wv = w_s[q * L1 + l];
+          if (n1 == n2) wv = wv + wv;
+          acc += wv * c_s[n2 * H + lm];
+        }
+        u_s[n1 * H + lm] = acc;
+      }
+    }
+  }
+  __syncwarp();
+
+  // ---- per-pair forces ----
+  T *gb = bas;                // g   [N][33]
+  T *db = gb + N * 33;        // dg  [N][33]
+  T *yb = db + N * 33;        // Y   [H][33]
+  T *yg = yb + H * 33;        // dY  [3H][33]
+  const int beg = offset[atom], end = offset[atom + 1];
+  for (int p0 = beg; p0 < end; p0 += 32) {
+    const int p = p0 + lane;
+    const bool valid = p < end;
+    T fx = T(0), fy = T(0), fz = T(0);
+    int sj = 0;
+    bool keep = false;
+    T r = T(1), x = T(1), y = T(0), z = T(0);
+    if (valid) {
+      sj = nbr_s[p];
+      const dvec4 rd = rel[p];
+      const double rcut = a.cutoffs[si * NS + sj];
+      keep = g.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+      if (sizeof(T) == 8) {
+        r = T(rd.x);
+        x = T(rd.y);
+        y = T(rd.z);
+        z = T(rd.w);
+      } else {
+        const float4 rf = rel32[p];
+        x = T(rf.x);
+        y = T(rf.y);
+        z = T(rf.z);
+        r = T(rf.w);
+      }
+      radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, gb + lane, db + lane, 33);
+      real_harmonics<T>(x, y, z, a.lmax, yb + lane, yg + lane, 33);
+    }
+    __syncwarp();
+    if (valid && keep && !empty) {
+      const T *us = u_s + sj * N * H;
+      T fr = T(0);
+      for (int lm = 0; lm < H; lm++) {
+        T ag = T(0), bd = T(0);
+        for (int n = 0; n < N; n++) {
+          const T uv = us[n * H + lm];
+          ag += uv * gb[n * 33 + lane];
+          bd += uv * db[n * 33 + lane];
+        }
+        fr += bd * yb[lm * 33 + lane];
+        fx += ag * yg[(3 * lm + 0) * 33 + lane];
+        fy += ag * yg[(3 * lm + 1) * 33 + lane];
+        fz += ag * yg[(3 * lm + 2) * 33 + lane];
+      }
+      const T ir = T(1) / r;
+      fx += fr * x * ir;
+      fy += fr * y * ir;
+      fz += fr * z * ir;
+    }
+    if (valid) {
+      pair_f[(size_t)p * 4 + 0] = fx;
+      pair_f[(size_t)p * 4 + 1] = fy;
+      pair_f[(size_t)p * 4 + 2] = fz;
+      pair_f[(size_t)p * 4 + 3] = T(0);
+    }
+    __syncwarp();
+  }
+}
+
+// Stored derivatives of b2.cpp:181-242 for a list of structure pairs (FP64):
+// rows 3*idx + comp of dp = d p_i / d r_ij and force_dots = dp . p_i.
+// One warp per pair.
+__global__ void __launch_bounds__(128)
+k_b2_dp(B2Args a, int npl, const int *__restrict__ plist,
+        const int *__restrict__ nbr_i, const int *__restrict__ nbr_s,
+        const dvec4 *__restrict__ rel, const int *__restrict__ species,
+        const int *__restrict__ pair_tab, const double *__restrict__ c_in,
+        const double *__restrict__ p_in, double *__restrict__ dp, int ldd,
+        double *__restrict__ force_dots) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int idx = blockIdx.x * nwarps + warp;
+  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
+  const int sb = NS * N * H;
+  double *base = reinterpret_cast<double *>(smem_raw) + (size_t)warp * (sb + 3 * N * H + 2 * N + 4 * H);
+  double *c_s = base;                 // [sb]
+  double *dc = c_s + sb;              // [3][N][H]
+  double *gb = dc + 3 * N * H;        // [N] g, [N] dg
+  double *yb = gb + 2 * N;            // [H] Y, [3H] dY
+  if (idx >= npl) return;
+  const int p = plist[idx];
+  const int i = nbr_i[p], sj = nbr_s[p];
+  const int si = species[i];
+  const dvec4 rd = rel[p];
+  const double rcut = a.cutoffs[si * NS + sj];
+  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)i * sb + k];
+  if (lane == 0) {
+    radial_basis<double>(rd.x, a.r1, rcut, N, a.cutoff_kind, gb, gb + N, 1);
+    real_harmonics<double>(rd.y, rd.z, rd.w, a.lmax, yb, yb + H, 1);
+  }
+  __syncwarp();
+  const double u[3] = {rd.y / rd.x, rd.z / rd.x, rd.w / rd.x};
+  for (int k = lane; k < 3 * N * H; k += 32) {
+    const int comp = k / (N * H), rem = k - comp * N * H, n = rem / H, lm = rem - n * H;
+    dc[k] = gb[N + n] * u[comp] * yb[lm] + gb[n] * yb[H + 3 * lm + comp];
+  }
+  __syncwarp();
+  const int L1 = a.lmax + 1;
+  double fdot[3] = {0, 0, 0};
+  for (int d = lane; d < nd; d += 32) {
+    const int q = d / L1, l = d - q * L1;
+    const int pr = pair_tab[q];
+    const int n1 = pr & 0xffff, n2 = pr >> 16;
+    const bool in1 = (n1 / N) == sj, in2 = (n2 / N) == sj;
+    const double pv = p_in[(size_t)i * nd + d];
+    for (int comp = 0; comp < 3; comp++) {
+      double v = 0.0;
+      for (int m = 0; m < 2 * l + 1; m++) {
+        const int lm = l * l + m;
+        if (in2) v += c_s[n1 * H + lm] * dc[comp * N * H + (n2 % N) * H + lm];
+        if (in1) v += dc[comp * N * H + (n1 % N) * H + lm] * c_s[n2 * H + lm];
+      }
+      dp[(size_t)(3 * idx + comp) * ldd + d] = v;
+      fdot[comp] += v * pv;
+    }
+  }
+  for (int comp = 0; comp < 3; comp++) {
+    double v = warp_sum(fdot[comp]);
+    if (lane == 0) force_dots[3 * idx + comp] = v;
+  }
+}
+
+int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
+                 const int *nbr_s, const dvec4 *rel, const int *species,
+                 const int *pair_tab, const double *c_in, const double *p_in,
+                 double *dp, int ldd, double *force_dots, cudaStream_t stream) {
+  if (npl == 0) return 0;
+  const int sb = a.n_species * a.N * a.H;
+  size_t per = sizeof(double) * (sb + 3 * a.N * a.H + 2 * a.N + 4 * a.H);
+  int wpb = 4;
+  while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
+  size_t smem = per * wpb;
+  if (smem > 227 * 1024) return -1;
+  if (cudaFuncSetAttribute(k_b2_dp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  k_b2_dp<<<ceil_div(npl, wpb), 32 * wpb, smem, stream>>>(
+      a, npl, plist, nbr_i, nbr_s, rel, species, pair_tab, c_in, p_in, dp, ldd,
+      force_dots);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// F_i = sum over pairs of i (f_ij - f_ji), per-atom virial sum f_ij (x) r_ij.
+template <typename T>
+__global__ void k_gather(int noa, const int *__restrict__ offset,
+                         const int *__restrict__ rev, const dvec4 *__restrict__ rel,
+                         const T *__restrict__ pair_f, double *__restrict__ forces,
+                         double *__restrict__ atom_vir) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= noa) return;
+  double F[3] = {0, 0, 0}, V[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int p = offset[i]; p < offset[i + 1]; p++) {
+    const int q = rev[p];
+    const double f0 = double(pair_f[(size_t)p * 4 + 0]);
+    const double f1 = double(pair_f[(size_t)p * 4 + 1]);
+    const double f2 = double(pair_f[(size_t)p * 4 + 2]);
+    F[0] += f0;
+    F[1] += f1;
+    F[2] += f2;
+    if (q >= 0) {  // always present for a periodic list; -1 is reported upstream
+      F[0] -= double(pair_f[(size_t)q * 4 + 0]);
+      F[1] -= double(pair_f[(size_t)q * 4 + 1]);
+      F[2] -= double(pair_f[(size_t)q * 4 + 2]);
+    }
+    const dvec4 r = rel[p];
+    const double rr[3] = {r.y, r.z, r.w}, ff[3] = {f0, f1, f2};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) V[a * 3 + b] += ff[a] * rr[b];
+  }
+  forces[3 * i + 0] = F[0];
+  forces[3 * i + 1] = F[1];
+  forces[3 * i + 2] = F[2];
+#pragma unroll
+  for (int k = 0; k < 9; k++) atom_vir[(size_t)9 * i + k] = V[k];
+}
+
+// Deterministic reduction of atom energies and virials: out[0] = E,
+// out[1..9] = sum f (x) r.  One block.
+__global__ void k_reduce(int noa, const double *__restrict__ atom_e,
+                         const double *__restrict__ atom_vir, double *__restrict__ out) {
+  __shared__ double sm[10][256];
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = threadIdx.x; i < noa; i += blockDim.x) {
+    acc[0] += atom_e[i];
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[1 + k] += atom_vir[(size_t)9 * i + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 10; k++) sm[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int k = 0; k < 10; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 10) out[threadIdx.x] = sm[threadIdx.x][0];
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers.
+// ---------------------------------------------------------------------------
+size_t forward_smem_per_warp(const B2Args &a, size_t elem) {
+  const int sb = a.n_species * a.N * a.H;
+  size_t b = elem * ((size_t)(a.N + a.H) * (a.window + 1) + 2 * (size_t)sb) +
+             sizeof(int) * a.window;
+  return (b + 15) & ~(size_t)15;
+}
+
+size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
+  const int sb = a.n_species * a.N * a.H;
+  size_t b = elem * ((size_t)a.n_d + 2 * (size_t)sb + (size_t)(2 * a.N + 4 * a.H) * 33);
+  return (b + 15) & ~(size_t)15;
+}
+
+template <typename T>
+int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
+                      const int *row_of_atom, const int *pair_tab, T *c_out,
+                      T *p_out, double *norm_out, double *phat64, __half *phat_hi,
+                      __half *phat_lo, int ldp, cudaStream_t stream) {
+  if (a.noa == 0) return 0;
+  a.smem_per_warp = forward_smem_per_warp(a, sizeof(T));
+  int wpb = 4;
+  while (wpb > 1 && a.smem_per_warp * wpb > 200 * 1024) wpb >>= 1;
+  size_t smem = a.smem_per_warp * wpb;
+  if (smem > 227 * 1024) return -1;
+  auto kern = k_b2_forward<T>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
+      a, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom, pair_tab,
+      c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename T>
+int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
+                      const int *species, const int *row_of_atom,
+                      const int *pair_tab, const T *c_in, const double *norm_in,
+                      double *atom_e, T *pair_f, double *forces, double *atom_vir,
+                      double *reduce_out, bool gather, cudaStream_t stream) {
+  if (a.noa == 0) return 0;
+  a.smem_per_warp_adj = adjoint_smem_per_warp(a, sizeof(T));
+  int wpb = 4;
+  while (wpb > 1 && a.smem_per_warp_adj * wpb > 200 * 1024) wpb >>= 1;
+  size_t smem = a.smem_per_warp_adj * wpb;
+  if (smem > 227 * 1024) return -1;
+  auto kern = k_b2_adjoint<T>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
+      a, g, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom,
+      pair_tab, c_in, norm_in, atom_e, pair_f);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  if (!gather) return 0;
+  k_gather<T><<<ceil_div(a.noa, 128), 128, 0, stream>>>(
+      a.noa, nb.offset, nb.rev, nb.rel, pair_f, forces, atom_vir);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  k_reduce<<<1, 256, 0, stream>>>(a.noa, atom_e, atom_vir, reduce_out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template int launch_b2_forward<float>(B2Args, const Neigh &, const int *, const int *,
+                                      const int *, float *, float *, double *,
+                                      double *, __half *, __half *, int, cudaStream_t);
+template int launch_b2_forward<double>(B2Args, const Neigh &, const int *, const int *,
+                                       const int *, double *, double *, double *,
+                                       double *, __half *, __half *, int, cudaStream_t);
+template int launch_b2_adjoint<float>(B2Args, const AdjArgs &, const Neigh &,
+                                      const int *, const int *, const int *,
+                                      const float *, const double *, double *,
+                                      float *, double *, double *, double *,
+                                      bool, cudaStream_t);
+template int launch_b2_adjoint<double>(B2Args, const AdjArgs &, const Neigh &,
+                                       const int *, const int *, const int *,
+                                       const double *, const double *, double *,
+                                       double *, double *, double *, double *,
+                                       bool, cudaStream_t);
+
+}  // namespace fpp

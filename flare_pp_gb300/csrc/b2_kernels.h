@@ -1,0 +1,76 @@
+// Launch interface of the B2 forward / adjoint kernels.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+#include <cstddef>
+
+namespace fpp {
+
+constexpr int kMaxSpecies = 8;
+
+struct B2Args {
+  int noa;
+  int n_species, N, lmax, H, n_d;
+  int cutoff_kind;  // CutoffKind
+  int window;       // neighbors staged per pass in the forward kernel
+  int strict;       // pair filter rsq < rc^2 (pair style) instead of r <= rc (B2)
+  double r1;
+  double cutoffs[kMaxSpecies * kMaxSpecies];
+  size_t smem_per_warp;      // filled by the launcher
+  size_t smem_per_warp_adj;  // filled by the launcher
+};
+
+enum WMode { kWFromV2 = 0, kWFromV1 = 1, kWGiven = 2 };
+
+struct AdjArgs {
+  int mode;              // WMode
+  int strict;            // pair filter rsq < rc^2 (pair style) instead of r <= rc
+  double empty_thresh;   // on |p|^2 for the mapped forms
+  // mapped power 2: V = beta phat rows (one of V32 / V64), phat operands
+  const float *V32;
+  const double *V64;
+  int ldv;
+  const double *phat64;
+  const __half *phat_hi, *phat_lo;
+  int ldp;
+  // mapped power 1: beta vector per species [n_species][n_d]
+  const double *beta1;
+  // given dE/dp and energies per operand row (row stride ldp)
+  const double *w_given;
+  const double *e_given;
+};
+
+struct Neigh {
+  const int *offset;
+  const dvec4 *rel;
+  const float4 *rel32;
+  const int *nbr_s;
+  const int *rev;
+};
+
+int upload_harmonic_tables(cudaStream_t stream);
+size_t forward_smem_per_warp(const B2Args &a, size_t elem);
+size_t adjoint_smem_per_warp(const B2Args &a, size_t elem);
+
+template <typename T>
+int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
+                      const int *row_of_atom, const int *pair_tab, T *c_out,
+                      T *p_out, double *norm_out, double *phat64, __half *phat_hi,
+                      __half *phat_lo, int ldp, cudaStream_t stream);
+
+template <typename T>
+int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
+                      const int *species, const int *row_of_atom,
+                      const int *pair_tab, const T *c_in, const double *norm_in,
+                      double *atom_e, T *pair_f, double *forces, double *atom_vir,
+                      double *reduce_out, bool gather, cudaStream_t stream);
+
+int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
+                 const int *nbr_s, const dvec4 *rel, const int *species,
+                 const int *pair_tab, const double *c_in, const double *p_in,
+                 double *dp, int ldd, double *force_dots, cudaStream_t stream);
+
+}  // namespace fpp

@@ -1,0 +1,148 @@
+// Per-neighbor bases on the device: chebyshev x cutoff radial functions and
+// real spherical harmonics with Cartesian gradients.
+//
+// Radial: T_n((r - r1)/(rc - r1)) with T_0 = 1, T_1 = x, T_n = 2x T_{n-1} -
+// T_{n-2}, zero outside [r1, rc], times the quadratic (r - rc)^2 or cosine
+// (cos(pi r / rc) + 1)/2 cutoff -- the functions of src/flare_pp/radial.cpp:
+// 138-169 and src/flare_pp/cutoffs.cpp:44-73.
+//
+// Harmonics: the orthonormal real harmonics without Condon-Shortley phase at
+// index l*l + l + m (the convention of src/flare_pp/y_grad.cpp:667), derived
+// here from the solid-harmonic recurrence
+//   r^l Y_lm = N_lm Q_l^|m|(z, r^2) T_m(x, y) (* sqrt 2 for m != 0),
+//   T_m = Re / Im (x + i y)^|m|, Q_m^m = (2m-1)!!, Q_{m+1}^m = (2m+1) z Q_m^m,
+//   Q_l^m = ((2l-1) z Q_{l-1}^m - (l+m-1) r^2 Q_{l-2}^m) / (l - m),
+// evaluated on the unit vector; gradients differentiate the recurrence and
+// use grad Y(r) = (grad R(u) - l Y(u) u) / |r|.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace fpp {
+
+// Normalisation N_lm * (sqrt 2 if m > 0) at [l*(kMaxL+1) + m], and the double
+// factorials (2m-1)!! at [m].
+struct HarmonicTables {
+  double norm[(kMaxL + 1) * (kMaxL + 1)];
+  double dfact[kMaxL + 1];
+};
+static __constant__ HarmonicTables c_harm;  // uploaded by upload_harmonic_tables()
+
+// g_n and dg_n/dr into out_g[n * stride], out_dg[n * stride].
+template <typename T>
+__device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_kind,
+                                             T *out_g, T *out_dg, int stride) {
+  T fc, dfc;
+  if (r > rc) {
+    fc = T(0);
+    dfc = T(0);
+  } else if (cutoff_kind == kQuadratic) {
+    T d = r - rc;
+    fc = d * d;
+    dfc = T(2) * d;
+  } else {
+    const T pi = T(3.14159265358979323846);
+    fc = T(0.5) * (cos(pi * r / rc) + T(1));
+    dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
+  }
+  const bool inside = !(r < r1 || r > rc);
+  const T c = T(1) / (rc - r1);
+  const T x = (r - r1) * c;
+  T tm2 = 0, tm1 = 0, dm2 = 0, dm1 = 0;
+  for (int n = 0; n < N; n++) {
+    T t, dt;
+    if (n == 0) {
+      t = T(1);
+      dt = T(0);
+    } else if (n == 1) {
+      t = x;
+      dt = c;
+    } else {
+      t = T(2) * x * tm1 - tm2;
+      dt = T(2) * tm1 * c + T(2) * x * dm1 - dm2;
+    }
+    tm2 = tm1;
+    tm1 = t;
+    dm2 = dm1;
+    dm1 = dt;
+    T gv = inside ? t : T(0), dv = inside ? dt : T(0);
+    out_g[n * stride] = gv * fc;
+    if (out_dg) out_dg[n * stride] = dv * fc + gv * dfc;
+  }
+}
+
+// Y_lm at out[lm * stride]; with grad != nullptr also the Cartesian gradient
+// at grad[(3*lm + k) * stride].
+template <typename T>
+__device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
+                                               T *grad, int stride) {
+  const T r = sqrt(x * x + y * y + z * z);
+  const T ir = T(1) / r;
+  const T ux = x * ir, uy = y * ir, uz = z * ir;
+  T A = T(1), B = T(0), Aprev = T(1), Bprev = T(0);
+  for (int m = 0; m <= lmax; m++) {
+    if (m > 0) {
+      Aprev = A;
+      Bprev = B;
+      T a2 = ux * A - uy * B;
+      T b2 = uy * A + ux * B;
+      A = a2;
+      B = b2;
+    }
+    // derivatives of A_m, B_m with respect to x and y
+    const T Ax = T(m) * Aprev, Ay = -T(m) * Bprev;
+    const T Bx = T(m) * Bprev, By = T(m) * Aprev;
+    T q2 = 0, q1 = 0, qz2 = 0, qz1 = 0, qr2 = 0, qr1 = 0;
+    for (int l = m; l <= lmax; l++) {
+      T q, qz, qr;
+      if (l == m) {
+        q = T(c_harm.dfact[m]);
+        qz = T(0);
+        qr = T(0);
+      } else if (l == m + 1) {
+        q = T(2 * m + 1) * uz * q1;
+        qz = T(2 * m + 1) * q1;
+        qr = T(0);
+      } else {
+        const T a = T(2 * l - 1), b = T(l + m - 1), inv = T(1) / T(l - m);
+        q = (a * uz * q1 - b * q2) * inv;
+        qz = (a * (q1 + uz * qz1) - b * qz2) * inv;
+        qr = (a * uz * qr1 - b * (q2 + qr2)) * inv;
+      }
+      q2 = q1;
+      q1 = q;
+      qz2 = qz1;
+      qz1 = qz;
+      qr2 = qr1;
+      qr1 = qr;
+      const T nrm = T(c_harm.norm[l * (kMaxL + 1) + m]);
+      const int ip = l * l + l + m;
+      const T R = nrm * q * A;
+      out[ip * stride] = R;
+      if (grad) {
+        const T Rx = nrm * (qr * T(2) * ux * A + q * Ax);
+        const T Ry = nrm * (qr * T(2) * uy * A + q * Ay);
+        const T Rz = nrm * (qz + qr * T(2) * uz) * A;
+        grad[(3 * ip + 0) * stride] = (Rx - T(l) * R * ux) * ir;
+        grad[(3 * ip + 1) * stride] = (Ry - T(l) * R * uy) * ir;
+        grad[(3 * ip + 2) * stride] = (Rz - T(l) * R * uz) * ir;
+      }
+      if (m > 0) {
+        const int im = l * l + l - m;
+        const T S = nrm * q * B;
+        out[im * stride] = S;
+        if (grad) {
+          const T Sx = nrm * (qr * T(2) * ux * B + q * Bx);
+          const T Sy = nrm * (qr * T(2) * uy * B + q * By);
+          const T Sz = nrm * (qz + qr * T(2) * uz) * B;
+          grad[(3 * im + 0) * stride] = (Sx - T(l) * S * ux) * ir;
+          grad[(3 * im + 1) * stride] = (Sy - T(l) * S * uy) * ir;
+          grad[(3 * im + 2) * stride] = (Sz - T(l) * S * uz) * ir;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace fpp

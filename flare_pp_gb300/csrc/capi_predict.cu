@@ -1,0 +1,816 @@
+// C ABI: descriptors, model, predictions.
+#include <cublas_v2.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "b2_kernels.h"
+#include "capi_state.h"
+#include "common.cuh"
+#include "gemm_tc.h"
+#include "internal.h"
+#include "kernel_form.h"
+
+namespace fpp {
+
+static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+#define FPP_CUBLAS(call)                                                     \
+  do {                                                                       \
+    cublasStatus_t _s = (call);                                              \
+    if (_s != CUBLAS_STATUS_SUCCESS)                                         \
+      return fail(FPP_ERR_CUDA, std::string("cuBLAS: ") + #call + " status " + \
+                                    std::to_string((int)_s));                \
+  } while (0)
+
+static int get_cublas(fpp_model *m, cudaStream_t st, cublasHandle_t *out) {
+  if (!m->cublas) {
+    cublasHandle_t h;
+    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS)
+      return fail(FPP_ERR_CUDA, "cublasCreate failed");
+    cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH);
+    m->cublas = h;
+  }
+  cublasHandle_t h = (cublasHandle_t)m->cublas;
+  if (cublasSetStream(h, st) != CUBLAS_STATUS_SUCCESS)
+    return fail(FPP_ERR_CUDA, "cublasSetStream failed");
+  *out = h;
+  return FPP_OK;
+}
+
+static int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st) {
+  if (buf.ptr) return FPP_OK;
+  FPP_TRY(buf.reserve(sizeof(int) * tab.size()));
+  FPP_CUDA(cudaMemcpyAsync(buf.ptr, tab.data(), sizeof(int) * tab.size(),
+                           cudaMemcpyHostToDevice, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  return FPP_OK;
+}
+
+int ensure_layout(fpp_structure *s, int ns, cudaStream_t st) {
+  StructureState &S = s->st;
+  for (int i = 0; i < S.noa; i++)
+    if (S.species_host[i] >= ns)
+      return fail(FPP_ERR_INVALID, "structure species exceeds the descriptor's n_species");
+  if (s->layout_species == ns && s->row_of_atom.ptr) return FPP_OK;
+  s->n_rows.assign(ns, 0);
+  s->row_off.assign(ns, 0);
+  for (int i = 0; i < S.noa; i++) s->n_rows[S.species_host[i]]++;
+  int r = 0;
+  for (int k = 0; k < ns; k++) {
+    s->row_off[k] = r;
+    r += round_up(std::max(s->n_rows[k], 1), 128);
+  }
+  s->total_rows = r;
+  std::vector<int> roa(std::max(S.noa, 1), 0), cnt(ns, 0);
+  for (int i = 0; i < S.noa; i++) {
+    int sp = S.species_host[i];
+    roa[i] = s->row_off[sp] + cnt[sp]++;
+  }
+  FPP_TRY(s->row_of_atom.reserve(sizeof(int) * roa.size()));
+  FPP_CUDA(cudaMemcpyAsync(s->row_of_atom.ptr, roa.data(), sizeof(int) * roa.size(),
+                           cudaMemcpyHostToDevice, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  s->layout_species = ns;
+  return FPP_OK;
+}
+
+// Reserve a buffer and zero it when it had to grow.
+static int reserve_zero(DevBuf &b, size_t bytes, cudaStream_t st) {
+  bool grow = bytes > b.bytes || !b.ptr;
+  FPP_TRY(b.reserve(bytes));
+  if (grow) FPP_CUDA(cudaMemsetAsync(b.ptr, 0, b.bytes, st));
+  return FPP_OK;
+}
+
+static Neigh neigh_of(StructureState &S) {
+  Neigh nb;
+  nb.offset = S.nbr_offset.as<int>();
+  nb.rel = S.nbr_rel.as<dvec4>();
+  nb.rel32 = S.nbr_rel32.as<float4>();
+  nb.nbr_s = S.nbr_s.as<int>();
+  nb.rev = S.nbr_rev.as<int>();
+  return nb;
+}
+
+// FP64 forward: c64, norm64 (atom order), phat64 rows, optional p64 atom order.
+static int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want_p,
+                     cudaStream_t st) {
+  StructureState &S = s->st;
+  B2Args a = a0;
+  a.noa = S.noa;
+  const int ldp = round_up(a.n_d, 64);
+  const int sb = a.n_species * a.N * a.H;
+  FPP_TRY(ensure_layout(s, a.n_species, st));
+  FPP_TRY(S.c64.reserve(sizeof(double) * std::max(1, S.noa) * sb));
+  FPP_TRY(S.norm64.reserve(sizeof(double) * std::max(1, S.noa)));
+  FPP_TRY(reserve_zero(S.p64, want_p ? sizeof(double) * std::max(1, S.noa) * a.n_d : 8, st));
+  FPP_TRY(reserve_zero(S.V64, sizeof(double) * (size_t)s->total_rows * ldp, st));
+  FPP_TRY(reserve_zero(S.w64, sizeof(double) * (size_t)s->total_rows * ldp, st));
+  FPP_TRY(reserve_zero(S.phat64, sizeof(double) * (size_t)s->total_rows * ldp, st));
+  if (launch_b2_forward<double>(a, neigh_of(S), S.species.as<int>(),
+                                s->row_of_atom.as<int>(), pair_tab, S.c64.as<double>(),
+                                want_p ? S.p64.as<double>() : nullptr,
+                                S.norm64.as<double>(), S.phat64.as<double>(),
+                                nullptr, nullptr, ldp, st) != 0)
+    return fail(FPP_ERR_CUDA, "B2 forward (FP64) launch failed");
+  return FPP_OK;
+}
+
+// Mixed forward: c32, pn64 (atom order), split fp16 phat rows.
+static int forward32(fpp_structure *s, const B2Args &a0, const int *pair_tab,
+                     cudaStream_t st) {
+  StructureState &S = s->st;
+  B2Args a = a0;
+  a.noa = S.noa;
+  const int ldp = round_up(a.n_d, 64);
+  const int sb = a.n_species * a.N * a.H;
+  FPP_TRY(ensure_layout(s, a.n_species, st));
+  FPP_TRY(S.c32.reserve(sizeof(float) * std::max(1, S.noa) * sb));
+  FPP_TRY(S.pn64.reserve(sizeof(double) * std::max(1, S.noa)));
+  FPP_TRY(reserve_zero(S.phat_hi, sizeof(__half) * (size_t)s->total_rows * ldp, st));
+  FPP_TRY(reserve_zero(S.phat_lo, sizeof(__half) * (size_t)s->total_rows * ldp, st));
+  if (launch_b2_forward<float>(a, neigh_of(S), S.species.as<int>(),
+                               s->row_of_atom.as<int>(), pair_tab, S.c32.as<float>(),
+                               nullptr, S.pn64.as<double>(), nullptr,
+                               S.phat_hi.as<__half>(), S.phat_lo.as<__half>(), ldp,
+                               st) != 0)
+    return fail(FPP_ERR_CUDA, "B2 forward (FP32) launch failed");
+  return FPP_OK;
+}
+
+static int finish_outputs(fpp_structure *s, cudaStream_t st, double *energy,
+                          double *forces, double *stress, double *atom_energies,
+                          int on_device) {
+  StructureState &S = s->st;
+  double red[10];
+  FPP_CUDA(cudaMemcpyAsync(red, S.reduce_out.ptr, sizeof(red), cudaMemcpyDeviceToHost, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  FPP_TRY(check_status(S, st, "prediction"));
+  const double vi = 1.0 / S.ci.volume;
+  // -(1/V) sum f_a r_b, order xx xy xz yy yz zz
+  double sv[6] = {-red[1] * vi, -red[2] * vi, -red[3] * vi,
+                  -red[5] * vi, -red[6] * vi, -red[9] * vi};
+  cudaMemcpyKind k = on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+  cudaMemcpyKind kd = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (energy) FPP_CUDA(cudaMemcpyAsync(energy, &red[0], sizeof(double), k, st));
+  if (stress) FPP_CUDA(cudaMemcpyAsync(stress, sv, sizeof(sv), k, st));
+  if (forces && S.noa)
+    FPP_CUDA(cudaMemcpyAsync(forces, S.forces.ptr, sizeof(double) * 3 * S.noa, kd, st));
+  if (atom_energies && S.noa)
+    FPP_CUDA(cudaMemcpyAsync(atom_energies, S.atom_e.ptr, sizeof(double) * S.noa, kd, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  return FPP_OK;
+}
+
+static int adjoint_buffers(StructureState &S, size_t elem) {
+  const size_t np = std::max<int64_t>(S.n_pairs, 1);
+  FPP_TRY(S.atom_e.reserve(sizeof(double) * std::max(1, S.noa)));
+  FPP_TRY(S.pair_f.reserve(elem * 4 * np));
+  FPP_TRY(S.forces.reserve(sizeof(double) * 3 * std::max(1, S.noa)));
+  FPP_TRY(S.atom_vir.reserve(sizeof(double) * 9 * std::max(1, S.noa)));
+  FPP_TRY(S.reduce_out.reserve(sizeof(double) * 16));
+  return FPP_OK;
+}
+
+static int model_check(fpp_model *m, fpp_structure *s) {
+  if (!m || !s) return fail(FPP_ERR_INVALID, "null handle");
+  for (int k = 0; k < m->n_species; k++)
+    if (m->sp[k].n_sparse < 0) return fail(FPP_ERR_INVALID, "sparse set missing");
+  return FPP_OK;
+}
+
+}  // namespace fpp
+
+using namespace fpp;
+
+extern "C" {
+
+int fpp_b2_pair_count(const fpp_b2 *b2, fpp_structure *s, int64_t *n_desc_pairs,
+                      void *stream) {
+  (void)stream;
+  if (!b2 || !s || !n_desc_pairs) return fail(FPP_ERR_INVALID, "null argument");
+  StructureState &S = s->st;
+  const int ns = b2->args.n_species;
+  for (int i = 0; i < S.noa; i++)
+    if (S.species_host[i] >= ns)
+      return fail(FPP_ERR_INVALID, "structure species exceeds the descriptor's n_species");
+  std::vector<int> nbr_i(S.n_pairs), nbr_s(S.n_pairs);
+  std::vector<dvec4> rel(S.n_pairs);
+  FPP_CUDA(cudaDeviceSynchronize());
+  if (S.n_pairs) {
+    FPP_CUDA(cudaMemcpy(nbr_i.data(), S.nbr_i.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(nbr_s.data(), S.nbr_s.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(rel.data(), S.nbr_rel.ptr, sizeof(dvec4) * S.n_pairs, cudaMemcpyDeviceToHost));
+  }
+  int64_t c = 0;
+  for (int64_t p = 0; p < S.n_pairs; p++)
+    if (rel[p].x <= b2->args.cutoffs[S.species_host[nbr_i[p]] * ns + nbr_s[p]]) c++;
+  *n_desc_pairs = c;
+  return FPP_OK;
+}
+
+int fpp_b2_compute(const fpp_b2 *b2c, fpp_structure *s, double *descriptors, double *norms,
+                   int32_t *desc_neighbor_count, int32_t *desc_neighbor_indices,
+                   double *desc_neighbor_coordinates, double *force_dervs,
+                   double *force_dots, void *stream) {
+  if (!b2c || !s) return fail(FPP_ERR_INVALID, "null argument");
+  fpp_b2 *b2 = const_cast<fpp_b2 *>(b2c);
+  cudaStream_t st = (cudaStream_t)stream;
+  StructureState &S = s->st;
+  const B2Args &a = b2->args;
+  FPP_TRY(upload_pair_tab(b2->pair_tab, b2->pair_tab_host, st));
+  FPP_TRY(forward64(s, a, b2->pair_tab.as<int>(), true, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  if (descriptors && S.noa)
+    FPP_CUDA(cudaMemcpy(descriptors, S.p64.ptr, sizeof(double) * S.noa * a.n_d,
+                        cudaMemcpyDeviceToHost));
+  if (norms && S.noa)
+    FPP_CUDA(cudaMemcpy(norms, S.norm64.ptr, sizeof(double) * S.noa, cudaMemcpyDeviceToHost));
+  const bool want_pairs = desc_neighbor_count || desc_neighbor_indices ||
+                          desc_neighbor_coordinates || force_dervs || force_dots;
+  if (!want_pairs) return FPP_OK;
+  const int ns = a.n_species;
+  std::vector<int> off(S.noa + 1, 0), nbr_i(S.n_pairs), nbr_j(S.n_pairs), nbr_s(S.n_pairs);
+  std::vector<dvec4> rel(S.n_pairs);
+  if (S.noa)
+    FPP_CUDA(cudaMemcpy(off.data(), S.nbr_offset.ptr, sizeof(int) * (S.noa + 1),
+                        cudaMemcpyDeviceToHost));
+  if (S.n_pairs) {
+    FPP_CUDA(cudaMemcpy(nbr_i.data(), S.nbr_i.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(nbr_j.data(), S.nbr_j.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(nbr_s.data(), S.nbr_s.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(rel.data(), S.nbr_rel.ptr, sizeof(dvec4) * S.n_pairs, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> plist;
+  for (int i = 0; i < S.noa; i++) {
+    int c = 0;
+    for (int p = off[i]; p < off[i + 1]; p++) {
+      if (rel[p].x <= a.cutoffs[S.species_host[i] * ns + nbr_s[p]]) {
+        if (desc_neighbor_indices) desc_neighbor_indices[plist.size()] = nbr_j[p];
+        if (desc_neighbor_coordinates) {
+          desc_neighbor_coordinates[3 * plist.size() + 0] = rel[p].y;
+          desc_neighbor_coordinates[3 * plist.size() + 1] = rel[p].z;
+          desc_neighbor_coordinates[3 * plist.size() + 2] = rel[p].w;
+        }
+        plist.push_back(p);
+        c++;
+      }
+    }
+    if (desc_neighbor_count) desc_neighbor_count[i] = c;
+  }
+  if ((force_dervs || force_dots) && !plist.empty()) {
+    const int npl = (int)plist.size();
+    DevBuf d_plist, d_dp, d_fd;
+    FPP_TRY(d_plist.reserve(sizeof(int) * npl));
+    FPP_TRY(d_dp.reserve(sizeof(double) * 3 * (size_t)npl * a.n_d));
+    FPP_TRY(d_fd.reserve(sizeof(double) * 3 * npl));
+    FPP_CUDA(cudaMemcpy(d_plist.ptr, plist.data(), sizeof(int) * npl, cudaMemcpyHostToDevice));
+    B2Args aa = a;
+    aa.noa = S.noa;
+    if (launch_b2_dp(aa, npl, d_plist.as<int>(), S.nbr_i.as<int>(), S.nbr_s.as<int>(),
+                     S.nbr_rel.as<dvec4>(), S.species.as<int>(), b2->pair_tab.as<int>(),
+                     S.c64.as<double>(), S.p64.as<double>(), d_dp.as<double>(), a.n_d,
+                     d_fd.as<double>(), st) != 0)
+      return fail(FPP_ERR_CUDA, "stored-derivative kernel launch failed");
+    FPP_CUDA(cudaStreamSynchronize(st));
+    if (force_dervs)
+      FPP_CUDA(cudaMemcpy(force_dervs, d_dp.ptr, sizeof(double) * 3 * (size_t)npl * a.n_d,
+                          cudaMemcpyDeviceToHost));
+    if (force_dots)
+      FPP_CUDA(cudaMemcpy(force_dots, d_fd.ptr, sizeof(double) * 3 * npl,
+                          cudaMemcpyDeviceToHost));
+  }
+  return FPP_OK;
+}
+
+int fpp_model_create(const fpp_b2 *b2, double sigma, double power, fpp_model **out) {
+  if (!b2 || !out) return fail(FPP_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (!std::isfinite(sigma) || !std::isfinite(power))
+    return fail(FPP_ERR_NUMERIC, "sigma and power must be finite");
+  auto *m = new fpp_model();
+  m->args = b2->args;
+  m->pair_tab_host = b2->pair_tab_host;
+  m->sigma = sigma;
+  m->power = power;
+  m->n_species = b2->args.n_species;
+  m->n_d = b2->args.n_d;
+  m->ldb = round_up(m->n_d, 64);
+  m->sp.resize(m->n_species);
+  *out = m;
+  return FPP_OK;
+}
+
+int fpp_model_destroy(fpp_model *m) {
+  if (m && m->cublas) cublasDestroy((cublasHandle_t)m->cublas);
+  delete m;
+  return FPP_OK;
+}
+
+int fpp_model_set_sparse(fpp_model *m, int32_t species, int32_t n_sparse,
+                         const double *descriptors, const double *norms,
+                         const double *alpha) {
+  if (!m) return fail(FPP_ERR_INVALID, "null model");
+  if (species < 0 || species >= m->n_species) return fail(FPP_ERR_INVALID, "bad species");
+  if (n_sparse < 0 || (n_sparse > 0 && (!descriptors || !norms || !alpha)))
+    return fail(FPP_ERR_INVALID, "bad sparse arrays");
+  auto &sp = m->sp[species];
+  const int nd = m->n_d;
+  sp.n_sparse = n_sparse;
+  sp.desc.assign(descriptors, descriptors + (size_t)n_sparse * nd);
+  sp.norms.assign(norms, norms + n_sparse);
+  sp.alpha.assign(alpha, alpha + n_sparse);
+  std::vector<double> dhat((size_t)std::max(n_sparse, 1) * nd, 0.0);
+  for (int k = 0; k < n_sparse; k++)
+    if (norms[k] >= 1e-8)
+      for (int d = 0; d < nd; d++) dhat[(size_t)k * nd + d] = descriptors[(size_t)k * nd + d] / norms[k];
+  const size_t n1 = std::max(n_sparse, 1);
+  FPP_TRY(sp.d_desc.reserve(sizeof(double) * n1 * nd));
+  FPP_TRY(sp.d_dhat.reserve(sizeof(double) * n1 * nd));
+  FPP_TRY(sp.d_norms.reserve(sizeof(double) * n1));
+  FPP_TRY(sp.d_alpha.reserve(sizeof(double) * n1));
+  if (n_sparse) {
+    FPP_CUDA(cudaMemcpy(sp.d_desc.ptr, descriptors, sizeof(double) * n_sparse * nd, cudaMemcpyHostToDevice));
+    FPP_CUDA(cudaMemcpy(sp.d_dhat.ptr, dhat.data(), sizeof(double) * n_sparse * nd, cudaMemcpyHostToDevice));
+    FPP_CUDA(cudaMemcpy(sp.d_norms.ptr, norms, sizeof(double) * n_sparse, cudaMemcpyHostToDevice));
+    // empty sparse environments carry no weight (normalized_dot_product.cpp:157)
+    std::vector<double> aeff(n_sparse);
+    for (int k = 0; k < n_sparse; k++) aeff[k] = norms[k] >= 1e-8 ? alpha[k] : 0.0;
+    FPP_CUDA(cudaMemcpy(sp.d_alpha.ptr, aeff.data(), sizeof(double) * n_sparse, cudaMemcpyHostToDevice));
+  }
+  int off = 0;
+  for (auto &x : m->sp) {
+    x.sparse_offset = off;
+    off += x.n_sparse;
+  }
+  m->n_sparse_total = off;
+  m->beta_power = 0;
+  return FPP_OK;
+}
+
+int fpp_model_set_R_inv(fpp_model *m, int32_t n, const double *R_inv) {
+  if (!m || !R_inv) return fail(FPP_ERR_INVALID, "null argument");
+  if (n != m->n_sparse_total)
+    return fail(FPP_ERR_INVALID, "R_inv size does not match the sparse set");
+  FPP_TRY(m->R_inv.reserve(sizeof(double) * std::max(1, n) * std::max(1, n)));
+  if (n) FPP_CUDA(cudaMemcpy(m->R_inv.ptr, R_inv, sizeof(double) * n * n, cudaMemcpyHostToDevice));
+  m->has_R_inv = true;
+  return FPP_OK;
+}
+
+// dense symmetric beta (host, n_d x n_d) -> device FP64 and split fp16 operands
+static int upload_beta(fpp_model *m, int s, const std::vector<double> &B) {
+  const int nd = m->n_d, ldb = m->ldb;
+  auto &sp = m->sp[s];
+  std::vector<double> pad((size_t)nd * ldb, 0.0);
+  double amax = 0;
+  for (int i = 0; i < nd; i++)
+    for (int j = 0; j < nd; j++) {
+      pad[(size_t)i * ldb + j] = B[(size_t)i * nd + j];
+      amax = std::max(amax, std::fabs(B[(size_t)i * nd + j]));
+    }
+  double scale = 1.0;
+  if (amax > 0) scale = std::ldexp(1.0, (int)std::floor(std::log2(16384.0 / amax)));
+  std::vector<__half> hi(pad.size()), lo(pad.size());
+  for (size_t k = 0; k < pad.size(); k++) {
+    const float x = (float)(pad[k] * scale);
+    const __half h = __float2half_rn(x);
+    const float rem = (float)((pad[k] * scale - (double)__half2float(h)) * 2048.0);
+    hi[k] = h;
+    lo[k] = __float2half_rn(rem);
+  }
+  sp.beta_scale = scale;
+  FPP_TRY(sp.beta64.reserve(sizeof(double) * pad.size()));
+  FPP_TRY(sp.beta_hi.reserve(sizeof(__half) * pad.size()));
+  FPP_TRY(sp.beta_lo.reserve(sizeof(__half) * pad.size()));
+  FPP_CUDA(cudaMemcpy(sp.beta64.ptr, pad.data(), sizeof(double) * pad.size(), cudaMemcpyHostToDevice));
+  FPP_CUDA(cudaMemcpy(sp.beta_hi.ptr, hi.data(), sizeof(__half) * hi.size(), cudaMemcpyHostToDevice));
+  FPP_CUDA(cudaMemcpy(sp.beta_lo.ptr, lo.data(), sizeof(__half) * lo.size(), cudaMemcpyHostToDevice));
+  return FPP_OK;
+}
+
+int fpp_model_compute_beta(fpp_model *m, double *beta_packed, void *stream) {
+  if (!m) return fail(FPP_ERR_INVALID, "null model");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nd = m->n_d, ns = m->n_species;
+  const double sig2 = m->sigma * m->sigma;
+  if (m->power == 1.0) {
+    std::vector<double> b1((size_t)ns * nd, 0.0);
+    for (int s = 0; s < ns; s++) {
+      auto &sp = m->sp[s];
+      for (int k = 0; k < sp.n_sparse; k++) {
+        if (sp.norms[k] < 1e-8) continue;
+        for (int d = 0; d < nd; d++)
+          b1[(size_t)s * nd + d] += sig2 * sp.desc[(size_t)k * nd + d] / sp.norms[k] * sp.alpha[k];
+      }
+    }
+    FPP_TRY(m->beta1.reserve(sizeof(double) * b1.size()));
+    FPP_CUDA(cudaMemcpy(m->beta1.ptr, b1.data(), sizeof(double) * b1.size(), cudaMemcpyHostToDevice));
+    if (beta_packed) std::memcpy(beta_packed, b1.data(), sizeof(double) * b1.size());
+    m->beta_power = 1;
+    return FPP_OK;
+  }
+  if (m->power != 2.0)
+    return fail(FPP_ERR_UNSUPPORTED, "mapped coefficients exist for power 1 and 2 only");
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m, st, &h));
+  const size_t np = (size_t)nd * (nd + 1) / 2;
+  for (int s = 0; s < ns; s++) {
+    auto &sp = m->sp[s];
+    std::vector<double> B((size_t)nd * nd, 0.0);
+    if (sp.n_sparse > 0) {
+      // B = sig2 * Dhat^T diag(alpha) Dhat  (cuBLAS, FP64)
+      DevBuf da, dB;
+      FPP_TRY(da.reserve(sizeof(double) * (size_t)sp.n_sparse * nd));
+      FPP_TRY(dB.reserve(sizeof(double) * (size_t)nd * nd));
+      std::vector<double> dh((size_t)sp.n_sparse * nd, 0.0), ds((size_t)sp.n_sparse * nd, 0.0);
+      for (int k = 0; k < sp.n_sparse; k++) {
+        if (sp.norms[k] < 1e-8) continue;
+        for (int d = 0; d < nd; d++) {
+          const double v = sp.desc[(size_t)k * nd + d] / sp.norms[k];
+          ds[(size_t)k * nd + d] = v * sp.alpha[k] * sig2;
+        }
+      }
+      FPP_CUDA(cudaMemcpy(da.ptr, ds.data(), sizeof(double) * ds.size(), cudaMemcpyHostToDevice));
+      const double one = 1.0, zero = 0.0;
+      FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, nd, nd, sp.n_sparse, &one,
+                             da.as<double>(), nd, sp.d_dhat.as<double>(), nd, &zero,
+                             dB.as<double>(), nd));
+      FPP_CUDA(cudaStreamSynchronize(st));
+      FPP_CUDA(cudaMemcpy(B.data(), dB.ptr, sizeof(double) * B.size(), cudaMemcpyDeviceToHost));
+      // symmetrise the rounding of the two triangles
+      for (int i = 0; i < nd; i++)
+        for (int j = i + 1; j < nd; j++) {
+          const double v = 0.5 * (B[(size_t)i * nd + j] + B[(size_t)j * nd + i]);
+          B[(size_t)i * nd + j] = B[(size_t)j * nd + i] = v;
+        }
+    }
+    FPP_TRY(upload_beta(m, s, B));
+    if (beta_packed) {
+      size_t c = 0;
+      for (int i = 0; i < nd; i++)
+        for (int j = i; j < nd; j++, c++)
+          beta_packed[(size_t)s * np + c] = (i == j ? 1.0 : 2.0) * B[(size_t)i * nd + j];
+    }
+  }
+  m->beta_power = 2;
+  return FPP_OK;
+}
+
+int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed) {
+  if (!m || !beta_packed) return fail(FPP_ERR_INVALID, "null argument");
+  const int nd = m->n_d, ns = m->n_species;
+  if (power == 1) {
+    FPP_TRY(m->beta1.reserve(sizeof(double) * (size_t)ns * nd));
+    FPP_CUDA(cudaMemcpy(m->beta1.ptr, beta_packed, sizeof(double) * (size_t)ns * nd,
+                        cudaMemcpyHostToDevice));
+    m->beta_power = 1;
+    return FPP_OK;
+  }
+  if (power != 2) return fail(FPP_ERR_INVALID, "power must be 1 or 2");
+  const size_t np = (size_t)nd * (nd + 1) / 2;
+  for (int s = 0; s < ns; s++) {
+    std::vector<double> B((size_t)nd * nd, 0.0);
+    size_t c = 0;
+    for (int i = 0; i < nd; i++)
+      for (int j = i; j < nd; j++, c++) {
+        const double v = beta_packed[(size_t)s * np + c];
+        if (i == j)
+          B[(size_t)i * nd + j] = v;
+        else
+          B[(size_t)i * nd + j] = B[(size_t)j * nd + i] = v / 2;
+      }
+    FPP_TRY(upload_beta(m, s, B));
+  }
+  m->beta_power = 2;
+  return FPP_OK;
+}
+
+}  // extern "C"
+
+namespace fpp {
+
+// Forward, contraction and adjoint of the mapped form; leaves atom_e, pair_f
+// and (with gather) forces / reduce_out in the structure workspace.
+int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
+                int strict) {
+  FPP_TRY(model_check(m, s));
+  if (m->beta_power == 0)
+    return fail(FPP_ERR_INVALID, "mapped coefficients not set (fpp_model_compute_beta)");
+  if (precision != FPP_PREC_FP64 && precision != FPP_PREC_MIXED)
+    return fail(FPP_ERR_INVALID, "bad precision");
+  StructureState &S = s->st;
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  const int nd = m->n_d, ldp = round_up(nd, 64);
+  B2Args a = m->args;
+  a.noa = S.noa;
+  a.strict = strict;
+  const bool gather = !strict;
+  AdjArgs g;
+  std::memset(&g, 0, sizeof(g));
+  g.mode = m->beta_power == 2 ? kWFromV2 : kWFromV1;
+  g.strict = strict;
+  g.empty_thresh = 1e-8;
+  g.ldp = ldp;
+  g.ldv = ldp;
+  g.beta1 = m->beta1.as<double>();
+  if (!strict) FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
+  if (precision == FPP_PREC_FP64) {
+    FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+    double *phat = S.phat64.as<double>();
+    if (m->beta_power == 2) {
+      cublasHandle_t h;
+      FPP_TRY(get_cublas(m, st, &h));
+      const double one = 1.0, zero = 0.0;
+      for (int sp = 0; sp < m->n_species; sp++) {
+        if (s->n_rows[sp] == 0) continue;
+        FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nd, s->n_rows[sp], nd, &one,
+                               m->sp[sp].beta64.as<double>(), m->ldb,
+                               phat + (size_t)s->row_off[sp] * ldp, ldp, &zero,
+                               S.V64.as<double>() + (size_t)s->row_off[sp] * ldp, ldp));
+      }
+      g.V64 = S.V64.as<double>();
+    }
+    g.phat64 = phat;
+    FPP_TRY(adjoint_buffers(S, sizeof(double)));
+    if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
+                                  s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
+                                  S.c64.as<double>(), S.norm64.as<double>(),
+                                  S.atom_e.as<double>(), S.pair_f.as<double>(),
+                                  S.forces.as<double>(), S.atom_vir.as<double>(),
+                                  S.reduce_out.as<double>(), gather, st) != 0)
+      return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
+  } else {
+    FPP_TRY(forward32(s, a, m->pair_tab.as<int>(), st));
+    if (m->beta_power == 2) {
+      FPP_TRY(reserve_zero(S.V, sizeof(float) * (size_t)s->total_rows * ldp, st));
+      for (int sp = 0; sp < m->n_species; sp++) {
+        if (s->n_rows[sp] == 0) continue;
+        SplitGemmArgs ga;
+        ga.a_hi = S.phat_hi.as<__half>();
+        ga.a_lo = S.phat_lo.as<__half>();
+        ga.a_rows = s->total_rows;
+        ga.lda = ldp;
+        ga.row0 = s->row_off[sp];
+        ga.b_hi = m->sp[sp].beta_hi.as<__half>();
+        ga.b_lo = m->sp[sp].beta_lo.as<__half>();
+        ga.b_rows = nd;
+        ga.ldb = m->ldb;
+        ga.M = s->n_rows[sp];
+        ga.N = nd;
+        ga.K = nd;
+        ga.out_scale = (float)(1.0 / (16384.0 * m->sp[sp].beta_scale));
+        ga.V = S.V.as<float>() + (size_t)s->row_off[sp] * ldp;
+        ga.ldv = ldp;
+        ga.status = S.status.as<DeviceStatus>();
+        int rc = launch_split_gemm(ga, st);
+        if (rc != 0)
+          return fail(FPP_ERR_CUDA, "split-fp16 contraction launch failed (" +
+                                        std::to_string(rc) + ")");
+      }
+      g.V32 = S.V.as<float>();
+    }
+    g.phat_hi = S.phat_hi.as<__half>();
+    g.phat_lo = S.phat_lo.as<__half>();
+    FPP_TRY(adjoint_buffers(S, sizeof(float)));
+    if (launch_b2_adjoint<float>(a, g, neigh_of(S), S.species.as<int>(),
+                                 s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
+                                 S.c32.as<float>(), S.pn64.as<double>(),
+                                 S.atom_e.as<double>(), S.pair_f.as<float>(),
+                                 S.forces.as<double>(), S.atom_vir.as<double>(),
+                                 S.reduce_out.as<double>(), gather, st) != 0)
+      return fail(FPP_ERR_CUDA, "adjoint (mixed) launch failed");
+  }
+  return FPP_OK;
+}
+
+}  // namespace fpp
+
+extern "C" {
+
+int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision, double *energy,
+                       double *forces, double *stress, double *atom_energies,
+                       int outputs_on_device, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  FPP_TRY(mapped_core(m, s, precision, st, 0));
+  return finish_outputs(s, st, energy, forces, stress, atom_energies, outputs_on_device);
+}
+
+// Full FP64 kernel matrix on the device: K (n_sparse_total x n_out) row-major.
+static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, DevBuf &K) {
+  StructureState &S = s->st;
+  const int nd = m->n_d, ldp = round_up(nd, 64), noa = S.noa;
+  const int n_out = 1 + 3 * noa + 6;
+  const double sig2 = m->sigma * m->sigma;
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  B2Args a = m->args;
+  a.noa = noa;
+  FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), true, st));
+  double *phat = S.phat64.as<double>();
+  FPP_TRY(K.reserve(sizeof(double) * (size_t)std::max(1, m->n_sparse_total) * n_out));
+  FPP_CUDA(cudaMemsetAsync(K.ptr, 0, sizeof(double) * (size_t)m->n_sparse_total * n_out, st));
+  // row-ordered atom norms
+  DevBuf rown;
+  FPP_TRY(rown.reserve(sizeof(double) * std::max(1, s->total_rows)));
+  FPP_CUDA(cudaMemsetAsync(rown.ptr, 0, sizeof(double) * s->total_rows, st));
+  if (launch_gather_rows(noa, s->row_of_atom.as<int>(), S.norm64.as<double>(),
+                         rown.as<double>(), st) != 0)
+    return fail(FPP_ERR_CUDA, "gather launch failed");
+  // neighbor data on the host to form the per-species descriptor pair lists
+  std::vector<int> off(noa + 1, 0), nbr_i(S.n_pairs), nbr_s(S.n_pairs);
+  std::vector<dvec4> rel(S.n_pairs);
+  FPP_CUDA(cudaStreamSynchronize(st));
+  if (noa) FPP_CUDA(cudaMemcpy(off.data(), S.nbr_offset.ptr, sizeof(int) * (noa + 1), cudaMemcpyDeviceToHost));
+  if (S.n_pairs) {
+    FPP_CUDA(cudaMemcpy(nbr_i.data(), S.nbr_i.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(nbr_s.data(), S.nbr_s.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(rel.data(), S.nbr_rel.ptr, sizeof(dvec4) * S.n_pairs, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> local(noa, 0), cnt(m->n_species, 0);
+  for (int i = 0; i < noa; i++) local[i] = cnt[S.species_host[i]]++;
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m, st, &h));
+  const double one = 1.0, zero = 0.0;
+  for (int sp = 0; sp < m->n_species; sp++) {
+    const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
+    if (Ss == 0) continue;
+    double *Kb = K.as<double>() + (size_t)m->sp[sp].sparse_offset * n_out;
+    if (nsa == 0) continue;
+    std::vector<int> plist, qatom, dmap(std::max<int64_t>(S.n_pairs, 1), -1);
+    for (int64_t p = 0; p < S.n_pairs; p++) {
+      const int i = nbr_i[p];
+      if (S.species_host[i] != sp) continue;
+      if (!(rel[p].x <= a.cutoffs[sp * a.n_species + nbr_s[p]])) continue;
+      dmap[p] = (int)plist.size();
+      plist.push_back((int)p);
+      qatom.push_back(local[i]);
+    }
+    const int nq = (int)plist.size();
+    DevBuf d_ndm;
+    FPP_TRY(d_ndm.reserve(sizeof(double) * (size_t)Ss * nsa));
+    const double *Dh = m->sp[sp].d_dhat.as<double>();
+    const double *Ph = phat + (size_t)s->row_off[sp] * ldp;
+    // ndm[k][i] = dhat_k . phat_i  (row-major S x n_s)
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, nsa, Ss, nd, &one, Ph, ldp, Dh, nd,
+                           &zero, d_ndm.as<double>(), nsa));
+    const double *anorm = rown.as<double>() + s->row_off[sp];
+    if (launch_envs_energy(Ss, nsa, d_ndm.as<double>(), nsa, m->sp[sp].d_norms.as<double>(),
+                           anorm, sig2, m->power, Kb, n_out, st) != 0)
+      return fail(FPP_ERR_CUDA, "envs energy launch failed");
+    if (nq == 0) continue;
+    DevBuf d_plist, d_qatom, d_dmap, d_dp, d_sfd, d_fd;
+    FPP_TRY(d_plist.reserve(sizeof(int) * nq));
+    FPP_TRY(d_qatom.reserve(sizeof(int) * nq));
+    FPP_TRY(d_dmap.reserve(sizeof(int) * dmap.size()));
+    FPP_TRY(d_dp.reserve(sizeof(double) * 3 * (size_t)nq * nd));
+    FPP_TRY(d_sfd.reserve(sizeof(double) * 3 * nq));
+    FPP_TRY(d_fd.reserve(sizeof(double) * 3 * (size_t)nq * Ss));
+    FPP_CUDA(cudaMemcpyAsync(d_plist.ptr, plist.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
+    FPP_CUDA(cudaMemcpyAsync(d_qatom.ptr, qatom.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
+    FPP_CUDA(cudaMemcpyAsync(d_dmap.ptr, dmap.data(), sizeof(int) * dmap.size(), cudaMemcpyHostToDevice, st));
+    if (launch_b2_dp(a, nq, d_plist.as<int>(), S.nbr_i.as<int>(), S.nbr_s.as<int>(),
+                     S.nbr_rel.as<dvec4>(), S.species.as<int>(), m->pair_tab.as<int>(),
+                     S.c64.as<double>(), S.p64.as<double>(), d_dp.as<double>(), nd,
+                     d_sfd.as<double>(), st) != 0)
+      return fail(FPP_ERR_CUDA, "stored-derivative kernel launch failed");
+    // fd[k][r] = dhat_k . dp_r  (row-major S x 3nq)
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, 3 * nq, Ss, nd, &one,
+                           d_dp.as<double>(), nd, Dh, nd, &zero, d_fd.as<double>(), 3 * nq));
+    if (launch_envs_fkv(Ss, nq, d_fd.as<double>(), 3 * nq, d_ndm.as<double>(), nsa,
+                        d_qatom.as<int>(), d_sfd.as<double>(),
+                        m->sp[sp].d_norms.as<double>(), anorm, sig2, m->power, st) != 0 ||
+        launch_envs_force(Ss, noa, d_fd.as<double>(), 3 * nq, S.nbr_offset.as<int>(),
+                          S.nbr_rev.as<int>(), d_dmap.as<int>(), Kb, n_out, st) != 0 ||
+        launch_envs_stress(Ss, nq, d_fd.as<double>(), 3 * nq, d_plist.as<int>(),
+                           S.nbr_rel.as<dvec4>(), 1.0 / S.ci.volume, noa, Kb, n_out,
+                           st) != 0)
+      return fail(FPP_ERR_CUDA, "envs assembly launch failed");
+    FPP_CUDA(cudaStreamSynchronize(st));  // scratch buffers are freed at scope exit
+  }
+  return FPP_OK;
+}
+
+int fpp_envs_struc(fpp_model *m, fpp_structure *s, double *kernel_mat, void *stream) {
+  FPP_TRY(model_check(m, s));
+  if (!kernel_mat) return fail(FPP_ERR_INVALID, "null output");
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf K;
+  FPP_TRY(envs_struc_device(m, s, st, K));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  const size_t n = (size_t)m->n_sparse_total * (1 + 3 * s->st.noa + 6);
+  if (n) FPP_CUDA(cudaMemcpy(kernel_mat, K.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return FPP_OK;
+}
+
+int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *variance_efs,
+                void *stream) {
+  FPP_TRY(model_check(m, s));
+  if (!mean_efs) return fail(FPP_ERR_INVALID, "null output");
+  if (m->power < 2.0 - 1e-12) {
+    // the reference's force-force kernel throws for power < 2 with a zero dot
+    // product; the mean needs no such term, so only reject what diverges
+    if (m->power < 1.0) return fail(FPP_ERR_UNSUPPORTED, "power < 1");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  StructureState &S = s->st;
+  const int noa = S.noa, nd = m->n_d, ldp = round_up(nd, 64);
+  const int n_out = 1 + 3 * noa + 6;
+  const int nst = m->n_sparse_total;
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m, st, &h));
+  const double one = 1.0, zero = 0.0;
+  if (variance_efs) {
+    if (!m->has_R_inv) return fail(FPP_ERR_INVALID, "R_inv not set (fpp_model_set_R_inv)");
+    DevBuf K, alpha, mean, V, var;
+    FPP_TRY(envs_struc_device(m, s, st, K));
+    std::vector<double> al(std::max(nst, 1), 0.0);
+    for (auto &x : m->sp)
+      for (int k = 0; k < x.n_sparse; k++) al[x.sparse_offset + k] = x.alpha[k];
+    FPP_TRY(alpha.reserve(sizeof(double) * al.size()));
+    FPP_TRY(mean.reserve(sizeof(double) * n_out));
+    FPP_TRY(V.reserve(sizeof(double) * (size_t)n_out * std::max(nst, 1)));
+    FPP_TRY(var.reserve(sizeof(double) * n_out));
+    FPP_CUDA(cudaMemcpyAsync(alpha.ptr, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st));
+    FPP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, n_out, nst, &one, K.as<double>(), n_out,
+                           alpha.as<double>(), 1, &zero, mean.as<double>(), 1));
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, nst, n_out, nst, &one,
+                           m->R_inv.as<double>(), nst, K.as<double>(), n_out, &zero,
+                           V.as<double>(), nst));
+    if (launch_row_sq(n_out, nst, V.as<double>(), nst, var.as<double>(), st) != 0)
+      return fail(FPP_ERR_CUDA, "variance launch failed");
+    FPP_CUDA(cudaStreamSynchronize(st));
+    FPP_CUDA(cudaMemcpy(mean_efs, mean.ptr, sizeof(double) * n_out, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(variance_efs, var.ptr, sizeof(double) * n_out, cudaMemcpyDeviceToHost));
+    return FPP_OK;
+  }
+  // mean through the adjoint
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  B2Args a = m->args;
+  a.noa = noa;
+  FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+  double *phat = S.phat64.as<double>();
+  DevBuf rown, E, zc, Z, G;
+  FPP_TRY(rown.reserve(sizeof(double) * std::max(1, s->total_rows)));
+  FPP_TRY(E.reserve(sizeof(double) * std::max(1, s->total_rows)));
+  FPP_TRY(zc.reserve(sizeof(double) * std::max(1, s->total_rows)));
+  FPP_CUDA(cudaMemsetAsync(rown.ptr, 0, sizeof(double) * s->total_rows, st));
+  FPP_CUDA(cudaMemsetAsync(E.ptr, 0, sizeof(double) * s->total_rows, st));
+  FPP_CUDA(cudaMemsetAsync(zc.ptr, 0, sizeof(double) * s->total_rows, st));
+  FPP_CUDA(cudaMemsetAsync(S.w64.ptr, 0, sizeof(double) * (size_t)s->total_rows * ldp, st));
+  if (launch_gather_rows(noa, s->row_of_atom.as<int>(), S.norm64.as<double>(),
+                         rown.as<double>(), st) != 0)
+    return fail(FPP_ERR_CUDA, "gather launch failed");
+  FPP_TRY(G.reserve(sizeof(double) * (size_t)s->total_rows * ldp));
+  for (int sp = 0; sp < m->n_species; sp++) {
+    const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
+    if (Ss == 0 || nsa == 0) continue;
+    const size_t r0 = s->row_off[sp];
+    FPP_TRY(Z.reserve(sizeof(double) * (size_t)nsa * Ss));
+    const double *Dh = m->sp[sp].d_dhat.as<double>();
+    // Z[i][k] = phat_i . dhat_k
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one, Dh, nd,
+                           phat + r0 * ldp, ldp, &zero, Z.as<double>(), Ss));
+    if (launch_kernel_c(nsa, Ss, Z.as<double>(), Ss, m->sp[sp].d_alpha.as<double>(),
+                        rown.as<double>() + r0, m->sigma * m->sigma, m->power,
+                        E.as<double>() + r0, zc.as<double>() + r0, st) != 0)
+      return fail(FPP_ERR_CUDA, "kernel-form launch failed");
+    // G[i][d] = sum_k C[i][k] dhat_k[d]
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nd, nsa, Ss, &one, Dh, nd,
+                           Z.as<double>(), Ss, &zero, G.as<double>() + r0 * ldp, ldp));
+    if (launch_kernel_w(nsa, nd, G.as<double>() + r0 * ldp, ldp, phat + r0 * ldp, ldp,
+                        zc.as<double>() + r0, rown.as<double>() + r0,
+                        S.w64.as<double>() + r0 * ldp, ldp, st) != 0)
+      return fail(FPP_ERR_CUDA, "kernel-form launch failed");
+    FPP_CUDA(cudaStreamSynchronize(st));  // Z is reused by the next species
+  }
+  AdjArgs g;
+  std::memset(&g, 0, sizeof(g));
+  g.mode = kWGiven;
+  g.ldp = ldp;
+  g.w_given = S.w64.as<double>();
+  g.e_given = E.as<double>();
+  FPP_TRY(adjoint_buffers(S, sizeof(double)));
+  FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
+  if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
+                                s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
+                                S.c64.as<double>(), S.norm64.as<double>(),
+                                S.atom_e.as<double>(), S.pair_f.as<double>(),
+                                S.forces.as<double>(), S.atom_vir.as<double>(),
+                                S.reduce_out.as<double>(), true, st) != 0)
+    return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
+  double e, stress[6];
+  std::vector<double> F(3 * (size_t)noa);
+  FPP_TRY(finish_outputs(s, st, &e, F.data(), stress, nullptr, 0));
+  mean_efs[0] = e;
+  for (size_t k = 0; k < F.size(); k++) mean_efs[1 + k] = F[k];
+  for (int k = 0; k < 6; k++) mean_efs[1 + 3 * noa + k] = stress[k];
+  return FPP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// Definitions of the opaque C ABI handles.
+#pragma once
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "b2_kernels.h"
+#include "internal.h"
+
+struct fpp_structure {
+  fpp::StructureState st;
+  int version = 0;
+  // species-sorted row layout used by the contraction operands
+  int layout_species = -1;
+  std::vector<int> row_off;     // per species, first row (multiple of 128)
+  std::vector<int> n_rows;      // per species, atom count
+  int total_rows = 0;
+  fpp::DevBuf row_of_atom;      // int32[noa]
+};
+
+struct fpp_b2 {
+  fpp::B2Args args{};
+  double rcut = 0;
+  double max_cutoff = 0;
+  std::vector<int> pair_tab_host;
+  fpp::DevBuf pair_tab;  // uploaded lazily
+};
+
+struct fpp_model {
+  fpp::B2Args args{};
+  std::vector<int> pair_tab_host;
+  fpp::DevBuf pair_tab;
+  double sigma = 1, power = 2;
+  int n_species = 1, n_d = 0;
+  int ldb = 0;                          // padded row length of beta operands
+  struct Species {
+    int n_sparse = 0;
+    int sparse_offset = 0;              // into the stacked alpha / R_inv
+    std::vector<double> desc;           // unnormalised rows (host copy)
+    std::vector<double> norms, alpha;
+    fpp::DevBuf d_desc;                 // double[n_sparse * n_d] unnormalised
+    fpp::DevBuf d_dhat;                 // double[n_sparse * n_d] normalised (0 if empty)
+    fpp::DevBuf d_norms, d_alpha;       // double[n_sparse]
+    fpp::DevBuf beta64;                 // double[n_d * ldb] dense symmetric
+    fpp::DevBuf beta_hi, beta_lo;       // half[n_d_pad * ldb] split operands
+    double beta_scale = 1;              // beta ~ (hi + lo/2048) / beta_scale
+  };
+  std::vector<Species> sp;
+  int beta_power = 0;                   // 0: no mapped coefficients yet
+  fpp::DevBuf beta1;                    // double[n_species * n_d] (power 1)
+  int n_sparse_total = 0;
+  fpp::DevBuf R_inv;                    // double[n * n]
+  bool has_R_inv = false;
+  void *cublas = nullptr;               // cublasHandle_t
+};
+
+namespace fpp {
+int prepare_structure(fpp_structure *s, cudaStream_t stream);
+int ensure_layout(fpp_structure *s, int n_species, cudaStream_t stream);
+int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
+                int strict);
+}  // namespace fpp

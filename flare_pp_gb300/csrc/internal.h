@@ -1,0 +1,108 @@
+// Internal host-side state behind the C ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/flare_pp_gb300.h"
+
+namespace fpp {
+
+// Thread-local error reporting for the C ABI.
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+#define FPP_CUDA(call)                                    \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return ::fpp::cuda_fail(_e, #call); \
+  } while (0)
+#define FPP_TRY(call)                 \
+  do {                                \
+    int _rc = (call);                 \
+    if (_rc != FPP_OK) return _rc;    \
+  } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), bytes(o.bytes) {
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  ~DevBuf();
+  int reserve(size_t n);  // at least n bytes; contents not preserved
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Cell quantities of Structure (structure.cpp:15-35), computed on the host
+// with the oracle's operation order and no contraction.
+struct CellInfo {
+  double cell[9];
+  double ct[9], ct_inv[9], cdot[9], cdot_inv[9];
+  double volume;
+  double height[3];  // distance between opposite faces
+  double single_sweep_cutoff;
+  double cutoff;
+  int sweep;
+  int nb[3];         // neighbor-search bins per lattice direction
+};
+
+int make_cell_info(const double *cell, double cutoff, CellInfo *ci);
+
+struct StructureState {
+  int noa = 0;
+  int n_species_max = 0;
+  CellInfo ci{};
+  std::vector<int32_t> species_host;
+  // atoms
+  DevBuf positions;      // double[noa*3]
+  DevBuf species;        // int32[noa]
+  DevBuf wrapped;        // dvec4[noa] (x, y, z, unused)
+  DevBuf wrapped32;      // float4[noa]
+  DevBuf frac;           // dvec4[noa] wrapped fractional coordinates
+  DevBuf atom_bin;       // int32[noa]
+  DevBuf bin_count;      // int32[n_bins]
+  DevBuf bin_start;      // int32[n_bins + 1]
+  DevBuf bin_cursor;     // int32[n_bins]
+  DevBuf bin_atoms;      // int32[noa]
+  // neighbors (CSR over atoms, reference order)
+  int64_t n_pairs = 0;
+  DevBuf nbr_count;      // int32[noa]
+  DevBuf nbr_offset;     // int32[noa + 1]  (int64 when n_pairs >= 2^31 is rejected)
+  DevBuf nbr_key_tmp;    // int64[n_pairs]
+  DevBuf nbr_key;        // int64[n_pairs]  j * n_shift + shift index
+  DevBuf nbr_i;          // int32[n_pairs]  central atom
+  DevBuf nbr_j;          // int32[n_pairs]  neighbor atom (structure index)
+  DevBuf nbr_s;          // int32[n_pairs]  neighbor species
+  DevBuf nbr_rel;        // dvec4[n_pairs] (r, x, y, z)
+  DevBuf nbr_rel32;      // float4[n_pairs]  (x, y, z, r)
+  DevBuf nbr_rev;        // int32[n_pairs]  index of the reverse pair
+  DevBuf scan_tmp;       // CUB scratch
+  DevBuf status;         // DeviceStatus
+  // descriptor / prediction workspace (sized by the callers)
+  DevBuf c64, p64, norm64;            // FP64 single-bond, B2, norms
+  DevBuf phat64;                      // FP64 normalised B2 rows (species-sorted)
+  DevBuf c32, p32, pn64;              // FP32 single-bond, B2, FP64 norms
+  DevBuf phat_hi, phat_lo;            // split fp16 operands (species-sorted)
+  DevBuf order, order_inv;            // species-sorted atom order
+  DevBuf V, V64;                      // beta p products
+  DevBuf w64;                         // dE/dp (FP64 path)
+  DevBuf pair_f;                      // double3/float per pair force
+  DevBuf atom_e;                      // per-atom energies (double)
+  DevBuf atom_vir;                    // per-atom virial partials (double[6])
+  DevBuf forces;                      // double[noa*3]
+  DevBuf reduce_out;                  // double[16]
+  std::vector<int> species_count;     // per species atom count
+};
+
+int build_neighbors(StructureState &st, cudaStream_t stream);
+int check_status(StructureState &st, cudaStream_t stream, const char *what);
+
+}  // namespace fpp

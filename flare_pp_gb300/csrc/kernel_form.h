@@ -1,0 +1,30 @@
+// Launch interface of the FP64 kernel-form helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace fpp {
+int launch_kernel_c(int rows, int S, double *Z, int ldz, const double *alpha_eff,
+                    const double *rownorm, double sig2, double power, double *E,
+                    double *zc, cudaStream_t st);
+int launch_kernel_w(int rows, int nd, const double *G, int ldg, const double *phat,
+                    int ldp, const double *zc, const double *rownorm, double *w,
+                    int ldw, cudaStream_t st);
+int launch_gather_rows(int noa, const int *row_of_atom, const double *v_atom,
+                       double *v_row, cudaStream_t st);
+int launch_envs_energy(int S, int ns, const double *ndm, int ldn, const double *snorm,
+                       const double *anorm, double sig2, double power, double *K,
+                       int ldk, cudaStream_t st);
+int launch_envs_fkv(int S, int nq, double *fd, int ldf, const double *ndm, int ldn,
+                    const int *q_atom, const double *sfd, const double *snorm,
+                    const double *anorm, double sig2, double power, cudaStream_t st);
+int launch_envs_force(int S, int noa, const double *fkv, int ldf, const int *offset,
+                      const int *rev, const int *dmap, double *K, int ldk,
+                      cudaStream_t st);
+int launch_envs_stress(int S, int nq, const double *fkv, int ldf, const int *q_pair,
+                       const dvec4 *rel, double vol_inv, int noa, double *K, int ldk,
+                       cudaStream_t st);
+int launch_row_sq(int rows, int cols, const double *V, int ldv, double *out,
+                  cudaStream_t st);
+}  // namespace fpp

@@ -1,0 +1,496 @@
+// Periodic neighbor list on the GPU with the reference's exact semantics.
+//
+// The reference (src/flare_pp/structure.cpp:52-118) scans every pair (i, j)
+// and every image shift s in [-sweep, sweep]^3, keeps dist < cutoff &&
+// dist != 0, and orders each atom's list by j, then s1, s2, s3.  Here the
+// same (j, s) pairs are found through bins in fractional coordinates:
+//   1. wrap_bin    wrapped positions (reference formula, exact FP64 order),
+//                  fractional coordinates and a bin per atom
+//   2. bin sort    counting sort of atoms into bins
+//   3. count       warp per atom; candidates from the bins reachable for each
+//                  shift, an FP32 pre-filter with a safety margin, then the
+//                  reference's FP64 distance for the survivors
+//   4. fill        same enumeration, writes the keys j * n_shift + shift
+//   5. sort_geom   per atom, ranks the keys (unique) into reference order and
+//                  recomputes the FP64 geometry of each pair
+//   6. reverse     index of the (j, i, -s) pair for the deterministic force
+//                  gather
+// All FP64 arithmetic that decides membership or is returned uses explicitly
+// rounded operations, so results equal the oracle bit for bit.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <cstdio>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace fpp {
+
+struct CellDev {
+  double cell[9], ct[9], ct_inv[9], cdot[9], cdot_inv[9];
+  float cell32[9];
+  double cutoff;
+  float cutoff_pref;   // FP32 pre-filter radius (cutoff plus margin)
+  double delta[3];     // fractional reach per lattice direction
+  int sweep, ns, n_shift;
+  int nb[3];
+};
+
+static CellDev make_dev(const CellInfo &ci) {
+  CellDev d;
+  for (int k = 0; k < 9; k++) {
+    d.cell[k] = ci.cell[k];
+    d.ct[k] = ci.ct[k];
+    d.ct_inv[k] = ci.ct_inv[k];
+    d.cdot[k] = ci.cdot[k];
+    d.cdot_inv[k] = ci.cdot_inv[k];
+    d.cell32[k] = (float)ci.cell[k];
+  }
+  d.cutoff = ci.cutoff;
+  double cmax = 0;
+  for (int k = 0; k < 9; k++) cmax = fmax(cmax, fabs(ci.cell[k]));
+  double margin = 1e-3 + 1e-5 * (cmax * (2 * ci.sweep + 2) + ci.cutoff);
+  d.cutoff_pref = (float)(ci.cutoff + margin);
+  for (int k = 0; k < 3; k++)
+    d.delta[k] = (ci.cutoff + margin) / ci.height[k] + 1e-9;
+  d.sweep = ci.sweep;
+  d.ns = 2 * ci.sweep + 1;
+  d.n_shift = d.ns * d.ns * d.ns;
+  for (int k = 0; k < 3; k++) d.nb[k] = ci.nb[k];
+  return d;
+}
+
+// (n,3) x (3,3) row with the sum order ((a0 b0 + a1 b1) + a2 b2).
+__device__ __forceinline__ void mm3(const double a[3], const double *m,
+                                    double out[3]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+    out[j] = dadd(dadd(dmul(a[0], m[0 * 3 + j]), dmul(a[1], m[1 * 3 + j])),
+                  dmul(a[2], m[2 * 3 + j]));
+}
+
+// Structure::wrap_positions (structure.cpp:120-133) plus binning.
+__global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
+                           dvec4 *__restrict__ wp, float4 *__restrict__ wp32,
+                           dvec4 *__restrict__ frac, int *__restrict__ atom_bin,
+                           int *__restrict__ bin_count, DeviceStatus *st) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= noa) return;
+  double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+  if (!isfinite(p[0]) || !isfinite(p[1]) || !isfinite(p[2])) {
+    set_status(st, FPP_ERR_NUMERIC, 1, i);
+    p[0] = p[1] = p[2] = 0.0;
+  }
+  double t[3], rel[3], rw[3], w[3];
+  mm3(p, cd.ct, t);
+  mm3(t, cd.cdot_inv, rel);
+#pragma unroll
+  for (int k = 0; k < 3; k++) rw[k] = dsub(rel[k], floor(rel[k]));
+  mm3(rw, cd.cdot, t);
+  mm3(t, cd.ct_inv, w);
+  wp[i] = dvec4{w[0], w[1], w[2], 0.0};
+  wp32[i] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+  frac[i] = dvec4{rw[0], rw[1], rw[2], 0.0};
+  int b[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    int v = (int)floor(rw[k] * cd.nb[k]);
+    b[k] = min(max(v, 0), cd.nb[k] - 1);
+  }
+  int bin = (b[0] * cd.nb[1] + b[1]) * cd.nb[2] + b[2];
+  atom_bin[i] = bin;
+  atomicAdd(&bin_count[bin], 1);
+}
+
+__global__ void k_bin_scatter(int noa, const int *__restrict__ atom_bin,
+                              const int *__restrict__ bin_start,
+                              int *__restrict__ bin_cursor,
+                              int *__restrict__ bin_atoms) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= noa) return;
+  int b = atom_bin[i];
+  int slot = atomicAdd(&bin_cursor[b], 1);
+  bin_atoms[bin_start[b] + slot] = i;
+}
+
+// Exact FP64 image distance of the reference (structure.cpp:69-77):
+// im = ((diff + s1 c0) + s2 c1) + s3 c2, dist = sqrt((x^2 + y^2) + z^2).
+__device__ __forceinline__ double exact_image(const dvec4 &wi, const dvec4 &wj,
+                                              const CellDev &cd, int s1, int s2,
+                                              int s3, double im[3]) {
+  double diff[3] = {dsub(wj.x, wi.x), dsub(wj.y, wi.y), dsub(wj.z, wi.z)};
+  double a = (double)s1, b = (double)s2, c = (double)s3;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double v = dadd(diff[k], dmul(a, cd.cell[0 * 3 + k]));
+    v = dadd(v, dmul(b, cd.cell[1 * 3 + k]));
+    im[k] = dadd(v, dmul(c, cd.cell[2 * 3 + k]));
+  }
+  return __dsqrt_rn(dadd(dadd(dmul(im[0], im[0]), dmul(im[1], im[1])),
+                         dmul(im[2], im[2])));
+}
+
+// Enumerate the candidate (j, s) pairs of atom i; `emit` is called by each
+// lane for each accepted pair.  All lanes of the warp call this together.
+template <typename Emit>
+__device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
+                                                const dvec4 *__restrict__ wp,
+                                                const float4 *__restrict__ wp32,
+                                                const dvec4 *__restrict__ frac,
+                                                const int *__restrict__ bin_start,
+                                                const int *__restrict__ bin_atoms,
+                                                Emit emit) {
+  const int lane = threadIdx.x & 31;
+  const dvec4 wi = wp[i];
+  const float4 pi = wp32[i];
+  const dvec4 fi = frac[i];
+  const double fik[3] = {fi.x, fi.y, fi.z};
+  const float rc2 = cd.cutoff_pref * cd.cutoff_pref;
+  for (int s1 = -cd.sweep; s1 <= cd.sweep; s1++) {
+    for (int s2 = -cd.sweep; s2 <= cd.sweep; s2++) {
+      for (int s3 = -cd.sweep; s3 <= cd.sweep; s3++) {
+        const int sv[3] = {s1, s2, s3};
+        int lo[3], hi[3];
+        bool empty = false;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          double c = fik[k] - (double)sv[k];
+          int l = (int)floor((c - cd.delta[k]) * cd.nb[k]);
+          int h = (int)floor((c + cd.delta[k]) * cd.nb[k]);
+          l = max(l, 0);
+          h = min(h, cd.nb[k] - 1);
+          if (l > h) empty = true;
+          lo[k] = l;
+          hi[k] = h;
+        }
+        if (empty) continue;
+        const int sidx = ((s1 + cd.sweep) * cd.ns + (s2 + cd.sweep)) * cd.ns +
+                         (s3 + cd.sweep);
+        const float sx = s1 * cd.cell32[0] + s2 * cd.cell32[3] + s3 * cd.cell32[6];
+        const float sy = s1 * cd.cell32[1] + s2 * cd.cell32[4] + s3 * cd.cell32[7];
+        const float sz = s1 * cd.cell32[2] + s2 * cd.cell32[5] + s3 * cd.cell32[8];
+        for (int b0 = lo[0]; b0 <= hi[0]; b0++)
+          for (int b1 = lo[1]; b1 <= hi[1]; b1++)
+            for (int b2 = lo[2]; b2 <= hi[2]; b2++) {
+              int bin = (b0 * cd.nb[1] + b1) * cd.nb[2] + b2;
+              int beg = bin_start[bin], end = bin_start[bin + 1];
+              for (int base = beg; base < end; base += 32) {
+                int t = base + lane;
+                bool ok = false;
+                int j = -1;
+                if (t < end) {
+                  j = bin_atoms[t];
+                  float4 pj = wp32[j];
+                  float dx = (pj.x - pi.x) + sx;
+                  float dy = (pj.y - pi.y) + sy;
+                  float dz = (pj.z - pi.z) + sz;
+                  if (dx * dx + dy * dy + dz * dz < rc2) {
+                    double im[3];
+                    double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
+                    ok = (dist < cd.cutoff) && (dist != 0.0);
+                  }
+                }
+                emit(ok, j, sidx);
+              }
+            }
+      }
+    }
+  }
+}
+
+__global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
+                        const float4 *__restrict__ wp32,
+                        const dvec4 *__restrict__ frac,
+                        const int *__restrict__ bin_start,
+                        const int *__restrict__ bin_atoms,
+                        int *__restrict__ count) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= noa) return;
+  int lane = threadIdx.x & 31;
+  int n = 0;
+  enumerate_pairs(i, cd, wp, wp32, frac, bin_start, bin_atoms,
+                  [&](bool ok, int, int) { n += ok ? 1 : 0; });
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if (lane == 0) count[i] = n;
+}
+
+__global__ void k_fill(int noa, CellDev cd, const dvec4 *__restrict__ wp,
+                       const float4 *__restrict__ wp32,
+                       const dvec4 *__restrict__ frac,
+                       const int *__restrict__ bin_start,
+                       const int *__restrict__ bin_atoms,
+                       const int *__restrict__ offset,
+                       long long *__restrict__ keys) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= noa) return;
+  int lane = threadIdx.x & 31;
+  int pos = offset[i];
+  const int n_shift = cd.n_shift;
+  enumerate_pairs(i, cd, wp, wp32, frac, bin_start, bin_atoms,
+                  [&](bool ok, int j, int sidx) {
+                    unsigned m = __ballot_sync(0xffffffffu, ok);
+                    if (ok) {
+                      int r = __popc(m & ((1u << lane) - 1u));
+                      keys[pos + r] = (long long)j * n_shift + sidx;
+                    }
+                    pos += __popc(m);
+                  });
+}
+
+// Rank the unique keys of each atom's segment and write the pair geometry in
+// reference order.
+__global__ void k_sort_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp,
+                            const int *__restrict__ species,
+                            const int *__restrict__ offset,
+                            const long long *__restrict__ keys_tmp,
+                            long long *__restrict__ keys, int *__restrict__ nbr_i,
+                            int *__restrict__ nbr_j, int *__restrict__ nbr_s,
+                            dvec4 *__restrict__ rel, float4 *__restrict__ rel32) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= noa) return;
+  int lane = threadIdx.x & 31;
+  int beg = offset[i], end = offset[i + 1];
+  const dvec4 wi = wp[i];
+  for (int e = beg + lane; e < end; e += 32) {
+    long long key = keys_tmp[e];
+    int rank = 0;
+    for (int f = beg; f < end; f++) rank += (keys_tmp[f] < key) ? 1 : 0;
+    int out = beg + rank;
+    int j = (int)(key / cd.n_shift);
+    int sidx = (int)(key - (long long)j * cd.n_shift);
+    int s3 = sidx % cd.ns - cd.sweep;
+    int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
+    int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
+    double im[3];
+    double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
+    keys[out] = key;
+    nbr_i[out] = i;
+    nbr_j[out] = j;
+    nbr_s[out] = species[j];
+    rel[out] = dvec4{dist, im[0], im[1], im[2]};
+    rel32[out] = make_float4((float)im[0], (float)im[1], (float)im[2], (float)dist);
+  }
+}
+
+// Reverse pair: (i, j, s) -> (j, i, -s), found by binary search in j's list.
+__global__ void k_reverse(long long n_pairs, CellDev cd,
+                          const int *__restrict__ offset,
+                          const long long *__restrict__ keys,
+                          const int *__restrict__ nbr_i,
+                          const int *__restrict__ nbr_j, int *__restrict__ rev,
+                          DeviceStatus *st) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  int i = nbr_i[p], j = nbr_j[p];
+  int sidx = (int)(keys[p] - (long long)j * cd.n_shift);
+  long long want = (long long)i * cd.n_shift + (cd.n_shift - 1 - sidx);
+  int lo = offset[j], hi = offset[j + 1] - 1, found = -1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    long long k = keys[mid];
+    if (k == want) {
+      found = mid;
+      break;
+    }
+    if (k < want)
+      lo = mid + 1;
+    else
+      hi = mid - 1;
+  }
+  if (found < 0) set_status(st, FPP_ERR_NUMERIC, 6, (int)p);
+  rev[p] = found;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+static void inv3(const double a[9], double out[9], double *det_out) {
+  double c00 = a[4] * a[8] - a[5] * a[7];
+  double c01 = a[5] * a[6] - a[3] * a[8];
+  double c02 = a[3] * a[7] - a[4] * a[6];
+  double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  out[0] = c00 / det;
+  out[3] = c01 / det;
+  out[6] = c02 / det;
+  out[1] = (a[2] * a[7] - a[1] * a[8]) / det;
+  out[4] = (a[0] * a[8] - a[2] * a[6]) / det;
+  out[7] = (a[1] * a[6] - a[0] * a[7]) / det;
+  out[2] = (a[1] * a[5] - a[2] * a[4]) / det;
+  out[5] = (a[2] * a[3] - a[0] * a[5]) / det;
+  out[8] = (a[0] * a[4] - a[1] * a[3]) / det;
+  if (det_out) *det_out = det;
+}
+
+static double dot3(const double *a, const double *b) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+
+int make_cell_info(const double *cell, double cutoff, CellInfo *ci) {
+  for (int k = 0; k < 9; k++) {
+    if (!std::isfinite(cell[k])) return fail(FPP_ERR_NUMERIC, "cell is not finite");
+    ci->cell[k] = cell[k];
+  }
+  if (!(cutoff > 0) || !std::isfinite(cutoff))
+    return fail(FPP_ERR_INVALID, "cutoff must be positive and finite");
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) ci->ct[i * 3 + j] = cell[j * 3 + i];
+  double det_ct, det;
+  inv3(ci->ct, ci->ct_inv, &det_ct);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      ci->cdot[i * 3 + j] = (cell[i * 3 + 0] * ci->ct[0 * 3 + j] +
+                             cell[i * 3 + 1] * ci->ct[1 * 3 + j]) +
+                            cell[i * 3 + 2] * ci->ct[2 * 3 + j];
+  inv3(ci->cdot, ci->cdot_inv, nullptr);
+  double tmp[9];
+  inv3(cell, tmp, &det);
+  if (!(std::fabs(det) > 0) || !std::isfinite(det))
+    return fail(FPP_ERR_INVALID, "cell is singular");
+  ci->volume = std::fabs(det);
+  // get_single_sweep_cutoff (structure.cpp:135-165)
+  const double *v1 = cell, *v2 = cell + 3, *v3 = cell + 6;
+  double ab = dot3(v1, v2), ac = dot3(v1, v3), bc = dot3(v2, v3);
+  double a = std::sqrt(dot3(v1, v1)), b = std::sqrt(dot3(v2, v2)),
+         c = std::sqrt(dot3(v3, v3));
+  auto h = [](double x, double cs) { return x * std::sqrt(1 - cs * cs); };
+  double cand[6] = {h(a, ab / (a * b)), h(b, ab / (a * b)), h(a, ac / (a * c)),
+                    h(c, ac / (a * c)), h(b, bc / (b * c)), h(c, bc / (b * c))};
+  double ssc = cand[0];
+  for (int k = 0; k < 6; k++)
+    if (cand[k] < ssc) ssc = cand[k];
+  ci->single_sweep_cutoff = ssc;
+  ci->cutoff = cutoff;
+  double sw = std::ceil(cutoff / ssc);
+  if (!(sw >= 1) || sw > 16)
+    return fail(FPP_ERR_CAPACITY, "cutoff needs more than 16 periodic sweeps");
+  ci->sweep = (int)sw;
+  // face-to-face heights: volume / |a_j x a_k|
+  for (int k = 0; k < 3; k++) {
+    const double *p = cell + 3 * ((k + 1) % 3), *q = cell + 3 * ((k + 2) % 3);
+    double cx = p[1] * q[2] - p[2] * q[1];
+    double cy = p[2] * q[0] - p[0] * q[2];
+    double cz = p[0] * q[1] - p[1] * q[0];
+    ci->height[k] = ci->volume / std::sqrt(cx * cx + cy * cy + cz * cz);
+    int nb = (int)std::floor(ci->height[k] / (cutoff * (1 + 1e-6) + 1e-6));
+    ci->nb[k] = std::min(std::max(nb, 1), 1024);
+  }
+  long long nbins = (long long)ci->nb[0] * ci->nb[1] * ci->nb[2];
+  while (nbins > (1ll << 22)) {
+    for (int k = 0; k < 3; k++) ci->nb[k] = std::max(1, ci->nb[k] / 2);
+    nbins = (long long)ci->nb[0] * ci->nb[1] * ci->nb[2];
+  }
+  return FPP_OK;
+}
+
+int check_status(StructureState &st, cudaStream_t stream, const char *what) {
+  DeviceStatus h{};
+  FPP_CUDA(cudaMemcpyAsync(&h, st.status.ptr, sizeof(h), cudaMemcpyDeviceToHost,
+                           stream));
+  FPP_CUDA(cudaStreamSynchronize(stream));
+  if (h.code != 0) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: device status %d at %d (index %d)", what,
+             h.code, h.where, h.info);
+    return fail(h.code, buf);
+  }
+  return FPP_OK;
+}
+
+int build_neighbors(StructureState &st, cudaStream_t stream) {
+  const int noa = st.noa;
+  CellDev cd = make_dev(st.ci);
+  const int nbins = st.ci.nb[0] * st.ci.nb[1] * st.ci.nb[2];
+  FPP_TRY(st.status.reserve(sizeof(DeviceStatus)));
+  FPP_CUDA(cudaMemsetAsync(st.status.ptr, 0, sizeof(DeviceStatus), stream));
+  FPP_TRY(st.nbr_count.reserve(sizeof(int) * (noa + 1)));
+  FPP_TRY(st.nbr_offset.reserve(sizeof(int) * (noa + 1)));
+  if (noa == 0) {
+    st.n_pairs = 0;
+    FPP_CUDA(cudaMemsetAsync(st.nbr_offset.ptr, 0, sizeof(int), stream));
+    return FPP_OK;
+  }
+  FPP_TRY(st.wrapped.reserve(sizeof(dvec4) * noa));
+  FPP_TRY(st.wrapped32.reserve(sizeof(float4) * noa));
+  FPP_TRY(st.frac.reserve(sizeof(dvec4) * noa));
+  FPP_TRY(st.atom_bin.reserve(sizeof(int) * noa));
+  FPP_TRY(st.bin_atoms.reserve(sizeof(int) * noa));
+  FPP_TRY(st.bin_count.reserve(sizeof(int) * (nbins + 1)));
+  FPP_TRY(st.bin_start.reserve(sizeof(int) * (nbins + 1)));
+  FPP_TRY(st.bin_cursor.reserve(sizeof(int) * nbins));
+  FPP_CUDA(cudaMemsetAsync(st.bin_count.ptr, 0, sizeof(int) * (nbins + 1), stream));
+  FPP_CUDA(cudaMemsetAsync(st.bin_cursor.ptr, 0, sizeof(int) * nbins, stream));
+  DeviceStatus *dst = st.status.as<DeviceStatus>();
+
+  const int tb = 256;
+  k_wrap_bin<<<ceil_div(noa, tb), tb, 0, stream>>>(
+      noa, st.positions.as<double>(), cd, st.wrapped.as<dvec4>(),
+      st.wrapped32.as<float4>(), st.frac.as<dvec4>(), st.atom_bin.as<int>(),
+      st.bin_count.as<int>(), dst);
+  FPP_CUDA(cudaGetLastError());
+
+  size_t tmp_bytes = 0, t2 = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, st.bin_count.as<int>(),
+                                st.bin_start.as<int>(), nbins + 1, stream);
+  cub::DeviceScan::ExclusiveSum(nullptr, t2, st.nbr_count.as<int>(),
+                                st.nbr_offset.as<int>(), noa + 1, stream);
+  FPP_TRY(st.scan_tmp.reserve(std::max(tmp_bytes, t2)));
+  tmp_bytes = st.scan_tmp.bytes;
+  FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
+                                         st.bin_count.as<int>(),
+                                         st.bin_start.as<int>(), nbins + 1, stream));
+  k_bin_scatter<<<ceil_div(noa, tb), tb, 0, stream>>>(
+      noa, st.atom_bin.as<int>(), st.bin_start.as<int>(), st.bin_cursor.as<int>(),
+      st.bin_atoms.as<int>());
+  FPP_CUDA(cudaGetLastError());
+
+  const int wpb = 4;  // warps per block, one atom per warp
+  dim3 grid(ceil_div(noa, wpb)), block(32 * wpb);
+  FPP_CUDA(cudaMemsetAsync(st.nbr_count.as<int>() + noa, 0, sizeof(int), stream));
+  k_count<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
+                                      st.wrapped32.as<float4>(),
+                                      st.frac.as<dvec4>(), st.bin_start.as<int>(),
+                                      st.bin_atoms.as<int>(), st.nbr_count.as<int>());
+  FPP_CUDA(cudaGetLastError());
+  tmp_bytes = st.scan_tmp.bytes;
+  FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
+                                         st.nbr_count.as<int>(),
+                                         st.nbr_offset.as<int>(), noa + 1, stream));
+  int total = 0;
+  FPP_CUDA(cudaMemcpyAsync(&total, st.nbr_offset.as<int>() + noa, sizeof(int),
+                           cudaMemcpyDeviceToHost, stream));
+  FPP_CUDA(cudaStreamSynchronize(stream));
+  FPP_TRY(check_status(st, stream, "neighbor wrap"));
+  if (total < 0) return fail(FPP_ERR_CAPACITY, "more than 2^31 neighbor pairs");
+  st.n_pairs = total;
+  size_t np = (size_t)std::max(total, 1);
+  FPP_TRY(st.nbr_key_tmp.reserve(sizeof(long long) * np));
+  FPP_TRY(st.nbr_key.reserve(sizeof(long long) * np));
+  FPP_TRY(st.nbr_i.reserve(sizeof(int) * np));
+  FPP_TRY(st.nbr_j.reserve(sizeof(int) * np));
+  FPP_TRY(st.nbr_s.reserve(sizeof(int) * np));
+  FPP_TRY(st.nbr_rel.reserve(sizeof(dvec4) * np));
+  FPP_TRY(st.nbr_rel32.reserve(sizeof(float4) * np));
+  FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
+  if (total == 0) return FPP_OK;
+  k_fill<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
+                                     st.wrapped32.as<float4>(), st.frac.as<dvec4>(),
+                                     st.bin_start.as<int>(), st.bin_atoms.as<int>(),
+                                     st.nbr_offset.as<int>(),
+                                     st.nbr_key_tmp.as<long long>());
+  FPP_CUDA(cudaGetLastError());
+  k_sort_geom<<<grid, block, 0, stream>>>(
+      noa, cd, st.wrapped.as<dvec4>(), st.species.as<int>(),
+      st.nbr_offset.as<int>(), st.nbr_key_tmp.as<long long>(),
+      st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_j.as<int>(),
+      st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
+  FPP_CUDA(cudaGetLastError());
+  k_reverse<<<ceil_div(total, tb), tb, 0, stream>>>(
+      total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
+      st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst);
+  FPP_CUDA(cudaGetLastError());
+  return FPP_OK;
+}
+
+}  // namespace fpp

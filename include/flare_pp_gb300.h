@@ -1,0 +1,212 @@
+/*
+ * flare_pp_gb300 -- C ABI of the GB300 (sm_103a) implementation of the
+ * flare++ prediction path: periodic neighbor lists, the B2 descriptor, the
+ * NormalizedDotProduct kernel against a sparse set, SparseGP mean / SOR
+ * variance prediction, and the mapped-beta pair style.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: FPP_OK (0) or a negative
+ *    FPP_ERR_* code; fpp_last_error() gives the message for the calling
+ *    thread.
+ *  - Matrices are row-major.  A cell is 3x3 with the lattice vectors as rows
+ *    (the reference's Structure::cell).  Positions are noa x 3.
+ *  - Pointers documented as "host" are read or written synchronously; the
+ *    ones documented as "device" must be device memory and are used in
+ *    stream order on `stream` (a cudaStream_t passed as void*, NULL for the
+ *    legacy default stream).
+ *  - The library allocates and owns the device memory behind each handle.
+ *  - No entry point is safe to call concurrently on the same handle.
+ *
+ * Each declaration names the reference interface it replaces
+ * (mir-group/flare_pp, paths relative to the project root).
+ */
+#ifndef FLARE_PP_GB300_H
+#define FLARE_PP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPP_VERSION 1
+
+enum fpp_status {
+  FPP_OK = 0,
+  FPP_ERR_INVALID = -1,     /* bad argument: size, pointer, enum value */
+  FPP_ERR_CUDA = -2,        /* a CUDA runtime or library call failed */
+  FPP_ERR_OOM = -3,         /* a device allocation failed */
+  FPP_ERR_TIMEOUT = -4,     /* a device-side wait ran out of its spin budget */
+  FPP_ERR_UNSUPPORTED = -5, /* valid input this library does not implement */
+  FPP_ERR_CAPACITY = -6,    /* input beyond a documented maximum */
+  FPP_ERR_NUMERIC = -7      /* non-finite input, or a zero dot product with
+                               power < 2 in the force-force kernel */
+};
+
+enum fpp_precision {
+  FPP_PREC_FP64 = 0,  /* FP64 descriptors, FP64 contractions (cuBLAS DGEMM) */
+  FPP_PREC_MIXED = 1  /* FP32 descriptors with compensated sums, tcgen05
+                         contraction on split-fp16 operands, FP32 accumulate */
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *fpp_last_error(void);
+/* FPP_VERSION of the loaded library. */
+int fpp_version(void);
+
+/* ------------------------------------------------------------------------
+ * Structure: periodic cell + neighbor list built on the GPU.
+ * Replaces Structure::Structure(cell, species, positions, cutoff, ...)
+ * (src/flare_pp/structure.h:92-97) with compute_neighbors
+ * (src/flare_pp/structure.cpp:52-118), wrap_positions (:120-133) and
+ * get_single_sweep_cutoff (:135-165).  Neighbor counts, order (j ascending,
+ * then image shifts s1, s2, s3 ascending) and FP64 distances are identical
+ * to the reference algorithm.
+ * ---------------------------------------------------------------------- */
+typedef struct fpp_structure fpp_structure;
+
+/* cell: host 9 doubles; species: host noa ints in [0, n_species);
+ * positions: host noa*3 doubles.  Builds the neighbor list (dist < cutoff,
+ * dist != 0).  noa may be 0. */
+int fpp_structure_create(const double *cell, const int32_t *species,
+                         const double *positions, int32_t noa, double cutoff,
+                         void *stream, fpp_structure **out);
+/* New positions for the same cell, species and cutoff; rebuilds the
+ * neighbor list.  positions_on_device != 0 means `positions` is a device
+ * pointer (noa*3 doubles). */
+int fpp_structure_set_positions(fpp_structure *s, const double *positions,
+                                int positions_on_device, void *stream);
+int fpp_structure_destroy(fpp_structure *s);
+/* noa, total neighbors, sweep, volume. */
+int fpp_structure_info(const fpp_structure *s, int32_t *noa,
+                       int64_t *n_neighbors, int32_t *sweep, double *volume);
+/* Host copies of the reference's neighbor attributes (structure.h:12-49);
+ * any pointer may be NULL.  relative_positions is n_neighbors x 4
+ * (r, x, y, z); wrapped_positions is noa x 3. */
+int fpp_structure_get_neighbors(const fpp_structure *s, int32_t *neighbor_count,
+                                int32_t *cumulative_neighbor_count,
+                                int32_t *structure_indices,
+                                int32_t *neighbor_species,
+                                double *relative_positions,
+                                double *wrapped_positions);
+
+/* ------------------------------------------------------------------------
+ * B2 descriptor settings.  Replaces B2::B2(radial_basis, cutoff_function,
+ * radial_hyps, cutoff_hyps, descriptor_settings[, cutoffs])
+ * (src/flare_pp/descriptors/b2.h:34-46, b2.cpp:13-50).
+ * Supported: radial_basis "chebyshev"; cutoff_function "quadratic" or
+ * "cosine".  descriptor_settings = {n_species, N, lmax}, lmax <= 8,
+ * n_species * N <= 64.  cutoffs is n_species x n_species (NULL: every entry
+ * radial_hyps[1]).
+ * ---------------------------------------------------------------------- */
+typedef struct fpp_b2 fpp_b2;
+
+int fpp_b2_create(const char *radial_basis, const char *cutoff_function,
+                  const double *radial_hyps, int32_t n_radial_hyps,
+                  const double *cutoff_hyps, int32_t n_cutoff_hyps,
+                  const int32_t *descriptor_settings, const double *cutoffs,
+                  fpp_b2 **out);
+int fpp_b2_destroy(fpp_b2 *b2);
+/* n_d = n_rad (n_rad + 1) / 2 * (lmax + 1), n_rad = n_species * N. */
+int fpp_b2_n_descriptors(const fpp_b2 *b2, int32_t *n_descriptors);
+
+/* B2::compute_struc (b2.cpp:76-179) on the GPU, in FP64.  Host outputs in
+ * atom order (the caller regroups them by species): descriptors noa x n_d,
+ * norms noa.  With with_derivatives != 0 it also returns the descriptor
+ * neighbor list (pairs with r <= cutoffs[s_i][s_j], b2.cpp:277) and the
+ * stored derivatives of b2.cpp:181-242:
+ *   desc_neighbor_count        noa
+ *   desc_neighbor_indices      n_desc_pairs        (structure index of j)
+ *   desc_neighbor_coordinates  n_desc_pairs x 3
+ *   force_dervs                3 n_desc_pairs x n_d (row 3*pair + comp)
+ *   force_dots                 3 n_desc_pairs
+ * n_desc_pairs is returned first through fpp_b2_pair_count.  Any output
+ * pointer may be NULL. */
+int fpp_b2_pair_count(const fpp_b2 *b2, fpp_structure *s, int64_t *n_desc_pairs,
+                      void *stream);
+int fpp_b2_compute(const fpp_b2 *b2, fpp_structure *s, double *descriptors,
+                   double *norms, int32_t *desc_neighbor_count,
+                   int32_t *desc_neighbor_indices,
+                   double *desc_neighbor_coordinates, double *force_dervs,
+                   double *force_dots, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Model: one NormalizedDotProduct kernel (sigma, power) over B2, with its
+ * sparse set and weights.  Replaces the prediction state of
+ * SparseGP(std::vector<Kernel*>, sigma_e, sigma_f, sigma_s)
+ * (src/flare_pp/bffs/sparse_gp.h:48-49) over NormalizedDotProduct(sigma,
+ * power) (src/flare_pp/kernels/normalized_dot_product.h:11-73).
+ * ---------------------------------------------------------------------- */
+typedef struct fpp_model fpp_model;
+
+int fpp_model_create(const fpp_b2 *b2, double sigma, double power,
+                     fpp_model **out);
+int fpp_model_destroy(fpp_model *m);
+/* Sparse environments of one species, as the rows of
+ * ClusterDescriptor::descriptors[s] (descriptor.h:61-90), their norms and
+ * the matching slice of SparseGP::alpha.  Host arrays. */
+int fpp_model_set_sparse(fpp_model *m, int32_t species, int32_t n_sparse,
+                         const double *descriptors, const double *norms,
+                         const double *alpha);
+/* R_inv of SparseGP::update_matrices_QR (sparse_gp.cpp:604-606), n x n with
+ * n the total sparse count in species order; enables SOR variance. */
+int fpp_model_set_R_inv(fpp_model *m, int32_t n, const double *R_inv);
+/* Mapped coefficients of compute_map_coeff_pow2 / _pow1
+ * (normalized_dot_product.cpp:645-759), computed on the GPU in FP64 from the
+ * sparse set and alpha.  Needed by fpp_predict_mapped / fpp_pair_compute.
+ * beta_packed (host, optional): n_species x n_d (n_d+1)/2 for power 2,
+ * n_species x n_d for power 1, in the reference's packed layout. */
+int fpp_model_compute_beta(fpp_model *m, double *beta_packed, void *stream);
+/* Load mapped coefficients directly, in the potential file's packed layout
+ * (pair_flare.cpp:363-395: off-diagonals stored doubled). */
+int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed);
+
+/* ------------------------------------------------------------------------
+ * Prediction.
+ * ---------------------------------------------------------------------- */
+/* NormalizedDotProduct::envs_struc (normalized_dot_product.cpp:115-210) for
+ * the model's sparse set against the structure, FP64: kernel_mat is host,
+ * n_sparse_total x (1 + 3 noa + 6), row-major. */
+int fpp_envs_struc(fpp_model *m, fpp_structure *s, double *kernel_mat,
+                   void *stream);
+
+/* SparseGP::predict_mean (sparse_gp.cpp:612-628) and, with variance_efs !=
+ * NULL, predict_SOR (:630-649), in the kernel form, FP64.  mean_efs and
+ * variance_efs are host arrays of 1 + 3 noa + 6: energy, forces, stress
+ * (xx, xy, xz, yy, yz, zz). */
+int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs,
+                double *variance_efs, void *stream);
+
+/* Energy, forces and stress of the same model through its mapped
+ * coefficients (the pair style's evaluation, pair_flare.cpp:95-180, on the
+ * periodic structure), in `precision`.  Outputs are host arrays unless
+ * outputs_on_device != 0: energy (1), forces (noa x 3), stress (6, flare
+ * order), atom_energies (noa, optional).  Requires fpp_model_compute_beta
+ * or fpp_model_set_beta. */
+int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
+                       double *energy, double *forces, double *stress,
+                       double *atom_energies, int outputs_on_device,
+                       void *stream);
+
+/* ------------------------------------------------------------------------
+ * PairFLARE::compute(eflag, vflag) (lammps_plugins/pair_flare.cpp:68-184)
+ * with LAMMPS-shaped host arrays: x is nall x 3 (owned then ghost atoms),
+ * type is 1-based (nall), the full neighbor list is given as numneigh[inum]
+ * and the concatenated neighbor indices (local or ghost, into x) in ilist
+ * order.  Forces are ADDED into f (nall x 3); eng_vdwl receives the summed
+ * energy, virial[6] the LAMMPS virial (xx, yy, zz, xy, xz, yz) from
+ * ev_tally_xyz, eatom (optional, nall) the per-atom energies.  Requires
+ * mapped coefficients on the model.
+ * ---------------------------------------------------------------------- */
+int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
+                     const double *x, const int32_t *type, int32_t inum,
+                     const int32_t *ilist, const int32_t *numneigh,
+                     const int32_t *neighbors, int precision, double *f,
+                     double *eng_vdwl, double *virial, double *eatom,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLARE_PP_GB300_H */

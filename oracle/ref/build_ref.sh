@@ -1,0 +1,21 @@
+#!/bin/sh
+# Build oracle/_ref/libflare_ref.so from the reference's own L0 math sources
+# (radial.cpp, cutoffs.cpp, y_grad.cpp), compiled where they lie in the
+# reference tree, plus oracle/ref/ref_shim.cpp.  Only the tiny Eigen stand-in
+# in oracle/ref/stub is added; no reference file is copied or modified.
+# Usage: oracle/ref/build_ref.sh [reference_root]
+set -e
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-/root/reference}"
+SRC="$REF/src/flare_pp"
+OUT="$HERE/../_ref"
+if [ ! -f "$SRC/radial.cpp" ]; then
+  echo "reference sources not found under $REF" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+g++ -O2 -std=c++17 -fPIC -shared -ffp-contract=off \
+  -I"$HERE/stub" -I"$SRC" -I"$SRC/descriptors" \
+  "$SRC/radial.cpp" "$SRC/cutoffs.cpp" "$SRC/y_grad.cpp" \
+  "$HERE/ref_shim.cpp" -o "$OUT/libflare_ref.so"
+echo "built $OUT/libflare_ref.so"

@@ -1,0 +1,108 @@
+"""Shared seeded workloads and oracle-trained models for the tests."""
+import numpy as np
+
+from oracle.b2 import B2 as OB2, ClusterDescriptor as OCD
+from oracle.geometry import Structure as OStructure
+from oracle.kernel import NormalizedDotProduct as ONDP
+from oracle.sparse_gp import SparseGP as OSGP
+from oracle import predict as opred
+from flare_pp_gb300 import synth
+
+
+def settings(n_species, N, lmax, rc, cutoffs=None, cutoff_function="quadratic"):
+    cut = np.full((n_species, n_species), rc) if cutoffs is None else np.asarray(cutoffs)
+    return dict(n_species=n_species, N=N, lmax=lmax, r1=0.0, cutoffs=cut,
+                cutoff_function=cutoff_function)
+
+
+def config1_model(n_frames=5, n_sparse=50, power=2):
+    """FCC Al 108 atoms, 5 LJ-labelled frames, 50 sparse environments:
+    trained with the oracle's SparseGP (E, F, S labels, QR solve)."""
+    rc = 5.0
+    b2 = OB2("chebyshev", "quadratic", [0, rc], [], [1, 8, 3])
+    kern = ONDP(2.0, power)
+    gp = OSGP([kern], 0.001, 0.05, 0.006)
+    rng = np.random.default_rng(101)
+    frames = []
+    for k in range(n_frames):
+        cell, sp, pos = synth.fcc_al_108(101, k)
+        s = OStructure(cell, sp, pos, rc, [b2])
+        e, f, st, _ = synth.lennard_jones(cell, pos)
+        s.energy = np.array([e])
+        s.forces = f.reshape(-1)
+        s.stresses = st
+        gp.add_training_structure(s)
+        frames.append(s)
+    allc = [(k, a) for k in range(n_frames) for a in range(108)]
+    pick = rng.choice(len(allc), n_sparse, replace=False)
+    for k in range(n_frames):
+        atoms = sorted(allc[p][1] for p in pick if allc[p][0] == k)
+        gp.add_specific_environments(frames[k], atoms)
+    gp.update_matrices_QR()
+    return dict(b2=b2, kernel=kern, gp=gp, frames=frames, rc=rc,
+                settings=settings(1, 8, 3, rc))
+
+
+def site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
+                      noise=0.01, seed=0):
+    """Sparse set drawn from the frames' atoms; weights fitted (the
+    reference's QR solve) to Lennard-Jones site energies."""
+    rng = np.random.default_rng(seed)
+    ns = b2.descriptor_settings[0]
+    kern = ONDP(sigma, power)
+    dvs, ys = [], []
+    for (cell, sp, pos) in frames:
+        s = OStructure(cell, sp, pos, b2.cutoffs.max(), [])
+        b2.store_dervs = False
+        dv = b2.compute_struc(s)
+        dvs.append(dv)
+        _, _, _, site = synth.lennard_jones(cell, pos)
+        ys.append(site)
+    sparse = OCD()
+    sparse.initialize_cluster(ns, dvs[0].n_descriptors)
+    for s_ in range(ns):
+        pool = [(f, k) for f, dv in enumerate(dvs) for k in range(dv.n_clusters_by_type[s_])]
+        pick = rng.choice(len(pool), min(n_sparse_per_species, len(pool)), replace=False)
+        by_frame = {}
+        for p in sorted(pick):
+            by_frame.setdefault(pool[p][0], []).append(pool[p][1])
+        for f, ks in by_frame.items():
+            cl = [[] for _ in range(ns)]
+            cl[s_] = ks
+            sparse.add_clusters_by_type(dvs[f], cl)
+    train = OCD()
+    for dv in dvs:
+        train.add_all_clusters(dv)
+    y = np.concatenate([np.concatenate([ys[f][dv.atom_indices[s_]] for f, dv in enumerate(dvs)])
+                        for s_ in range(ns)])
+    Kuu = kern.envs_envs(sparse, sparse)
+    Kuf = kern.envs_envs(sparse, train)
+    n = Kuu.shape[0]
+    L = np.linalg.cholesky(Kuu + 1e-8 * np.eye(n))
+    A = np.vstack([Kuf.T / noise, L.T])
+    b = np.concatenate([y / noise, np.zeros(n)])
+    Q, R = np.linalg.qr(A)
+    import scipy.linalg as sla
+    R_inv = sla.solve_triangular(R, np.eye(n))
+    alpha = R_inv @ (Q.T @ b)
+    return dict(kernel=kern, sparse=sparse, alpha=alpha, R_inv=R_inv, sigma=sigma,
+                power=power)
+
+
+def to_gpu_model(b2_settings_list, oracle_sparse, alpha, sigma, power, R_inv=None,
+                 cutoffs=None):
+    """A GPU SparseGP loaded with the same sparse set and weights."""
+    import flare_pp_gb300 as fg
+    ns, N, lmax, rc = b2_settings_list
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, rc], [], [ns, N, lmax], cutoffs)
+    cd = fg.ClusterDescriptor()
+    cd.initialize_cluster(ns, oracle_sparse.n_descriptors)
+    cd.descriptors = [np.array(d) for d in oracle_sparse.descriptors]
+    cd.descriptor_norms = [np.array(n) for n in oracle_sparse.descriptor_norms]
+    cd.cutoff_values = [np.array(c) for c in oracle_sparse.cutoff_values]
+    cd.n_clusters_by_type = list(oracle_sparse.n_clusters_by_type)
+    cd.cumulative_type_count = list(oracle_sparse.cumulative_type_count)
+    cd.n_clusters = oracle_sparse.n_clusters
+    gp = fg.SparseGP([fg.NormalizedDotProduct(sigma, power)], 0.001, 0.05, 0.006)
+    gp.set_model(b2, cd, alpha, R_inv)
+    return gp, b2

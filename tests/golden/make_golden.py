@@ -1,0 +1,82 @@
+"""Record golden vectors from the reference's own L0 math.
+
+Builds oracle/_ref/libflare_ref.so from the reference sources
+(oracle/ref/build_ref.sh: radial.cpp, cutoffs.cpp, y_grad.cpp compiled where
+they lie) and evaluates:
+  * get_Y (y_grad.cpp:667) up to l = 10 at seeded random vectors,
+  * get_complex_Y (y_grad.cpp:24) up to l = 6,
+  * calculate_radial (radial.cpp:344) with the chebyshev basis and the
+    quadratic and cosine cutoffs (cutoffs.cpp:44-73), N = 12.
+Writes tests/golden/l0_golden.npz.  Run from the repository root:
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def main(ref_root="/root/reference"):
+    subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root],
+                   check=True)
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libflare_ref.so"))
+    D = ctypes.POINTER(ctypes.c_double)
+    cd = ctypes.c_double
+    rng = np.random.default_rng(20261203)
+    out = {}
+    # real harmonics
+    lmax = 10
+    H = (lmax + 1) ** 2
+    vecs = rng.normal(size=(64, 3)) * rng.uniform(0.3, 6.0, size=(64, 1))
+    vecs[0] = [0.0, 0.0, 1.7]        # on the z axis
+    vecs[1] = [2.16, 7.12, -3.14]    # the vector of ctests/test_y_grad.cpp
+    Ys = np.zeros((4, len(vecs), H))
+    for i, v in enumerate(vecs):
+        bufs = [np.zeros(H) for _ in range(4)]
+        lib.ref_get_Y(cd(v[0]), cd(v[1]), cd(v[2]), lmax,
+                      *[b.ctypes.data_as(D) for b in bufs])
+        for k in range(4):
+            Ys[k, i] = bufs[k]
+    out["Y_vecs"] = vecs
+    out["Y"], out["Yx"], out["Yy"], out["Yz"] = Ys
+    # complex harmonics (re, im interleaved)
+    lc = 6
+    Hc = (lc + 1) ** 2
+    Yc = np.zeros((4, len(vecs), 2 * Hc))
+    for i, v in enumerate(vecs):
+        bufs = [np.zeros(2 * Hc) for _ in range(4)]
+        lib.ref_get_complex_Y(cd(v[0]), cd(v[1]), cd(v[2]), lc,
+                              *[b.ctypes.data_as(D) for b in bufs])
+        for k in range(4):
+            Yc[k, i] = bufs[k]
+    out["Yc"], out["Ycx"], out["Ycy"], out["Ycz"] = Yc
+    # radial basis x cutoff
+    N, rc, r1 = 12, 5.5, 0.0
+    dirs = rng.normal(size=(64, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rs = np.concatenate([rng.uniform(0.5, rc, 60), [rc, rc - 1e-9, 1e-3, rc + 0.1]])
+    pts = dirs * rs[:, None]
+    out["rad_pts"] = pts
+    for cut in ("quadratic", "cosine"):
+        G = np.zeros((4, len(pts), N))
+        for i, p in enumerate(pts):
+            bufs = [np.zeros(N) for _ in range(4)]
+            r = float(np.linalg.norm(p))
+            rcv = lib.ref_calculate_radial(b"chebyshev", cut.encode(), cd(p[0]),
+                                           cd(p[1]), cd(p[2]), cd(r), cd(rc), N,
+                                           cd(r1), *[b.ctypes.data_as(D) for b in bufs])
+            assert rcv == 0
+            for k in range(4):
+                G[k, i] = bufs[k]
+        out[f"g_{cut}"] = G
+    out["rad_N"], out["rad_rc"], out["rad_r1"] = N, rc, r1
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "l0_golden.npz"), **out)
+    print("wrote tests/golden/l0_golden.npz")
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])
