@@ -1,0 +1,362 @@
+"""E+F(+stress) throughput of the flare++ prediction path on GB300.
+
+Workload (one step): the 32,768-atom two-species BCC alloy (32x32x16 cells,
+a = 3.0 A, 0.08 A rattle, B2 chebyshev N=12 lmax=4, rc 5.5 A) against a sparse
+GP with 2000 environments per species and power-2 NormalizedDotProduct
+kernel, evaluated through its mapped coefficients (the pair style's form):
+GPU neighbor list, B2 forward pass, split-fp16 tcgen05 contraction, adjoint
+forces / virial.  Each step uses new positions (small seeded displacements).
+
+Contract: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+prints one JSON line.  N > 1 runs as torchrun ranks, one independent replica
+per GPU (the path is not sharded across GPUs); value = atoms/s of all ranks.
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "E+F atoms/s at 32k atoms"
+UNIT = "atoms/s"
+WORKLOAD = "bcc_alloy_32k (32768 atoms, 2 species, B2 N=12 lmax=4, rc 5.5, 2000 sparse/species, power 2)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0,
+                "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per contraction launch from the committed ncu summary."""
+    fn = os.path.join(ROOT, "profiles", "contraction_bcc32k.txt")
+    try:
+        txt = open(fn).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch\s*=\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def build_workload(device):
+    import torch
+    from flare_pp_gb300 import synth, Structure
+    w = synth.bcc_alloy_32k_model(device=device)
+    st = Structure(w["cell"], w["species"], w["positions"], 5.5)
+    return w, st
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from flare_pp_gb300 import _lib
+    from flare_pp_gb300._lib import check, lib, ptr
+    w, st = build_workload(dev)
+    gp = w["gp"]
+    noa = st.noa
+    gp._ensure_mapped()
+    K, W = args.steps, args.warmup
+    rng = np.random.default_rng(1234 + rank)
+    pos0 = np.asarray(w["positions"])
+    disp = [pos0 + rng.normal(scale=0.01, size=pos0.shape) for _ in range(K + W)]
+    dpos = torch.tensor(np.stack(disp), dtype=torch.float64, device=dev)
+    out_e = torch.zeros(1, dtype=torch.float64, device=dev)
+    out_f = torch.zeros((noa, 3), dtype=torch.float64, device=dev)
+    out_s = torch.zeros(6, dtype=torch.float64, device=dev)
+    L = lib()
+    mh, sh = gp._model.handle, st.handle
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def step(k, prec):
+        check(L.fpp_structure_set_positions(sh, dpos[k].data_ptr(), 1, stream))
+        check(L.fpp_predict_mapped(mh, sh, prec, out_e.data_ptr(), out_f.data_ptr(),
+                                   out_s.data_ptr(), None, 1, stream))
+
+    n_pairs = st.n_neighbors
+    # ---- device-resident timing (value) ----
+    for k in range(W):
+        step(k, _lib.FPP_PREC_MIXED)
+    check(L.fpp_structure_set_profiling(sh, 1))
+    stage = np.zeros(4)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for k in range(W, W + K):
+        step(k, _lib.FPP_PREC_MIXED)
+        ms4 = np.zeros(4)
+        check(L.fpp_structure_stage_times(sh, ptr(ms4)))
+        stage += ms4
+    ev1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    check(L.fpp_structure_set_profiling(sh, 0))
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / K
+    value = world * noa * K / (ms_total / 1e3)
+    stage /= K
+    # ---- end-to-end through the public API with host buffers ----
+    pinned = torch.from_numpy(np.stack(disp[:K])).pin_memory()
+    he = np.zeros(1)
+    hf = np.zeros((noa, 3))
+    hs = np.zeros(6)
+    for k in range(min(2, K)):   # warm
+        check(L.fpp_structure_set_positions(sh, pinned[k].data_ptr(), 0, stream))
+        check(L.fpp_predict_mapped(mh, sh, _lib.FPP_PREC_MIXED, ptr(he), ptr(hf), ptr(hs),
+                                   None, 0, stream))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(K):
+        check(L.fpp_structure_set_positions(sh, pinned[k].data_ptr(), 0, stream))
+        check(L.fpp_predict_mapped(mh, sh, _lib.FPP_PREC_MIXED, ptr(he), ptr(hf), ptr(hs),
+                                   None, 0, stream))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * noa * K / e2e_s
+    # ---- plain FP64 GPU form (same path, FP64 everywhere, cuBLAS DGEMM) ----
+    step(0, _lib.FPP_PREC_FP64)
+    torch.cuda.synchronize()
+    k64 = max(1, min(2, K))
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for k in range(k64):
+        step(k, _lib.FPP_PREC_FP64)
+    f1.record()
+    torch.cuda.synchronize()
+    fp64_ms = f0.elapsed_time(f1) / k64
+    e64 = out_e.item()
+    f64_forces = out_f.clone()
+    step(0, _lib.FPP_PREC_MIXED)
+    torch.cuda.synchronize()
+    err_e = abs(out_e.item() - e64) / noa
+    err_f = (out_f - f64_forces).abs().max().item()
+    # ---- roofline of the dominant kernel (the contraction) ----
+    peaks, peak_src = measured_peaks()
+    nd = gp._model.n_descriptors
+    flop = 2.0 * noa * nd * nd            # algorithmic, counted once
+    contract_ms = stage[2]
+    achieved = flop / (contract_ms * 1e-3) / 1e12
+    peak = float(peaks["bf16_tflops"])
+    roof = {"kernel": "k_split_gemm (contraction P.beta, 2 launches/step)",
+            "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
+            "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+            "peak_source": f"{peak_src} bf16 dense burst",
+            "note": "algorithmic 2*n_atoms*n_d^2 FLOP per step; the split-fp16 form "
+                    "issues 3 MMAs per product",
+            "traffic": profiled_traffic()}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(w, seconds=args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16x3/fp32 (descriptors fp32, contraction split-fp16, accumulate fp32)",
+        "data": "synthetic (seeded BCC alloy; model fitted to Lennard-Jones site energies)",
+        "config": {"workload": WORKLOAD, "n_atoms": noa, "n_pairs": int(n_pairs),
+                   "n_descriptors": nd, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (per-step working set ~0.6 GB)"},
+        "stage_ms": {"neighbors": round(stage[0], 4), "descriptors": round(stage[1], 4),
+                     "contraction": round(stage[2], 4), "adjoint": round(stage[3], 4)},
+        "roofline": roof,
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT,
+                "h2d_bytes_per_step": int(noa * 3 * 8),
+                "d2h_bytes_per_step": int(noa * 3 * 8 + 8 + 6 * 8)},
+        "fp64_gpu": {"value": round(world * noa / (fp64_ms / 1e3), 1), "unit": UNIT,
+                     "ms_per_step": round(fp64_ms, 3)},
+        "errors_vs_fp64": {"energy_per_atom_eV": err_e, "force_max_eV_per_A": err_f},
+        "gpu_launches": int(K * launches_per_step(2)),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def launches_per_step(n_species):
+    # neighbors: wrap_bin, bin_scatter, count, fill, sort_geom, reverse (+2 CUB
+    # scans); forward; contraction per species; adjoint, gather, reduce
+    return 6 + 2 + 1 + n_species + 3
+
+
+def cpu_baseline(w, seconds=15.0):
+    """The oracle's C restatement of the pair style (per-atom GEMV form, FP64,
+    OpenMP over atoms) on this host's cores, on a bounded sample of atoms."""
+    from oracle import cfast
+    from oracle import predict as opred
+    import torch
+    gp = w["gp"]
+    nd = gp._model.n_descriptors
+    beta = gp.mapping_coefficients
+    B = opred.unpack_beta(beta, nd)
+    settings = dict(n_species=2, N=12, lmax=4, r1=0.0,
+                    cutoffs=np.full((2, 2), 5.5))
+    threads = cfast.max_threads()
+    noa = len(w["species"])
+    n = 256
+    t0 = time.perf_counter()
+    cfast.beta_form(w["cell"], w["species"], w["positions"], settings, B,
+                    atoms=np.arange(n), n_threads=threads)
+    dt = time.perf_counter() - t0
+    n2 = int(min(noa, max(n, n * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    cfast.beta_form(w["cell"], w["species"], w["positions"], settings, B,
+                    atoms=np.arange(n2), n_threads=threads)
+    dt2 = time.perf_counter() - t0
+    return {"value": round(n2 / dt2, 2), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} of {noa} atoms (E, forces, stress of those atoms), "
+                      f"{dt2:.1f} s"}
+
+
+def run_reference(args):
+    """The reference's CPU algorithm for the path (the oracle port: the
+    reference's own sources need Eigen/nlohmann_json and cannot be built
+    here), all host threads, on a bounded sample of the workload per step."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import torch
+    from oracle import cfast
+    from oracle import predict as opred
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else None
+    w, st = build_workload(dev if dev is not None else "cpu")
+    gp = w["gp"]
+    gp._ensure_mapped()
+    B = opred.unpack_beta(gp.mapping_coefficients, gp._model.n_descriptors)
+    settings = dict(n_species=2, N=12, lmax=4, r1=0.0, cutoffs=np.full((2, 2), 5.5))
+    threads = cfast.max_threads()
+    noa = len(w["species"])
+    sample = min(noa, args.ref_atoms)
+    atoms = np.arange(sample)
+    for _ in range(args.warmup):
+        cfast.beta_form(w["cell"], w["species"], w["positions"], settings, B,
+                        atoms=atoms[: max(64, sample // 8)], n_threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cfast.beta_form(w["cell"], w["species"], w["positions"], settings, B,
+                        atoms=atoms, n_threads=threads)
+    dt = time.perf_counter() - t0
+    value = sample * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic (seeded BCC alloy; model fitted to Lennard-Jones site energies)",
+            "config": {"workload": WORKLOAD, "n_atoms": noa, "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads,
+                             "kind": "port",
+                             "sample": f"{sample} of {noa} atoms per step"},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-atoms", type=int, default=2048)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -87,7 +87,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
              const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
              T *__restrict__ c_out, T *__restrict__ p_out,
              double *__restrict__ norm_out, double *__restrict__ phat64,
-             __half *__restrict__ phat_hi, __half *__restrict__ phat_lo, int ldp) {
+             __half *__restrict__ phat_hi, __half *__restrict__ phat_lo, int ldp,
+             const float *__restrict__ pbar) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
@@ -181,7 +182,7 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   // B2 contraction: p[d] with d = q (lmax+1) + l, pair q = (n1, n2 >= n1)
   const int L1 = a.lmax + 1;
   const int nd = a.n_d;
-  double nsq = 0.0;
+  Acc<T> nacc;
   for (int d = lane; d < nd; d += 32) {
     const int q = d / L1, l = d - q * L1;
     const int pr = pair_tab[q];
@@ -189,10 +190,10 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     const T *c1 = c_s + n1 * H + l * l, *c2 = c_s + n2 * H + l * l;
     T v = T(0);
     for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
-    nsq += double(v) * double(v);
+    nacc.add(v * v);
     if (p_out) p_out[(size_t)atom * nd + d] = v;
   }
-  nsq = warp_sum(nsq);
+  double nsq = warp_sum(double(nacc.s) + double(nacc.c));
   const double nrm = sqrt(nsq);
   if (lane == 0) norm_out[atom] = nrm;
   const int row = row_of_atom[atom];
@@ -206,7 +207,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
     if (phat64) phat64[(size_t)row * ldp + d] = double(v) * inv;
     if (phat_hi) {
-      const float x = float(double(v) * inv) * 16384.0f;
+      // centred operand: delta = phat - pbar, scaled by 2^13 (|delta| <= 2)
+      const float x = (float(double(v) * inv) - pbar[(size_t)si * nd + d]) * 8192.0f;
       const __half h = __float2half_rn(x);
       const float rem = (x - __half2float(h)) * 2048.0f;
       phat_hi[(size_t)row * ldp + d] = h;
@@ -248,45 +250,58 @@ k_b2_adjoint(B2Args a, AdjArgs g, const int *__restrict__ offset,
   // ---- w = dE/dp and the atom energy ----
   bool empty;
   double e = 0.0;
-  if (g.mode == kWFromV2 || g.mode == kWFromV1) {
-    empty = g.mode == kWFromV2 ? (nrm * nrm < g.empty_thresh)
-                               : (nrm * nrm < g.empty_thresh);
-    // phat reconstructed from the contraction operands
+  if ((g.mode == kWFromV2 || g.mode == kWFromV1) && g.phat64) {
+    // FP64 form: E = phat . (beta phat) (or phat . beta1), w = dE/dp
+    empty = nrm * nrm < g.empty_thresh;
     double dot = 0.0;
     for (int d = lane; d < nd; d += 32) {
-      double ph, v;
-      if (g.phat64) {
-        ph = g.phat64[(size_t)row * g.ldp + d];
-      } else {
-        ph = (double(__half2float(g.phat_hi[(size_t)row * g.ldp + d])) +
-              double(__half2float(g.phat_lo[(size_t)row * g.ldp + d])) * (1.0 / 2048.0)) *
-             (1.0 / 16384.0);
-      }
-      if (g.mode == kWFromV2)
-        v = g.V64 ? g.V64[(size_t)row * g.ldv + d] : double(g.V32[(size_t)row * g.ldv + d]);
-      else
-        v = g.beta1[(size_t)si * nd + d];
+      const double ph = g.phat64[(size_t)row * g.ldp + d];
+      const double v = g.mode == kWFromV2 ? g.V64[(size_t)row * g.ldv + d]
+                                          : g.beta1[(size_t)si * nd + d];
       dot += ph * v;
     }
     dot = warp_sum(dot);
     e = empty ? 0.0 : dot;
     const double inv = empty ? 0.0 : 1.0 / nrm;
     for (int d = lane; d < nd; d += 32) {
-      double ph, v;
-      if (g.phat64) {
-        ph = g.phat64[(size_t)row * g.ldp + d];
-      } else {
-        ph = (double(__half2float(g.phat_hi[(size_t)row * g.ldp + d])) +
-              double(__half2float(g.phat_lo[(size_t)row * g.ldp + d])) * (1.0 / 2048.0)) *
-             (1.0 / 16384.0);
-      }
-      if (g.mode == kWFromV2) {
-        v = g.V64 ? g.V64[(size_t)row * g.ldv + d] : double(g.V32[(size_t)row * g.ldv + d]);
-        w_s[d] = T(2.0 * (v - e * ph) * inv);
-      } else {
-        v = g.beta1[(size_t)si * nd + d];
-        w_s[d] = T((v - e * ph) * inv);
-      }
+      const double ph = g.phat64[(size_t)row * g.ldp + d];
+      if (g.mode == kWFromV2)
+        w_s[d] = T(2.0 * (g.V64[(size_t)row * g.ldv + d] - e * ph) * inv);
+      else
+        w_s[d] = T((g.beta1[(size_t)si * nd + d] - e * ph) * inv);
+    }
+  } else if (g.mode == kWFromV2 || g.mode == kWFromV1) {
+    // mixed form on the centred operand delta = phat - pbar (float):
+    //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
+    //            g = beta pbar, c0 = pbar^T beta pbar;  dE/dp = 2 (g + V - E phat)/|p|
+    //   power 1: E = phat . beta1,                      dE/dp = (beta1 - E phat)/|p|
+    empty = nrm * nrm < g.empty_thresh;
+    Acc<float> acc;
+    for (int d = lane; d < nd; d += 32) {
+      const size_t o = (size_t)row * g.ldp + d;
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
+                       (1.0f / 8192.0f);
+      const float pb = g.pbar[(size_t)si * nd + d];
+      if (g.mode == kWFromV2)
+        acc.add((2.0f * g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) * dl);
+      else
+        acc.add(float(g.beta1[(size_t)si * nd + d]) * (pb + dl));
+    }
+    const double dot = warp_sum(double(acc.s) + double(acc.c)) +
+                       (g.mode == kWFromV2 ? g.c0[si] : 0.0);
+    e = empty ? 0.0 : dot;
+    const float ef = float(e);
+    const float inv = empty ? 0.0f : float(1.0 / nrm);
+    for (int d = lane; d < nd; d += 32) {
+      const size_t o = (size_t)row * g.ldp + d;
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
+                       (1.0f / 8192.0f);
+      const float ph = g.pbar[(size_t)si * nd + d] + dl;
+      if (g.mode == kWFromV2)
+        w_s[d] = T(2.0f * ((g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) -
+                           ef * ph) * inv);
+      else
+        w_s[d] = T((float(g.beta1[(size_t)si * nd + d]) - ef * ph) * inv);
     }
   } else {  // kWGiven: dE/dp supplied per atom (kernel form)
     empty = false;
@@ -545,7 +560,7 @@ template <typename T>
 int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
                       const int *row_of_atom, const int *pair_tab, T *c_out,
                       T *p_out, double *norm_out, double *phat64, __half *phat_hi,
-                      __half *phat_lo, int ldp, cudaStream_t stream) {
+                      __half *phat_lo, int ldp, const float *pbar, cudaStream_t stream) {
   if (a.noa == 0) return 0;
   a.smem_per_warp = forward_smem_per_warp(a, sizeof(T));
   int wpb = 4;
@@ -558,7 +573,7 @@ int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
     return -1;
   kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
       a, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom, pair_tab,
-      c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp);
+      c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp, pbar);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -592,10 +607,12 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
 
 template int launch_b2_forward<float>(B2Args, const Neigh &, const int *, const int *,
                                       const int *, float *, float *, double *,
-                                      double *, __half *, __half *, int, cudaStream_t);
+                                      double *, __half *, __half *, int, const float *,
+                                      cudaStream_t);
 template int launch_b2_forward<double>(B2Args, const Neigh &, const int *, const int *,
                                        const int *, double *, double *, double *,
-                                       double *, __half *, __half *, int, cudaStream_t);
+                                       double *, __half *, __half *, int, const float *,
+                                       cudaStream_t);
 template int launch_b2_adjoint<float>(B2Args, const AdjArgs &, const Neigh &,
                                       const int *, const int *, const int *,
                                       const float *, const double *, double *,

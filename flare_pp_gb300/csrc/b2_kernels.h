@@ -34,8 +34,11 @@ struct AdjArgs {
   const double *V64;
   int ldv;
   const double *phat64;
-  const __half *phat_hi, *phat_lo;
+  const __half *phat_hi, *phat_lo;  // mixed: centred operand delta = phat - pbar
   int ldp;
+  const float *pbar;                // [n_species][n_d] centre of the mixed operand
+  const float *gvec;                // [n_species][n_d] beta pbar
+  double c0[kMaxSpecies];           // pbar^T beta pbar
   // mapped power 1: beta vector per species [n_species][n_d]
   const double *beta1;
   // given dE/dp and energies per operand row (row stride ldp)
@@ -59,7 +62,7 @@ template <typename T>
 int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
                       const int *row_of_atom, const int *pair_tab, T *c_out,
                       T *p_out, double *norm_out, double *phat64, __half *phat_hi,
-                      __half *phat_lo, int ldp, cudaStream_t stream);
+                      __half *phat_lo, int ldp, const float *pbar, cudaStream_t stream);
 
 template <typename T>
 int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,

@@ -65,7 +65,11 @@ static int ensure_tables(cudaStream_t stream) {
 
 int prepare_structure(fpp_structure *s, cudaStream_t stream) {
   FPP_TRY(ensure_tables(stream));
-  return build_neighbors(s->st, stream);
+  s->st.mark(0, stream);
+  int rc = build_neighbors(s->st, stream);
+  s->st.mark(1, stream);
+  s->st.ev_nb = s->st.profile;
+  return rc;
 }
 
 }  // namespace fpp
@@ -142,6 +146,39 @@ int fpp_structure_set_positions(fpp_structure *s, const double *positions,
                              cs));
   s->version++;
   FPP_TRY(prepare_structure(s, cs));
+  return FPP_OK;
+}
+
+int fpp_structure_set_profiling(fpp_structure *s, int on) {
+  if (!s) return fail(FPP_ERR_INVALID, "null structure");
+  StructureState &S = s->st;
+  if (on && !S.ev[0])
+    for (auto &e : S.ev) FPP_CUDA(cudaEventCreate(&e));
+  S.profile = on != 0;
+  S.ev_nb = S.ev_pred = false;
+  return FPP_OK;
+}
+
+int fpp_structure_stage_times(fpp_structure *s, double *ms4) {
+  if (!s || !ms4) return fail(FPP_ERR_INVALID, "null argument");
+  StructureState &S = s->st;
+  for (int k = 0; k < 4; k++) ms4[k] = 0.0;
+  if (!S.ev[0]) return FPP_OK;
+  float t;
+  if (S.ev_nb) {
+    FPP_CUDA(cudaEventSynchronize(S.ev[1]));
+    FPP_CUDA(cudaEventElapsedTime(&t, S.ev[0], S.ev[1]));
+    ms4[0] = t;
+  }
+  if (S.ev_pred) {
+    FPP_CUDA(cudaEventSynchronize(S.ev[5]));
+    FPP_CUDA(cudaEventElapsedTime(&t, S.ev[2], S.ev[3]));
+    ms4[1] = t;
+    FPP_CUDA(cudaEventElapsedTime(&t, S.ev[3], S.ev[4]));
+    ms4[2] = t;
+    FPP_CUDA(cudaEventElapsedTime(&t, S.ev[4], S.ev[5]));
+    ms4[3] = t;
+  }
   return FPP_OK;
 }
 

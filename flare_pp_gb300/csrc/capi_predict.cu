@@ -19,6 +19,7 @@
 namespace fpp {
 
 static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+static int center_from_sparse(fpp_model *m);
 
 #define FPP_CUBLAS(call)                                                     \
   do {                                                                       \
@@ -117,14 +118,14 @@ static int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bo
                                 s->row_of_atom.as<int>(), pair_tab, S.c64.as<double>(),
                                 want_p ? S.p64.as<double>() : nullptr,
                                 S.norm64.as<double>(), S.phat64.as<double>(),
-                                nullptr, nullptr, ldp, st) != 0)
+                                nullptr, nullptr, ldp, nullptr, st) != 0)
     return fail(FPP_ERR_CUDA, "B2 forward (FP64) launch failed");
   return FPP_OK;
 }
 
 // Mixed forward: c32, pn64 (atom order), split fp16 phat rows.
 static int forward32(fpp_structure *s, const B2Args &a0, const int *pair_tab,
-                     cudaStream_t st) {
+                     const float *pbar, cudaStream_t st) {
   StructureState &S = s->st;
   B2Args a = a0;
   a.noa = S.noa;
@@ -139,7 +140,7 @@ static int forward32(fpp_structure *s, const B2Args &a0, const int *pair_tab,
                                s->row_of_atom.as<int>(), pair_tab, S.c32.as<float>(),
                                nullptr, S.pn64.as<double>(), nullptr,
                                S.phat_hi.as<__half>(), S.phat_lo.as<__half>(), ldp,
-                               st) != 0)
+                               pbar, st) != 0)
     return fail(FPP_ERR_CUDA, "B2 forward (FP32) launch failed");
   return FPP_OK;
 }
@@ -386,6 +387,7 @@ static int upload_beta(fpp_model *m, int s, const std::vector<double> &B) {
     lo[k] = __float2half_rn(rem);
   }
   sp.beta_scale = scale;
+  sp.B_host = B;
   FPP_TRY(sp.beta64.reserve(sizeof(double) * pad.size()));
   FPP_TRY(sp.beta_hi.reserve(sizeof(__half) * pad.size()));
   FPP_TRY(sp.beta_lo.reserve(sizeof(__half) * pad.size()));
@@ -414,7 +416,7 @@ int fpp_model_compute_beta(fpp_model *m, double *beta_packed, void *stream) {
     FPP_CUDA(cudaMemcpy(m->beta1.ptr, b1.data(), sizeof(double) * b1.size(), cudaMemcpyHostToDevice));
     if (beta_packed) std::memcpy(beta_packed, b1.data(), sizeof(double) * b1.size());
     m->beta_power = 1;
-    return FPP_OK;
+    return center_from_sparse(m);
   }
   if (m->power != 2.0)
     return fail(FPP_ERR_UNSUPPORTED, "mapped coefficients exist for power 1 and 2 only");
@@ -460,7 +462,7 @@ int fpp_model_compute_beta(fpp_model *m, double *beta_packed, void *stream) {
     }
   }
   m->beta_power = 2;
-  return FPP_OK;
+  return center_from_sparse(m);
 }
 
 int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed) {
@@ -471,7 +473,7 @@ int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed) {
     FPP_CUDA(cudaMemcpy(m->beta1.ptr, beta_packed, sizeof(double) * (size_t)ns * nd,
                         cudaMemcpyHostToDevice));
     m->beta_power = 1;
-    return FPP_OK;
+    return center_from_sparse(m);
   }
   if (power != 2) return fail(FPP_ERR_INVALID, "power must be 1 or 2");
   const size_t np = (size_t)nd * (nd + 1) / 2;
@@ -489,12 +491,106 @@ int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed) {
     FPP_TRY(upload_beta(m, s, B));
   }
   m->beta_power = 2;
-  return FPP_OK;
+  return center_from_sparse(m);
 }
 
 }  // extern "C"
 
 namespace fpp {
+
+// Centre of the mixed operand for every species: pbar (rounded to FP32, the
+// values the kernels use), g = beta pbar and c0 = pbar^T beta pbar in FP64.
+static int set_center(fpp_model *m, const std::vector<std::vector<double>> &pbar) {
+  const int nd = m->n_d, ns = m->n_species;
+  std::vector<float> pb((size_t)ns * nd, 0.f), gv((size_t)ns * nd, 0.f);
+  m->c0.assign(ns, 0.0);
+  for (int s = 0; s < ns; s++) {
+    std::vector<double> p(nd, 0.0);
+    for (int d = 0; d < nd; d++) {
+      pb[(size_t)s * nd + d] = (float)pbar[s][d];
+      p[d] = (double)pb[(size_t)s * nd + d];
+    }
+    if (m->beta_power == 2 && !m->sp[s].B_host.empty()) {
+      const double *B = m->sp[s].B_host.data();
+      double c0 = 0;
+      for (int a = 0; a < nd; a++) {
+        double acc = 0;
+        for (int b = 0; b < nd; b++) acc += B[(size_t)a * nd + b] * p[b];
+        gv[(size_t)s * nd + a] = (float)acc;
+        c0 += p[a] * acc;
+      }
+      m->c0[s] = c0;
+    }
+  }
+  // g is used in FP32; c0 must then be consistent with the same pbar: the
+  // energy splits as c0 + 2 g.delta + delta.V exactly for any pbar, and the
+  // FP32 rounding of g only enters through delta (small).
+  FPP_TRY(m->pbar32.reserve(sizeof(float) * pb.size()));
+  FPP_TRY(m->g32.reserve(sizeof(float) * gv.size()));
+  FPP_CUDA(cudaMemcpy(m->pbar32.ptr, pb.data(), sizeof(float) * pb.size(), cudaMemcpyHostToDevice));
+  FPP_CUDA(cudaMemcpy(m->g32.ptr, gv.data(), sizeof(float) * gv.size(), cudaMemcpyHostToDevice));
+  m->needs_center = false;
+  return FPP_OK;
+}
+
+// pbar from the sparse set: the normalised mean of its unit descriptors.
+static int center_from_sparse(fpp_model *m) {
+  const int nd = m->n_d;
+  std::vector<std::vector<double>> pbar(m->n_species, std::vector<double>(nd, 0.0));
+  bool all = true;
+  for (int s = 0; s < m->n_species; s++) {
+    auto &sp = m->sp[s];
+    if (sp.n_sparse == 0) all = false;
+    for (int k = 0; k < sp.n_sparse; k++) {
+      if (sp.norms[k] < 1e-8) continue;
+      for (int d = 0; d < nd; d++) pbar[s][d] += sp.desc[(size_t)k * nd + d] / sp.norms[k];
+    }
+    double n = 0;
+    for (double v : pbar[s]) n += v * v;
+    n = std::sqrt(n);
+    if (n > 0)
+      for (double &v : pbar[s]) v /= n;
+  }
+  FPP_TRY(set_center(m, pbar));
+  m->needs_center = !all;  // species without sparse environments: calibrate later
+  return FPP_OK;
+}
+
+// pbar from a structure: the normalised mean of its atoms' unit descriptors
+// (FP64 forward pass), for species the sparse set does not cover.
+static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st) {
+  StructureState &S = s->st;
+  const int nd = m->n_d, ldp = round_up(nd, 64);
+  B2Args a = m->args;
+  a.noa = S.noa;
+  a.strict = 0;
+  FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  std::vector<std::vector<double>> pbar(m->n_species, std::vector<double>(nd, 0.0));
+  std::vector<float> old((size_t)m->n_species * nd, 0.f);
+  if (m->pbar32.ptr)
+    FPP_CUDA(cudaMemcpy(old.data(), m->pbar32.ptr, sizeof(float) * old.size(),
+                        cudaMemcpyDeviceToHost));
+  for (int sp = 0; sp < m->n_species; sp++) {
+    double n0 = 0;
+    for (int d = 0; d < nd; d++) {
+      pbar[sp][d] = old[(size_t)sp * nd + d];
+      n0 += pbar[sp][d] * pbar[sp][d];
+    }
+    if (n0 > 0 || s->n_rows[sp] == 0) continue;  // already centred, or no atoms
+    std::vector<double> rows((size_t)s->n_rows[sp] * ldp);
+    FPP_CUDA(cudaMemcpy(rows.data(), S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp,
+                        sizeof(double) * rows.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < s->n_rows[sp]; i++)
+      for (int d = 0; d < nd; d++) pbar[sp][d] += rows[(size_t)i * ldp + d];
+    double n = 0;
+    for (double v : pbar[sp]) n += v * v;
+    n = std::sqrt(n);
+    if (n > 0)
+      for (double &v : pbar[sp]) v /= n;
+  }
+  return set_center(m, pbar);
+}
 
 // Forward, contraction and adjoint of the mapped form; leaves atom_e, pair_f
 // and (with gather) forces / reduce_out in the structure workspace.
@@ -521,8 +617,10 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
   g.ldv = ldp;
   g.beta1 = m->beta1.as<double>();
   if (!strict) FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
+  S.mark(2, st);
   if (precision == FPP_PREC_FP64) {
     FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+    S.mark(3, st);
     double *phat = S.phat64.as<double>();
     if (m->beta_power == 2) {
       cublasHandle_t h;
@@ -537,6 +635,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
       }
       g.V64 = S.V64.as<double>();
     }
+    S.mark(4, st);
     g.phat64 = phat;
     FPP_TRY(adjoint_buffers(S, sizeof(double)));
     if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
@@ -547,7 +646,9 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
                                   S.reduce_out.as<double>(), gather, st) != 0)
       return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
   } else {
-    FPP_TRY(forward32(s, a, m->pair_tab.as<int>(), st));
+    if (m->needs_center) FPP_TRY(center_from_structure(m, s, st));
+    FPP_TRY(forward32(s, a, m->pair_tab.as<int>(), m->pbar32.as<float>(), st));
+    S.mark(3, st);
     if (m->beta_power == 2) {
       FPP_TRY(reserve_zero(S.V, sizeof(float) * (size_t)s->total_rows * ldp, st));
       for (int sp = 0; sp < m->n_species; sp++) {
@@ -565,7 +666,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
         ga.M = s->n_rows[sp];
         ga.N = nd;
         ga.K = nd;
-        ga.out_scale = (float)(1.0 / (16384.0 * m->sp[sp].beta_scale));
+        ga.out_scale = (float)(1.0 / (8192.0 * m->sp[sp].beta_scale));
         ga.V = S.V.as<float>() + (size_t)s->row_off[sp] * ldp;
         ga.ldv = ldp;
         ga.status = S.status.as<DeviceStatus>();
@@ -576,8 +677,12 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
       }
       g.V32 = S.V.as<float>();
     }
+    S.mark(4, st);
     g.phat_hi = S.phat_hi.as<__half>();
     g.phat_lo = S.phat_lo.as<__half>();
+    g.pbar = m->pbar32.as<float>();
+    g.gvec = m->g32.as<float>();
+    for (int k = 0; k < m->n_species; k++) g.c0[k] = m->c0[k];
     FPP_TRY(adjoint_buffers(S, sizeof(float)));
     if (launch_b2_adjoint<float>(a, g, neigh_of(S), S.species.as<int>(),
                                  s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
@@ -587,6 +692,8 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
                                  S.reduce_out.as<double>(), gather, st) != 0)
       return fail(FPP_ERR_CUDA, "adjoint (mixed) launch failed");
   }
+  S.mark(5, st);
+  S.ev_pred = S.profile;
   return FPP_OK;
 }
 

@@ -44,9 +44,15 @@ struct fpp_model {
     fpp::DevBuf beta64;                 // double[n_d * ldb] dense symmetric
     fpp::DevBuf beta_hi, beta_lo;       // half[n_d_pad * ldb] split operands
     double beta_scale = 1;              // beta ~ (hi + lo/2048) / beta_scale
+    std::vector<double> B_host;         // dense beta (n_d x n_d), power 2
   };
   std::vector<Species> sp;
   int beta_power = 0;                   // 0: no mapped coefficients yet
+  // centre of the mixed-precision operand (per species): pbar, beta pbar,
+  // pbar^T beta pbar; calibrated on the first structure when no sparse set
+  fpp::DevBuf pbar32, g32;
+  std::vector<double> c0;
+  bool needs_center = true;
   fpp::DevBuf beta1;                    // double[n_species * n_d] (power 1)
   int n_sparse_total = 0;
   fpp::DevBuf R_inv;                    // double[n * n]

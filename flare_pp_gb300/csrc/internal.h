@@ -100,6 +100,17 @@ struct StructureState {
   DevBuf forces;                      // double[noa*3]
   DevBuf reduce_out;                  // double[16]
   std::vector<int> species_count;     // per species atom count
+  // stage timing (fpp_structure_set_profiling)
+  bool profile = false;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool ev_nb = false, ev_pred = false;  // which stages were recorded last
+  void mark(int k, cudaStream_t s) {
+    if (profile && ev[k]) cudaEventRecord(ev[k], s);
+  }
+  ~StructureState() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
 };
 
 int build_neighbors(StructureState &st, cudaStream_t stream);

@@ -122,3 +122,90 @@ def lennard_jones(cell, positions, eps=0.4, sig=2.6, rc=None):
     S /= vol
     stress = np.array([S[0, 0], S[0, 1], S[0, 2], S[1, 1], S[1, 2], S[2, 2]])
     return site.sum(), F, stress, site
+
+
+# --------------------------------------------------------------------------
+# Model synthesis for the benchmarks: a sparse GP over B2 whose sparse set is
+# drawn from seeded frames and whose weights are the reference's QR solve
+# (sparse_gp.cpp:576-610: LLT(Kuu + 1e-8 I), A = [Kuf^T / noise; L^T],
+# alpha = R^-1 Q^T b) fitted to Lennard-Jones site energies, so that the
+# weights carry the cancellations of a real fit.  Descriptors come from the
+# GPU library in FP64; the dense FP64 algebra runs in torch on the GPU.
+# --------------------------------------------------------------------------
+def fit_site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
+                          noise=0.01, seed=0, device="cuda"):
+    import torch
+    from .api import ClusterDescriptor, Structure
+    rng = np.random.default_rng(seed)
+    ns = b2.descriptor_settings[0]
+    rc = float(np.max(b2.cutoffs))
+    store = b2.store_dervs
+    b2.store_dervs = False
+    dvs, ys = [], []
+    try:
+        for (cell, sp, pos) in frames:
+            s = Structure(cell, sp, pos, rc, [b2])
+            dvs.append(s.descriptors[0])
+            ys.append(lennard_jones(cell, pos)[3])
+    finally:
+        b2.store_dervs = store
+    sparse = ClusterDescriptor()
+    sparse.initialize_cluster(ns, dvs[0].n_descriptors)
+    for s_ in range(ns):
+        pool = [(f, k) for f, dv in enumerate(dvs) for k in range(dv.n_clusters_by_type[s_])]
+        pick = rng.choice(len(pool), min(n_sparse_per_species, len(pool)), replace=False)
+        by_frame = {}
+        for p in sorted(pick):
+            by_frame.setdefault(pool[p][0], []).append(pool[p][1])
+        for f in sorted(by_frame):
+            cl = [[] for _ in range(ns)]
+            cl[s_] = by_frame[f]
+            sparse.add_clusters_by_type(dvs[f], cl)
+    train = ClusterDescriptor()
+    for dv in dvs:
+        train.add_all_clusters(dv)
+    y = np.concatenate([np.concatenate([ys[f][dv.atom_indices[s_]] for f, dv in enumerate(dvs)])
+                        for s_ in range(ns)])
+    dev = torch.device(device)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+
+    def norm_rows(d, n):
+        d, n = t(d), t(n)
+        ok = n >= 1e-8
+        return torch.where(ok[:, None], d / torch.where(ok, n, torch.ones_like(n))[:, None],
+                           torch.zeros_like(d))
+
+    sig2 = sigma * sigma
+    n = sparse.n_clusters
+    Kuu = torch.zeros((n, n), dtype=torch.float64, device=dev)
+    Kuf = torch.zeros((n, train.n_clusters), dtype=torch.float64, device=dev)
+    for s_ in range(ns):
+        a0, a1 = sparse.cumulative_type_count[s_], sparse.cumulative_type_count[s_] + sparse.n_clusters_by_type[s_]
+        b0, b1 = train.cumulative_type_count[s_], train.cumulative_type_count[s_] + train.n_clusters_by_type[s_]
+        dh = norm_rows(sparse.descriptors[s_], sparse.descriptor_norms[s_])
+        ph = norm_rows(train.descriptors[s_], train.descriptor_norms[s_])
+        Kuu[a0:a1, a0:a1] = sig2 * (dh @ dh.T) ** power
+        Kuf[a0:a1, b0:b1] = sig2 * (dh @ ph.T) ** power
+    L = torch.linalg.cholesky(Kuu + 1e-8 * torch.eye(n, dtype=torch.float64, device=dev))
+    A = torch.cat([Kuf.T / noise, L.T], 0)
+    b = torch.cat([t(y) / noise, torch.zeros(n, dtype=torch.float64, device=dev)])
+    Q, R = torch.linalg.qr(A)
+    alpha = torch.linalg.solve_triangular(R, (Q.T @ b)[:, None], upper=True)[:, 0]
+    return dict(sparse=sparse, alpha=alpha.cpu().numpy(), sigma=sigma, power=power,
+                n_train=train.n_clusters)
+
+
+def bcc_alloy_32k_model(seed=303, n_sparse=2000, device="cuda"):
+    """The 32,768-atom two-species BCC workload (32x32x16 cells, a=3.0 A,
+    rattle 0.08 A, rc 5.5 A, chebyshev N=12, lmax=4, quadratic cutoff) and a
+    model with n_sparse environments per species drawn from four
+    16x8x8-cell frames of the same alloy (seeds seed+1..seed+4)."""
+    from .api import B2, NormalizedDotProduct, SparseGP
+    b2 = B2("chebyshev", "quadratic", [0.0, 5.5], [], [2, 12, 4])
+    frames = [bcc_alloy((16, 8, 8), seed + k) for k in range(1, 5)]
+    fit = fit_site_energy_model(b2, frames, n_sparse, sigma=2.0, power=2, seed=seed,
+                                device=device)
+    gp = SparseGP([NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
+    gp.set_model(b2, fit["sparse"], fit["alpha"])
+    cell, sp, pos = bcc_alloy((32, 32, 16), seed)
+    return dict(b2=b2, gp=gp, cell=cell, species=sp, positions=pos, fit=fit)

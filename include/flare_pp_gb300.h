@@ -90,6 +90,14 @@ int fpp_structure_get_neighbors(const fpp_structure *s, int32_t *neighbor_count,
                                 double *relative_positions,
                                 double *wrapped_positions);
 
+/* Stage timing (instrumentation; no counterpart in the reference).  With
+ * profiling on, each prediction on this structure records CUDA events on its
+ * stream around four stages; fpp_structure_stage_times returns the last
+ * call's GPU milliseconds for: neighbor list, descriptor forward pass,
+ * contraction (the GEMMs), adjoint (forces, virial, reductions). */
+int fpp_structure_set_profiling(fpp_structure *s, int on);
+int fpp_structure_stage_times(fpp_structure *s, double *ms4);
+
 /* ------------------------------------------------------------------------
  * B2 descriptor settings.  Replaces B2::B2(radial_basis, cutoff_function,
  * radial_hyps, cutoff_hyps, descriptor_settings[, cutoffs])
