@@ -52,6 +52,7 @@ SIGNATURES = {
     "fpp_model_set_R_inv": (_c_int, [_vp, _i32, _vp]),
     "fpp_model_compute_beta": (_c_int, [_vp, _vp, _vp]),
     "fpp_model_set_beta": (_c_int, [_vp, _i32, _vp]),
+    "fpp_envs_envs": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_envs_struc": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_predict": (_c_int, [_vp, _vp, _vp, _vp, _vp]),
     "fpp_predict_mapped": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),

@@ -191,6 +191,8 @@ class ClusterDescriptor:
     def add_clusters_by_type(self, dv, clusters):
         """descriptor.cpp:104-140."""
         self.initialize_cluster(dv.n_types, dv.n_descriptors)
+        if getattr(dv, "descriptor_calculator", None) is not None:
+            self.descriptor_calculator = dv.descriptor_calculator
         for s in range(self.n_types):
             idx = np.asarray(clusters[s], dtype=np.int64)
             self.descriptors[s] = np.vstack([self.descriptors[s],
@@ -320,23 +322,19 @@ class NormalizedDotProduct:
                                    _stream(stream)))
         return K
 
-    def envs_envs(self, envs1, envs2, hyps=None):
-        """envs_envs (normalized_dot_product.cpp:27-87)."""
-        sig2 = (self.sigma if hyps is None else float(hyps[0])) ** 2
+    def envs_envs(self, envs1, envs2, hyps=None, stream=None):
+        """envs_envs (normalized_dot_product.cpp:27-87), FP64 on the GPU."""
+        sigma = self.sigma if hyps is None else float(hyps[0])
+        b2 = _descriptor_of(envs1) or _descriptor_of(envs2)
+        m1 = _Model(b2, sigma, self.power, envs1)
+        m2 = _Model(b2, sigma, self.power, envs2)
         K = np.zeros((envs1.n_clusters, envs2.n_clusters))
-        for s in range(envs1.n_types):
-            d1, d2 = envs1.descriptors[s], envs2.descriptors[s]
-            n1, n2 = envs1.descriptor_norms[s], envs2.descriptor_norms[s]
-            if len(n1) == 0 or len(n2) == 0:
-                continue
-            ok1, ok2 = n1 >= 1e-8, n2 >= 1e-8
-            h1 = np.where(ok1[:, None], d1 / np.where(ok1, n1, 1)[:, None], 0)
-            h2 = np.where(ok2[:, None], d2 / np.where(ok2, n2, 1)[:, None], 0)
-            v = sig2 * (h1 @ h2.T) ** self.power
-            v = np.where(ok1[:, None] & ok2[None, :], v, 0.0)
-            c1, c2 = envs1.cumulative_type_count[s], envs2.cumulative_type_count[s]
-            K[c1:c1 + len(n1), c2:c2 + len(n2)] += v
+        check(lib().fpp_envs_envs(m1.handle, m2.handle, ptr(K), _stream(stream)))
         return K
+
+
+def _descriptor_of(envs):
+    return getattr(envs, "descriptor_calculator", None)
 
 
 class _Model(_Handle):

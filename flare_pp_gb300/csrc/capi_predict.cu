@@ -803,6 +803,41 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
   return FPP_OK;
 }
 
+int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream) {
+  if (!m1 || !m2 || !kernel_mat) return fail(FPP_ERR_INVALID, "null argument");
+  if (m1->n_d != m2->n_d || m1->n_species != m2->n_species)
+    return fail(FPP_ERR_INVALID, "models differ in descriptor size or species");
+  cudaStream_t st = (cudaStream_t)stream;
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m1, st, &h));
+  const int n1 = m1->n_sparse_total, n2 = m2->n_sparse_total, nd = m1->n_d;
+  DevBuf K, Z, a1, a2;
+  FPP_TRY(K.reserve(sizeof(double) * std::max(1, n1) * std::max(1, n2)));
+  FPP_CUDA(cudaMemsetAsync(K.ptr, 0, sizeof(double) * (size_t)n1 * n2, st));
+  const double one = 1.0, zero = 0.0;
+  for (int s = 0; s < m1->n_species; s++) {
+    const int S1 = m1->sp[s].n_sparse, S2 = m2->sp[s].n_sparse;
+    if (S1 == 0 || S2 == 0) continue;
+    FPP_TRY(Z.reserve(sizeof(double) * (size_t)S1 * S2));
+    // Z[i][j] = dhat1_i . dhat2_j  (row-major S1 x S2)
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, S2, S1, nd, &one,
+                           m2->sp[s].d_dhat.as<double>(), nd, m1->sp[s].d_dhat.as<double>(), nd,
+                           &zero, Z.as<double>(), S2));
+    if (launch_envs_block(S1, S2, Z.as<double>(), m1->sp[s].d_norms.as<double>(),
+                          m2->sp[s].d_norms.as<double>(), m1->sigma * m1->sigma, m1->power,
+                          K.as<double>() + (size_t)m1->sp[s].sparse_offset * n2 +
+                              m2->sp[s].sparse_offset,
+                          n2, st) != 0)
+      return fail(FPP_ERR_CUDA, "envs_envs launch failed");
+    FPP_CUDA(cudaStreamSynchronize(st));
+  }
+  FPP_CUDA(cudaStreamSynchronize(st));
+  if ((size_t)n1 * n2)
+    FPP_CUDA(cudaMemcpy(kernel_mat, K.ptr, sizeof(double) * (size_t)n1 * n2,
+                        cudaMemcpyDeviceToHost));
+  return FPP_OK;
+}
+
 int fpp_envs_struc(fpp_model *m, fpp_structure *s, double *kernel_mat, void *stream) {
   FPP_TRY(model_check(m, s));
   if (!kernel_mat) return fail(FPP_ERR_INVALID, "null output");

@@ -178,6 +178,11 @@ int fpp_model_set_beta(fpp_model *m, int32_t power, const double *beta_packed);
 int fpp_envs_struc(fpp_model *m, fpp_structure *s, double *kernel_mat,
                    void *stream);
 
+/* NormalizedDotProduct::envs_envs (normalized_dot_product.cpp:27-87): the
+ * kernel between the sparse sets of two models over the same descriptor
+ * (m1's sigma and power), FP64; kernel_mat is host, n1 x n2 row-major. */
+int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream);
+
 /* SparseGP::predict_mean (sparse_gp.cpp:612-628) and, with variance_efs !=
  * NULL, predict_SOR (:630-649), in the kernel form, FP64.  mean_efs and
  * variance_efs are host arrays of 1 + 3 noa + 6: energy, forces, stress

@@ -258,3 +258,43 @@ def test_device_errors_are_reported(gpu_lib, c1):
     gs = fg.Structure(cell, sp, pos, 5.0)
     with pytest.raises(FlareGpuError):
         c1["ggp"].predict_mapped(gs, "mixed")
+
+
+def test_autograd_forces_and_stress_finite_differences(gpu_lib, c2):
+    """Forces from the adjoint (torch.autograd) against central differences
+    (h = 1e-4 A) on 20 seeded atoms, and the virial stress against strain
+    differences, in the FP64 form (the mixed form is checked against the
+    FP64 oracle above)."""
+    import torch
+    from flare_pp_gb300.autograd import FlareEnergy, energy_forces_stress
+    gp, gs = c2["ggp"], c2["gs"]
+    pos0 = torch.tensor(gs.positions, dtype=torch.float64, device="cuda")
+    e, F, S = energy_forces_stress(gp, gs, pos0, "fp64")
+    np.testing.assert_allclose(F.cpu().numpy(), c2["ref"]["forces"], rtol=0, atol=1e-8)
+    rng = np.random.default_rng(20)
+    h = 1e-4
+    for a in rng.choice(gs.noa, 20, replace=False):
+        for comp in range(3):
+            pp, pm = pos0.clone(), pos0.clone()
+            pp[a, comp] += h
+            pm[a, comp] -= h
+            ep = FlareEnergy.apply(pp, gp, gs, "fp64").item()
+            em = FlareEnergy.apply(pm, gp, gs, "fp64").item()
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - F[a, comp].item()) < 1e-5 + 1e-6 * abs(fd)
+    # stress = -(1/V) dE/d(strain) with x -> (1 + eps) x and cell -> cell (1 + eps)
+    FlareEnergy.apply(pos0, gp, gs, "fp64")
+    cell0 = np.array(gs.cell)
+    V = abs(np.linalg.det(cell0))
+    idx = {(0, 0): 0, (0, 1): 1, (0, 2): 2, (1, 1): 3, (1, 2): 4, (2, 2): 5}
+    for (i, j), k in idx.items():
+        vals = []
+        for sgn in (1, -1):
+            eps = np.zeros((3, 3))
+            eps[i, j] += sgn * h / 2
+            eps[j, i] += sgn * h / 2
+            Fm = np.eye(3) + eps
+            st = fg.Structure(cell0 @ Fm, gs.species, gs.positions @ Fm, 5.5)
+            vals.append(c2["ggp"].predict_mapped(st, "fp64")[0])
+        fd = -(vals[0] - vals[1]) / (2 * h) / V
+        assert abs(fd - S[k].item()) < 1e-6 + 1e-5 * abs(fd), (i, j, fd, S[k].item())
