@@ -211,6 +211,8 @@ def run_ours(args):
     f1.record()
     torch.cuda.synchronize()
     fp64_ms = f0.elapsed_time(f1) / k64
+    step(0, _lib.FPP_PREC_FP64)
+    torch.cuda.synchronize()
     e64 = out_e.item()
     f64_forces = out_f.clone()
     step(0, _lib.FPP_PREC_MIXED)

@@ -381,9 +381,27 @@ class _Model(_Handle):
 
 
 # --------------------------------------------------------------------------
+def update_matrices_QR(Kuu, Kuf, y, noise_vector, jitter=1e-8, stream=None):
+    """The QR solve of SparseGP::update_matrices_QR (sparse_gp.cpp:576-610),
+    FP64 on the GPU.  Returns alpha, R_inv, L_inv."""
+    Kuu = f64(Kuu)
+    Kuf = f64(Kuf)
+    n = Kuu.shape[0]
+    m = Kuf.shape[1] if Kuf.ndim == 2 else 0
+    y = f64(y)
+    nv = f64(noise_vector)
+    alpha = np.zeros(n)
+    R_inv = np.zeros((n, n))
+    L_inv = np.zeros((n, n))
+    check(lib().fpp_update_matrices_QR(n, m, ptr(Kuu), ptr(Kuf), ptr(y), ptr(nv),
+                                       float(jitter), ptr(alpha), ptr(R_inv),
+                                       ptr(L_inv), _stream(stream)))
+    return alpha, R_inv, L_inv
+
+
 class SparseGP:
-    """Prediction side of SparseGP (sparse_gp.h:12-112) for one
-    NormalizedDotProduct kernel over one B2 descriptor."""
+    """SparseGP (sparse_gp.h:12-112) for one NormalizedDotProduct kernel over
+    one B2 descriptor: training solve and prediction on the GPU."""
 
     def __init__(self, kernels, energy_noise, force_noise, stress_noise):
         self.kernels = list(kernels)
@@ -392,11 +410,94 @@ class SparseGP:
         self.energy_noise = energy_noise
         self.force_noise = force_noise
         self.stress_noise = stress_noise
+        self.Kuu_jitter = 1e-8
         self.sparse_descriptors = []
+        self.sparse_indices = [[]]
+        self.training_structures = []
+        self.training_atom_indices = []
+        self.y = np.zeros(0)
+        self.noise_vector = np.zeros(0)
         self.alpha = None
         self.R_inv = None
         self.Sigma = None
         self._model = None
+        self._mapped = False
+
+    # ---- training (sparse_gp.cpp:135-610) -------------------------------
+    def _sparse(self, structure):
+        if not self.sparse_descriptors:
+            dv = structure.descriptors[0]
+            cd = ClusterDescriptor()
+            cd.initialize_cluster(dv.n_types, dv.n_descriptors)
+            cd.descriptor_calculator = dv.descriptor_calculator
+            self.sparse_descriptors = [cd]
+        return self.sparse_descriptors[0]
+
+    def add_specific_environments(self, structure, atoms):
+        """sparse_gp.cpp:135-183."""
+        sd = self._sparse(structure)
+        dv = structure.descriptors[0]
+        atoms = list(atoms)
+        self.sparse_indices[0].append(atoms)
+        by_type = [[k for k in range(len(dv.atom_indices[t])) for a in atoms
+                    if dv.atom_indices[t][k] == a] for t in range(dv.n_types)]
+        sd.add_clusters_by_type(dv, by_type)
+
+    def add_all_environments(self, structure):
+        """sparse_gp.cpp:305-331."""
+        self._sparse(structure).add_all_clusters(structure.descriptors[0])
+        self.sparse_indices[0].append(list(range(structure.noa)))
+
+    def add_training_structure(self, structure, atom_indices=(-1,)):
+        """sparse_gp.cpp:464-552 (labels energy, forces, stress)."""
+        self._sparse(structure)
+        if atom_indices[0] == -1:
+            atoms = list(range(structure.noa))
+            n_force = len(structure.forces)
+        else:
+            atoms = list(atom_indices)
+            n_force = 3 * len(atoms)
+        n_e, n_s = len(structure.energy), len(structure.stresses)
+        parts = [f64(structure.energy)]
+        if n_force:
+            f = f64(structure.forces).reshape(-1)
+            parts.append(np.concatenate([f[3 * a:3 * a + 3] for a in atoms]))
+        parts.append(f64(structure.stresses))
+        self.y = np.concatenate([self.y] + parts)
+        self.noise_vector = np.concatenate([
+            self.noise_vector, np.full(n_e, 1 / self.energy_noise ** 2),
+            np.full(n_force, 1 / self.force_noise ** 2),
+            np.full(n_s, 1 / self.stress_noise ** 2)])
+        self.training_structures.append(structure)
+        self.training_atom_indices.append(atoms)
+
+    def _kuf_columns(self, structure, atoms):
+        k = self.kernels[0]
+        K = k.envs_struc(self.sparse_descriptors[0], structure.descriptors[0])
+        n = structure.noa
+        cols = []
+        if len(structure.energy):
+            cols.append(K[:, 0:1])
+        if len(structure.forces):
+            for a in atoms:
+                cols.append(K[:, 1 + 3 * a:4 + 3 * a])
+        if len(structure.stresses):
+            cols.append(K[:, 1 + 3 * n:7 + 3 * n])
+        return np.hstack(cols) if cols else np.zeros((K.shape[0], 0))
+
+    def update_matrices_QR(self):
+        """sparse_gp.cpp:576-610: Kuu, Kuf and the QR solve on the GPU."""
+        sd = self.sparse_descriptors[0]
+        k = self.kernels[0]
+        self.Kuu = k.envs_envs(sd, sd)
+        self.Kuf = np.hstack([self._kuf_columns(s, a) for s, a in
+                              zip(self.training_structures, self.training_atom_indices)])
+        self.alpha, self.R_inv, self.L_inv = update_matrices_QR(
+            self.Kuu, self.Kuf, self.y, self.noise_vector, self.Kuu_jitter)
+        self.Sigma = self.R_inv @ self.R_inv.T
+        self.Kuu_inverse = self.L_inv.T @ self.L_inv
+        self.b2 = sd.descriptor_calculator
+        self._model = _Model(self.b2, k.sigma, k.power, sd, self.alpha, self.R_inv)
         self._mapped = False
 
     def set_model(self, b2, sparse_descriptors, alpha, R_inv=None):

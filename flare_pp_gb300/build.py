@@ -1,6 +1,6 @@
 """Build libflare_pp_gb300.so in-tree with nvcc for sm_103a.
 
-Each CUDA translation unit is compiled in parallel, then linked with cuBLAS.  Usage:
+Each CUDA translation unit is compiled in parallel, then linked with cuBLAS and cuSOLVER.  Usage:
 
     python -m flare_pp_gb300.build        # or flare_pp_gb300.build.build()
 """
@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflare_pp_gb300.so")
 SOURCES = ["neighbors.cu", "b2_kernels.cu", "gemm_tc.cu", "kernel_form.cu",
-           "capi_core.cu", "capi_predict.cu", "capi_pair.cu"]
+           "capi_core.cu", "capi_predict.cu", "capi_pair.cu", "capi_solve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
     for d in libdirs:
         if os.path.isdir(d):
             link += ["-L", d]
-    link += ["-lcublas"]
+    link += ["-lcublas", "-lcusolver"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

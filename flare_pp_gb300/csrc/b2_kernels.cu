@@ -37,6 +37,8 @@ int upload_harmonic_tables(cudaStream_t stream) {
         if (m > 0) v *= sqrt(2.0);
       }
       t.norm[l * (kMaxL + 1) + m] = v;
+      t.norm_hi[l * (kMaxL + 1) + m] = (float)v;
+      t.norm_lo[l * (kMaxL + 1) + m] = (float)(v - (double)(float)v);
     }
   for (int m = 0; m <= kMaxL; m++) {
     double d = 1;

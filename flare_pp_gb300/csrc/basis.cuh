@@ -21,13 +21,22 @@
 
 namespace fpp {
 
-// Normalisation N_lm * (sqrt 2 if m > 0) at [l*(kMaxL+1) + m], and the double
-// factorials (2m-1)!! at [m].
+// Normalisation N_lm * (sqrt 2 if m > 0) at [l*(kMaxL+1) + m] (with an FP32
+// hi/lo split, so FP32 evaluation carries no systematic rounding of the
+// constants), and the double factorials (2m-1)!! at [m].
 struct HarmonicTables {
   double norm[(kMaxL + 1) * (kMaxL + 1)];
+  float norm_hi[(kMaxL + 1) * (kMaxL + 1)];
+  float norm_lo[(kMaxL + 1) * (kMaxL + 1)];
   double dfact[kMaxL + 1];
 };
 static __constant__ HarmonicTables c_harm;  // uploaded by upload_harmonic_tables()
+
+// N_lm * v, with the constant kept to ~48 bits in FP32
+__device__ __forceinline__ double norm_scale(int k, double v) { return c_harm.norm[k] * v; }
+__device__ __forceinline__ float norm_scale(int k, float v) {
+  return fmaf(c_harm.norm_hi[k], v, c_harm.norm_lo[k] * v);
+}
 
 // g_n and dg_n/dr into out_g[n * stride], out_dg[n * stride].
 template <typename T>
@@ -47,8 +56,10 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
     dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
   }
   const bool inside = !(r < r1 || r > rc);
+  // x by a correctly rounded division: a rounded reciprocal would shift every
+  // pair's argument the same way and bias the descriptors in FP32
   const T c = T(1) / (rc - r1);
-  const T x = (r - r1) * c;
+  const T x = (r - r1) / (rc - r1);
   T tm2 = 0, tm1 = 0, dm2 = 0, dm1 = 0;
   for (int n = 0; n < N; n++) {
     T t, dt;
@@ -105,10 +116,10 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
         qz = T(2 * m + 1) * q1;
         qr = T(0);
       } else {
-        const T a = T(2 * l - 1), b = T(l + m - 1), inv = T(1) / T(l - m);
-        q = (a * uz * q1 - b * q2) * inv;
-        qz = (a * (q1 + uz * qz1) - b * qz2) * inv;
-        qr = (a * uz * qr1 - b * (q2 + qr2)) * inv;
+        const T a = T(2 * l - 1), b = T(l + m - 1), dv = T(l - m);
+        q = (a * uz * q1 - b * q2) / dv;
+        qz = (a * (q1 + uz * qz1) - b * qz2) / dv;
+        qr = (a * uz * qr1 - b * (q2 + qr2)) / dv;
       }
       q2 = q1;
       q1 = q;
@@ -116,26 +127,26 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
       qz1 = qz;
       qr2 = qr1;
       qr1 = qr;
-      const T nrm = T(c_harm.norm[l * (kMaxL + 1) + m]);
+      const int kn = l * (kMaxL + 1) + m;
       const int ip = l * l + l + m;
-      const T R = nrm * q * A;
+      const T R = norm_scale(kn, q * A);
       out[ip * stride] = R;
       if (grad) {
-        const T Rx = nrm * (qr * T(2) * ux * A + q * Ax);
-        const T Ry = nrm * (qr * T(2) * uy * A + q * Ay);
-        const T Rz = nrm * (qz + qr * T(2) * uz) * A;
+        const T Rx = norm_scale(kn, qr * T(2) * ux * A + q * Ax);
+        const T Ry = norm_scale(kn, qr * T(2) * uy * A + q * Ay);
+        const T Rz = norm_scale(kn, (qz + qr * T(2) * uz) * A);
         grad[(3 * ip + 0) * stride] = (Rx - T(l) * R * ux) * ir;
         grad[(3 * ip + 1) * stride] = (Ry - T(l) * R * uy) * ir;
         grad[(3 * ip + 2) * stride] = (Rz - T(l) * R * uz) * ir;
       }
       if (m > 0) {
         const int im = l * l + l - m;
-        const T S = nrm * q * B;
+        const T S = norm_scale(kn, q * B);
         out[im * stride] = S;
         if (grad) {
-          const T Sx = nrm * (qr * T(2) * ux * B + q * Bx);
-          const T Sy = nrm * (qr * T(2) * uy * B + q * By);
-          const T Sz = nrm * (qz + qr * T(2) * uz) * B;
+          const T Sx = norm_scale(kn, qr * T(2) * ux * B + q * Bx);
+          const T Sy = norm_scale(kn, qr * T(2) * uy * B + q * By);
+          const T Sz = norm_scale(kn, (qz + qr * T(2) * uz) * B);
           grad[(3 * im + 0) * stride] = (Sx - T(l) * S * ux) * ir;
           grad[(3 * im + 1) * stride] = (Sy - T(l) * S * uy) * ir;
           grad[(3 * im + 2) * stride] = (Sz - T(l) * S * uz) * ir;

@@ -31,8 +31,11 @@ struct CellDev {
   double cell[9], ct[9], ct_inv[9], cdot[9], cdot_inv[9];
   float cell32[9];
   double cutoff;
-  float cutoff_pref;   // FP32 pre-filter radius (cutoff plus margin)
-  double delta[3];     // fractional reach per lattice direction
+  float in2, out2, zero2;  // FP32 squared-distance bands: surely inside below
+                           // in2, surely outside above out2, and distances
+                           // below sqrt(zero2) re-checked for dist == 0;
+                           // everything between is decided in exact FP64
+  float delta32[3];        // fractional reach per lattice direction
   int sweep, ns, n_shift;
   int nb[3];
 };
@@ -50,10 +53,15 @@ static CellDev make_dev(const CellInfo &ci) {
   d.cutoff = ci.cutoff;
   double cmax = 0;
   for (int k = 0; k < 9; k++) cmax = fmax(cmax, fabs(ci.cell[k]));
+  // FP32 positions are within 2^-24 |x| of the FP64 ones; the margin covers
+  // that error many times over for any cell below ~10^4 A
   double margin = 1e-3 + 1e-5 * (cmax * (2 * ci.sweep + 2) + ci.cutoff);
-  d.cutoff_pref = (float)(ci.cutoff + margin);
+  d.in2 = (float)((ci.cutoff - margin) * (ci.cutoff - margin));
+  if (ci.cutoff <= margin) d.in2 = 0.f;
+  d.out2 = (float)((ci.cutoff + margin) * (ci.cutoff + margin));
+  d.zero2 = (float)(margin * margin);
   for (int k = 0; k < 3; k++)
-    d.delta[k] = (ci.cutoff + margin) / ci.height[k] + 1e-9;
+    d.delta32[k] = (float)((ci.cutoff + 2 * margin) / ci.height[k] + 1e-6);
   d.sweep = ci.sweep;
   d.ns = 2 * ci.sweep + 1;
   d.n_shift = d.ns * d.ns * d.ns;
@@ -73,7 +81,7 @@ __device__ __forceinline__ void mm3(const double a[3], const double *m,
 // Structure::wrap_positions (structure.cpp:120-133) plus binning.
 __global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
                            dvec4 *__restrict__ wp, float4 *__restrict__ wp32,
-                           dvec4 *__restrict__ frac, int *__restrict__ atom_bin,
+                           float4 *__restrict__ frac, int *__restrict__ atom_bin,
                            int *__restrict__ bin_count, DeviceStatus *st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= noa) return;
@@ -91,7 +99,7 @@ __global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
   mm3(t, cd.ct_inv, w);
   wp[i] = dvec4{w[0], w[1], w[2], 0.0};
   wp32[i] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
-  frac[i] = dvec4{rw[0], rw[1], rw[2], 0.0};
+  frac[i] = make_float4((float)rw[0], (float)rw[1], (float)rw[2], 0.f);
   int b[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -133,20 +141,21 @@ __device__ __forceinline__ double exact_image(const dvec4 &wi, const dvec4 &wj,
 
 // Enumerate the candidate (j, s) pairs of atom i; `emit` is called by each
 // lane for each accepted pair.  All lanes of the warp call this together.
+// Candidates are screened in FP32; only pairs whose FP32 distance lies within
+// the margin band around the cutoff (or near zero) are decided by the
+// reference's exact FP64 distance, so the accepted set is the reference's.
 template <typename Emit>
 __device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
                                                 const dvec4 *__restrict__ wp,
                                                 const float4 *__restrict__ wp32,
-                                                const dvec4 *__restrict__ frac,
+                                                const float4 *__restrict__ frac,
                                                 const int *__restrict__ bin_start,
                                                 const int *__restrict__ bin_atoms,
                                                 Emit emit) {
   const int lane = threadIdx.x & 31;
-  const dvec4 wi = wp[i];
   const float4 pi = wp32[i];
-  const dvec4 fi = frac[i];
-  const double fik[3] = {fi.x, fi.y, fi.z};
-  const float rc2 = cd.cutoff_pref * cd.cutoff_pref;
+  const float4 fi = frac[i];
+  const float fik[3] = {fi.x, fi.y, fi.z};
   for (int s1 = -cd.sweep; s1 <= cd.sweep; s1++) {
     for (int s2 = -cd.sweep; s2 <= cd.sweep; s2++) {
       for (int s3 = -cd.sweep; s3 <= cd.sweep; s3++) {
@@ -155,9 +164,9 @@ __device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
         bool empty = false;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          double c = fik[k] - (double)sv[k];
-          int l = (int)floor((c - cd.delta[k]) * cd.nb[k]);
-          int h = (int)floor((c + cd.delta[k]) * cd.nb[k]);
+          const float c = fik[k] - (float)sv[k];
+          int l = (int)floorf((c - cd.delta32[k]) * cd.nb[k]);
+          int h = (int)floorf((c + cd.delta32[k]) * cd.nb[k]);
           l = max(l, 0);
           h = min(h, cd.nb[k] - 1);
           if (l > h) empty = true;
@@ -185,9 +194,12 @@ __device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
                   float dx = (pj.x - pi.x) + sx;
                   float dy = (pj.y - pi.y) + sy;
                   float dz = (pj.z - pi.z) + sz;
-                  if (dx * dx + dy * dy + dz * dz < rc2) {
+                  const float d2 = dx * dx + dy * dy + dz * dz;
+                  if (d2 < cd.in2 && d2 > cd.zero2) {
+                    ok = true;
+                  } else if (d2 <= cd.out2) {
                     double im[3];
-                    double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
+                    double dist = exact_image(wp[i], wp[j], cd, s1, s2, s3, im);
                     ok = (dist < cd.cutoff) && (dist != 0.0);
                   }
                 }
@@ -201,7 +213,7 @@ __device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
 
 __global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
                         const float4 *__restrict__ wp32,
-                        const dvec4 *__restrict__ frac,
+                        const float4 *__restrict__ frac,
                         const int *__restrict__ bin_start,
                         const int *__restrict__ bin_atoms,
                         int *__restrict__ count) {
@@ -218,7 +230,7 @@ __global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
 
 __global__ void k_fill(int noa, CellDev cd, const dvec4 *__restrict__ wp,
                        const float4 *__restrict__ wp32,
-                       const dvec4 *__restrict__ frac,
+                       const float4 *__restrict__ frac,
                        const int *__restrict__ bin_start,
                        const int *__restrict__ bin_atoms,
                        const int *__restrict__ offset,
@@ -413,7 +425,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   }
   FPP_TRY(st.wrapped.reserve(sizeof(dvec4) * noa));
   FPP_TRY(st.wrapped32.reserve(sizeof(float4) * noa));
-  FPP_TRY(st.frac.reserve(sizeof(dvec4) * noa));
+  FPP_TRY(st.frac.reserve(sizeof(float4) * noa));
   FPP_TRY(st.atom_bin.reserve(sizeof(int) * noa));
   FPP_TRY(st.bin_atoms.reserve(sizeof(int) * noa));
   FPP_TRY(st.bin_count.reserve(sizeof(int) * (nbins + 1)));
@@ -426,7 +438,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   const int tb = 256;
   k_wrap_bin<<<ceil_div(noa, tb), tb, 0, stream>>>(
       noa, st.positions.as<double>(), cd, st.wrapped.as<dvec4>(),
-      st.wrapped32.as<float4>(), st.frac.as<dvec4>(), st.atom_bin.as<int>(),
+      st.wrapped32.as<float4>(), st.frac.as<float4>(), st.atom_bin.as<int>(),
       st.bin_count.as<int>(), dst);
   FPP_CUDA(cudaGetLastError());
 
@@ -450,7 +462,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_CUDA(cudaMemsetAsync(st.nbr_count.as<int>() + noa, 0, sizeof(int), stream));
   k_count<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
                                       st.wrapped32.as<float4>(),
-                                      st.frac.as<dvec4>(), st.bin_start.as<int>(),
+                                      st.frac.as<float4>(), st.bin_start.as<int>(),
                                       st.bin_atoms.as<int>(), st.nbr_count.as<int>());
   FPP_CUDA(cudaGetLastError());
   tmp_bytes = st.scan_tmp.bytes;
@@ -475,7 +487,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
   if (total == 0) return FPP_OK;
   k_fill<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
-                                     st.wrapped32.as<float4>(), st.frac.as<dvec4>(),
+                                     st.wrapped32.as<float4>(), st.frac.as<float4>(),
                                      st.bin_start.as<int>(), st.bin_atoms.as<int>(),
                                      st.nbr_offset.as<int>(),
                                      st.nbr_key_tmp.as<long long>());

@@ -129,13 +129,12 @@ def lennard_jones(cell, positions, eps=0.4, sig=2.6, rc=None):
 # drawn from seeded frames and whose weights are the reference's QR solve
 # (sparse_gp.cpp:576-610: LLT(Kuu + 1e-8 I), A = [Kuf^T / noise; L^T],
 # alpha = R^-1 Q^T b) fitted to Lennard-Jones site energies, so that the
-# weights carry the cancellations of a real fit.  Descriptors come from the
-# GPU library in FP64; the dense FP64 algebra runs in torch on the GPU.
+# weights carry the cancellations of a real fit.  Descriptors, kernel
+# matrices and the QR solve all run in the GPU library in FP64.
 # --------------------------------------------------------------------------
 def fit_site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
                           noise=0.01, seed=0, device="cuda"):
-    import torch
-    from .api import ClusterDescriptor, Structure
+    from .api import ClusterDescriptor, NormalizedDotProduct, Structure, update_matrices_QR
     rng = np.random.default_rng(seed)
     ns = b2.descriptor_settings[0]
     rc = float(np.max(b2.cutoffs))
@@ -166,32 +165,11 @@ def fit_site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
         train.add_all_clusters(dv)
     y = np.concatenate([np.concatenate([ys[f][dv.atom_indices[s_]] for f, dv in enumerate(dvs)])
                         for s_ in range(ns)])
-    dev = torch.device(device)
-    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
-
-    def norm_rows(d, n):
-        d, n = t(d), t(n)
-        ok = n >= 1e-8
-        return torch.where(ok[:, None], d / torch.where(ok, n, torch.ones_like(n))[:, None],
-                           torch.zeros_like(d))
-
-    sig2 = sigma * sigma
-    n = sparse.n_clusters
-    Kuu = torch.zeros((n, n), dtype=torch.float64, device=dev)
-    Kuf = torch.zeros((n, train.n_clusters), dtype=torch.float64, device=dev)
-    for s_ in range(ns):
-        a0, a1 = sparse.cumulative_type_count[s_], sparse.cumulative_type_count[s_] + sparse.n_clusters_by_type[s_]
-        b0, b1 = train.cumulative_type_count[s_], train.cumulative_type_count[s_] + train.n_clusters_by_type[s_]
-        dh = norm_rows(sparse.descriptors[s_], sparse.descriptor_norms[s_])
-        ph = norm_rows(train.descriptors[s_], train.descriptor_norms[s_])
-        Kuu[a0:a1, a0:a1] = sig2 * (dh @ dh.T) ** power
-        Kuf[a0:a1, b0:b1] = sig2 * (dh @ ph.T) ** power
-    L = torch.linalg.cholesky(Kuu + 1e-8 * torch.eye(n, dtype=torch.float64, device=dev))
-    A = torch.cat([Kuf.T / noise, L.T], 0)
-    b = torch.cat([t(y) / noise, torch.zeros(n, dtype=torch.float64, device=dev)])
-    Q, R = torch.linalg.qr(A)
-    alpha = torch.linalg.solve_triangular(R, (Q.T @ b)[:, None], upper=True)[:, 0]
-    return dict(sparse=sparse, alpha=alpha.cpu().numpy(), sigma=sigma, power=power,
+    kern = NormalizedDotProduct(sigma, power)
+    Kuu = kern.envs_envs(sparse, sparse)
+    Kuf = kern.envs_envs(sparse, train)
+    alpha, _, _ = update_matrices_QR(Kuu, Kuf, y, np.full(len(y), 1 / noise ** 2))
+    return dict(sparse=sparse, alpha=alpha, sigma=sigma, power=power,
                 n_train=train.n_clusters)
 
 

@@ -202,6 +202,22 @@ int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
                        void *stream);
 
 /* ------------------------------------------------------------------------
+ * SparseGP::update_matrices_QR (src/flare_pp/bffs/sparse_gp.cpp:576-610) in
+ * FP64 on the GPU (cuSOLVER):
+ *   L = chol(Kuu + jitter I),  A = [diag(sqrt(noise)) Kuf^T ; L^T],  A = Q R,
+ *   alpha = R^-1 Q^T [sqrt(noise) y ; 0],  R_inv = R^-1,  L_inv = L^-1.
+ * Host arrays: Kuu n x n, Kuf n x m (row-major), y and noise_vector m (the
+ * reference's 1/sigma^2 per label).  Outputs (host, each optional): alpha n,
+ * R_inv n x n, L_inv n x n (row-major).  FPP_ERR_NUMERIC if Kuu + jitter I
+ * is not positive definite.
+ * ---------------------------------------------------------------------- */
+int fpp_update_matrices_QR(int32_t n, int32_t m, const double *Kuu,
+                           const double *Kuf, const double *y,
+                           const double *noise_vector, double jitter,
+                           double *alpha, double *R_inv, double *L_inv,
+                           void *stream);
+
+/* ------------------------------------------------------------------------
  * PairFLARE::compute(eflag, vflag) (lammps_plugins/pair_flare.cpp:68-184)
  * with LAMMPS-shaped host arrays: x is nall x 3 (owned then ghost atoms),
  * type is 1-based (nall), the full neighbor list is given as numneigh[inum]

@@ -298,3 +298,35 @@ def test_autograd_forces_and_stress_finite_differences(gpu_lib, c2):
             vals.append(c2["ggp"].predict_mapped(st, "fp64")[0])
         fd = -(vals[0] - vals[1]) / (2 * h) / V
         assert abs(fd - S[k].item()) < 1e-6 + 1e-5 * abs(fd), (i, j, fd, S[k].item())
+
+
+def test_training_solve_matches_oracle(gpu_lib):
+    """SparseGP training on the GPU (B2 with stored derivatives, envs_envs,
+    envs_struc columns, cuSOLVER QR) against the oracle's update_matrices_QR
+    on the config-1 training set (E, F, S labels)."""
+    m = fixtures.config1_model(n_frames=3, n_sparse=30)
+    ogp = m["gp"]
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, 5.0], [], [1, 8, 3])
+    gp = fg.SparseGP([fg.NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
+    frames = []
+    for k, of in enumerate(ogp.training_structures):
+        s = fg.Structure(of.cell, of.species, of.positions, 5.0, [b2])
+        s.energy, s.forces, s.stresses = of.energy, of.forces, of.stresses
+        gp.add_training_structure(s)
+        frames.append(s)
+    for k, atoms in enumerate(ogp.sparse_indices[0]):
+        gp.add_specific_environments(frames[k], atoms)
+    gp.update_matrices_QR()
+    np.testing.assert_allclose(gp.Kuu, ogp.Kuu_mat, rtol=0, atol=1e-10 * np.abs(ogp.Kuu_mat).max())
+    np.testing.assert_allclose(gp.Kuf, ogp.Kuf_mat, rtol=0, atol=1e-9 * np.abs(ogp.Kuf_mat).max())
+    # alpha carries the conditioning of the solve: compare predictions and
+    # alpha relative to its scale
+    np.testing.assert_allclose(gp.alpha, ogp.alpha, rtol=0, atol=1e-5 * np.abs(ogp.alpha).max())
+    cell, sp, pos = synth.fcc_al_108(101, 5)
+    os_ = OStructure(cell, sp, pos, 5.0, [m["b2"]])
+    ogp.predict_SOR(os_)
+    gs = fg.Structure(cell, sp, pos, 5.0)
+    gp.predict_SOR(gs)
+    np.testing.assert_allclose(gs.mean_efs, os_.mean_efs, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(gs.variance_efs[1:], os_.variance_efs[1:], rtol=1e-4,
+                               atol=1e-8)
