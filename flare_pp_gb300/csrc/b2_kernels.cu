@@ -79,8 +79,36 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward.
+// Forward: one warp per atom.
+//   1. stage the bases of up to W neighbors (one neighbor per lane) and list
+//      the staged neighbors by species (warp ballots);
+//   2. lane = (l, m) column: for each species, run over its listed neighbors
+//      accumulating the N radial channels in registers (plain sums over 16
+//      neighbors, folded into compensated per-channel sums in shared memory);
+//   3. B2 contraction per radial pair (n1, n2 >= n1) into shared memory with
+//      a compensated norm, then the normalized / split outputs.
 // ---------------------------------------------------------------------------
+template <typename T> struct FwdLayout {
+  int W, GP;            // window, padded radial stride (multiple of 4)
+  size_t stage, csum;   // bytes: staging (reused for p), c sums + compensation
+  size_t lists, total;
+};
+
+template <typename T>
+__host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
+  FwdLayout<T> L;
+  L.W = a.window;
+  L.GP = (a.N + 3) & ~3;
+  const int sb = a.n_species * a.N * a.H;
+  size_t st = sizeof(T) * ((size_t)L.W * L.GP + (size_t)a.H * (L.W + 1));
+  size_t pb = sizeof(T) * (size_t)a.n_d;
+  L.stage = ((st > pb ? st : pb) + 15) & ~(size_t)15;
+  L.csum = (sizeof(T) * 2 * (size_t)sb + 15) & ~(size_t)15;
+  L.lists = (sizeof(int) * ((size_t)a.n_species * L.W + 2 * L.W + a.n_species) + 15) & ~(size_t)15;
+  L.total = L.stage + L.csum + L.lists;
+  return L;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_b2_forward(B2Args a, const int *__restrict__ offset,
@@ -95,17 +123,18 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
   const int atom = blockIdx.x * nwarps + warp;
-  const int N = a.N, H = a.H, NS = a.n_species, W = a.window;
-  const int WS = W + 1;  // padded stride (conflict-free lane columns)
+  const FwdLayout<T> Lay = fwd_layout<T>(a);
+  const int N = a.N, H = a.H, NS = a.n_species, W = Lay.W, GP = Lay.GP;
+  const int WS = W + 1;
   const int sb = NS * N * H;
-  // per-warp carve-out
-  const size_t per_warp = a.smem_per_warp;
-  unsigned char *base = smem_raw + per_warp * warp;
-  T *g_s = reinterpret_cast<T *>(base);           // [N][WS]
-  T *y_s = g_s + N * WS;                          // [H][WS]
-  T *c_s = y_s + H * WS;                          // [sb]
-  T *cc_s = c_s + sb;                             // [sb] compensation
-  int *sp_s = reinterpret_cast<int *>(cc_s + sb); // [W]
+  unsigned char *base = smem_raw + Lay.total * warp;
+  T *g_s = reinterpret_cast<T *>(base);               // [W][GP]
+  T *y_s = g_s + (size_t)W * GP;                      // [H][WS]
+  T *p_s = reinterpret_cast<T *>(base);               // [n_d] (after staging)
+  T *c_s = reinterpret_cast<T *>(base + Lay.stage);   // [sb] running sums
+  T *cc_s = c_s + sb;                                 // [sb] compensation
+  int *list = reinterpret_cast<int *>(base + Lay.stage + Lay.csum);  // [NS][W]
+  int *cnt_s = list + NS * W;                         // [NS]
   if (atom >= a.noa) return;
 
   for (int k = lane; k < sb; k += 32) {
@@ -117,57 +146,91 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   __syncwarp();
   for (int w0 = beg; w0 < end; w0 += W) {
     const int cnt = min(W, end - w0);
-    // stage bases, one neighbor per lane
-    for (int b = lane; b < cnt; b += 32) {
-      const int p = w0 + b;
-      const int sj = nbr_s[p];
-      const dvec4 rd = rel[p];
-      const double rcut = a.cutoffs[si * NS + sj];
-      const bool keep = a.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
-      T r, x, y, z;
-      if (sizeof(T) == 8) {
-        r = T(rd.x);
-        x = T(rd.y);
-        y = T(rd.z);
-        z = T(rd.w);
-      } else {
-        const float4 rf = rel32[p];
-        x = T(rf.x);
-        y = T(rf.y);
-        z = T(rf.z);
-        r = T(rf.w);
+    // ---- 1. stage bases and species lists ----
+    if (lane < NS) cnt_s[lane] = 0;
+    __syncwarp();
+    for (int b0 = 0; b0 < cnt; b0 += 32) {
+      const int b = b0 + lane;
+      int sj = -1;
+      if (b < cnt) {
+        const int p = w0 + b;
+        const int sp = nbr_s[p];
+        const dvec4 rd = rel[p];
+        const double rcut = a.cutoffs[si * NS + sp];
+        const bool keep = a.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+        T r, x, y, z;
+        if (sizeof(T) == 8) {
+          r = T(rd.x);
+          x = T(rd.y);
+          y = T(rd.z);
+          z = T(rd.w);
+        } else {
+          const float4 rf = rel32[p];
+          x = T(rf.x);
+          y = T(rf.y);
+          z = T(rf.z);
+          r = T(rf.w);
+        }
+        if (keep) {
+          sj = sp;
+          radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, g_s + (size_t)b * GP,
+                          nullptr, 1);
+          real_harmonics<T>(x, y, z, a.lmax, y_s + b, nullptr, WS);
+        }
       }
-      sp_s[b] = keep ? sj : -1;
-      radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, g_s + b, nullptr, WS);
-      real_harmonics<T>(x, y, z, a.lmax, y_s + b, nullptr, WS);
+      for (int sp = 0; sp < NS; sp++) {
+        const unsigned m = __ballot_sync(0xffffffffu, sj == sp);
+        if (sj == sp) list[sp * W + cnt_s[sp] + __popc(m & ((1u << lane) - 1u))] = b;
+        __syncwarp();
+        if (lane == 0) cnt_s[sp] += __popc(m);
+        __syncwarp();
+      }
     }
     __syncwarp();
-    // accumulate: lane owns column lm, registers hold the N radial channels
-    for (int s = 0; s < NS; s++) {
+    // ---- 2. accumulate: lane owns column lm ----
+    for (int sp = 0; sp < NS; sp++) {
+      const int ns_ = cnt_s[sp];
+      if (ns_ == 0) continue;
+      const int *ls = list + sp * W;
       for (int lm0 = 0; lm0 < H; lm0 += 32) {
         const int lm = lm0 + lane;
         const bool act = lm < H;
         const int lmc = act ? lm : 0;
-        Acc<T> acc[kMaxN];
+        T sum[kMaxN], comp[kMaxN];
 #pragma unroll
         for (int n = 0; n < kMaxN; n++)
           if (n < N) {
-            acc[n].s = c_s[(s * N + n) * H + lmc];
-            acc[n].c = cc_s[(s * N + n) * H + lmc];
+            sum[n] = c_s[(sp * N + n) * H + lmc];
+            comp[n] = cc_s[(sp * N + n) * H + lmc];
           }
-        for (int b = 0; b < cnt; b++) {
-          if (sp_s[b] != s) continue;
-          const T yv = y_s[lmc * WS + b];
+        for (int k0 = 0; k0 < ns_; k0 += 16) {
+          T chunk[kMaxN];
+#pragma unroll
+          for (int n = 0; n < kMaxN; n++) chunk[n] = T(0);
+          const int k1 = min(ns_, k0 + 16);
+          for (int k = k0; k < k1; k++) {
+            const int b = ls[k];
+            const T yv = y_s[lmc * WS + b];
+            const T *gb = g_s + (size_t)b * GP;
+#pragma unroll
+            for (int n = 0; n < kMaxN; n++)
+              if (n < N) chunk[n] += gb[n] * yv;
+          }
 #pragma unroll
           for (int n = 0; n < kMaxN; n++)
-            if (n < N) acc[n].add(g_s[n * WS + b] * yv);
+            if (n < N) {  // Kahan fold of the chunk
+              const T yk = chunk[n] - comp[n];
+              const T t = sum[n] + yk;
+              comp[n] = (t - sum[n]) - yk;
+              sum[n] = t;
+            }
         }
         if (act) {
 #pragma unroll
           for (int n = 0; n < kMaxN; n++)
             if (n < N) {
-              c_s[(s * N + n) * H + lm] = acc[n].s;
-              cc_s[(s * N + n) * H + lm] = acc[n].c;
+              c_s[(sp * N + n) * H + lm] = sum[n];
+              cc_s[(sp * N + n) * H + lm] = comp[n];
             }
         }
       }
@@ -176,41 +239,41 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   }
   // fold the compensation and publish c
   for (int k = lane; k < sb; k += 32) {
-    T v = c_s[k] + cc_s[k];
+    T v = c_s[k] - cc_s[k];
     c_s[k] = v;
     c_out[(size_t)atom * sb + k] = v;
   }
   __syncwarp();
-  // B2 contraction: p[d] with d = q (lmax+1) + l, pair q = (n1, n2 >= n1)
+  // ---- 3. B2 contraction per radial pair q, all l ----
   const int L1 = a.lmax + 1;
   const int nd = a.n_d;
+  const int npair = nd / L1;
   Acc<T> nacc;
-  for (int d = lane; d < nd; d += 32) {
-    const int q = d / L1, l = d - q * L1;
+  for (int q = lane; q < npair; q += 32) {
     const int pr = pair_tab[q];
     const int n1 = pr & 0xffff, n2 = pr >> 16;
-    const T *c1 = c_s + n1 * H + l * l, *c2 = c_s + n2 * H + l * l;
-    T v = T(0);
-    for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
-    nacc.add(v * v);
-    if (p_out) p_out[(size_t)atom * nd + d] = v;
+    const T *c1 = c_s + n1 * H, *c2 = c_s + n2 * H;
+    for (int l = 0; l < L1; l++) {
+      T v = T(0);
+      for (int m = l * l; m < (l + 1) * (l + 1); m++) v += c1[m] * c2[m];
+      p_s[q * L1 + l] = v;
+      nacc.add(v * v);
+    }
   }
-  double nsq = warp_sum(double(nacc.s) + double(nacc.c));
+  const double nsq = warp_sum(double(nacc.s) + double(nacc.c));
   const double nrm = sqrt(nsq);
   if (lane == 0) norm_out[atom] = nrm;
+  __syncwarp();
   const int row = row_of_atom[atom];
   const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+  const float invf = float(inv);
   for (int d = lane; d < nd; d += 32) {
-    const int q = d / L1, l = d - q * L1;
-    const int pr = pair_tab[q];
-    const int n1 = pr & 0xffff, n2 = pr >> 16;
-    const T *c1 = c_s + n1 * H + l * l, *c2 = c_s + n2 * H + l * l;
-    T v = T(0);
-    for (int m = 0; m < 2 * l + 1; m++) v += c1[m] * c2[m];
+    const T v = p_s[d];
+    if (p_out) p_out[(size_t)atom * nd + d] = v;
     if (phat64) phat64[(size_t)row * ldp + d] = double(v) * inv;
     if (phat_hi) {
       // centred operand: delta = phat - pbar, scaled by 2^13 (|delta| <= 2)
-      const float x = (float(double(v) * inv) - pbar[(size_t)si * nd + d]) * 8192.0f;
+      const float x = (float(v) * invf - pbar[(size_t)si * nd + d]) * 8192.0f;
       const __half h = __float2half_rn(x);
       const float rem = (x - __half2float(h)) * 2048.0f;
       phat_hi[(size_t)row * ldp + d] = h;
@@ -220,41 +283,34 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint.
+// Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
+// u = dE/dc = (W + W^T) c per l, written to global memory.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(128)
-k_b2_adjoint(B2Args a, AdjArgs g, const int *__restrict__ offset,
-             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
-             const int *__restrict__ nbr_s, const int *__restrict__ species,
-             const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
-             const T *__restrict__ c_in, const double *__restrict__ norm_in,
-             double *__restrict__ atom_e, T *__restrict__ pair_f) {
+k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
+        const int *__restrict__ row_of_atom, const T *__restrict__ c_in,
+        const double *__restrict__ norm_in, double *__restrict__ atom_e,
+        T *__restrict__ u_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
   const int atom = blockIdx.x * nwarps + warp;
   const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
-  const int sb = NS * N * H;
+  const int sb = NS * N * H, nr = NS * N;
   const int L1 = a.lmax + 1;
   unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
   T *w_s = reinterpret_cast<T *>(base);  // [nd]
   T *c_s = w_s + nd;                     // [sb]
-  T *u_s = c_s + sb;                     // [sb]
-  T *bas = u_s + sb;                     // [(2N + 4H)][33]
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
   const double nrm = norm_in[atom];
-
   for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
 
-  // ---- w = dE/dp and the atom energy ----
-  bool empty;
   double e = 0.0;
   if ((g.mode == kWFromV2 || g.mode == kWFromV1) && g.phat64) {
-    // FP64 form: E = phat . (beta phat) (or phat . beta1), w = dE/dp
-    empty = nrm * nrm < g.empty_thresh;
+    const bool empty = nrm * nrm < g.empty_thresh;
     double dot = 0.0;
     for (int d = lane; d < nd; d += 32) {
       const double ph = g.phat64[(size_t)row * g.ldp + d];
@@ -277,17 +333,16 @@ k_b2_adjoint(B2Args a, AdjArgs g, const int *__restrict__ offset,
     //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
     //            g = beta pbar, c0 = pbar^T beta pbar;  dE/dp = 2 (g + V - E phat)/|p|
     //   power 1: E = phat . beta1,                      dE/dp = (beta1 - E phat)/|p|
-    empty = nrm * nrm < g.empty_thresh;
+    const bool empty = nrm * nrm < g.empty_thresh;
     Acc<float> acc;
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
       const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
                        (1.0f / 8192.0f);
-      const float pb = g.pbar[(size_t)si * nd + d];
       if (g.mode == kWFromV2)
         acc.add((2.0f * g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) * dl);
       else
-        acc.add(float(g.beta1[(size_t)si * nd + d]) * (pb + dl));
+        acc.add(float(g.beta1[(size_t)si * nd + d]) * (g.pbar[(size_t)si * nd + d] + dl));
     }
     const double dot = warp_sum(double(acc.s) + double(acc.c)) +
                        (g.mode == kWFromV2 ? g.c0[si] : 0.0);
@@ -305,98 +360,97 @@ k_b2_adjoint(B2Args a, AdjArgs g, const int *__restrict__ offset,
       else
         w_s[d] = T((float(g.beta1[(size_t)si * nd + d]) - ef * ph) * inv);
     }
-  } else {  // kWGiven: dE/dp supplied per atom (kernel form)
-    empty = false;
+  } else {  // kWGiven: dE/dp supplied per operand row (kernel form)
     for (int d = lane; d < nd; d += 32) w_s[d] = T(g.w_given[(size_t)row * g.ldp + d]);
     e = g.e_given ? g.e_given[row] : 0.0;
   }
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
-
-  // ---- u = dE/dc ----
+  // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
   for (int lm0 = 0; lm0 < H; lm0 += 32) {
     const int lm = lm0 + lane;
-    if (lm < H) {
-      int l = 0;
-      while ((l + 1) * (l + 1) <= lm) l++;
-      for (int n1 = 0; n1 < NS * N; n1++) {
-        T acc = T(0);
-        const int nr = NS * N;
-        for (int n2 = 0; n2 < nr; n2++) {
-          const int lo = min(n1, n2), hi = max(n1, n2);
-          const int q = lo * nr - (lo * (lo - 1)) / 2 + (hi - lo);
-          T wv = w_s[q * L1 + l];
-          if (n1 == n2) wv = wv + wv;
-          acc += wv * c_s[n2 * H + lm];
-        }
-        u_s[n1 * H + lm] = acc;
+    if (lm >= H) continue;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) l++;
+    for (int n1 = 0; n1 < nr; n1++) {
+      T acc = T(0);
+      // n2 < n1: pair (n2, n1), index q = n2 nr - n2 (n2 - 1)/2 + (n1 - n2)
+      int q = n1;  // n2 = 0
+      for (int n2 = 0; n2 < n1; n2++) {
+        acc += w_s[q * L1 + l] * c_s[n2 * H + lm];
+        q += nr - n2 - 1;
       }
+      // n2 >= n1: pair (n1, n2)
+      q = n1 * nr - (n1 * (n1 - 1)) / 2;
+      acc += T(2) * w_s[q * L1 + l] * c_s[n1 * H + lm];
+      for (int n2 = n1 + 1; n2 < nr; n2++) acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
+      u_out[(size_t)atom * sb + n1 * H + lm] = acc;
     }
   }
-  __syncwarp();
+}
 
-  // ---- per-pair forces ----
-  T *gb = bas;                // g   [N][33]
-  T *db = gb + N * 33;        // dg  [N][33]
-  T *yb = db + N * 33;        // Y   [H][33]
-  T *yg = yb + H * 33;        // dY  [3H][33]
-  const int beg = offset[atom], end = offset[atom + 1];
-  for (int p0 = beg; p0 < end; p0 += 32) {
-    const int p = p0 + lane;
-    const bool valid = p < end;
-    T fx = T(0), fy = T(0), fz = T(0);
-    int sj = 0;
-    bool keep = false;
-    T r = T(1), x = T(1), y = T(0), z = T(0);
-    if (valid) {
-      sj = nbr_s[p];
-      const dvec4 rd = rel[p];
-      const double rcut = a.cutoffs[si * NS + sj];
-      keep = g.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
-      if (sizeof(T) == 8) {
-        r = T(rd.x);
-        x = T(rd.y);
-        y = T(rd.z);
-        z = T(rd.w);
-      } else {
-        const float4 rf = rel32[p];
-        x = T(rf.x);
-        y = T(rf.y);
-        z = T(rf.z);
-        r = T(rf.w);
-      }
-      radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, gb + lane, db + lane, 33);
-      real_harmonics<T>(x, y, z, a.lmax, yb + lane, yg + lane, 33);
+// ---------------------------------------------------------------------------
+// Adjoint, part 2 (one thread per pair):
+//   f_ij = sum_{n, lm} u_i[s_j N + n, lm] (g'_n Y_lm r_hat + g_n grad Y_lm)
+// with g, g' in registers and the harmonics generated in order and consumed
+// immediately.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nbr_i,
+             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
+             const int *__restrict__ nbr_s, const int *__restrict__ species,
+             const T *__restrict__ u, T *__restrict__ pair_f) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const int N = a.N, H = a.H, NS = a.n_species;
+  const int sb = NS * N * H;
+  const int i = nbr_i[p], sj = nbr_s[p], si = species[i];
+  const dvec4 rd = rel[p];
+  const double rcut = a.cutoffs[si * NS + sj];
+  const bool keep = strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+  T f[3] = {T(0), T(0), T(0)};
+  if (keep) {
+    T r, x, y, z;
+    if (sizeof(T) == 8) {
+      r = T(rd.x);
+      x = T(rd.y);
+      y = T(rd.z);
+      z = T(rd.w);
+    } else {
+      const float4 rf = rel32[p];
+      x = T(rf.x);
+      y = T(rf.y);
+      z = T(rf.z);
+      r = T(rf.w);
     }
-    __syncwarp();
-    if (valid && keep && !empty) {
-      const T *us = u_s + sj * N * H;
-      T fr = T(0);
-      for (int lm = 0; lm < H; lm++) {
-        T ag = T(0), bd = T(0);
-        for (int n = 0; n < N; n++) {
-          const T uv = us[n * H + lm];
-          ag += uv * gb[n * 33 + lane];
-          bd += uv * db[n * 33 + lane];
+    T gr[kMaxN], dg[kMaxN];
+    radial_basis_reg<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, gr, dg);
+    const T *ur = u + (size_t)i * sb + (size_t)sj * N * H;
+    T fr = T(0);
+    harmonics_visit<T>(x, y, z, a.lmax, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
+      T ag = T(0), bd = T(0);
+#pragma unroll
+      for (int n = 0; n < kMaxN; n++)
+        if (n < N) {
+          const T uv = ur[n * H + lm];
+          ag += uv * gr[n];
+          bd += uv * dg[n];
         }
-        fr += bd * yb[lm * 33 + lane];
-        fx += ag * yg[(3 * lm + 0) * 33 + lane];
-        fy += ag * yg[(3 * lm + 1) * 33 + lane];
-        fz += ag * yg[(3 * lm + 2) * 33 + lane];
-      }
-      const T ir = T(1) / r;
-      fx += fr * x * ir;
-      fy += fr * y * ir;
-      fz += fr * z * ir;
-    }
-    if (valid) {
-      pair_f[(size_t)p * 4 + 0] = fx;
-      pair_f[(size_t)p * 4 + 1] = fy;
-      pair_f[(size_t)p * 4 + 2] = fz;
-      pair_f[(size_t)p * 4 + 3] = T(0);
-    }
-    __syncwarp();
+      fr += bd * Yv;
+      f[0] += ag * Yx;
+      f[1] += ag * Yy;
+      f[2] += ag * Yz;
+    });
+    const T ir = T(1) / r;
+    f[0] += fr * x * ir;
+    f[1] += fr * y * ir;
+    f[2] += fr * z * ir;
   }
+  pair_f[(size_t)p * 4 + 0] = f[0];
+  pair_f[(size_t)p * 4 + 1] = f[1];
+  pair_f[(size_t)p * 4 + 2] = f[2];
+  pair_f[(size_t)p * 4 + 3] = T(0);
 }
 
 // Stored derivatives of b2.cpp:181-242 for a list of structure pairs (FP64):
@@ -483,53 +537,76 @@ int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-// F_i = sum over pairs of i (f_ij - f_ji), per-atom virial sum f_ij (x) r_ij.
+// F_i = sum over pairs of i (f_ij - f_ji); each block also reduces its atoms'
+// energies and virials (sum f_ij (x) r_ij) into one partial row (fixed tree
+// order, so the result is deterministic).  128 threads per block.
 template <typename T>
-__global__ void k_gather(int noa, const int *__restrict__ offset,
-                         const int *__restrict__ rev, const dvec4 *__restrict__ rel,
-                         const T *__restrict__ pair_f, double *__restrict__ forces,
-                         double *__restrict__ atom_vir) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= noa) return;
-  double F[3] = {0, 0, 0}, V[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int p = offset[i]; p < offset[i + 1]; p++) {
-    const int q = rev[p];
-    const double f0 = double(pair_f[(size_t)p * 4 + 0]);
-    const double f1 = double(pair_f[(size_t)p * 4 + 1]);
-    const double f2 = double(pair_f[(size_t)p * 4 + 2]);
-    F[0] += f0;
-    F[1] += f1;
-    F[2] += f2;
-    if (q >= 0) {  // always present for a periodic list; -1 is reported upstream
-      F[0] -= double(pair_f[(size_t)q * 4 + 0]);
-      F[1] -= double(pair_f[(size_t)q * 4 + 1]);
-      F[2] -= double(pair_f[(size_t)q * 4 + 2]);
+__global__ void __launch_bounds__(128)
+k_gather(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
+         const float4 *__restrict__ rel32, const dvec4 *__restrict__ rel,
+         const T *__restrict__ pair_f, const double *__restrict__ atom_e,
+         double *__restrict__ forces, double *__restrict__ partial) {
+  __shared__ double sm[10][128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < noa) {
+    double F[3] = {0, 0, 0};
+    for (int p = offset[i]; p < offset[i + 1]; p++) {
+      const int q = rev[p];
+      const double f0 = double(pair_f[(size_t)p * 4 + 0]);
+      const double f1 = double(pair_f[(size_t)p * 4 + 1]);
+      const double f2 = double(pair_f[(size_t)p * 4 + 2]);
+      F[0] += f0;
+      F[1] += f1;
+      F[2] += f2;
+      if (q >= 0) {  // always present for a periodic list; -1 is reported upstream
+        F[0] -= double(pair_f[(size_t)q * 4 + 0]);
+        F[1] -= double(pair_f[(size_t)q * 4 + 1]);
+        F[2] -= double(pair_f[(size_t)q * 4 + 2]);
+      }
+      double rr[3];
+      if (sizeof(T) == 8) {
+        const dvec4 r = rel[p];
+        rr[0] = r.y;
+        rr[1] = r.z;
+        rr[2] = r.w;
+      } else {
+        const float4 r = rel32[p];
+        rr[0] = r.x;
+        rr[1] = r.y;
+        rr[2] = r.z;
+      }
+      const double ff[3] = {f0, f1, f2};
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) acc[1 + a * 3 + b] += ff[a] * rr[b];
     }
-    const dvec4 r = rel[p];
-    const double rr[3] = {r.y, r.z, r.w}, ff[3] = {f0, f1, f2};
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) V[a * 3 + b] += ff[a] * rr[b];
+    forces[3 * i + 0] = F[0];
+    forces[3 * i + 1] = F[1];
+    forces[3 * i + 2] = F[2];
+    acc[0] = atom_e[i];
   }
-  forces[3 * i + 0] = F[0];
-  forces[3 * i + 1] = F[1];
-  forces[3 * i + 2] = F[2];
 #pragma unroll
-  for (int k = 0; k < 9; k++) atom_vir[(size_t)9 * i + k] = V[k];
+  for (int k = 0; k < 10; k++) sm[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int st = 64; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+#pragma unroll
+      for (int k = 0; k < 10; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 10) partial[(size_t)blockIdx.x * 10 + threadIdx.x] = sm[threadIdx.x][0];
 }
 
-// Deterministic reduction of atom energies and virials: out[0] = E,
-// out[1..9] = sum f (x) r.  One block.
-__global__ void k_reduce(int noa, const double *__restrict__ atom_e,
-                         const double *__restrict__ atom_vir, double *__restrict__ out) {
+// Sum of the per-block partial rows: out[0] = E, out[1..9] = sum f (x) r.
+__global__ void k_reduce(int nblocks, const double *__restrict__ partial,
+                         double *__restrict__ out) {
   __shared__ double sm[10][256];
   double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int i = threadIdx.x; i < noa; i += blockDim.x) {
-    acc[0] += atom_e[i];
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
 #pragma unroll
-    for (int k = 0; k < 9; k++) acc[1 + k] += atom_vir[(size_t)9 * i + k];
-  }
+    for (int k = 0; k < 10; k++) acc[k] += partial[(size_t)b * 10 + k];
 #pragma unroll
   for (int k = 0; k < 10; k++) sm[k][threadIdx.x] = acc[k];
   __syncthreads();
@@ -546,15 +623,12 @@ __global__ void k_reduce(int noa, const double *__restrict__ atom_e,
 // Host launchers.
 // ---------------------------------------------------------------------------
 size_t forward_smem_per_warp(const B2Args &a, size_t elem) {
-  const int sb = a.n_species * a.N * a.H;
-  size_t b = elem * ((size_t)(a.N + a.H) * (a.window + 1) + 2 * (size_t)sb) +
-             sizeof(int) * a.window;
-  return (b + 15) & ~(size_t)15;
+  return elem == sizeof(float) ? fwd_layout<float>(a).total : fwd_layout<double>(a).total;
 }
 
 size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
   const int sb = a.n_species * a.N * a.H;
-  size_t b = elem * ((size_t)a.n_d + 2 * (size_t)sb + (size_t)(2 * a.N + 4 * a.H) * 33);
+  size_t b = elem * ((size_t)a.n_d + (size_t)sb);
   return (b + 15) & ~(size_t)15;
 }
 
@@ -564,10 +638,11 @@ int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
                       T *p_out, double *norm_out, double *phat64, __half *phat_hi,
                       __half *phat_lo, int ldp, const float *pbar, cudaStream_t stream) {
   if (a.noa == 0) return 0;
-  a.smem_per_warp = forward_smem_per_warp(a, sizeof(T));
+  a.window = 32;
+  const size_t per = fwd_layout<T>(a).total;
   int wpb = 4;
-  while (wpb > 1 && a.smem_per_warp * wpb > 200 * 1024) wpb >>= 1;
-  size_t smem = a.smem_per_warp * wpb;
+  while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
+  size_t smem = per * wpb;
   if (smem > 227 * 1024) return -1;
   auto kern = k_b2_forward<T>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -584,26 +659,33 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                       const int *species, const int *row_of_atom,
                       const int *pair_tab, const T *c_in, const double *norm_in,
                       double *atom_e, T *pair_f, double *forces, double *atom_vir,
-                      double *reduce_out, bool gather, cudaStream_t stream) {
+                      double *reduce_out, bool gather, T *u_buf, long long n_pairs,
+                      const int *nbr_i, cudaStream_t stream) {
+  (void)pair_tab;
   if (a.noa == 0) return 0;
   a.smem_per_warp_adj = adjoint_smem_per_warp(a, sizeof(T));
   int wpb = 4;
   while (wpb > 1 && a.smem_per_warp_adj * wpb > 200 * 1024) wpb >>= 1;
   size_t smem = a.smem_per_warp_adj * wpb;
   if (smem > 227 * 1024) return -1;
-  auto kern = k_b2_adjoint<T>;
+  auto kern = k_b2_wu<T>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -1;
-  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
-      a, g, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom,
-      pair_tab, c_in, norm_in, atom_e, pair_f);
+  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom, c_in,
+                                                         norm_in, atom_e, u_buf);
   if (cudaGetLastError() != cudaSuccess) return -1;
+  if (n_pairs > 0) {
+    k_pair_force<T><<<(unsigned)((n_pairs + 127) / 128), 128, 0, stream>>>(
+        a, g.strict, n_pairs, nbr_i, nb.rel, nb.rel32, nb.nbr_s, species, u_buf, pair_f);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+  }
   if (!gather) return 0;
-  k_gather<T><<<ceil_div(a.noa, 128), 128, 0, stream>>>(
-      a.noa, nb.offset, nb.rev, nb.rel, pair_f, forces, atom_vir);
+  const int nblk = ceil_div(a.noa, 128);
+  k_gather<T><<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32, nb.rel, pair_f,
+                                        atom_e, forces, atom_vir);
   if (cudaGetLastError() != cudaSuccess) return -1;
-  k_reduce<<<1, 256, 0, stream>>>(a.noa, atom_e, atom_vir, reduce_out);
+  k_reduce<<<1, 256, 0, stream>>>(nblk, atom_vir, reduce_out);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -619,11 +701,12 @@ template int launch_b2_adjoint<float>(B2Args, const AdjArgs &, const Neigh &,
                                       const int *, const int *, const int *,
                                       const float *, const double *, double *,
                                       float *, double *, double *, double *,
-                                      bool, cudaStream_t);
+                                      bool, float *, long long, const int *, cudaStream_t);
 template int launch_b2_adjoint<double>(B2Args, const AdjArgs &, const Neigh &,
                                        const int *, const int *, const int *,
                                        const double *, const double *, double *,
                                        double *, double *, double *, double *,
-                                       bool, cudaStream_t);
+                                       bool, double *, long long, const int *,
+                                       cudaStream_t);
 
 }  // namespace fpp

@@ -69,7 +69,8 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                       const int *species, const int *row_of_atom,
                       const int *pair_tab, const T *c_in, const double *norm_in,
                       double *atom_e, T *pair_f, double *forces, double *atom_vir,
-                      double *reduce_out, bool gather, cudaStream_t stream);
+                      double *reduce_out, bool gather, T *u_buf, long long n_pairs,
+                      const int *nbr_i, cudaStream_t stream);
 
 int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
                  const int *nbr_s, const dvec4 *rel, const int *species,

@@ -83,6 +83,50 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
   }
 }
 
+// Register version: g[n], dg[n] for n < N in fully unrolled arrays.
+template <typename T>
+__device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cutoff_kind,
+                                                 T (&g)[kMaxN], T (&dg)[kMaxN]) {
+  T fc, dfc;
+  if (r > rc) {
+    fc = T(0);
+    dfc = T(0);
+  } else if (cutoff_kind == kQuadratic) {
+    const T d = r - rc;
+    fc = d * d;
+    dfc = T(2) * d;
+  } else {
+    const T pi = T(3.14159265358979323846);
+    fc = T(0.5) * (cos(pi * r / rc) + T(1));
+    dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
+  }
+  const bool inside = !(r < r1 || r > rc);
+  const T c = T(1) / (rc - r1);
+  const T x = (r - r1) / (rc - r1);
+  T tm2 = 0, tm1 = 0, dm2 = 0, dm1 = 0;
+#pragma unroll
+  for (int n = 0; n < kMaxN; n++) {
+    T t, dt;
+    if (n == 0) {
+      t = T(1);
+      dt = T(0);
+    } else if (n == 1) {
+      t = x;
+      dt = c;
+    } else {
+      t = T(2) * x * tm1 - tm2;
+      dt = T(2) * tm1 * c + T(2) * x * dm1 - dm2;
+    }
+    tm2 = tm1;
+    tm1 = t;
+    dm2 = dm1;
+    dm1 = dt;
+    const T gv = inside ? t : T(0), dv = inside ? dt : T(0);
+    g[n] = (n < N) ? gv * fc : T(0);
+    dg[n] = (n < N) ? dv * fc + gv * dfc : T(0);
+  }
+}
+
 // Y_lm at out[lm * stride]; with grad != nullptr also the Cartesian gradient
 // at grad[(3*lm + k) * stride].
 template <typename T>
@@ -151,6 +195,69 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
           grad[(3 * im + 1) * stride] = (Sy - T(l) * S * uy) * ir;
           grad[(3 * im + 2) * stride] = (Sz - T(l) * S * uz) * ir;
         }
+      }
+    }
+  }
+}
+
+// The same harmonics with gradients, handed to visit(lm, Y, dY/dx, dY/dy,
+// dY/dz) one by one as the recurrence produces them (nothing is stored).
+template <typename T, typename Visit>
+__device__ __forceinline__ void harmonics_visit(T x, T y, T z, int lmax, Visit visit) {
+  const T r = sqrt(x * x + y * y + z * z);
+  const T ir = T(1) / r;
+  const T ux = x * ir, uy = y * ir, uz = z * ir;
+  T A = T(1), B = T(0), Aprev = T(1), Bprev = T(0);
+  for (int m = 0; m <= lmax; m++) {
+    if (m > 0) {
+      Aprev = A;
+      Bprev = B;
+      const T a2 = ux * A - uy * B;
+      const T b2 = uy * A + ux * B;
+      A = a2;
+      B = b2;
+    }
+    const T Ax = T(m) * Aprev, Ay = -T(m) * Bprev;
+    const T Bx = T(m) * Bprev, By = T(m) * Aprev;
+    T q2 = 0, q1 = 0, qz2 = 0, qz1 = 0, qr2 = 0, qr1 = 0;
+    for (int l = m; l <= lmax; l++) {
+      T q, qz, qr;
+      if (l == m) {
+        q = T(c_harm.dfact[m]);
+        qz = T(0);
+        qr = T(0);
+      } else if (l == m + 1) {
+        q = T(2 * m + 1) * uz * q1;
+        qz = T(2 * m + 1) * q1;
+        qr = T(0);
+      } else {
+        const T a = T(2 * l - 1), b = T(l + m - 1), dv = T(l - m);
+        q = (a * uz * q1 - b * q2) / dv;
+        qz = (a * (q1 + uz * qz1) - b * qz2) / dv;
+        qr = (a * uz * qr1 - b * (q2 + qr2)) / dv;
+      }
+      q2 = q1;
+      q1 = q;
+      qz2 = qz1;
+      qz1 = qz;
+      qr2 = qr1;
+      qr1 = qr;
+      const int kn = l * (kMaxL + 1) + m;
+      {
+        const T R = norm_scale(kn, q * A);
+        const T Rx = norm_scale(kn, qr * T(2) * ux * A + q * Ax);
+        const T Ry = norm_scale(kn, qr * T(2) * uy * A + q * Ay);
+        const T Rz = norm_scale(kn, (qz + qr * T(2) * uz) * A);
+        visit(l * l + l + m, R, (Rx - T(l) * R * ux) * ir, (Ry - T(l) * R * uy) * ir,
+              (Rz - T(l) * R * uz) * ir);
+      }
+      if (m > 0) {
+        const T S = norm_scale(kn, q * B);
+        const T Sx = norm_scale(kn, qr * T(2) * ux * B + q * Bx);
+        const T Sy = norm_scale(kn, qr * T(2) * uy * B + q * By);
+        const T Sz = norm_scale(kn, (qz + qr * T(2) * uz) * B);
+        visit(l * l + l - m, S, (Sx - T(l) * S * ux) * ir, (Sy - T(l) * S * uy) * ir,
+              (Sz - T(l) * S * uz) * ir);
       }
     }
   }

@@ -169,8 +169,9 @@ static int finish_outputs(fpp_structure *s, cudaStream_t st, double *energy,
   return FPP_OK;
 }
 
-static int adjoint_buffers(StructureState &S, size_t elem) {
+static int adjoint_buffers(StructureState &S, size_t elem, int sb) {
   const size_t np = std::max<int64_t>(S.n_pairs, 1);
+  FPP_TRY(S.u.reserve(elem * (size_t)std::max(1, S.noa) * sb));
   FPP_TRY(S.atom_e.reserve(sizeof(double) * std::max(1, S.noa)));
   FPP_TRY(S.pair_f.reserve(elem * 4 * np));
   FPP_TRY(S.forces.reserve(sizeof(double) * 3 * std::max(1, S.noa)));
@@ -637,13 +638,14 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     }
     S.mark(4, st);
     g.phat64 = phat;
-    FPP_TRY(adjoint_buffers(S, sizeof(double)));
+    FPP_TRY(adjoint_buffers(S, sizeof(double), a.n_species * a.N * a.H));
     if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
                                   s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
                                   S.c64.as<double>(), S.norm64.as<double>(),
                                   S.atom_e.as<double>(), S.pair_f.as<double>(),
                                   S.forces.as<double>(), S.atom_vir.as<double>(),
-                                  S.reduce_out.as<double>(), gather, st) != 0)
+                                  S.reduce_out.as<double>(), gather,
+                                  S.u.as<double>(), S.n_pairs, S.nbr_i.as<int>(), st) != 0)
       return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
   } else {
     if (m->needs_center) FPP_TRY(center_from_structure(m, s, st));
@@ -683,13 +685,14 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     g.pbar = m->pbar32.as<float>();
     g.gvec = m->g32.as<float>();
     for (int k = 0; k < m->n_species; k++) g.c0[k] = m->c0[k];
-    FPP_TRY(adjoint_buffers(S, sizeof(float)));
+    FPP_TRY(adjoint_buffers(S, sizeof(float), a.n_species * a.N * a.H));
     if (launch_b2_adjoint<float>(a, g, neigh_of(S), S.species.as<int>(),
                                  s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
                                  S.c32.as<float>(), S.pn64.as<double>(),
                                  S.atom_e.as<double>(), S.pair_f.as<float>(),
                                  S.forces.as<double>(), S.atom_vir.as<double>(),
-                                 S.reduce_out.as<double>(), gather, st) != 0)
+                                 S.reduce_out.as<double>(), gather,
+                                 S.u.as<float>(), S.n_pairs, S.nbr_i.as<int>(), st) != 0)
       return fail(FPP_ERR_CUDA, "adjoint (mixed) launch failed");
   }
   S.mark(5, st);
@@ -937,14 +940,15 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
   g.ldp = ldp;
   g.w_given = S.w64.as<double>();
   g.e_given = E.as<double>();
-  FPP_TRY(adjoint_buffers(S, sizeof(double)));
+  FPP_TRY(adjoint_buffers(S, sizeof(double), a.n_species * a.N * a.H));
   FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
   if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
                                 s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
                                 S.c64.as<double>(), S.norm64.as<double>(),
                                 S.atom_e.as<double>(), S.pair_f.as<double>(),
                                 S.forces.as<double>(), S.atom_vir.as<double>(),
-                                S.reduce_out.as<double>(), true, st) != 0)
+                                S.reduce_out.as<double>(), true, S.u.as<double>(),
+                                S.n_pairs, S.nbr_i.as<int>(), st) != 0)
     return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
   double e, stress[6];
   std::vector<double> F(3 * (size_t)noa);

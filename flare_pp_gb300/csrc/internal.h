@@ -94,6 +94,7 @@ struct StructureState {
   DevBuf order, order_inv;            // species-sorted atom order
   DevBuf V, V64;                      // beta p products
   DevBuf w64;                         // dE/dp (FP64 path)
+  DevBuf u;                           // dE/dc per atom (adjoint)
   DevBuf pair_f;                      // double3/float per pair force
   DevBuf atom_e;                      // per-atom energies (double)
   DevBuf atom_vir;                    // per-atom virial partials (double[6])
