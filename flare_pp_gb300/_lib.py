@@ -46,6 +46,7 @@ SIGNATURES = {
     "fpp_b2_n_descriptors": (_c_int, [_vp, _P(_i32)]),
     "fpp_b2_pair_count": (_c_int, [_vp, _vp, _P(_i64), _vp]),
     "fpp_b2_compute": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fpp_b2_descriptors_noalloc": (_c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fpp_model_create": (_c_int, [_vp, _dbl, _dbl, _P(_vp)]),
     "fpp_model_destroy": (_c_int, [_vp]),
     "fpp_model_set_sparse": (_c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),

@@ -138,6 +138,30 @@ int fpp_b2_compute(const fpp_b2 *b2, fpp_structure *s, double *descriptors,
                    double *desc_neighbor_coordinates, double *force_dervs,
                    double *force_dots, void *stream);
 
+/* B2 descriptors with no device allocation (no counterpart in the reference).
+ * For callers that may not allocate device memory when they need descriptors:
+ * an MD engine whose memory pool owns the GPU, code running while a stream is
+ * captured into a CUDA graph, a loop with a fixed memory budget.  All pointers
+ * are device memory supplied by the caller:
+ *   species      n_atoms, in [0, n_species)
+ *   offsets      n_atoms + 1 CSR offsets into the pair arrays
+ *   rel          n_pairs x 4 doubles (r, x, y, z of r_ij = x_j - x_i), 32-byte
+ *                aligned (the layout of fpp_structure_get_neighbors)
+ *   nbr_species  n_pairs
+ *   descriptors  n_atoms x n_d (output, FP64), norms n_atoms (output)
+ * Pairs enter when r <= cutoffs[s_i][s_j], as in B2::compute_struc.  The
+ * kernel's scratch lives in fixed device arrays of this library (8 MiB, held
+ * by every GPU that loads it until the process exits), which limits a call to
+ * n_atoms * n_species * N * (lmax+1)^2 <= 2^20 (and n_atoms <= 65536);
+ * larger calls return FPP_ERR_CAPACITY.  The first call on a device resolves
+ * the arrays' addresses and uploads constant tables: make it before any
+ * stream capture.  Calls share the scratch: two calls that overlap on the GPU
+ * (different streams, or different threads) race. */
+int fpp_b2_descriptors_noalloc(const fpp_b2 *b2, int32_t n_atoms,
+                               const int32_t *species, const int32_t *offsets,
+                               const double *rel, const int32_t *nbr_species,
+                               double *descriptors, double *norms, void *stream);
+
 /* ------------------------------------------------------------------------
  * Model: one NormalizedDotProduct kernel (sigma, power) over B2, with its
  * sparse set and weights.  Replaces the prediction state of
