@@ -53,7 +53,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -62,7 +62,18 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def wait_first(self, limit_s):
+        t0 = time.perf_counter()
+        while self.proc is not None and not self.lines and time.perf_counter() - t0 < limit_s:
+            time.sleep(0.02)
+
+    def mark_begin(self):
+        self.t_begin = time.perf_counter()
+
+    def mark_end(self):
+        self.t_end = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
@@ -74,7 +85,13 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # samples taken while the timed steps ran (one sample period of slack
+        # on each side: nvidia-smi prints a sample up to 100 ms after taking it)
+        b = getattr(self, "t_begin", -1e30)
+        e = getattr(self, "t_end", 1e30) + 0.1
+        for t, ln in self.lines:
+            if t < b or t > e:
+                continue
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -152,35 +169,44 @@ def run_ours(args):
 
     n_pairs = st.n_neighbors
     # ---- device-resident timing (value) ----
+    clocks = ClockSampler(local)
+    clocks.start()
     for k in range(W):
         step(k, _lib.FPP_PREC_MIXED)
-    check(L.fpp_structure_set_profiling(sh, 1))
-    stage = np.zeros(4)
+    clocks.wait_first(3.0)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    clocks.mark_begin()
+    torch.cuda.profiler.start()   # a profiler started with capture off sees only these steps
     ev0.record()
     for k in range(W, W + K):
         step(k, _lib.FPP_PREC_MIXED)
-        ms4 = np.zeros(4)
-        check(L.fpp_structure_stage_times(sh, ptr(ms4)))
-        stage += ms4
     ev1.record()
     torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    clocks.mark_end()
     clk = clocks.stop()
     ms_total = ev0.elapsed_time(ev1)
-    check(L.fpp_structure_set_profiling(sh, 0))
     if world > 1:
         t = torch.tensor([ms_total], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_total = float(t.item())
     ms_step = ms_total / K
     value = world * noa * K / (ms_total / 1e3)
-    stage /= K
+    # ---- per-stage device times (separate pass: the event reads synchronize) ----
+    check(L.fpp_structure_set_profiling(sh, 1))
+    stage = np.zeros(4)
+    n_stage = min(K, 20)
+    for k in range(n_stage):
+        step(W + k, _lib.FPP_PREC_MIXED)
+        ms4 = np.zeros(4)
+        check(L.fpp_structure_stage_times(sh, ptr(ms4)))
+        stage += ms4
+    check(L.fpp_structure_set_profiling(sh, 0))
+    stage /= n_stage
     # ---- end-to-end through the public API with host buffers ----
     pinned = torch.from_numpy(np.stack(disp[:K])).pin_memory()
     he = np.zeros(1)
@@ -265,9 +291,10 @@ def run_ours(args):
 
 
 def launches_per_step(n_species):
-    # neighbors: wrap_bin, bin_scatter, count, fill, sort_geom, reverse (+2 CUB
-    # scans); forward; contraction per species; adjoint, gather, reduce
-    return 6 + 2 + 1 + n_species + 3
+    # neighbors: wrap_bin, bin_scatter, enum, 2 CUB scan kernels (compiled into
+    # the library), compact_geom, reverse; descriptors: forward; contraction:
+    # one split GEMM per species; adjoint: wu, pair_force, gather, reduce
+    return 7 + 1 + n_species + 4
 
 
 def cpu_baseline(w, seconds=15.0):
@@ -345,7 +372,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")

@@ -72,6 +72,9 @@ struct StructureState {
   DevBuf bin_start;      // int32[n_bins + 1]
   DevBuf bin_cursor;     // int32[n_bins]
   DevBuf bin_atoms;      // int32[noa]
+  DevBuf binned;         // float4[noa] positions in bin order, atom index in .w
+  DevBuf slab;           // int64[noa * 256] per-atom sorted neighbor keys
+  DevBuf flags;          // int32[4] device flags (slab overflow)
   // neighbors (CSR over atoms, reference order)
   int64_t n_pairs = 0;
   DevBuf nbr_count;      // int32[noa]

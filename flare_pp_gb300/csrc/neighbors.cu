@@ -114,12 +114,17 @@ __global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
 __global__ void k_bin_scatter(int noa, const int *__restrict__ atom_bin,
                               const int *__restrict__ bin_start,
                               int *__restrict__ bin_cursor,
-                              int *__restrict__ bin_atoms) {
+                              int *__restrict__ bin_atoms,
+                              const float4 *__restrict__ wp32,
+                              float4 *__restrict__ binned) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= noa) return;
   int b = atom_bin[i];
   int slot = atomicAdd(&bin_cursor[b], 1);
   bin_atoms[bin_start[b] + slot] = i;
+  float4 q = wp32[i];
+  q.w = __int_as_float(i);  // FP32 position and atom index in one 16-byte load
+  binned[bin_start[b] + slot] = q;
 }
 
 // Exact FP64 image distance of the reference (structure.cpp:69-77):
@@ -208,6 +213,166 @@ __device__ __forceinline__ void enumerate_pairs(int i, const CellDev &cd,
             }
       }
     }
+  }
+}
+
+// Single-pass enumeration (one warp per atom): the candidate bin ranges of
+// all shifts are listed in shared memory, candidates are then tested 32 at a
+// time across ranges (FP32, exact FP64 only in the band around the cutoff),
+// accepted keys are collected and rank-sorted in shared memory and written to
+// a per-atom slab of kSlabCap keys.  An atom with more neighbors sets
+// *overflow and the caller rebuilds with the two-pass kernels below.
+constexpr int kSlabCap = 256;
+constexpr int kMaxRanges = 64;
+constexpr int kEnumWarps = 4;
+
+__global__ void __launch_bounds__(32 * kEnumWarps)
+k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restrict__ wp32,
+       const float4 *__restrict__ frac, const int *__restrict__ bin_start,
+       const float4 *__restrict__ binned, int *__restrict__ count,
+       long long *__restrict__ slab, int *__restrict__ overflow) {
+  __shared__ long long s_keys[kEnumWarps][kSlabCap];
+  __shared__ int s_rstart[kEnumWarps][kMaxRanges];
+  __shared__ int s_rpre[kEnumWarps][kMaxRanges + 1];
+  __shared__ int s_rsidx[kEnumWarps][kMaxRanges];
+  __shared__ float4 s_rshift[kEnumWarps][kMaxRanges];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kEnumWarps + w;
+  if (i >= noa) return;
+  const float4 pi = wp32[i];
+  const float4 fi = frac[i];
+  const float fik[3] = {fi.x, fi.y, fi.z};
+  int nacc = 0, nr = 0, tot = 0;
+  if (lane == 0) s_rpre[w][0] = 0;
+  __syncwarp();
+  auto flush = [&]() {
+    for (int base = 0; base < tot; base += 32) {
+      const int t = base + lane;
+      bool ok = false;
+      long long key = 0;
+      if (t < tot) {
+        int lo = 0, hi = nr - 1;  // last range with rpre <= t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_rpre[w][mid] <= t)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        const float4 q = binned[s_rstart[w][lo] + (t - s_rpre[w][lo])];
+        const float4 sh = s_rshift[w][lo];
+        const float dx = (q.x - pi.x) + sh.x;
+        const float dy = (q.y - pi.y) + sh.y;
+        const float dz = (q.z - pi.z) + sh.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const int j = __float_as_int(q.w);
+        const int sidx = s_rsidx[w][lo];
+        if (d2 < cd.in2 && d2 > cd.zero2) {
+          ok = true;
+        } else if (d2 <= cd.out2) {
+          const int s3 = sidx % cd.ns - cd.sweep;
+          const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
+          const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
+          double im[3];
+          const double dist = exact_image(wp[i], wp[j], cd, s1, s2, s3, im);
+          ok = (dist < cd.cutoff) && (dist != 0.0);
+        }
+        key = (long long)j * cd.n_shift + sidx;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (ok) {
+        const int pos = nacc + __popc(m & ((1u << lane) - 1u));
+        if (pos < kSlabCap) s_keys[w][pos] = key;
+      }
+      nacc += __popc(m);
+    }
+    nr = 0;
+    tot = 0;
+    __syncwarp();
+  };
+  for (int s1 = -cd.sweep; s1 <= cd.sweep; s1++)
+    for (int s2 = -cd.sweep; s2 <= cd.sweep; s2++)
+      for (int s3 = -cd.sweep; s3 <= cd.sweep; s3++) {
+        const int sv[3] = {s1, s2, s3};
+        int lo[3], hi[3];
+        bool empty = false;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const float c = fik[k] - (float)sv[k];
+          int l = (int)floorf((c - cd.delta32[k]) * cd.nb[k]);
+          int h = (int)floorf((c + cd.delta32[k]) * cd.nb[k]);
+          lo[k] = max(l, 0);
+          hi[k] = min(h, cd.nb[k] - 1);
+          if (lo[k] > hi[k]) empty = true;
+        }
+        if (empty) continue;
+        const int sidx = ((s1 + cd.sweep) * cd.ns + (s2 + cd.sweep)) * cd.ns + (s3 + cd.sweep);
+        const float4 sh = make_float4(
+            s1 * cd.cell32[0] + s2 * cd.cell32[3] + s3 * cd.cell32[6],
+            s1 * cd.cell32[1] + s2 * cd.cell32[4] + s3 * cd.cell32[7],
+            s1 * cd.cell32[2] + s2 * cd.cell32[5] + s3 * cd.cell32[8], 0.f);
+        for (int b0 = lo[0]; b0 <= hi[0]; b0++)
+          for (int b1 = lo[1]; b1 <= hi[1]; b1++) {
+            // bins along the last direction are contiguous: one range
+            const int bin_lo = (b0 * cd.nb[1] + b1) * cd.nb[2] + lo[2];
+            const int bin_hi = (b0 * cd.nb[1] + b1) * cd.nb[2] + hi[2];
+            const int st = bin_start[bin_lo], cn = bin_start[bin_hi + 1] - st;
+            if (cn == 0) continue;
+            if (nr == kMaxRanges) flush();
+            if (lane == 0) {
+              s_rstart[w][nr] = st;
+              s_rsidx[w][nr] = sidx;
+              s_rshift[w][nr] = sh;
+              s_rpre[w][nr + 1] = tot + cn;
+            }
+            __syncwarp();
+            tot += cn;
+            nr++;
+          }
+      }
+  flush();
+  if (lane == 0) count[i] = nacc;
+  if (nacc > kSlabCap) {
+    if (lane == 0) atomicExch(overflow, 1);
+    return;
+  }
+  for (int e = lane; e < nacc; e += 32) {
+    const long long key = s_keys[w][e];
+    int rank = 0;
+    for (int f = 0; f < nacc; f++) rank += (s_keys[w][f] < key) ? 1 : 0;
+    slab[(size_t)i * kSlabCap + rank] = key;
+  }
+}
+
+// Slab -> CSR in reference order, with the FP64 geometry of every pair.
+__global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp,
+                               const int *__restrict__ species,
+                               const int *__restrict__ offset,
+                               const long long *__restrict__ slab,
+                               long long *__restrict__ keys, int *__restrict__ nbr_i,
+                               int *__restrict__ nbr_j, int *__restrict__ nbr_s,
+                               dvec4 *__restrict__ rel, float4 *__restrict__ rel32) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= noa) return;
+  const int lane = threadIdx.x & 31;
+  const int beg = offset[i], n = offset[i + 1] - beg;
+  const dvec4 wi = wp[i];
+  for (int e = lane; e < n; e += 32) {
+    const long long key = slab[(size_t)i * kSlabCap + e];
+    const int j = (int)(key / cd.n_shift);
+    const int sidx = (int)(key - (long long)j * cd.n_shift);
+    const int s3 = sidx % cd.ns - cd.sweep;
+    const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
+    const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
+    double im[3];
+    const double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
+    const int out = beg + e;
+    keys[out] = key;
+    nbr_i[out] = i;
+    nbr_j[out] = j;
+    nbr_s[out] = species[j];
+    rel[out] = dvec4{dist, im[0], im[1], im[2]};
+    rel32[out] = make_float4((float)im[0], (float)im[1], (float)im[2], (float)dist);
   }
 }
 
@@ -452,32 +617,55 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
                                          st.bin_count.as<int>(),
                                          st.bin_start.as<int>(), nbins + 1, stream));
+  FPP_TRY(st.binned.reserve(sizeof(float4) * noa));
   k_bin_scatter<<<ceil_div(noa, tb), tb, 0, stream>>>(
       noa, st.atom_bin.as<int>(), st.bin_start.as<int>(), st.bin_cursor.as<int>(),
-      st.bin_atoms.as<int>());
+      st.bin_atoms.as<int>(), st.wrapped32.as<float4>(), st.binned.as<float4>());
   FPP_CUDA(cudaGetLastError());
 
   const int wpb = 4;  // warps per block, one atom per warp
   dim3 grid(ceil_div(noa, wpb)), block(32 * wpb);
   FPP_CUDA(cudaMemsetAsync(st.nbr_count.as<int>() + noa, 0, sizeof(int), stream));
-  k_count<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
-                                      st.wrapped32.as<float4>(),
-                                      st.frac.as<float4>(), st.bin_start.as<int>(),
-                                      st.bin_atoms.as<int>(), st.nbr_count.as<int>());
+  // single pass into the per-atom slab
+  FPP_TRY(st.slab.reserve(sizeof(long long) * (size_t)noa * kSlabCap));
+  FPP_TRY(st.flags.reserve(sizeof(int) * 4));
+  FPP_CUDA(cudaMemsetAsync(st.flags.ptr, 0, sizeof(int) * 4, stream));
+  k_enum<<<ceil_div(noa, kEnumWarps), 32 * kEnumWarps, 0, stream>>>(
+      noa, cd, st.wrapped.as<dvec4>(), st.wrapped32.as<float4>(), st.frac.as<float4>(),
+      st.bin_start.as<int>(), st.binned.as<float4>(), st.nbr_count.as<int>(),
+      st.slab.as<long long>(), st.flags.as<int>());
   FPP_CUDA(cudaGetLastError());
   tmp_bytes = st.scan_tmp.bytes;
   FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
                                          st.nbr_count.as<int>(),
                                          st.nbr_offset.as<int>(), noa + 1, stream));
-  int total = 0;
-  FPP_CUDA(cudaMemcpyAsync(&total, st.nbr_offset.as<int>() + noa, sizeof(int),
+  int hinfo[2] = {0, 0};
+  FPP_CUDA(cudaMemcpyAsync(&hinfo[0], st.nbr_offset.as<int>() + noa, sizeof(int),
                            cudaMemcpyDeviceToHost, stream));
+  FPP_CUDA(cudaMemcpyAsync(&hinfo[1], st.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost,
+                           stream));
   FPP_CUDA(cudaStreamSynchronize(stream));
   FPP_TRY(check_status(st, stream, "neighbor wrap"));
+  const bool overflow = hinfo[1] != 0;
+  int total = hinfo[0];
+  if (overflow) {
+    // some atom has more than kSlabCap neighbors: two-pass count / fill
+    k_count<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
+                                        st.wrapped32.as<float4>(), st.frac.as<float4>(),
+                                        st.bin_start.as<int>(), st.bin_atoms.as<int>(),
+                                        st.nbr_count.as<int>());
+    FPP_CUDA(cudaGetLastError());
+    tmp_bytes = st.scan_tmp.bytes;
+    FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
+                                           st.nbr_count.as<int>(),
+                                           st.nbr_offset.as<int>(), noa + 1, stream));
+    FPP_CUDA(cudaMemcpyAsync(&total, st.nbr_offset.as<int>() + noa, sizeof(int),
+                             cudaMemcpyDeviceToHost, stream));
+    FPP_CUDA(cudaStreamSynchronize(stream));
+  }
   if (total < 0) return fail(FPP_ERR_CAPACITY, "more than 2^31 neighbor pairs");
   st.n_pairs = total;
   size_t np = (size_t)std::max(total, 1);
-  FPP_TRY(st.nbr_key_tmp.reserve(sizeof(long long) * np));
   FPP_TRY(st.nbr_key.reserve(sizeof(long long) * np));
   FPP_TRY(st.nbr_i.reserve(sizeof(int) * np));
   FPP_TRY(st.nbr_j.reserve(sizeof(int) * np));
@@ -486,18 +674,28 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_TRY(st.nbr_rel32.reserve(sizeof(float4) * np));
   FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
   if (total == 0) return FPP_OK;
-  k_fill<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
-                                     st.wrapped32.as<float4>(), st.frac.as<float4>(),
-                                     st.bin_start.as<int>(), st.bin_atoms.as<int>(),
-                                     st.nbr_offset.as<int>(),
-                                     st.nbr_key_tmp.as<long long>());
-  FPP_CUDA(cudaGetLastError());
-  k_sort_geom<<<grid, block, 0, stream>>>(
-      noa, cd, st.wrapped.as<dvec4>(), st.species.as<int>(),
-      st.nbr_offset.as<int>(), st.nbr_key_tmp.as<long long>(),
-      st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_j.as<int>(),
-      st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
-  FPP_CUDA(cudaGetLastError());
+  if (!overflow) {
+    k_compact_geom<<<grid, block, 0, stream>>>(
+        noa, cd, st.wrapped.as<dvec4>(), st.species.as<int>(), st.nbr_offset.as<int>(),
+        st.slab.as<long long>(), st.nbr_key.as<long long>(), st.nbr_i.as<int>(),
+        st.nbr_j.as<int>(), st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(),
+        st.nbr_rel32.as<float4>());
+    FPP_CUDA(cudaGetLastError());
+  } else {
+    FPP_TRY(st.nbr_key_tmp.reserve(sizeof(long long) * np));
+    k_fill<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
+                                       st.wrapped32.as<float4>(), st.frac.as<float4>(),
+                                       st.bin_start.as<int>(), st.bin_atoms.as<int>(),
+                                       st.nbr_offset.as<int>(),
+                                       st.nbr_key_tmp.as<long long>());
+    FPP_CUDA(cudaGetLastError());
+    k_sort_geom<<<grid, block, 0, stream>>>(
+        noa, cd, st.wrapped.as<dvec4>(), st.species.as<int>(),
+        st.nbr_offset.as<int>(), st.nbr_key_tmp.as<long long>(),
+        st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_j.as<int>(),
+        st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
+    FPP_CUDA(cudaGetLastError());
+  }
   k_reverse<<<ceil_div(total, tb), tb, 0, stream>>>(
       total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
       st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst);

@@ -203,6 +203,52 @@ def compute_b2(c, n_species, N, lmax, dc=None, ucum=None):
     return out
 
 
+def assemble_values(structure, ns, p, norms, dp, force_dots, sbd, store_dervs):
+    """Regroup per-atom descriptors and per-pair derivative rows by central
+    species into DescriptorValues (b2.cpp:103-178, b3.cpp:56-131)."""
+    ucount = sbd["unique_neighbor_count"]
+    ucum = sbd["cumulative_neighbor_count"]
+    dv = DescriptorValues()
+    noa = structure.noa
+    n_d = p.shape[1]
+    dv.n_descriptors = n_d
+    dv.n_types = ns
+    dv.n_atoms = noa
+    dv.volume = structure.volume
+    sp = structure.species
+    dv.cumulative_type_count = [0]
+    for s in range(ns):
+        atoms = np.nonzero(sp == s)[0]
+        n_s = len(atoms)
+        nn = ucount[atoms]
+        dv.n_clusters_by_type.append(n_s)
+        dv.cumulative_type_count.append(dv.cumulative_type_count[s] + n_s)
+        dv.n_clusters += n_s
+        dv.n_neighbors_by_type.append(int(nn.sum()))
+        dv.descriptors.append(p[atoms].copy())
+        dv.descriptor_norms.append(norms[atoms].copy())
+        dv.cutoff_values.append(np.ones(n_s))
+        dv.cutoff_dervs.append(np.zeros(3 * int(nn.sum())))
+        dv.neighbor_counts.append(nn.copy())
+        dv.cumulative_neighbor_counts.append(
+            np.concatenate([[0], np.cumsum(nn)[:-1]]).astype(np.int64)
+            if n_s else np.zeros(0, np.int64))
+        dv.atom_indices.append(atoms.copy())
+        pair_rows = (np.concatenate([np.arange(ucum[a], ucum[a + 1])
+                                     for a in atoms])
+                     if n_s else np.zeros(0, np.int64)).astype(np.int64)
+        dv.neighbor_indices.append(sbd["neighbor_indices"][pair_rows])
+        dv.neighbor_coordinates.append(sbd["neighbor_coordinates"][pair_rows])
+        if store_dervs:
+            frows = (3 * pair_rows[:, None] + np.arange(3)[None]).ravel()
+            dv.descriptor_force_dervs.append(dp[frows])
+            dv.descriptor_force_dots.append(force_dots[frows])
+        else:
+            dv.descriptor_force_dervs.append(None)
+            dv.descriptor_force_dots.append(None)
+    return dv
+
+
 class B2:
     """B2 descriptor calculator (b2.h:12-53, b2.cpp:13-50)."""
 
@@ -231,45 +277,9 @@ class B2:
         ucum = sbd["cumulative_neighbor_count"]
         b2 = compute_b2(sbd["c"], ns, N, lmax,
                         sbd["dc"] if self.store_dervs else None, ucum)
-        dv = DescriptorValues()
-        noa = structure.noa
-        n_d = b2["p"].shape[1]
-        dv.n_descriptors = n_d
-        dv.n_types = ns
-        dv.n_atoms = noa
-        dv.volume = structure.volume
-        sp = structure.species
-        dv.cumulative_type_count = [0]
-        for s in range(ns):
-            atoms = np.nonzero(sp == s)[0]
-            n_s = len(atoms)
-            nn = ucount[atoms]
-            dv.n_clusters_by_type.append(n_s)
-            dv.cumulative_type_count.append(dv.cumulative_type_count[s] + n_s)
-            dv.n_clusters += n_s
-            dv.n_neighbors_by_type.append(int(nn.sum()))
-            dv.descriptors.append(b2["p"][atoms].copy())
-            dv.descriptor_norms.append(b2["norms"][atoms].copy())
-            dv.cutoff_values.append(np.ones(n_s))
-            dv.cutoff_dervs.append(np.zeros(3 * int(nn.sum())))
-            dv.neighbor_counts.append(nn.copy())
-            dv.cumulative_neighbor_counts.append(
-                np.concatenate([[0], np.cumsum(nn)[:-1]]).astype(np.int64)
-                if n_s else np.zeros(0, np.int64))
-            dv.atom_indices.append(atoms.copy())
-            pair_rows = (np.concatenate([np.arange(ucum[a], ucum[a + 1])
-                                         for a in atoms])
-                         if n_s else np.zeros(0, np.int64)).astype(np.int64)
-            dv.neighbor_indices.append(sbd["neighbor_indices"][pair_rows])
-            dv.neighbor_coordinates.append(
-                sbd["neighbor_coordinates"][pair_rows])
-            if self.store_dervs:
-                frows = (3 * pair_rows[:, None] + np.arange(3)[None]).ravel()
-                dv.descriptor_force_dervs.append(b2["dp"][frows])
-                dv.descriptor_force_dots.append(b2["force_dots"][frows])
-            else:
-                dv.descriptor_force_dervs.append(None)
-                dv.descriptor_force_dots.append(None)
+        dv = assemble_values(structure, ns, b2["p"], b2["norms"],
+                             b2.get("dp"), b2.get("force_dots"), sbd,
+                             self.store_dervs)
         # extra, for the adjoint oracle: per-atom single-bond coefficients
         dv._c = sbd["c"]
         dv._p = b2["p"]

@@ -16,6 +16,7 @@ Both are checked in tests against the stored-derivative oracle.
 """
 import numpy as np
 
+from . import b3 as b3mod
 from .b2 import single_bond_multiple_cutoffs, compute_b2
 from .basis import calculate_radial, real_sph_harm
 
@@ -98,14 +99,34 @@ def lammps_virial(structure, f):
 
 
 def descriptors(structure, settings):
-    """c (noa, sb), p (noa, n_d), |p| for a B2 setting dict."""
+    """c (noa, sb), p (noa, n_d), |p| for a B2 or B3 setting dict (B3 when
+    settings["kind"] == "B3"; its c is complex)."""
     ns, N, lmax = settings["n_species"], settings["N"], settings["lmax"]
+    if settings.get("kind", "B2") == "B3":
+        sbd = b3mod.complex_single_bond(structure, ns, N, lmax, settings["r1"],
+                                        settings["rcut"], settings["cutoff_function"],
+                                        store_dervs=False)
+        out = b3mod.compute_b3(sbd["c"], ns, N, lmax)
+        return sbd["c"], out["p"], out["norms"]
     sbd = single_bond_multiple_cutoffs(structure, ns, N, lmax, settings["r1"],
                                        settings["cutoffs"],
                                        settings["cutoff_function"],
                                        store_dervs=False)
     b2 = compute_b2(sbd["c"], ns, N, lmax)
     return sbd["c"], b2["p"], b2["norms"]
+
+
+def descriptor_pair_forces(structure, settings, c, w, strict=False):
+    """f_ij from dE/dp = w through the descriptor's adjoint (B2 or B3)."""
+    ns, N, lmax = settings["n_species"], settings["N"], settings["lmax"]
+    if settings.get("kind", "B2") == "B3":
+        u = b3mod.b3_adjoint(c, w, ns, N, lmax)
+        return b3mod.pair_forces(structure, u, ns, N, lmax, settings["r1"],
+                                 settings["rcut"], settings["cutoff_function"])
+    u = b2_adjoint(c, w, ns, N, lmax)
+    return pair_forces(structure, u, ns, N, lmax, settings["r1"],
+                       settings["cutoffs"], settings["cutoff_function"],
+                       strict=strict)
 
 
 def beta_form(structure, settings, beta_matrices, power=2):
@@ -137,10 +158,7 @@ def beta_form(structure, settings, beta_matrices, power=2):
             e = (P @ bv) / nrm
             w[idx] = bv[None, :] / nrm[:, None] - e[:, None] * P / q[:, None]
         E[idx] = e
-    u = b2_adjoint(c, w, ns, N, lmax)
-    f = pair_forces(structure, u, ns, N, lmax, settings["r1"],
-                    settings["cutoffs"], settings["cutoff_function"],
-                    strict=True)
+    f = descriptor_pair_forces(structure, settings, c, w, strict=True)
     F = gather_forces(structure, f)
     return dict(energy=E.sum(), atom_energies=E, forces=F,
                 virial=lammps_virial(structure, f),
@@ -176,9 +194,7 @@ def kernel_form(structure, settings, sparse_descriptors, alpha, sigma, power):
         G = C @ Dh                                      # (n_s, n_d)
         zc = np.einsum("ik,ik->i", C, z)
         w[idx] = (G - zc[:, None] * Ph) / norms[idx, None]
-    u = b2_adjoint(c, w, ns, N, lmax)
-    f = pair_forces(structure, u, ns, N, lmax, settings["r1"],
-                    settings["cutoffs"], settings["cutoff_function"])
+    f = descriptor_pair_forces(structure, settings, c, w)
     F = gather_forces(structure, f)
     S = flare_stress(structure, f)
     mean = np.concatenate([[E.sum()], F.reshape(-1), S])

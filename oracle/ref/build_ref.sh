@@ -1,6 +1,7 @@
 #!/bin/sh
 # Build oracle/_ref/libflare_ref.so from the reference's own L0 math sources
-# (radial.cpp, cutoffs.cpp, y_grad.cpp), compiled where they lie in the
+# (radial.cpp, cutoffs.cpp, y_grad.cpp, descriptors/wigner3j.cpp), compiled
+# where they lie in the
 # reference tree, plus oracle/ref/ref_shim.cpp.  Only the tiny Eigen stand-in
 # in oracle/ref/stub is added; no reference file is copied or modified.
 # Usage: oracle/ref/build_ref.sh [reference_root]
@@ -17,5 +18,6 @@ mkdir -p "$OUT"
 g++ -O2 -std=c++17 -fPIC -shared -ffp-contract=off \
   -I"$HERE/stub" -I"$SRC" -I"$SRC/descriptors" \
   "$SRC/radial.cpp" "$SRC/cutoffs.cpp" "$SRC/y_grad.cpp" \
+  "$SRC/descriptors/wigner3j.cpp" \
   "$HERE/ref_shim.cpp" -o "$OUT/libflare_ref.so"
 echo "built $OUT/libflare_ref.so"

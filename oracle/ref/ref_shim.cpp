@@ -1,5 +1,6 @@
 // extern "C" entry points over the reference's own L0 math files
-// (src/flare_pp/radial.cpp, cutoffs.cpp, y_grad.cpp), compiled unmodified
+// (src/flare_pp/radial.cpp, cutoffs.cpp, y_grad.cpp, descriptors/wigner3j.cpp),
+// compiled unmodified
 // from the reference tree by oracle/ref/build_ref.sh.  Used only to record
 // golden vectors that pin the oracle's restatement.
 #include <cstring>
@@ -9,6 +10,7 @@
 #include "radial.h"
 #include "cutoffs.h"
 #include "y_grad.h"
+#include "wigner3j.h"
 
 extern "C" {
 
@@ -59,6 +61,14 @@ int ref_calculate_radial(const char *basis, const char *cutoff, double x,
   std::memcpy(gx, b.data(), N * sizeof(double));
   std::memcpy(gy, c.data(), N * sizeof(double));
   std::memcpy(gz, d.data(), N * sizeof(double));
+  return 0;
+}
+
+// compute_coeffs (wigner3j.cpp:5): the (lmax+1)^6 table of Wigner 3j symbols.
+int ref_compute_coeffs(int lmax, double *out, long n) {
+  Eigen::VectorXd w = compute_coeffs(lmax);
+  if (w.size() != n) return -1;
+  for (long i = 0; i < n; i++) out[i] = w(i);
   return 0;
 }
 }

@@ -15,6 +15,12 @@ def settings(n_species, N, lmax, rc, cutoffs=None, cutoff_function="quadratic"):
                 cutoff_function=cutoff_function)
 
 
+def settings_b3(n_species, N, lmax, rc, cutoff_function="quadratic"):
+    return dict(kind="B3", n_species=n_species, N=N, lmax=lmax, r1=0.0, rcut=rc,
+                cutoffs=np.full((n_species, n_species), rc),
+                cutoff_function=cutoff_function)
+
+
 def config1_model(n_frames=5, n_sparse=50, power=2):
     """FCC Al 108 atoms, 5 LJ-labelled frames, 50 sparse environments:
     trained with the oracle's SparseGP (E, F, S labels, QR solve)."""

@@ -1,12 +1,14 @@
 """Record golden vectors from the reference's own L0 math.
 
 Builds oracle/_ref/libflare_ref.so from the reference sources
-(oracle/ref/build_ref.sh: radial.cpp, cutoffs.cpp, y_grad.cpp compiled where
-they lie) and evaluates:
+(oracle/ref/build_ref.sh: radial.cpp, cutoffs.cpp, y_grad.cpp and
+descriptors/wigner3j.cpp compiled where they lie) and evaluates:
   * get_Y (y_grad.cpp:667) up to l = 10 at seeded random vectors,
   * get_complex_Y (y_grad.cpp:24) up to l = 6,
   * calculate_radial (radial.cpp:344) with the chebyshev basis and the
-    quadratic and cosine cutoffs (cutoffs.cpp:44-73), N = 12.
+    quadratic and cosine cutoffs (cutoffs.cpp:44-73), N = 12,
+  * compute_coeffs (descriptors/wigner3j.cpp:5), the Wigner 3j tables of
+    B3, for lmax = 0..4 (nonzero entries as index/value pairs).
 Writes tests/golden/l0_golden.npz.  Run from the repository root:
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -74,6 +76,14 @@ def main(ref_root="/root/reference"):
                 G[k, i] = bufs[k]
         out[f"g_{cut}"] = G
     out["rad_N"], out["rad_rc"], out["rad_r1"] = N, rc, r1
+    # Wigner 3j tables of B3
+    for lmax in range(5):
+        n = (lmax + 1) ** 6
+        tab = np.zeros(n)
+        assert lib.ref_compute_coeffs(lmax, tab.ctypes.data_as(D), ctypes.c_long(n)) == 0
+        nz = np.nonzero(tab)[0]
+        out[f"w3j_{lmax}_idx"] = nz.astype(np.int32)
+        out[f"w3j_{lmax}_val"] = tab[nz]
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "l0_golden.npz"), **out)
     print("wrote tests/golden/l0_golden.npz")
 

@@ -152,3 +152,83 @@ def test_qr_solve_matches_scipy():
     import scipy.linalg as sla
     ref = sla.lstsq(A, b)[0]
     np.testing.assert_allclose(gp.alpha, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+# ---------------------------------------------------------------- B3 ----
+from oracle import b3 as ob3  # noqa: E402
+
+
+@pytest.mark.parametrize("lmax", [0, 1, 2, 3, 4])
+def test_b3_wigner_tables_match_reference(gold, lmax):
+    # descriptors/wigner3j.cpp compute_coeffs, including the 57 entries of its
+    # lmax = 4 table that evaluate to 0
+    tab = np.zeros((lmax + 1) ** 6)
+    tab[gold[f"w3j_{lmax}_idx"]] = gold[f"w3j_{lmax}_val"]
+    np.testing.assert_allclose(ob3.w3j_table(lmax), tab, rtol=0, atol=1e-15)
+
+
+def test_complex_harmonics_match_reference(gold):
+    v = gold["Y_vecs"]
+    Y = ob3.complex_sph_harm(v[:, 0], v[:, 1], v[:, 2], 6)
+    for mine, key in zip(Y, ("Yc", "Ycx", "Ycy", "Ycz")):
+        ref = gold[key][:, 0::2] + 1j * gold[key][:, 1::2]
+        np.testing.assert_allclose(mine, ref, rtol=1e-12, atol=1e-12)
+
+
+def _b3_structure(rot=None, shift=None):
+    rng = np.random.default_rng(11)
+    cell = np.array([[6.6, 0.1, 0.0], [0.2, 6.9, 0.0], [0.0, 0.3, 7.1]])
+    pos = rng.uniform(0, 6.5, size=(10, 3))
+    sp = rng.integers(0, 2, size=10)
+    if shift is not None:
+        pos = pos + shift
+    if rot is not None:
+        cell, pos = cell @ rot.T, pos @ rot.T
+    return cell, sp, pos
+
+
+def test_b3_rotation_invariance():
+    # ctests/test_descriptor.cpp:9-48 (1e-10)
+    d = ob3.B3("chebyshev", "quadratic", [0, 3.8], [], [2, 3, 3])
+    cell, sp, pos = _b3_structure()
+    p0 = Structure(cell, sp, pos, 4.0, [d]).descriptors[0]
+    a, b = 0.7, 1.1
+    Rz = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    Rx = np.array([[1, 0, 0], [0, np.cos(b), -np.sin(b)], [0, np.sin(b), np.cos(b)]])
+    cell, sp, pos = _b3_structure(rot=Rx @ Rz)
+    p1 = Structure(cell, sp, pos, 4.0, [d]).descriptors[0]
+    for s in range(2):
+        np.testing.assert_allclose(p1.descriptors[s], p0.descriptors[s], atol=1e-10)
+
+
+def test_b3_kernel_route_and_finite_difference():
+    d = ob3.B3("chebyshev", "quadratic", [0, 3.8], [], [2, 2, 2])
+    cell, sp, pos = _b3_structure()
+    s = Structure(cell, sp, pos, 4.0, [d])
+    dv = s.descriptors[0]
+    kern = NormalizedDotProduct(1.3, 2)
+    envs = ClusterDescriptor(dv)
+    K = kern.envs_struc(envs, dv)
+    alpha = np.random.default_rng(4).normal(size=envs.n_clusters)
+    st = fixtures.settings_b3(2, 2, 2, 3.8)
+    kf = predict.kernel_form(s, st, envs, alpha, 1.3, 2)
+    # adjoint route (no stored derivatives) == stored-derivative route
+    np.testing.assert_allclose(kf["mean_efs"], K.T @ alpha, rtol=1e-9, atol=1e-9)
+    # forces are -dE/dx (central differences)
+    h = 1e-5
+    for a in (0, 7):
+        for c in range(3):
+            pp, pm = pos.copy(), pos.copy()
+            pp[a, c] += h
+            pm[a, c] -= h
+            ep = predict.kernel_form(Structure(cell, sp, pp, 4.0), st, envs, alpha, 1.3, 2)
+            em = predict.kernel_form(Structure(cell, sp, pm, 4.0), st, envs, alpha, 1.3, 2)
+            fd = -(ep["energy"] - em["energy"]) / (2 * h)
+            assert abs(fd - kf["forces"][a, c]) < 1e-6
+    # beta form == kernel form (tests/test_lammps.py:97-102)
+    beta = kern.compute_map_coeff_pow2(envs, alpha)
+    B = predict.unpack_beta(beta, dv.n_descriptors)
+    bf = predict.beta_form(s, st, B)
+    assert abs(bf["energy"] - kf["energy"]) < 1e-9
+    np.testing.assert_allclose(bf["forces"], kf["forces"], atol=1e-9)
+    np.testing.assert_allclose(bf["stress"], kf["stress"], atol=1e-9)
