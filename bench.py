@@ -26,9 +26,33 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "E+F atoms/s at 32k atoms"
 UNIT = "atoms/s"
-WORKLOAD = "bcc_alloy_32k (32768 atoms, 2 species, B2 N=12 lmax=4, rc 5.5, 2000 sparse/species, power 2)"
+# name -> (metric, description, data, model builder, descriptor settings)
+WORKLOADS = {
+    "bcc_alloy_32k": (
+        "E+F atoms/s at 32k atoms",
+        "bcc_alloy_32k (32768 atoms, 2 species, B2 N=12 lmax=4, rc 5.5, "
+        "2000 sparse/species, power 2)",
+        "synthetic (seeded BCC alloy; model fitted to Lennard-Jones site energies)",
+        "bcc_alloy_32k_model",
+        dict(kind="B2", n_species=2, N=12, lmax=4, r1=0.0, rcut=5.5,
+             cutoffs=np.full((2, 2), 5.5))),
+    "b3_fcc_1m": (
+        "E+F atoms/s at 1M atoms (B3)",
+        "b3_fcc_1m (1048576 atoms FCC Al 64^3 cells, B3 N=6 lmax=3, rc 5.0, "
+        "500 sparse, power 2)",
+        "synthetic (seeded FCC Al; model fitted to Lennard-Jones site energies)",
+        "fcc_al_b3_1m_model",
+        dict(kind="B3", n_species=1, N=6, lmax=3, r1=0.0, rcut=5.0,
+             cutoffs=np.full((1, 1), 5.0))),
+}
+METRIC, WORKLOAD, DATA = WORKLOADS["bcc_alloy_32k"][:3]
+SETTINGS = WORKLOADS["bcc_alloy_32k"][4]
+
+
+def select_workload(name):
+    global METRIC, WORKLOAD, DATA, SETTINGS
+    METRIC, WORKLOAD, DATA, _, SETTINGS = WORKLOADS[name]
 
 
 def dist_env():
@@ -117,9 +141,13 @@ def measured_peaks():
                 "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profiled_traffic():
+PROFILE_FILES = {"bcc_alloy_32k": "contraction_bcc32k.txt",
+                 "b3_fcc_1m": "contraction_b3_fcc1m.txt"}
+
+
+def profiled_traffic(workload="bcc_alloy_32k"):
     """DRAM bytes per contraction launch from the committed ncu summary."""
-    fn = os.path.join(ROOT, "profiles", "contraction_bcc32k.txt")
+    fn = os.path.join(ROOT, "profiles", PROFILE_FILES[workload])
     try:
         txt = open(fn).read()
     except OSError:
@@ -128,11 +156,10 @@ def profiled_traffic():
     return float(m.group(1)) if m else None
 
 
-def build_workload(device):
-    import torch
+def build_workload(device, name="bcc_alloy_32k"):
     from flare_pp_gb300 import synth, Structure
-    w = synth.bcc_alloy_32k_model(device=device)
-    st = Structure(w["cell"], w["species"], w["positions"], 5.5)
+    w = getattr(synth, WORKLOADS[name][3])(device=device)
+    st = Structure(w["cell"], w["species"], w["positions"], SETTINGS["rcut"])
     return w, st
 
 
@@ -146,7 +173,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     from flare_pp_gb300 import _lib
     from flare_pp_gb300._lib import check, lib, ptr
-    w, st = build_workload(dev)
+    w, st = build_workload(dev, args.workload)
     gp = w["gp"]
     noa = st.noa
     gp._ensure_mapped()
@@ -252,13 +279,15 @@ def run_ours(args):
     contract_ms = stage[2]
     achieved = flop / (contract_ms * 1e-3) / 1e12
     peak = float(peaks["bf16_tflops"])
-    roof = {"kernel": "k_split_gemm (contraction P.beta, 2 launches/step)",
+    nsp = SETTINGS["n_species"]
+    roof = {"kernel": f"k_split_gemm (contraction P.beta, {nsp} launch"
+                      f"{'es' if nsp > 1 else ''}/step)",
             "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "peak_source": f"{peak_src} bf16 dense burst",
             "note": "algorithmic 2*n_atoms*n_d^2 FLOP per step; the split-fp16 form "
                     "issues 3 MMAs per product",
-            "traffic": profiled_traffic()}
+            "traffic": profiled_traffic(args.workload)}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(w, seconds=args.cpu_seconds)
@@ -267,7 +296,7 @@ def run_ours(args):
         "steps": K, "warmup": W, "ms_per_step": round(ms_step, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp16x3/fp32 (descriptors fp32, contraction split-fp16, accumulate fp32)",
-        "data": "synthetic (seeded BCC alloy; model fitted to Lennard-Jones site energies)",
+        "data": DATA,
         "config": {"workload": WORKLOAD, "n_atoms": noa, "n_pairs": int(n_pairs),
                    "n_descriptors": nd, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (per-step working set ~0.6 GB)"},
@@ -280,7 +309,7 @@ def run_ours(args):
         "fp64_gpu": {"value": round(world * noa / (fp64_ms / 1e3), 1), "unit": UNIT,
                      "ms_per_step": round(fp64_ms, 3)},
         "errors_vs_fp64": {"energy_per_atom_eV": err_e, "force_max_eV_per_A": err_f},
-        "gpu_launches": int(K * launches_per_step(2)),
+        "gpu_launches": int(K * launches_per_step(SETTINGS["n_species"])),
         "clocks": clk,
         "cpu_baseline": cpu,
     }
@@ -291,10 +320,11 @@ def run_ours(args):
 
 
 def launches_per_step(n_species):
-    # neighbors: wrap_bin, bin_scatter, enum, 2 CUB scan kernels (compiled into
-    # the library), compact_geom, reverse; descriptors: forward; contraction:
-    # one split GEMM per species; adjoint: wu, pair_force, gather, reduce
-    return 7 + 1 + n_species + 4
+    # neighbors: wrap_bin, bin_scatter, enum, compact_geom, reverse and two
+    # CUB exclusive scans of two kernels each (compiled into the library);
+    # descriptors: forward; contraction: one split GEMM per species; adjoint:
+    # wu, pair_force, gather, reduce
+    return 9 + 1 + n_species + 4
 
 
 def cpu_baseline(w, seconds=15.0):
@@ -307,8 +337,7 @@ def cpu_baseline(w, seconds=15.0):
     nd = gp._model.n_descriptors
     beta = gp.mapping_coefficients
     B = opred.unpack_beta(beta, nd)
-    settings = dict(n_species=2, N=12, lmax=4, r1=0.0,
-                    cutoffs=np.full((2, 2), 5.5))
+    settings = SETTINGS
     threads = cfast.max_threads()
     noa = len(w["species"])
     n = 256
@@ -337,11 +366,11 @@ def run_reference(args):
     from oracle import cfast
     from oracle import predict as opred
     dev = torch.device("cuda", local) if torch.cuda.is_available() else None
-    w, st = build_workload(dev if dev is not None else "cpu")
+    w, st = build_workload(dev if dev is not None else "cpu", args.workload)
     gp = w["gp"]
     gp._ensure_mapped()
     B = opred.unpack_beta(gp.mapping_coefficients, gp._model.n_descriptors)
-    settings = dict(n_species=2, N=12, lmax=4, r1=0.0, cutoffs=np.full((2, 2), 5.5))
+    settings = SETTINGS
     threads = cfast.max_threads()
     noa = len(w["species"])
     sample = min(noa, args.ref_atoms)
@@ -359,7 +388,7 @@ def run_reference(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-            "data": "synthetic (seeded BCC alloy; model fitted to Lennard-Jones site energies)",
+            "data": DATA,
             "config": {"workload": WORKLOAD, "n_atoms": noa, "parallelism": "host threads"},
             "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads,
                              "kind": "port",
@@ -378,7 +407,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-atoms", type=int, default=2048)
+    ap.add_argument("--workload", default="bcc_alloy_32k", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    select_workload(args.workload)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -42,6 +42,7 @@ SIGNATURES = {
     "fpp_structure_set_profiling": (_c_int, [_vp, _c_int]),
     "fpp_structure_stage_times": (_c_int, [_vp, _vp]),
     "fpp_b2_create": (_c_int, [_cp, _cp, _vp, _i32, _vp, _i32, _vp, _vp, _P(_vp)]),
+    "fpp_b3_create": (_c_int, [_cp, _cp, _vp, _i32, _vp, _i32, _vp, _P(_vp)]),
     "fpp_b2_destroy": (_c_int, [_vp]),
     "fpp_b2_n_descriptors": (_c_int, [_vp, _P(_i32)]),
     "fpp_b2_pair_count": (_c_int, [_vp, _vp, _P(_i64), _vp]),

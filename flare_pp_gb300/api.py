@@ -300,6 +300,35 @@ class B2(_Handle):
 
 
 # --------------------------------------------------------------------------
+class B3(B2):
+    """B3 bispectrum (b3.h:29-33): one cutoff, radial_hyps[1], for every
+    species pair; lmax <= 4.  Same calls as B2 (compute_struc returns the
+    stored force derivatives of b3.cpp:206-240; models built on it predict
+    through the B3 adjoint)."""
+
+    def __init__(self, radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
+                 descriptor_settings):
+        self.radial_basis = radial_basis
+        self.cutoff_function = cutoff_function
+        self.radial_hyps = list(map(float, radial_hyps))
+        self.cutoff_hyps = list(map(float, cutoff_hyps))
+        self.descriptor_settings = [int(v) for v in descriptor_settings]
+        ns = self.descriptor_settings[0]
+        self.cutoffs = np.full((ns, ns), self.radial_hyps[1])
+        self.store_dervs = True
+        rh = f64(self.radial_hyps)
+        ch = f64(self.cutoff_hyps) if self.cutoff_hyps else f64([0.0])
+        ds = i32(self.descriptor_settings)
+        h = _lib.ctypes.c_void_p()
+        check(lib().fpp_b3_create(radial_basis.encode(), cutoff_function.encode(),
+                                  ptr(rh), len(rh), ptr(ch), len(self.cutoff_hyps),
+                                  ptr(ds), _lib.ctypes.byref(h)))
+        self._h = h.value
+        n = _lib.ctypes.c_int32()
+        check(lib().fpp_b2_n_descriptors(self._h, _lib.ctypes.byref(n)))
+        self.n_descriptors = n.value
+
+
 class NormalizedDotProduct:
     """k = sigma^2 (d.p / |d||p|)^power (normalized_dot_product.h:11-73)."""
 

@@ -20,9 +20,13 @@
 
 #include "basis.cuh"
 #include "b2_kernels.h"
+#include "b3.cuh"
 #include "common.cuh"
 
 namespace fpp {
+
+int upload_descriptor_tables(cudaStream_t stream) { return upload_b3_tables(stream); }
+int b3_n_ls_host(int lmax) { return b3_n_ls(lmax); }
 
 int upload_harmonic_tables(cudaStream_t stream) {
   HarmonicTables t;
@@ -91,7 +95,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <typename T> struct FwdLayout {
   int W, GP;            // window, padded radial stride (multiple of 4)
   size_t stage, csum;   // bytes: staging (reused for p), c sums + compensation
-  size_t lists, total;
+  size_t lists, cz;     // species lists; B3: complex c (re, im), rows padded to H+1
+  size_t total;
 };
 
 template <typename T>
@@ -105,7 +110,10 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
   L.stage = ((st > pb ? st : pb) + 15) & ~(size_t)15;
   L.csum = (sizeof(T) * 2 * (size_t)sb + 15) & ~(size_t)15;
   L.lists = (sizeof(int) * ((size_t)a.n_species * L.W + 2 * L.W + a.n_species) + 15) & ~(size_t)15;
-  L.total = L.stage + L.csum + L.lists;
+  L.cz = a.kind == kB3
+             ? (sizeof(T) * 2 * (size_t)a.n_species * a.N * (a.H + 1) + 15) & ~(size_t)15
+             : 0;
+  L.total = L.stage + L.csum + L.lists + L.cz;
   return L;
 }
 
@@ -244,11 +252,20 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     c_out[(size_t)atom * sb + k] = v;
   }
   __syncwarp();
-  // ---- 3. B2 contraction per radial pair q, all l ----
+  // ---- 3. B2 contraction per radial pair q, all l (B3: per radial triple) ----
   const int L1 = a.lmax + 1;
   const int nd = a.n_d;
-  const int npair = nd / L1;
+  const int npair = a.kind == kB3 ? 0 : nd / L1;
   Acc<T> nacc;
+  if (a.kind == kB3) {
+    T *zr = reinterpret_cast<T *>(base + Lay.stage + Lay.csum + Lay.lists);
+    T *zi = zr + (size_t)NS * N * (H + 1);
+    b3_to_complex<T>(c_s, NS * N, H, zr, zi, lane);
+    __syncwarp();
+    b3_contract<T>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, zr, zi, p_s, lane);
+    __syncwarp();
+    for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
+  }
   for (int q = lane; q < npair; q += 32) {
     const int pr = pair_tab[q];
     const int n1 = pr & 0xffff, n2 = pr >> 16;
@@ -282,32 +299,14 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   }
 }
 
-// ---------------------------------------------------------------------------
-// Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
-// u = dE/dc = (W + W^T) c per l, written to global memory.
-// ---------------------------------------------------------------------------
+// w = dE/dp of one atom into w_s[nd] (all lanes), returning the atom energy:
+// from the contraction V (mapped power 2), the beta vector (power 1), or
+// given per operand row (kernel form).
 template <typename T>
-__global__ void __launch_bounds__(128)
-k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
-        const int *__restrict__ row_of_atom, const T *__restrict__ c_in,
-        const double *__restrict__ norm_in, double *__restrict__ atom_e,
-        T *__restrict__ u_out) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nwarps = blockDim.x >> 5;
-  const int atom = blockIdx.x * nwarps + warp;
-  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
-  const int sb = NS * N * H, nr = NS * N;
-  const int L1 = a.lmax + 1;
-  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);  // [nd]
-  T *c_s = w_s + nd;                     // [sb]
-  if (atom >= a.noa) return;
-  const int si = species[atom];
-  const int row = row_of_atom[atom];
-  const double nrm = norm_in[atom];
-  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
-
+__device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, int si,
+                                            int row, double nrm, T *__restrict__ w_s,
+                                            int lane) {
+  const int nd = a.n_d;
   double e = 0.0;
   if ((g.mode == kWFromV2 || g.mode == kWFromV1) && g.phat64) {
     const bool empty = nrm * nrm < g.empty_thresh;
@@ -364,6 +363,36 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
     for (int d = lane; d < nd; d += 32) w_s[d] = T(g.w_given[(size_t)row * g.ldp + d]);
     e = g.e_given ? g.e_given[row] : 0.0;
   }
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
+// u = dE/dc = (W + W^T) c per l, written to global memory.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
+        const int *__restrict__ row_of_atom, const T *__restrict__ c_in,
+        const double *__restrict__ norm_in, double *__restrict__ atom_e,
+        T *__restrict__ u_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int atom = blockIdx.x * nwarps + warp;
+  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
+  const int sb = NS * N * H, nr = NS * N;
+  const int L1 = a.lmax + 1;
+  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
+  T *w_s = reinterpret_cast<T *>(base);  // [nd]
+  T *c_s = w_s + nd;                     // [sb]
+  if (atom >= a.noa) return;
+  const int si = species[atom];
+  const int row = row_of_atom[atom];
+  const double nrm = norm_in[atom];
+  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
+
+  const double e = adjoint_w<T>(a, g, si, row, nrm, w_s, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
@@ -386,6 +415,220 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
       for (int n2 = n1 + 1; n2 < nr; n2++) acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
       u_out[(size_t)atom * sb + n1 * H + lm] = acc;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// B3 adjoint, part 1 (one warp per atom): w = dE/dp, then the holomorphic
+// derivative u = dE/dc of the complex coefficients,
+//   u[n1, l1m1] += w_q W c[n2,l2m2] c[n3,l3m3]   (and the two permutations),
+// accumulated by each lane into its own column of shared memory (no atomics;
+// the 32 columns are summed in a fixed order), and mapped back to dE/dc_real
+// (the inverse of b3_to_complex's linear map), written to global memory.
+// ---------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a) {
+  const size_t nr = (size_t)a.n_species * a.N;
+  size_t b = sizeof(T) * ((size_t)a.n_d + 2 * nr * (a.H + 1) + 2 * nr * a.H +
+                          2 * nr * a.H * 32);
+  return (b + 15) & ~(size_t)15;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
+        const int *__restrict__ row_of_atom, const int *__restrict__ tri,
+        const T *__restrict__ c_in, const double *__restrict__ norm_in,
+        double *__restrict__ atom_e, T *__restrict__ u_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int atom = blockIdx.x * nwarps + warp;
+  const int H = a.H, H1 = a.H + 1, nd = a.n_d;
+  const int nr = a.n_species * a.N, sb = nr * H;
+  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
+  T *w_s = reinterpret_cast<T *>(base);  // [nd]
+  T *zr = w_s + nd;                      // [nr][H+1]
+  T *zi = zr + (size_t)nr * H1;
+  T *ur = zi + (size_t)nr * H1;          // [sb] summed u (re)
+  T *ui = ur + sb;                       // [sb] (im)
+  T *up = ui + sb;                       // [sb][2][32] per-lane partial u
+  if (atom >= a.noa) return;
+  const int si = species[atom];
+  const int row = row_of_atom[atom];
+  const double nrm = norm_in[atom];
+  // real c staged through ur (free until the reduction below)
+  for (int k = lane; k < sb; k += 32) ur[k] = c_in[(size_t)atom * sb + k];
+  const double e = adjoint_w<T>(a, g, si, row, nrm, w_s, lane);
+  if (lane == 0) atom_e[atom] = e;
+  __syncwarp();
+  b3_to_complex<T>(ur, nr, H, zr, zi, lane);
+  for (int k = 0; k < 2 * sb; k++) up[(size_t)k * 32 + lane] = T(0);
+  __syncwarp();
+  const int *beg = c_b3.beg + c_b3.ls_off[a.lmax];
+  const int n_ls = a.n_ls;
+  for (int t = 0; t < n_ls; t++) {
+    const int e0 = beg[t], e1 = beg[t + 1];
+    for (int r0 = 0; r0 < a.n_tri; r0 += 32) {
+      const int r = r0 + lane;
+      if (r >= a.n_tri) continue;
+      const T wq = w_s[r * n_ls + t];
+      const int tr = tri[r];
+      const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
+      for (int q = e0; q < e1; q++) {
+        const unsigned ix = c_b3.idx[q];
+        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
+        const T f = wq * T(c_b3.w[q]);
+        const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
+        const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
+        const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
+        T *p1 = up + (size_t)(2 * (n1 * H + i1)) * 32 + lane;
+        T *p2 = up + (size_t)(2 * (n2 * H + i2)) * 32 + lane;
+        T *p3 = up + (size_t)(2 * (n3 * H + i3)) * 32 + lane;
+        p1[0] += f * (br * cr - bi * ci);
+        p1[32] += f * (br * ci + bi * cr);
+        p2[0] += f * (ar * cr - ai * ci);
+        p2[32] += f * (ar * ci + ai * cr);
+        p3[0] += f * (ar * br - ai * bi);
+        p3[32] += f * (ar * bi + ai * br);
+      }
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < sb; k += 32) {
+    T sr = T(0), sm = T(0);
+    for (int j = 0; j < 32; j++) {
+      const int jj = (j + lane) & 31;  // rotated: the lanes read different banks
+      sr += up[(size_t)(2 * k) * 32 + jj];
+      sm += up[(size_t)(2 * k + 1) * 32 + jj];
+    }
+    ur[k] = sr;
+    ui[k] = sm;
+  }
+  __syncwarp();
+  // dE/dc_real: for m > 0 with u+ = u[l, m], u- = u[l, -m], s = (-1)^m:
+  //   dE/dR = (s Re u+ + Re u-) / sqrt 2,  dE/dS = (Im u- - s Im u+) / sqrt 2
+  const T is2 = T(0.70710678118654752440);
+  for (int k = lane; k < sb; k += 32) {
+    const int n = k / H, lm = k - n * H;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) l++;
+    const int m = lm - l * l - l;
+    const int am = m < 0 ? -m : m;
+    const int kp = n * H + l * l + l + am, km = n * H + l * l + l - am;
+    const T sg = (am & 1) ? T(-1) : T(1);
+    T v;
+    if (m == 0)
+      v = ur[k];
+    else if (m > 0)
+      v = (sg * ur[kp] + ur[km]) * is2;
+    else
+      v = (ui[km] - sg * ui[kp]) * is2;
+    u_out[(size_t)atom * sb + k] = v;
+  }
+}
+
+// Stored B3 derivatives (FP64) for a list of structure pairs, as b3.cpp:
+// 206-240: rows 3*idx + comp of dB3_i / dr_ij and force_dots = dp . p_i.
+// One warp per pair; lanes take radial triples.
+__host__ __device__ inline size_t b3_dp_smem_per_warp(const B2Args &a) {
+  const size_t nr = (size_t)a.n_species * a.N;
+  return sizeof(double) * (2 * nr * (a.H + 1) + 3 * (size_t)a.N * a.H +
+                           6 * (size_t)a.N * (a.H + 1) + nr * a.H + 2 * a.N + 4 * a.H);
+}
+
+__global__ void __launch_bounds__(128)
+k_b3_dp(B2Args a, int npl, const int *__restrict__ plist, const int *__restrict__ nbr_i,
+        const int *__restrict__ nbr_s, const dvec4 *__restrict__ rel,
+        const int *__restrict__ tri, const double *__restrict__ c_in,
+        const double *__restrict__ p_in, double *__restrict__ dp, int ldd,
+        double *__restrict__ force_dots) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int idx = blockIdx.x * nwarps + warp;
+  const int N = a.N, H = a.H, H1 = a.H + 1, nd = a.n_d;
+  const int nr = a.n_species * N;
+  double *base = reinterpret_cast<double *>(smem_raw) + (size_t)warp * (b3_dp_smem_per_warp(a) / 8);
+  double *zr = base;                    // [nr][H+1] complex c of atom i
+  double *zi = zr + (size_t)nr * H1;
+  double *dcr = zi + (size_t)nr * H1;   // [3][N][H] real derivative (s_j block)
+  double *dzr = dcr + 3 * N * H;        // [3][N][H+1] complex derivative
+  double *dzi = dzr + 3 * N * H1;
+  double *c_s = dzi + 3 * N * H1;       // [nr][H] real c
+  double *gb = c_s + (size_t)nr * H;    // [N] g, [N] dg
+  double *yb = gb + 2 * N;              // [H] Y, [3H] dY
+  if (idx >= npl) return;
+  const int p = plist[idx];
+  const int i = nbr_i[p], sj = nbr_s[p];
+  const dvec4 rd = rel[p];
+  const double rcut = a.cutoffs[0];
+  for (int k = lane; k < nr * H; k += 32) c_s[k] = c_in[(size_t)i * nr * H + k];
+  if (lane == 0) {
+    radial_basis<double>(rd.x, a.r1, rcut, N, a.cutoff_kind, gb, gb + N, 1);
+    real_harmonics<double>(rd.y, rd.z, rd.w, a.lmax, yb, yb + H, 1);
+  }
+  __syncwarp();
+  const double uv[3] = {rd.y / rd.x, rd.z / rd.x, rd.w / rd.x};
+  for (int k = lane; k < 3 * N * H; k += 32) {
+    const int comp = k / (N * H), rem = k - comp * N * H, n = rem / H, lm = rem - n * H;
+    dcr[k] = gb[N + n] * uv[comp] * yb[lm] + gb[n] * yb[H + 3 * lm + comp];
+  }
+  __syncwarp();
+  b3_to_complex<double>(c_s, nr, H, zr, zi, lane);
+  for (int comp = 0; comp < 3; comp++)
+    b3_to_complex<double>(dcr + comp * N * H, N, H, dzr + comp * N * H1,
+                          dzi + comp * N * H1, lane);
+  __syncwarp();
+  const int *beg = c_b3.beg + c_b3.ls_off[a.lmax];
+  const int n_ls = a.n_ls;
+  double fdot[3] = {0, 0, 0};
+  for (int t = 0; t < n_ls; t++) {
+    const int e0 = beg[t], e1 = beg[t + 1];
+    for (int r = lane; r < a.n_tri; r += 32) {
+      const int tr = tri[r];
+      const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
+      const bool in1 = n1 / N == sj, in2 = n2 / N == sj, in3 = n3 / N == sj;
+      const int d1 = n1 % N, d2 = n2 % N, d3 = n3 % N;
+      double v[3] = {0, 0, 0};
+      for (int q = e0; q < e1; q++) {
+        const unsigned ix = c_b3.idx[q];
+        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
+        const double w = c_b3.w[q];
+        const double ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
+        const double br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
+        const double cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
+        for (int comp = 0; comp < 3; comp++) {
+          const double *Dr = dzr + comp * N * H1, *Di = dzi + comp * N * H1;
+          double acc = 0.0;
+          if (in1) {  // Re(d1 b c)
+            const double xr = Dr[d1 * H1 + i1] * br - Di[d1 * H1 + i1] * bi;
+            const double xi = Dr[d1 * H1 + i1] * bi + Di[d1 * H1 + i1] * br;
+            acc += xr * cr - xi * ci;
+          }
+          if (in2) {  // Re(a d2 c)
+            const double xr = ar * Dr[d2 * H1 + i2] - ai * Di[d2 * H1 + i2];
+            const double xi = ar * Di[d2 * H1 + i2] + ai * Dr[d2 * H1 + i2];
+            acc += xr * cr - xi * ci;
+          }
+          if (in3) {  // Re(a b d3)
+            const double xr = ar * br - ai * bi, xi = ar * bi + ai * br;
+            acc += xr * Dr[d3 * H1 + i3] - xi * Di[d3 * H1 + i3];
+          }
+          v[comp] += w * acc;
+        }
+      }
+      const int d = r * n_ls + t;
+      const double pv = p_in[(size_t)i * nd + d];
+      for (int comp = 0; comp < 3; comp++) {
+        dp[(size_t)(3 * idx + comp) * ldd + d] = v[comp];
+        fdot[comp] += v[comp] * pv;
+      }
+    }
+  }
+  for (int comp = 0; comp < 3; comp++) {
+    const double v = warp_sum(fdot[comp]);
+    if (lane == 0) force_dots[3 * idx + comp] = v;
   }
 }
 
@@ -522,6 +765,20 @@ int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
                  const int *pair_tab, const double *c_in, const double *p_in,
                  double *dp, int ldd, double *force_dots, cudaStream_t stream) {
   if (npl == 0) return 0;
+  if (a.kind == kB3) {
+    const size_t per3 = b3_dp_smem_per_warp(a);
+    int w3 = 4;
+    while (w3 > 1 && per3 * w3 > 200 * 1024) w3 >>= 1;
+    const size_t sm3 = per3 * w3;
+    if (sm3 > 227 * 1024) return -1;
+    if (cudaFuncSetAttribute(k_b3_dp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm3) != cudaSuccess)
+      return -1;
+    k_b3_dp<<<ceil_div(npl, w3), 32 * w3, sm3, stream>>>(a, npl, plist, nbr_i, nbr_s, rel,
+                                                         pair_tab, c_in, p_in, dp, ldd,
+                                                         force_dots);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
   const int sb = a.n_species * a.N * a.H;
   size_t per = sizeof(double) * (sb + 3 * a.N * a.H + 2 * a.N + 4 * a.H);
   int wpb = 4;
@@ -661,19 +918,29 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                       double *atom_e, T *pair_f, double *forces, double *atom_vir,
                       double *reduce_out, bool gather, T *u_buf, long long n_pairs,
                       const int *nbr_i, cudaStream_t stream) {
-  (void)pair_tab;
   if (a.noa == 0) return 0;
-  a.smem_per_warp_adj = adjoint_smem_per_warp(a, sizeof(T));
+  a.smem_per_warp_adj = a.kind == kB3 ? b3_adjoint_smem_per_warp<T>(a)
+                                      : adjoint_smem_per_warp(a, sizeof(T));
   int wpb = 4;
   while (wpb > 1 && a.smem_per_warp_adj * wpb > 200 * 1024) wpb >>= 1;
   size_t smem = a.smem_per_warp_adj * wpb;
   if (smem > 227 * 1024) return -1;
-  auto kern = k_b2_wu<T>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return -1;
-  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom, c_in,
-                                                         norm_in, atom_e, u_buf);
+  if (a.kind == kB3) {
+    auto kern3 = k_b3_wu<T>;
+    if (cudaFuncSetAttribute(kern3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    kern3<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom,
+                                                            pair_tab, c_in, norm_in, atom_e,
+                                                            u_buf);
+  } else {
+    auto kern = k_b2_wu<T>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom, c_in,
+                                                           norm_in, atom_e, u_buf);
+  }
   if (cudaGetLastError() != cudaSuccess) return -1;
   if (n_pairs > 0) {
     k_pair_force<T><<<(unsigned)((n_pairs + 127) / 128), 128, 0, stream>>>(

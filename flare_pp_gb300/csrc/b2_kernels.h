@@ -11,8 +11,14 @@ namespace fpp {
 
 constexpr int kMaxSpecies = 8;
 
+enum DescKind { kB2 = 0, kB3 = 1 };
+
+// Shape of a B2 or B3 descriptor (kind); for B3, n_d = n_tri * n_ls and the
+// pair table passed to the kernels lists the radial triples instead of pairs.
 struct B2Args {
   int noa;
+  int kind;          // DescKind
+  int n_ls, n_tri;   // B3: triangles (l1, l2, l3) and radial triples
   int n_species, N, lmax, H, n_d;
   int cutoff_kind;  // CutoffKind
   int window;       // neighbors staged per pass in the forward kernel
@@ -55,6 +61,8 @@ struct Neigh {
 };
 
 int upload_harmonic_tables(cudaStream_t stream);
+int upload_descriptor_tables(cudaStream_t stream);  // B3 coupling tables
+int b3_n_ls_host(int lmax);
 size_t forward_smem_per_warp(const B2Args &a, size_t elem);
 size_t adjoint_smem_per_warp(const B2Args &a, size_t elem);
 

@@ -1,0 +1,196 @@
+// B3 bispectrum: coupling tables and the per-atom device stages.
+//
+// src/flare_pp/descriptors/b3.cpp:134-240 computes, per atom,
+//   B3[(n1 <= n2 <= n3), (l1, l2, l3)] =
+//       Re sum_{m1+m2+m3=0} W(l1 l2 l3; m1 m2 m3) c[n1,l1m1] c[n2,l2m2] c[n3,l3m3]
+// on complex single-bond coefficients c (complex harmonics with the
+// Condon-Shortley phase, src/flare_pp/y_grad.cpp:24), with the triangles
+// (l1, l2, l3) in loop order l1, l2, l3 and |l1-l2| <= l3 <= l1+l2.
+//
+// The complex coefficients are a fixed linear map of the real ones that the
+// B2 stages already accumulate: with R = c[l, m], S = c[l, -m] (real, m > 0),
+//   c[l, +m] = (-1)^m (R + i S) / sqrt 2,  c[l, -m] = (R - i S) / sqrt 2.
+// So the forward reuses the real accumulation, and the adjoint maps the
+// holomorphic derivative u = dE/dc back to dE/dc_real, after which the B2
+// pair-force kernel applies unchanged.
+//
+// W is the Wigner 3j symbol from Racah's formula.  The reference's table for
+// lmax = 4 (descriptors/wigner3j.cpp:590-1986) holds 0 at the 57 symbols whose
+// exact value is a non-integer rational (+-1/3, +-1/6): its generated source
+// writes them as C++ integer divisions.  The tables here reproduce that.
+//
+// Included by exactly one translation unit (the constant bank is static).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace fpp {
+
+constexpr int kB3MaxL = 4;
+constexpr int kB3MaxTerms = 2112;  // sum over lmax 0..4 of the m-terms (2052)
+constexpr int kB3MaxLs = 130;      // sum over lmax 0..4 of (n_ls + 1)
+
+struct B3Tables {
+  int ls_off[kB3MaxL + 2];    // start of each lmax's triangle offsets in beg[]
+  int beg[kB3MaxLs];          // per triangle: first term (absolute index)
+  unsigned idx[kB3MaxTerms];  // i1 | i2 << 8 | i3 << 16 (harmonic index l*l+l+m)
+  double w[kB3MaxTerms];
+};
+
+static __constant__ B3Tables c_b3;
+
+inline double b3_factorial(int n) {
+  double f = 1.0;
+  for (int k = 2; k <= n; k++) f *= k;
+  return f;
+}
+
+// Wigner 3j symbol by Racah's formula (all factorials <= 13! are exact).
+inline double b3_wigner3j(int l1, int l2, int l3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0 || l3 < std::abs(l1 - l2) || l3 > l1 + l2) return 0.0;
+  if (std::abs(m1) > l1 || std::abs(m2) > l2 || std::abs(m3) > l3) return 0.0;
+  const double tri = b3_factorial(l1 + l2 - l3) * b3_factorial(l1 - l2 + l3) *
+                     b3_factorial(-l1 + l2 + l3) / b3_factorial(l1 + l2 + l3 + 1);
+  const double pre = tri * b3_factorial(l1 + m1) * b3_factorial(l1 - m1) *
+                     b3_factorial(l2 + m2) * b3_factorial(l2 - m2) *
+                     b3_factorial(l3 + m3) * b3_factorial(l3 - m3);
+  int kmin = 0;
+  if (l2 - l3 - m1 > kmin) kmin = l2 - l3 - m1;
+  if (l1 - l3 + m2 > kmin) kmin = l1 - l3 + m2;
+  int kmax = l1 + l2 - l3;
+  if (l1 - m1 < kmax) kmax = l1 - m1;
+  if (l2 + m2 < kmax) kmax = l2 + m2;
+  double s = 0.0;
+  for (int k = kmin; k <= kmax; k++) {
+    const double d = b3_factorial(k) * b3_factorial(l3 - l2 + k + m1) *
+                     b3_factorial(l3 - l1 + k - m2) * b3_factorial(l1 + l2 - l3 - k) *
+                     b3_factorial(l1 - k - m1) * b3_factorial(l2 - k + m2);
+    s += ((k & 1) ? -1.0 : 1.0) / d;
+  }
+  const double sign = ((l1 - l2 - m3) % 2 != 0) ? -1.0 : 1.0;
+  return sign * std::sqrt(pre) * s;
+}
+
+// The coefficient compute_B3 applies for this lmax (see the header comment).
+inline double b3_reference_coeff(int l1, int l2, int l3, int m1, int m2, int m3,
+                                 int lmax) {
+  const double w = b3_wigner3j(l1, l2, l3, m1, m2, m3);
+  if (lmax == 4 && w != 0.0 && std::fabs(w) < 1.0) {
+    const double inv2 = 1.0 / (w * w);
+    const double k = std::round(std::sqrt(inv2));
+    if (k > 1.0 && std::fabs(inv2 - k * k) < 1e-9 * inv2) return 0.0;
+  }
+  return w;
+}
+
+inline int b3_n_ls(int lmax) {
+  int n = 0;
+  for (int l1 = 0; l1 <= lmax; l1++)
+    for (int l2 = 0; l2 <= lmax; l2++)
+      for (int l3 = 0; l3 <= lmax; l3++)
+        if (std::abs(l1 - l2) <= l3 && l3 <= l1 + l2) n++;
+  return n;
+}
+
+inline int upload_b3_tables(cudaStream_t stream) {
+  static B3Tables t;  // 25 KB: not on the stack
+  int nt = 0, nb = 0;
+  for (int lmax = 0; lmax <= kB3MaxL; lmax++) {
+    t.ls_off[lmax] = nb;
+    for (int l1 = 0; l1 <= lmax; l1++)
+      for (int l2 = 0; l2 <= lmax; l2++)
+        for (int l3 = 0; l3 <= lmax; l3++) {
+          if (std::abs(l1 - l2) > l3 || l3 > l1 + l2) continue;
+          t.beg[nb++] = nt;
+          for (int m1 = -l1; m1 <= l1; m1++)
+            for (int m2 = -l2; m2 <= l2; m2++) {
+              const int m3 = -m1 - m2;
+              if (std::abs(m3) > l3) continue;
+              const double w = b3_reference_coeff(l1, l2, l3, m1, m2, m3, lmax);
+              if (w == 0.0) continue;  // contributes exactly nothing
+              if (nt >= kB3MaxTerms) return -1;
+              t.idx[nt] = (unsigned)(l1 * l1 + l1 + m1) |
+                          ((unsigned)(l2 * l2 + l2 + m2) << 8) |
+                          ((unsigned)(l3 * l3 + l3 + m3) << 16);
+              t.w[nt] = w;
+              nt++;
+            }
+        }
+    t.beg[nb++] = nt;  // end of the last triangle of this lmax
+  }
+  t.ls_off[kB3MaxL + 1] = nb;
+  cudaError_t e =
+      cudaMemcpyToSymbolAsync(c_b3, &t, sizeof(t), 0, cudaMemcpyHostToDevice, stream);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+// Real single-bond block c (nr x H, row stride H) -> complex (zr, zi) with
+// row stride H + 1 (padded so that lanes on different radial rows hit
+// different banks).  Lane-strided; the caller synchronizes the warp.
+template <typename T>
+__device__ __forceinline__ void b3_to_complex(const T *__restrict__ c, int nr, int H,
+                                              T *__restrict__ zr, T *__restrict__ zi,
+                                              int lane) {
+  const T is2 = T(0.70710678118654752440);
+  for (int k = lane; k < nr * H; k += 32) {
+    const int n = k / H, lm = k - n * H;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) l++;
+    const int m = lm - l * l - l;
+    const int am = m < 0 ? -m : m;
+    const T R = c[n * H + l * l + l + am];
+    const T S = c[n * H + l * l + l - am];
+    T re, im;
+    if (m == 0) {
+      re = R;
+      im = T(0);
+    } else if (m > 0) {
+      const T sg = (am & 1) ? T(-1) : T(1);
+      re = sg * R * is2;
+      im = sg * S * is2;
+    } else {
+      re = R * is2;
+      im = -S * is2;
+    }
+    zr[n * (H + 1) + lm] = re;
+    zi[n * (H + 1) + lm] = im;
+  }
+}
+
+// p[r * n_ls + t] for every radial triple r (table tri: n1 | n2<<8 | n3<<16)
+// and triangle t; lanes take triples, all lanes walk the same term list.
+template <typename T>
+__device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H,
+                                            const int *__restrict__ tri,
+                                            const T *__restrict__ zr,
+                                            const T *__restrict__ zi, T *__restrict__ p,
+                                            int lane) {
+  const int H1 = H + 1;
+  const int *beg = c_b3.beg + c_b3.ls_off[lmax];
+  for (int t = 0; t < n_ls; t++) {
+    const int e0 = beg[t], e1 = beg[t + 1];
+    for (int r0 = 0; r0 < n_tri; r0 += 32) {
+      const int r = r0 + lane;
+      if (r >= n_tri) continue;
+      const int tr = tri[r];
+      const int o1 = (tr & 0xff) * H1, o2 = ((tr >> 8) & 0xff) * H1, o3 = (tr >> 16) * H1;
+      T acc = T(0);
+      for (int e = e0; e < e1; e++) {
+        const unsigned ix = c_b3.idx[e];
+        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
+        const T ar = zr[o1 + i1], ai = zi[o1 + i1];
+        const T br = zr[o2 + i2], bi = zi[o2 + i2];
+        const T cr = zr[o3 + i3], ci = zi[o3 + i3];
+        const T xr = ar * br - ai * bi, xi = ar * bi + ai * br;
+        acc += T(c_b3.w[e]) * (xr * cr - xi * ci);
+      }
+      p[r * n_ls + t] = acc;
+    }
+  }
+}
+
+}  // namespace fpp

@@ -49,14 +49,16 @@ int DevBuf::reserve(size_t n) {
 }
 
 static int ensure_tables(cudaStream_t stream) {
-  // the harmonic normalisation table lives in constant memory of this module;
-  // upload it once per device
+  // the harmonic normalisation and B3 coupling tables live in constant memory
+  // of this module; upload them once per device
   static int uploaded_mask = 0;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(FPP_ERR_CUDA, "no CUDA device");
   if (dev < 31 && (uploaded_mask >> dev) & 1) return FPP_OK;
   if (upload_harmonic_tables(stream) != 0)
     return fail(FPP_ERR_CUDA, "upload of harmonic tables failed");
+  if (upload_descriptor_tables(stream) != 0)
+    return fail(FPP_ERR_CUDA, "upload of B3 coupling tables failed");
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_fail(e, "upload of harmonic tables");
   if (dev < 31) uploaded_mask |= 1 << dev;
@@ -293,6 +295,34 @@ int fpp_b2_create(const char *radial_basis, const char *cutoff_function,
   std::vector<int> tab;
   for (int n1 = 0; n1 < nr; n1++)
     for (int n2 = n1; n2 < nr; n2++) tab.push_back(n1 | (n2 << 16));
+  b->pair_tab_host = tab;
+  *out = b;
+  return FPP_OK;
+}
+
+int fpp_b3_create(const char *radial_basis, const char *cutoff_function,
+                  const double *radial_hyps, int32_t n_radial_hyps,
+                  const double *cutoff_hyps, int32_t n_cutoff_hyps,
+                  const int32_t *descriptor_settings, fpp_b2 **out) {
+  if (!out || !descriptor_settings) return fail(FPP_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (descriptor_settings[2] < 0 || descriptor_settings[2] > 4)
+    return fail(FPP_ERR_CAPACITY, "B3 lmax must be 0..4 (b3.cpp:150-160)");
+  // one cutoff, radial_hyps[1], for every species pair (b3.cpp:258)
+  fpp_b2 *b = nullptr;
+  FPP_TRY(fpp_b2_create(radial_basis, cutoff_function, radial_hyps, n_radial_hyps,
+                        cutoff_hyps, n_cutoff_hyps, descriptor_settings, nullptr, &b));
+  B2Args &a = b->args;
+  const int nr = a.n_species * a.N;
+  a.kind = kB3;
+  a.n_ls = b3_n_ls_host(a.lmax);
+  a.n_tri = nr * (nr + 1) * (nr + 2) / 6;
+  a.n_d = a.n_tri * a.n_ls;
+  // radial triples n1 <= n2 <= n3 in the reference's counter order (b3.cpp:176-178)
+  std::vector<int> tab;
+  for (int n1 = 0; n1 < nr; n1++)
+    for (int n2 = n1; n2 < nr; n2++)
+      for (int n3 = n2; n3 < nr; n3++) tab.push_back(n1 | (n2 << 8) | (n3 << 16));
   b->pair_tab_host = tab;
   *out = b;
   return FPP_OK;

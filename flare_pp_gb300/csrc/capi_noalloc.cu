@@ -91,6 +91,8 @@ extern "C" int fpp_b2_descriptors_noalloc(const fpp_b2 *b2, int32_t n_atoms,
   if (!species || !offsets || !rel || !nbr_species || !descriptors || !norms)
     return fail(FPP_ERR_INVALID, "null argument");
   const B2Args &a0 = b2->args;
+  if (a0.kind != kB2)
+    return fail(FPP_ERR_UNSUPPORTED, "fpp_b2_descriptors_noalloc computes B2 descriptors only");
   const int nr = a0.n_species * a0.N;
   const size_t sb = (size_t)nr * a0.H;
   if (n_atoms > kNoAllocAtoms || (size_t)n_atoms * sb > kNoAllocC)

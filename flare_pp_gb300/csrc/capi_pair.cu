@@ -124,6 +124,8 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                                 double *eng_vdwl, double *virial, double *eatom,
                                 void *stream) {
   if (!m) return fail(FPP_ERR_INVALID, "null model");
+  if (m->args.kind != kB2)
+    return fail(FPP_ERR_UNSUPPORTED, "the pair style maps B2 models only (pair_flare.cpp)");
   if (nall < nlocal || nlocal < 0 || inum < 0 || inum > nall)
     return fail(FPP_ERR_INVALID, "bad atom counts");
   if (inum > 0 && (!x || !type || !ilist || !numneigh || !f))

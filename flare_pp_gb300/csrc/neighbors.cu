@@ -27,6 +27,11 @@
 
 namespace fpp {
 
+// Neighbor keys (j << kKeyBits) | shift index: ordered by j, then shift, as
+// the reference lists them; decoded with shifts (n_shift <= 2^kKeyBits).
+constexpr int kKeyBits = 20;
+constexpr long long kKeyMask = (1LL << kKeyBits) - 1;
+
 struct CellDev {
   double cell[9], ct[9], ct_inv[9], cdot[9], cdot_inv[9];
   float cell32[9];
@@ -277,7 +282,7 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
           const double dist = exact_image(wp[i], wp[j], cd, s1, s2, s3, im);
           ok = (dist < cd.cutoff) && (dist != 0.0);
         }
-        key = (long long)j * cd.n_shift + sidx;
+        key = ((long long)j << kKeyBits) | sidx;
       }
       const unsigned m = __ballot_sync(0xffffffffu, ok);
       if (ok) {
@@ -359,8 +364,8 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
   const dvec4 wi = wp[i];
   for (int e = lane; e < n; e += 32) {
     const long long key = slab[(size_t)i * kSlabCap + e];
-    const int j = (int)(key / cd.n_shift);
-    const int sidx = (int)(key - (long long)j * cd.n_shift);
+    const int j = (int)(key >> kKeyBits);
+    const int sidx = (int)(key & kKeyMask);
     const int s3 = sidx % cd.ns - cd.sweep;
     const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
     const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
@@ -404,13 +409,12 @@ __global__ void k_fill(int noa, CellDev cd, const dvec4 *__restrict__ wp,
   if (i >= noa) return;
   int lane = threadIdx.x & 31;
   int pos = offset[i];
-  const int n_shift = cd.n_shift;
   enumerate_pairs(i, cd, wp, wp32, frac, bin_start, bin_atoms,
                   [&](bool ok, int j, int sidx) {
                     unsigned m = __ballot_sync(0xffffffffu, ok);
                     if (ok) {
                       int r = __popc(m & ((1u << lane) - 1u));
-                      keys[pos + r] = (long long)j * n_shift + sidx;
+                      keys[pos + r] = ((long long)j << kKeyBits) | sidx;
                     }
                     pos += __popc(m);
                   });
@@ -435,8 +439,8 @@ __global__ void k_sort_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp,
     int rank = 0;
     for (int f = beg; f < end; f++) rank += (keys_tmp[f] < key) ? 1 : 0;
     int out = beg + rank;
-    int j = (int)(key / cd.n_shift);
-    int sidx = (int)(key - (long long)j * cd.n_shift);
+    int j = (int)(key >> kKeyBits);
+    int sidx = (int)(key & kKeyMask);
     int s3 = sidx % cd.ns - cd.sweep;
     int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
     int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
@@ -461,8 +465,8 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
   int i = nbr_i[p], j = nbr_j[p];
-  int sidx = (int)(keys[p] - (long long)j * cd.n_shift);
-  long long want = (long long)i * cd.n_shift + (cd.n_shift - 1 - sidx);
+  int sidx = (int)(keys[p] & kKeyMask);
+  long long want = ((long long)i << kKeyBits) | (cd.n_shift - 1 - sidx);
   int lo = offset[j], hi = offset[j + 1] - 1, found = -1;
   while (lo <= hi) {
     int mid = (lo + hi) >> 1;

@@ -187,3 +187,26 @@ def bcc_alloy_32k_model(seed=303, n_sparse=2000, device="cuda"):
     gp.set_model(b2, fit["sparse"], fit["alpha"])
     cell, sp, pos = bcc_alloy((32, 32, 16), seed)
     return dict(b2=b2, gp=gp, cell=cell, species=sp, positions=pos, fit=fit)
+
+
+def fcc_al(reps, seed, rattle=0.05, a=4.05):
+    """FCC aluminium supercell of reps conventional cells, rattled."""
+    rng = np.random.default_rng(seed)
+    return rattled(FCC_BASIS, a, reps, rattle, rng)
+
+
+def fcc_al_b3_1m_model(seed=505, n_sparse=500, reps=(64, 64, 64), device="cuda"):
+    """The B3 workload: FCC Al, a = 4.05 A, 64^3 conventional cells
+    (1,048,576 atoms), rattle 0.05 A, rc 5.0 A, chebyshev N=6, lmax=3,
+    quadratic cutoff, with n_sparse environments drawn from four 6x6x6-cell
+    frames (seeds seed+1..seed+4) and weights fitted to Lennard-Jones site
+    energies."""
+    from .api import B3, NormalizedDotProduct, SparseGP
+    b3 = B3("chebyshev", "quadratic", [0.0, 5.0], [], [1, 6, 3])
+    frames = [fcc_al((6, 6, 6), seed + k) for k in range(1, 5)]
+    fit = fit_site_energy_model(b3, frames, n_sparse, sigma=2.0, power=2, seed=seed,
+                                device=device)
+    gp = SparseGP([NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
+    gp.set_model(b3, fit["sparse"], fit["alpha"])
+    cell, sp, pos = fcc_al(reps, seed)
+    return dict(b2=b3, gp=gp, cell=cell, species=sp, positions=pos, fit=fit)

@@ -114,8 +114,21 @@ int fpp_b2_create(const char *radial_basis, const char *cutoff_function,
                   const double *cutoff_hyps, int32_t n_cutoff_hyps,
                   const int32_t *descriptor_settings, const double *cutoffs,
                   fpp_b2 **out);
+/* B3 descriptor settings.  Replaces B3::B3(radial_basis, cutoff_function,
+ * radial_hyps, cutoff_hyps, descriptor_settings)
+ * (src/flare_pp/descriptors/b3.h:29-33, b3.cpp:12-27).  The handle is an
+ * fpp_b2 of kind B3: every fpp_b2_* call and fpp_model_create accept it, and
+ * compute the bispectrum of b3.cpp:134-240 in its place (one cutoff,
+ * radial_hyps[1], for every species pair; lmax <= 4).
+ * n_d = C(n_rad + 2, 3) * n_ls, n_ls = 1, 5, 15, 34, 65 for lmax = 0..4.
+ * The coefficients are the reference's (descriptors/wigner3j.cpp), including
+ * the entries its lmax = 4 table holds as 0. */
+int fpp_b3_create(const char *radial_basis, const char *cutoff_function,
+                  const double *radial_hyps, int32_t n_radial_hyps,
+                  const double *cutoff_hyps, int32_t n_cutoff_hyps,
+                  const int32_t *descriptor_settings, fpp_b2 **out);
 int fpp_b2_destroy(fpp_b2 *b2);
-/* n_d = n_rad (n_rad + 1) / 2 * (lmax + 1), n_rad = n_species * N. */
+/* n_d = n_rad (n_rad + 1) / 2 * (lmax + 1), n_rad = n_species * N (B2). */
 int fpp_b2_n_descriptors(const fpp_b2 *b2, int32_t *n_descriptors);
 
 /* B2::compute_struc (b2.cpp:76-179) on the GPU, in FP64.  Host outputs in

@@ -314,6 +314,8 @@ class B3:
         self.radial_hyps = list(radial_hyps)
         self.cutoff_hyps = list(cutoff_hyps)
         self.descriptor_settings = list(descriptor_settings)
+        ns = descriptor_settings[0]
+        self.cutoffs = np.full((ns, ns), float(radial_hyps[1]))
         self.store_dervs = True
 
     def compute_struc(self, structure):

@@ -18,6 +18,7 @@
  *   - pair forces f_ij = u . d c / d r_ij added to atom i and subtracted from
  *     j (pair_flare.cpp:141-175); the stress is -(1/V) sum f_a r_b in the
  *     order xx, xy, xz, yy, yz, zz.
+ * B3 (oracle_b3_beta_form, below) follows the same per-atom form.
  * Radial basis: chebyshev x quadratic cutoff (radial.cpp:138-169, cutoffs.cpp:
  * 44-56).  Harmonics: the solid-harmonic recurrence of oracle/basis.py, which
  * tests pin against the reference's y_grad.cpp.
@@ -472,6 +473,314 @@ int oracle_beta_form(int noa, const double *cell, const int *species, const doub
   stress[4] = -vir[5] * vi;
   stress[5] = -vir[8] * vi;
   geo_free(&G);
+  return err;
+}
+
+/*
+ * B3 (src/flare_pp/descriptors/b3.cpp:134-382) in the same per-atom form:
+ * complex single bond from the real one (c[l,+m] = (-1)^m (R + iS)/sqrt2,
+ * c[l,-m] = (R - iS)/sqrt2 with R = c_real[l,m], S = c_real[l,-m]), the
+ * bispectrum over n1 <= n2 <= n3 and triangles (l1,l2,l3), E_i and w as for
+ * B2, u = dE/dc (holomorphic) mapped back to dE/dc_real, then the B2 pair
+ * forces.  Coefficients: Wigner 3j by Racah's formula, with the entries that
+ * the reference's lmax = 4 table holds as 0 (non-integer rationals written
+ * there as integer divisions, descriptors/wigner3j.cpp:590-1986).
+ */
+static double fact_(int n) {
+  double f = 1;
+  for (int k = 2; k <= n; k++) f *= k;
+  return f;
+}
+
+static double w3j_(int l1, int l2, int l3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0 || l3 < abs(l1 - l2) || l3 > l1 + l2) return 0;
+  if (abs(m1) > l1 || abs(m2) > l2 || abs(m3) > l3) return 0;
+  double pre = fact_(l1 + l2 - l3) * fact_(l1 - l2 + l3) * fact_(-l1 + l2 + l3) /
+               fact_(l1 + l2 + l3 + 1) * fact_(l1 + m1) * fact_(l1 - m1) * fact_(l2 + m2) *
+               fact_(l2 - m2) * fact_(l3 + m3) * fact_(l3 - m3);
+  int kmin = 0, kmax = l1 + l2 - l3;
+  if (l2 - l3 - m1 > kmin) kmin = l2 - l3 - m1;
+  if (l1 - l3 + m2 > kmin) kmin = l1 - l3 + m2;
+  if (l1 - m1 < kmax) kmax = l1 - m1;
+  if (l2 + m2 < kmax) kmax = l2 + m2;
+  double s = 0;
+  for (int k = kmin; k <= kmax; k++)
+    s += ((k & 1) ? -1.0 : 1.0) /
+         (fact_(k) * fact_(l3 - l2 + k + m1) * fact_(l3 - l1 + k - m2) *
+          fact_(l1 + l2 - l3 - k) * fact_(l1 - k - m1) * fact_(l2 - k + m2));
+  double w = (((l1 - l2 - m3) % 2) ? -1.0 : 1.0) * sqrt(pre) * s;
+  return w;
+}
+
+static double b3_coeff_(int l1, int l2, int l3, int m1, int m2, int m3, int lmax) {
+  double w = w3j_(l1, l2, l3, m1, m2, m3);
+  if (lmax == 4 && w != 0 && fabs(w) < 1) {
+    double inv2 = 1 / (w * w), k = floor(sqrt(inv2) + 0.5);
+    if (k > 1 && fabs(inv2 - k * k) < 1e-9 * inv2) return 0;
+  }
+  return w;
+}
+
+typedef struct {
+  int n_ls, n_terms;
+  int beg[70];
+  int i1[1500], i2[1500], i3[1500];
+  double w[1500];
+} B3T;
+
+static void b3_tables_(int lmax, B3T *T) {
+  int t = 0, e = 0;
+  for (int l1 = 0; l1 <= lmax; l1++)
+    for (int l2 = 0; l2 <= lmax; l2++)
+      for (int l3 = 0; l3 <= lmax; l3++) {
+        if (abs(l1 - l2) > l3 || l3 > l1 + l2) continue;
+        T->beg[t++] = e;
+        for (int m1 = -l1; m1 <= l1; m1++)
+          for (int m2 = -l2; m2 <= l2; m2++) {
+            int m3 = -m1 - m2;
+            if (abs(m3) > l3) continue;
+            double w = b3_coeff_(l1, l2, l3, m1, m2, m3, lmax);
+            if (w == 0) continue;
+            T->i1[e] = l1 * l1 + l1 + m1;
+            T->i2[e] = l2 * l2 + l2 + m2;
+            T->i3[e] = l3 * l3 + l3 + m3;
+            T->w[e] = w;
+            e++;
+          }
+      }
+  T->beg[t] = e;
+  T->n_ls = t;
+  T->n_terms = e;
+}
+
+/* real c (nr x H) -> complex (re, im) */
+static void to_complex_(const double *c, int nr, int lmax, double *zr, double *zi) {
+  const int H = (lmax + 1) * (lmax + 1);
+  const double is2 = 0.70710678118654752440;
+  for (int n = 0; n < nr; n++)
+    for (int l = 0; l <= lmax; l++) {
+      const double *cl = c + n * H + l * l + l;
+      double *r = zr + n * H + l * l + l, *im = zi + n * H + l * l + l;
+      r[0] = cl[0];
+      im[0] = 0;
+      for (int m = 1; m <= l; m++) {
+        double sg = (m & 1) ? -1 : 1, R = cl[m], S = cl[-m];
+        r[m] = sg * R * is2;
+        im[m] = sg * S * is2;
+        r[-m] = R * is2;
+        im[-m] = -S * is2;
+      }
+    }
+}
+
+int oracle_b3_beta_form(int noa, const double *cell, const int *species, const double *pos,
+                        int n_species, int N, int lmax, double r1, double rcut,
+                        const double *beta, int power, const int *atoms, int n_atoms,
+                        int n_threads, double *energy, double *forces, double *stress,
+                        double *atom_e) {
+  init_tables();
+  if (lmax > 4 || n_species * N > 64) return -3;
+  B3T *T = (B3T *)malloc(sizeof(B3T));
+  if (!T) return -1;
+  b3_tables_(lmax, T);
+  Geo G;
+  if (geo_init(&G, noa, cell, pos, rcut)) {
+    free(T);
+    return -1;
+  }
+  const int H = (lmax + 1) * (lmax + 1), nr = n_species * N, sb = nr * H;
+  const int ntri = nr * (nr + 1) * (nr + 2) / 6, nls = T->n_ls, nd = ntri * nls;
+  int *tri = (int *)malloc(sizeof(int) * 3 * ntri);
+  {
+    int k = 0;
+    for (int a = 0; a < nr; a++)
+      for (int b = a; b < nr; b++)
+        for (int c = b; c < nr; c++, k++) {
+          tri[3 * k] = a;
+          tri[3 * k + 1] = b;
+          tri[3 * k + 2] = c;
+        }
+  }
+  const int cap = 4096;
+  int na = atoms ? n_atoms : noa;
+  int err = 0;
+  double etot = 0, vir[9] = {0};
+  memset(forces, 0, sizeof(double) * 3 * noa);
+  if (atom_e) memset(atom_e, 0, sizeof(double) * noa);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel
+  {
+    int *js = (int *)malloc(sizeof(int) * cap);
+    double *rel = (double *)malloc(sizeof(double) * 4 * cap);
+    double *bas = (double *)malloc(sizeof(double) * (size_t)cap * (2 * N + 4 * H));
+    double *c = (double *)malloc(sizeof(double) * sb);
+    double *zr = (double *)malloc(sizeof(double) * sb);
+    double *zi = (double *)malloc(sizeof(double) * sb);
+    double *ur = (double *)malloc(sizeof(double) * sb);
+    double *ui = (double *)malloc(sizeof(double) * sb);
+    double *u = (double *)malloc(sizeof(double) * sb);
+    double *p = (double *)malloc(sizeof(double) * nd);
+    double *bp = (double *)malloc(sizeof(double) * nd);
+    double *w = (double *)malloc(sizeof(double) * nd);
+    double *F = (double *)calloc(3 * (size_t)noa, sizeof(double));
+    double lvir[9] = {0}, le = 0;
+    int lerr = (!js || !rel || !bas || !c || !zr || !zi || !ur || !ui || !u || !p || !bp ||
+                !w || !F || !tri)
+                   ? -1
+                   : 0;
+#pragma omp for schedule(dynamic, 16)
+    for (int ii = 0; ii < na; ii++) {
+      if (lerr) continue;
+      int i = atoms ? atoms[ii] : ii;
+      int si = species[i];
+      int nn = neighbors_of(&G, i, cap, js, rel);
+      if (nn > cap) {
+        lerr = -2;
+        continue;
+      }
+      memset(c, 0, sizeof(double) * sb);
+      for (int q = 0; q < nn; q++) {
+        int sj = species[js[q]];
+        double r = rel[4 * q + 3];
+        if (!(r <= rcut)) {  /* b3.cpp:258 */
+          js[q] = -1;
+          continue;
+        }
+        double *b = bas + (size_t)q * (2 * N + 4 * H);
+        radial(r, r1, rcut, N, b, b + N);
+        harmonics(rel[4 * q], rel[4 * q + 1], rel[4 * q + 2], lmax, b + 2 * N, b + 2 * N + H);
+        for (int n = 0; n < N; n++)
+          for (int lm = 0; lm < H; lm++) c[(sj * N + n) * H + lm] += b[n] * b[2 * N + lm];
+      }
+      to_complex_(c, nr, lmax, zr, zi);
+      double nsq = 0;
+      for (int r = 0; r < ntri; r++) {
+        const double *a1r = zr + tri[3 * r] * H, *a1i = zi + tri[3 * r] * H;
+        const double *a2r = zr + tri[3 * r + 1] * H, *a2i = zi + tri[3 * r + 1] * H;
+        const double *a3r = zr + tri[3 * r + 2] * H, *a3i = zi + tri[3 * r + 2] * H;
+        for (int t = 0; t < nls; t++) {
+          double v = 0;
+          for (int e = T->beg[t]; e < T->beg[t + 1]; e++) {
+            int x1 = T->i1[e], x2 = T->i2[e], x3 = T->i3[e];
+            double xr = a1r[x1] * a2r[x2] - a1i[x1] * a2i[x2];
+            double xi = a1r[x1] * a2i[x2] + a1i[x1] * a2r[x2];
+            v += T->w[e] * (xr * a3r[x3] - xi * a3i[x3]);
+          }
+          p[r * nls + t] = v;
+          nsq += v * v;
+        }
+      }
+      if (nsq < 1e-8) continue;
+      const double *Bm = beta + (size_t)si * (power == 2 ? (size_t)nd * nd : (size_t)nd);
+      double e = 0;
+      if (power == 2) {
+        for (int a = 0; a < nd; a++) {
+          const double *row = Bm + (size_t)a * nd;
+          double s = 0;
+          for (int k = 0; k < nd; k++) s += row[k] * p[k];
+          bp[a] = s;
+        }
+        for (int a = 0; a < nd; a++) e += p[a] * bp[a];
+        e /= nsq;
+        for (int a = 0; a < nd; a++) w[a] = 2 * (bp[a] - e * p[a]) / nsq;
+      } else {
+        double nr_ = sqrt(nsq);
+        for (int a = 0; a < nd; a++) e += p[a] * Bm[a];
+        e /= nr_;
+        for (int a = 0; a < nd; a++) w[a] = Bm[a] / nr_ - e * p[a] / nsq;
+      }
+      le += e;
+      if (atom_e) atom_e[i] = e;
+      /* u = dE/dc (complex), then dE/dc_real */
+      memset(ur, 0, sizeof(double) * sb);
+      memset(ui, 0, sizeof(double) * sb);
+      for (int r = 0; r < ntri; r++) {
+        int n1 = tri[3 * r], n2 = tri[3 * r + 1], n3 = tri[3 * r + 2];
+        for (int t = 0; t < nls; t++) {
+          double wq = w[r * nls + t];
+          for (int ee = T->beg[t]; ee < T->beg[t + 1]; ee++) {
+            int k1 = n1 * H + T->i1[ee], k2 = n2 * H + T->i2[ee], k3 = n3 * H + T->i3[ee];
+            double f = wq * T->w[ee];
+            double ar = zr[k1], ai = zi[k1], br = zr[k2], bi = zi[k2], cr = zr[k3], ci = zi[k3];
+            ur[k1] += f * (br * cr - bi * ci);
+            ui[k1] += f * (br * ci + bi * cr);
+            ur[k2] += f * (ar * cr - ai * ci);
+            ui[k2] += f * (ar * ci + ai * cr);
+            ur[k3] += f * (ar * br - ai * bi);
+            ui[k3] += f * (ar * bi + ai * br);
+          }
+        }
+      }
+      {
+        const double is2 = 0.70710678118654752440;
+        for (int n = 0; n < nr; n++)
+          for (int l = 0; l <= lmax; l++) {
+            int o = n * H + l * l + l;
+            u[o] = ur[o];
+            for (int m = 1; m <= l; m++) {
+              double sg = (m & 1) ? -1 : 1;
+              u[o + m] = (sg * ur[o + m] + ur[o - m]) * is2;
+              u[o - m] = (ui[o - m] - sg * ui[o + m]) * is2;
+            }
+          }
+      }
+      for (int q = 0; q < nn; q++) {
+        if (js[q] < 0) continue;
+        int j = js[q], sj = species[j];
+        const double *b = bas + (size_t)q * (2 * N + 4 * H);
+        double r = rel[4 * q + 3];
+        double ux = rel[4 * q] / r, uy = rel[4 * q + 1] / r, uz = rel[4 * q + 2] / r;
+        double f[3] = {0, 0, 0};
+        for (int n = 0; n < N; n++)
+          for (int lm = 0; lm < H; lm++) {
+            double uv = u[(sj * N + n) * H + lm];
+            double rad = b[N + n] * b[2 * N + lm];
+            f[0] += uv * (rad * ux + b[n] * b[2 * N + H + 3 * lm]);
+            f[1] += uv * (rad * uy + b[n] * b[2 * N + H + 3 * lm + 1]);
+            f[2] += uv * (rad * uz + b[n] * b[2 * N + H + 3 * lm + 2]);
+          }
+        for (int k = 0; k < 3; k++) {
+          F[3 * i + k] += f[k];
+          F[3 * j + k] -= f[k];
+          for (int k2 = 0; k2 < 3; k2++) lvir[3 * k + k2] += f[k] * rel[4 * q + k2];
+        }
+      }
+    }
+#pragma omp critical
+    {
+      if (lerr) err = lerr;
+      etot += le;
+      for (int k = 0; k < 9; k++) vir[k] += lvir[k];
+      if (F)
+        for (int k = 0; k < 3 * noa; k++) forces[k] += F[k];
+    }
+    free(js);
+    free(rel);
+    free(bas);
+    free(c);
+    free(zr);
+    free(zi);
+    free(ur);
+    free(ui);
+    free(u);
+    free(p);
+    free(bp);
+    free(w);
+    free(F);
+  }
+  *energy = etot;
+  double vi = 1.0 / G.volume;
+  stress[0] = -vir[0] * vi;
+  stress[1] = -vir[1] * vi;
+  stress[2] = -vir[2] * vi;
+  stress[3] = -vir[4] * vi;
+  stress[4] = -vir[5] * vi;
+  stress[5] = -vir[8] * vi;
+  geo_free(&G);
+  free(tri);
+  free(T);
   return err;
 }
 

@@ -17,14 +17,17 @@ def lib():
         vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
         _lib.oracle_beta_form.argtypes = [ci, vp, vp, vp, ci, ci, ci, cd, vp, vp, ci,
                                           vp, ci, ci, vp, vp, vp, vp]
+        _lib.oracle_b3_beta_form.restype = ctypes.c_int
+        _lib.oracle_b3_beta_form.argtypes = [ci, vp, vp, vp, ci, ci, ci, cd, cd, vp, ci,
+                                             vp, ci, ci, vp, vp, vp, vp]
         _lib.oracle_max_threads.restype = ctypes.c_int
     return _lib
 
 
 def beta_form(cell, species, positions, settings, beta, power=2, atoms=None,
               n_threads=0):
-    """Mapped-beta E/F/S (FP64).  beta: list of dense n_d x n_d (power 2) or
-    vectors (power 1).  Returns dict(energy, forces, stress, atom_energies)."""
+    """Mapped-beta E/F/S (FP64) for B2, or B3 when settings["kind"] == "B3".
+    beta: list of dense n_d x n_d (power 2) or vectors (power 1).  Returns dict(energy, forces, stress, atom_energies)."""
     cell = np.ascontiguousarray(cell, dtype=np.float64)
     sp = np.ascontiguousarray(species, dtype=np.int32)
     pos = np.ascontiguousarray(positions, dtype=np.float64)
@@ -37,11 +40,18 @@ def beta_form(cell, species, positions, settings, beta, power=2, atoms=None,
     e = ctypes.c_double()
     at = None if atoms is None else np.ascontiguousarray(atoms, dtype=np.int32)
     P = lambda a: None if a is None else a.ctypes.data
-    rc = lib().oracle_beta_form(
-        noa, P(cell), P(sp), P(pos), settings["n_species"], settings["N"],
-        settings["lmax"], ctypes.c_double(settings["r1"]), P(cut), P(B), power,
-        P(at), 0 if at is None else len(at), n_threads, ctypes.byref(e), P(F), P(S),
-        P(ae))
+    if settings.get("kind", "B2") == "B3":
+        rc = lib().oracle_b3_beta_form(
+            noa, P(cell), P(sp), P(pos), settings["n_species"], settings["N"],
+            settings["lmax"], ctypes.c_double(settings["r1"]),
+            ctypes.c_double(settings["rcut"]), P(B), power, P(at),
+            0 if at is None else len(at), n_threads, ctypes.byref(e), P(F), P(S), P(ae))
+    else:
+        rc = lib().oracle_beta_form(
+            noa, P(cell), P(sp), P(pos), settings["n_species"], settings["N"],
+            settings["lmax"], ctypes.c_double(settings["r1"]), P(cut), P(B), power,
+            P(at), 0 if at is None else len(at), n_threads, ctypes.byref(e), P(F), P(S),
+            P(ae))
     if rc != 0:
         raise RuntimeError(f"oracle_beta_form failed ({rc})")
     return dict(energy=e.value, forces=F, stress=S, atom_energies=ae)

@@ -96,11 +96,14 @@ def site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
 
 
 def to_gpu_model(b2_settings_list, oracle_sparse, alpha, sigma, power, R_inv=None,
-                 cutoffs=None):
+                 cutoffs=None, kind="B2"):
     """A GPU SparseGP loaded with the same sparse set and weights."""
     import flare_pp_gb300 as fg
     ns, N, lmax, rc = b2_settings_list
-    b2 = fg.B2("chebyshev", "quadratic", [0.0, rc], [], [ns, N, lmax], cutoffs)
+    if kind == "B3":
+        b2 = fg.B3("chebyshev", "quadratic", [0.0, rc], [], [ns, N, lmax])
+    else:
+        b2 = fg.B2("chebyshev", "quadratic", [0.0, rc], [], [ns, N, lmax], cutoffs)
     cd = fg.ClusterDescriptor()
     cd.initialize_cluster(ns, oracle_sparse.n_descriptors)
     cd.descriptors = [np.array(d) for d in oracle_sparse.descriptors]

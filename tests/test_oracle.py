@@ -232,3 +232,22 @@ def test_b3_kernel_route_and_finite_difference():
     assert abs(bf["energy"] - kf["energy"]) < 1e-9
     np.testing.assert_allclose(bf["forces"], kf["forces"], atol=1e-9)
     np.testing.assert_allclose(bf["stress"], kf["stress"], atol=1e-9)
+
+
+@pytest.mark.parametrize("lmax", [3, 4])
+def test_b3_c_oracle_matches_numpy(lmax):
+    from oracle import cfast
+    d = ob3.B3("chebyshev", "quadratic", [0, 3.8], [], [2, 2, lmax])
+    cell, sp, pos = _b3_structure()
+    s = Structure(cell, sp, pos, 4.0, [d])
+    envs = ClusterDescriptor(s.descriptors[0])
+    alpha = np.random.default_rng(5).normal(size=envs.n_clusters)
+    beta = NormalizedDotProduct(1.3, 2).compute_map_coeff_pow2(envs, alpha)
+    B = predict.unpack_beta(beta, s.descriptors[0].n_descriptors)
+    st = fixtures.settings_b3(2, 2, lmax, 3.8)
+    ref = predict.beta_form(Structure(cell, sp, pos, 4.0), st, B)
+    got = cfast.beta_form(cell, sp, pos, st, B, n_threads=2)
+    assert abs(got["energy"] - ref["energy"]) < 1e-10 * max(1, abs(ref["energy"]))
+    np.testing.assert_allclose(got["forces"], ref["forces"], atol=1e-9)
+    np.testing.assert_allclose(got["stress"], ref["stress"], atol=1e-10)
+    np.testing.assert_allclose(got["atom_energies"], ref["atom_energies"], atol=1e-10)
