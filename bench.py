@@ -279,9 +279,8 @@ def run_ours(args):
     contract_ms = stage[2]
     achieved = flop / (contract_ms * 1e-3) / 1e12
     peak = float(peaks["bf16_tflops"])
-    nsp = SETTINGS["n_species"]
-    roof = {"kernel": f"k_split_gemm (contraction P.beta, {nsp} launch"
-                      f"{'es' if nsp > 1 else ''}/step)",
+    roof = {"kernel": "k_split_gemm_grouped (contraction P.beta, one persistent launch "
+                      "over all species per step)",
             "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "peak_source": f"{peak_src} bf16 dense burst",
@@ -322,9 +321,9 @@ def run_ours(args):
 def launches_per_step(n_species):
     # neighbors: wrap_bin, bin_scatter, enum, compact_geom, reverse and two
     # CUB exclusive scans of two kernels each (compiled into the library);
-    # descriptors: forward; contraction: one split GEMM per species; adjoint:
-    # wu, pair_force, gather, reduce
-    return 9 + 1 + n_species + 4
+    # descriptors: forward; contraction: one grouped split GEMM; adjoint: wu,
+    # pair_force, gather, reduce
+    return 9 + 1 + 1 + 4
 
 
 def cpu_baseline(w, seconds=15.0):

@@ -56,6 +56,9 @@ SIGNATURES = {
     "fpp_model_set_beta": (_c_int, [_vp, _i32, _vp]),
     "fpp_envs_envs": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_envs_struc": (_c_int, [_vp, _vp, _vp, _vp]),
+    "fpp_kuf_batched": (_c_int, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "fpp_struc_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp, _vp]),
+    "fpp_self_kernel_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp]),
     "fpp_predict": (_c_int, [_vp, _vp, _vp, _vp, _vp]),
     "fpp_predict_mapped": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
     "fpp_update_matrices_QR": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _dbl, _vp, _vp,

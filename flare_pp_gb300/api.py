@@ -351,6 +351,27 @@ class NormalizedDotProduct:
                                    _stream(stream)))
         return K
 
+    def struc_struc(self, struc1, struc2, hyps=None, stream=None):
+        """struc_struc (normalized_dot_product.cpp:212-444), FP64 on the GPU:
+        the (1+3N1+6) x (1+3N2+6) energy/force/stress covariance of two
+        structures' DescriptorValues."""
+        sigma = self.sigma if hyps is None else float(hyps[0])
+        d = struc1.descriptor_calculator
+        K = np.zeros((1 + 3 * struc1.n_atoms + 6, 1 + 3 * struc2.n_atoms + 6))
+        check(lib().fpp_struc_struc(d._h, sigma, self.power, struc1.structure.handle,
+                                    struc2.structure.handle, ptr(K), _stream(stream)))
+        return K
+
+    def self_kernel_struc(self, struc, hyps=None, stream=None):
+        """self_kernel_struc (normalized_dot_product.cpp:446-578): the
+        diagonal of struc_struc(struc, struc)."""
+        sigma = self.sigma if hyps is None else float(hyps[0])
+        d = struc.descriptor_calculator
+        v = np.zeros(1 + 3 * struc.n_atoms + 6)
+        check(lib().fpp_self_kernel_struc(d._h, sigma, self.power,
+                                          struc.structure.handle, ptr(v), _stream(stream)))
+        return v
+
     def envs_envs(self, envs1, envs2, hyps=None, stream=None):
         """envs_envs (normalized_dot_product.cpp:27-87), FP64 on the GPU."""
         sigma = self.sigma if hyps is None else float(hyps[0])
@@ -514,13 +535,35 @@ class SparseGP:
             cols.append(K[:, 1 + 3 * n:7 + 3 * n])
         return np.hstack(cols) if cols else np.zeros((K.shape[0], 0))
 
+    def _kuf_batched(self, sd, k, stream=None):
+        """Kuf of all training structures in one device-resident pass
+        (fpp_kuf_batched; sparse_gp.cpp:392-462, 565-574)."""
+        strucs = self.training_structures
+        mask, offs, atoms, n_lab = [], [0], [], 0
+        for s, a in zip(strucs, self.training_atom_indices):
+            m = (1 if len(s.energy) else 0) | (2 if len(s.forces) else 0) | \
+                (4 if len(s.stresses) else 0)
+            mask.append(m)
+            if m & 2:
+                atoms.extend(a)
+                n_lab += 3 * len(a)
+            offs.append(len(atoms))
+            n_lab += (1 if m & 1 else 0) + (6 if m & 4 else 0)
+        model = _Model(sd.descriptor_calculator, k.sigma, k.power, sd)
+        Kuf = np.zeros((sd.n_clusters, n_lab))
+        hs = (_lib.ctypes.c_void_p * max(1, len(strucs)))(*[s.handle for s in strucs])
+        mask_a, offs_a = i32(mask), i32(offs)
+        atoms_a = i32(atoms if atoms else [0])
+        check(lib().fpp_kuf_batched(model.handle, hs, len(strucs), ptr(mask_a), ptr(offs_a),
+                                    ptr(atoms_a), ptr(Kuf), n_lab, _stream(stream)))
+        return Kuf
+
     def update_matrices_QR(self):
         """sparse_gp.cpp:576-610: Kuu, Kuf and the QR solve on the GPU."""
         sd = self.sparse_descriptors[0]
         k = self.kernels[0]
         self.Kuu = k.envs_envs(sd, sd)
-        self.Kuf = np.hstack([self._kuf_columns(s, a) for s, a in
-                              zip(self.training_structures, self.training_atom_indices)])
+        self.Kuf = self._kuf_batched(sd, k)
         self.alpha, self.R_inv, self.L_inv = update_matrices_QR(
             self.Kuu, self.Kuf, self.y, self.noise_vector, self.Kuu_jitter)
         self.Sigma = self.R_inv @ self.R_inv.T
@@ -564,6 +607,27 @@ class SparseGP:
                                 ptr(var), _stream(stream)))
         structure.mean_efs = out
         structure.variance_efs = var
+
+    def predict_DTC(self, structure, stream=None):
+        """sparse_gp.cpp:651-680 -> structure.mean_efs, structure.variance_efs:
+        variance = K_self - diag(K^T Kuu^-1 K) + diag(K^T Sigma K), with K the
+        environment/structure kernel and K_self the structure self kernel,
+        both from the GPU (the trained model's Kuu^-1 and Sigma)."""
+        if self.Sigma is None or self.Kuu_inverse is None:
+            raise ValueError("predict_DTC needs a model trained with update_matrices_QR")
+        k = self.kernels[0]
+        b2 = self._model.b2
+        if not structure.descriptors:
+            if not structure.descriptor_calculators:
+                structure.descriptor_calculators = [b2]
+            structure.compute_descriptors()
+        dv = structure.descriptors[0]
+        K = k.envs_struc(self.sparse_descriptors[0], dv, stream=stream)
+        structure.mean_efs = K.T @ self.alpha
+        k_self = k.self_kernel_struc(dv, stream=stream)
+        q_self = np.einsum("ij,ij->j", K, self.Kuu_inverse @ K)
+        v_sor = np.einsum("ij,ij->j", K, self.Sigma @ K)
+        structure.variance_efs = k_self - q_self + v_sor
 
     def predict_mapped(self, structure, precision="mixed", stream=None,
                        atom_energies=False):

@@ -26,6 +26,26 @@
 namespace fpp {
 
 int upload_descriptor_tables(cudaStream_t stream) { return upload_b3_tables(stream); }
+
+void fill_fp32_cutoffs(B2Args &a) {
+  a.r1f = (float)a.r1;
+  for (int k = 0; k < kMaxSpecies * kMaxSpecies; k++) {
+    const double rc = a.cutoffs[k];
+    a.cutoffs32[k] = (float)rc;
+    // fl32(r) < cut_lo  =>  r <= fl32(r) (1 + 2^-24) < rc, and symmetrically
+    a.cut_lo[k] = nextafterf((float)(rc * (1.0 - 1e-6)), 0.0f);
+    a.cut_hi[k] = nextafterf((float)(rc * (1.0 + 1e-6)), 3.0e38f);
+  }
+}
+
+// Descriptor filter r <= rc of b2.cpp:277 / b3.cpp:258 for a pair, FP32
+// first: only pairs within the band around rc read the FP64 distance.
+__device__ __forceinline__ bool keep_pair32(const B2Args &a, int k, float rf,
+                                            const dvec4 *__restrict__ rel, long long p) {
+  if (rf < a.cut_lo[k]) return true;
+  if (rf > a.cut_hi[k]) return false;
+  return rel[p].x <= a.cutoffs[k];
+}
 int b3_n_ls_host(int lmax) { return b3_n_ls(lmax); }
 
 int upload_harmonic_tables(cudaStream_t stream) {
@@ -80,6 +100,28 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Error-free sum a + b = s + e (Knuth's two-sum), FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Warp sum of the float-float values (hi, lo), kept as float-float: FP32
+// arithmetic only (FP64 instructions are scarce on this GPU).
+__device__ __forceinline__ void ff_warp_sum(float &hi, float &lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e += lo + l2;
+    hi = s + e;
+    lo = e - (hi - s);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -163,25 +205,37 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       if (b < cnt) {
         const int p = w0 + b;
         const int sp = nbr_s[p];
-        const dvec4 rd = rel[p];
-        const double rcut = a.cutoffs[si * NS + sp];
-        const bool keep = a.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
-        T r, x, y, z;
+        const int kc = si * NS + sp;
+        T r, x, y, z, r1t, rct;
+        bool keep;
         if (sizeof(T) == 8) {
+          const dvec4 rd = rel[p];
+          const double rcut = a.cutoffs[kc];
+          keep = a.strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
           r = T(rd.x);
           x = T(rd.y);
           y = T(rd.z);
           z = T(rd.w);
+          r1t = T(a.r1);
+          rct = T(rcut);
         } else {
           const float4 rf = rel32[p];
           x = T(rf.x);
           y = T(rf.y);
           z = T(rf.z);
           r = T(rf.w);
+          if (a.strict) {
+            const dvec4 rd = rel[p];
+            keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
+          } else {
+            keep = keep_pair32(a, kc, rf.w, rel, p);
+          }
+          r1t = T(a.r1f);
+          rct = T(a.cutoffs32[kc]);
         }
         if (keep) {
           sj = sp;
-          radial_basis<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, g_s + (size_t)b * GP,
+          radial_basis<T>(r, r1t, rct, N, a.cutoff_kind, g_s + (size_t)b * GP,
                           nullptr, 1);
           real_harmonics<T>(x, y, z, a.lmax, y_s + b, nullptr, WS);
         }
@@ -277,13 +331,28 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       nacc.add(v * v);
     }
   }
-  const double nsq = warp_sum(double(nacc.s) + double(nacc.c));
-  const double nrm = sqrt(nsq);
+  double nrm, inv;
+  float invf;
+  if (sizeof(T) == 8) {
+    const double nsq = warp_sum(double(nacc.s) + double(nacc.c));
+    nrm = sqrt(nsq);
+    inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    invf = float(inv);
+  } else {
+    // |p|^2 as float-float; sqrt and 1/sqrt by one correction step of the
+    // FP32 values (relative error ~1 ulp of FP32), no FP64 division or sqrt
+    float hi = float(nacc.s), lo = float(nacc.c);
+    ff_warp_sum(hi, lo);
+    const float r0 = sqrtf(hi);
+    const float rc = r0 > 0.0f ? (fmaf(-r0, r0, hi) + lo) / (2.0f * r0) : 0.0f;
+    const float y0 = r0 > 0.0f ? 1.0f / r0 : 0.0f;
+    invf = fmaf(-y0 * y0, rc, y0);
+    nrm = double(r0) + double(rc);
+    inv = double(invf);
+  }
   if (lane == 0) norm_out[atom] = nrm;
   __syncwarp();
   const int row = row_of_atom[atom];
-  const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
-  const float invf = float(inv);
   for (int d = lane; d < nd; d += 32) {
     const T v = p_s[d];
     if (p_out) p_out[(size_t)atom * nd + d] = v;
@@ -292,7 +361,7 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       // centred operand: delta = phat - pbar, scaled by 2^13 (|delta| <= 2)
       const float x = (float(v) * invf - pbar[(size_t)si * nd + d]) * 8192.0f;
       const __half h = __float2half_rn(x);
-      const float rem = (x - __half2float(h)) * 2048.0f;
+      const float rem = x - __half2float(h);  // residual (fp16, subnormal when tiny)
       phat_hi[(size_t)row * ldp + d] = h;
       phat_lo[(size_t)row * ldp + d] = __float2half_rn(rem);
     }
@@ -302,10 +371,9 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 // w = dE/dp of one atom into w_s[nd] (all lanes), returning the atom energy:
 // from the contraction V (mapped power 2), the beta vector (power 1), or
 // given per operand row (kernel form).
-template <typename T>
+template <typename T, typename Store>
 __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, int si,
-                                            int row, double nrm, T *__restrict__ w_s,
-                                            int lane) {
+                                            int row, double nrm, Store store, int lane) {
   const int nd = a.n_d;
   double e = 0.0;
   if ((g.mode == kWFromV2 || g.mode == kWFromV1) && g.phat64) {
@@ -323,9 +391,9 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     for (int d = lane; d < nd; d += 32) {
       const double ph = g.phat64[(size_t)row * g.ldp + d];
       if (g.mode == kWFromV2)
-        w_s[d] = T(2.0 * (g.V64[(size_t)row * g.ldv + d] - e * ph) * inv);
+        store(d, T(2.0 * (g.V64[(size_t)row * g.ldv + d] - e * ph) * inv));
       else
-        w_s[d] = T((g.beta1[(size_t)si * nd + d] - e * ph) * inv);
+        store(d, T((g.beta1[(size_t)si * nd + d] - e * ph) * inv));
     }
   } else if (g.mode == kWFromV2 || g.mode == kWFromV1) {
     // mixed form on the centred operand delta = phat - pbar (float):
@@ -336,31 +404,32 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     Acc<float> acc;
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
-      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o])) *
                        (1.0f / 8192.0f);
       if (g.mode == kWFromV2)
         acc.add((2.0f * g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) * dl);
       else
         acc.add(float(g.beta1[(size_t)si * nd + d]) * (g.pbar[(size_t)si * nd + d] + dl));
     }
-    const double dot = warp_sum(double(acc.s) + double(acc.c)) +
-                       (g.mode == kWFromV2 ? g.c0[si] : 0.0);
+    float hi = acc.s, lo = acc.c;
+    ff_warp_sum(hi, lo);
+    const double dot = (double(hi) + double(lo)) + (g.mode == kWFromV2 ? g.c0[si] : 0.0);
     e = empty ? 0.0 : dot;
     const float ef = float(e);
-    const float inv = empty ? 0.0f : float(1.0 / nrm);
+    const float inv = empty ? 0.0f : 1.0f / float(nrm);
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
-      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o])) *
                        (1.0f / 8192.0f);
       const float ph = g.pbar[(size_t)si * nd + d] + dl;
       if (g.mode == kWFromV2)
-        w_s[d] = T(2.0f * ((g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) -
-                           ef * ph) * inv);
+        store(d, T(2.0f * ((g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) -
+                           ef * ph) * inv));
       else
-        w_s[d] = T((float(g.beta1[(size_t)si * nd + d]) - ef * ph) * inv);
+        store(d, T((float(g.beta1[(size_t)si * nd + d]) - ef * ph) * inv));
     }
   } else {  // kWGiven: dE/dp supplied per operand row (kernel form)
-    for (int d = lane; d < nd; d += 32) w_s[d] = T(g.w_given[(size_t)row * g.ldp + d]);
+    for (int d = lane; d < nd; d += 32) store(d, T(g.w_given[(size_t)row * g.ldp + d]));
     e = g.e_given ? g.e_given[row] : 0.0;
   }
   return e;
@@ -370,12 +439,21 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
 // Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
 // u = dE/dc = (W + W^T) c per l, written to global memory.
 // ---------------------------------------------------------------------------
+// Dense symmetric form of w per l for the u product: rows of wd are
+// (n2, l) with n1 contiguous, row stride wd_stride(nr) (a multiple of 4 that
+// spreads the five l rows over different banks).
+__host__ __device__ inline int wd_stride(int nr) {
+  const int r4 = (nr + 3) & ~3;
+  return r4 + ((r4 % 8 == 0) ? 4 : 0);
+}
+constexpr int kDenseMaxNR = 32;
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
-        const int *__restrict__ row_of_atom, const T *__restrict__ c_in,
-        const double *__restrict__ norm_in, double *__restrict__ atom_e,
-        T *__restrict__ u_out) {
+        const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
+        const T *__restrict__ c_in, const double *__restrict__ norm_in,
+        double *__restrict__ atom_e, T *__restrict__ u_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
@@ -383,24 +461,81 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
   const int sb = NS * N * H, nr = NS * N;
   const int L1 = a.lmax + 1;
+  const bool dense = nr <= kDenseMaxNR;
+  const int NRP = wd_stride(nr);
   unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);  // [nd]
-  T *c_s = w_s + nd;                     // [sb]
+  T *w_s = reinterpret_cast<T *>(base);  // dense: [nr][L1][NRP]; else packed [nd]
+  T *c_s = w_s + (dense ? nr * L1 * NRP : nd);  // [sb]
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
   const double nrm = norm_in[atom];
   for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
 
-  const double e = adjoint_w<T>(a, g, si, row, nrm, w_s, lane);
+  double e;
+  if (dense) {
+    // packed index d = q L1 + l of the pair q = (n1 <= n2): scatter into the
+    // symmetric dense rows, diagonal doubled (the product rule's factor 2)
+    const unsigned magic = 0xFFFFFFFFu / (unsigned)L1 + 1u;  // exact d / L1 for d < 2^16
+    e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) {
+      const int q = L1 == 1 ? d : (int)__umulhi((unsigned)d, magic);
+      const int l = d - q * L1;
+      const int pr = pair_tab[q];
+      const int n1 = pr & 0xffff, n2 = pr >> 16;
+      if (n1 == n2) {
+        w_s[(n2 * L1 + l) * NRP + n1] = T(2) * v;
+      } else {
+        w_s[(n2 * L1 + l) * NRP + n1] = v;
+        w_s[(n1 * L1 + l) * NRP + n2] = v;
+      }
+    }, lane);
+  } else {
+    e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
+  }
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
+  const int NP = u_npad(a), usb = u_row_stride(a);
   for (int lm0 = 0; lm0 < H; lm0 += 32) {
     const int lm = lm0 + lane;
     if (lm >= H) continue;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
+    if (dense) {
+      // all n1 in registers; each n2 reads one dense row with 16-byte loads
+      T acc[kDenseMaxNR];
+#pragma unroll
+      for (int k = 0; k < kDenseMaxNR; k++) acc[k] = T(0);
+      for (int n2 = 0; n2 < nr; n2++) {
+        const T c = c_s[n2 * H + lm];
+        const T *wr = w_s + (n2 * L1 + l) * NRP;
+#pragma unroll
+        for (int k = 0; k < kDenseMaxNR; k += 4)
+          if (k < nr) {
+            T w4[4];
+            if (sizeof(T) == 4) {
+              const float4 q = *reinterpret_cast<const float4 *>(wr + k);
+              w4[0] = T(q.x);
+              w4[1] = T(q.y);
+              w4[2] = T(q.z);
+              w4[3] = T(q.w);
+            } else {
+              const double2 q0 = *reinterpret_cast<const double2 *>(wr + k);
+              const double2 q1 = *reinterpret_cast<const double2 *>(wr + k + 2);
+              w4[0] = T(q0.x);
+              w4[1] = T(q0.y);
+              w4[2] = T(q1.x);
+              w4[3] = T(q1.y);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[k + j] += w4[j] * c;
+          }
+      }
+#pragma unroll
+      for (int n1 = 0; n1 < kDenseMaxNR; n1++)
+        if (n1 < nr) u_out[(size_t)atom * usb + ((n1 / N) * H + lm) * NP + (n1 % N)] = acc[n1];
+      continue;
+    }
     for (int n1 = 0; n1 < nr; n1++) {
       T acc = T(0);
       // n2 < n1: pair (n2, n1), index q = n2 nr - n2 (n2 - 1)/2 + (n1 - n2)
@@ -413,7 +548,7 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
       q = n1 * nr - (n1 * (n1 - 1)) / 2;
       acc += T(2) * w_s[q * L1 + l] * c_s[n1 * H + lm];
       for (int n2 = n1 + 1; n2 < nr; n2++) acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
-      u_out[(size_t)atom * sb + n1 * H + lm] = acc;
+      u_out[(size_t)atom * usb + ((n1 / N) * H + lm) * NP + (n1 % N)] = acc;
     }
   }
 }
@@ -459,41 +594,13 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const double nrm = norm_in[atom];
   // real c staged through ur (free until the reduction below)
   for (int k = lane; k < sb; k += 32) ur[k] = c_in[(size_t)atom * sb + k];
-  const double e = adjoint_w<T>(a, g, si, row, nrm, w_s, lane);
+  const double e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   b3_to_complex<T>(ur, nr, H, zr, zi, lane);
   for (int k = 0; k < 2 * sb; k++) up[(size_t)k * 32 + lane] = T(0);
   __syncwarp();
-  const int *beg = c_b3.beg + c_b3.ls_off[a.lmax];
-  const int n_ls = a.n_ls;
-  for (int t = 0; t < n_ls; t++) {
-    const int e0 = beg[t], e1 = beg[t + 1];
-    for (int r0 = 0; r0 < a.n_tri; r0 += 32) {
-      const int r = r0 + lane;
-      if (r >= a.n_tri) continue;
-      const T wq = w_s[r * n_ls + t];
-      const int tr = tri[r];
-      const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
-      for (int q = e0; q < e1; q++) {
-        const unsigned ix = c_b3.idx[q];
-        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
-        const T f = wq * T(c_b3.w[q]);
-        const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
-        const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
-        const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
-        T *p1 = up + (size_t)(2 * (n1 * H + i1)) * 32 + lane;
-        T *p2 = up + (size_t)(2 * (n2 * H + i2)) * 32 + lane;
-        T *p3 = up + (size_t)(2 * (n3 * H + i3)) * 32 + lane;
-        p1[0] += f * (br * cr - bi * ci);
-        p1[32] += f * (br * ci + bi * cr);
-        p2[0] += f * (ar * cr - ai * ci);
-        p2[32] += f * (ar * ci + ai * cr);
-        p3[0] += f * (ar * br - ai * bi);
-        p3[32] += f * (ar * bi + ai * br);
-      }
-    }
-  }
+  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, tri, zr, zi, w_s, up, lane);
   __syncwarp();
   for (int k = lane; k < sb; k += 32) {
     T sr = T(0), sm = T(0);
@@ -524,7 +631,7 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
       v = (sg * ur[kp] + ur[km]) * is2;
     else
       v = (ui[km] - sg * ui[kp]) * is2;
-    u_out[(size_t)atom * sb + k] = v;
+    u_out[(size_t)atom * u_row_stride(a) + ((n / a.N) * H + lm) * u_npad(a) + (n % a.N)] = v;
   }
 }
 
@@ -649,36 +756,68 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
   const int N = a.N, H = a.H, NS = a.n_species;
   const int sb = NS * N * H;
   const int i = nbr_i[p], sj = nbr_s[p], si = species[i];
-  const dvec4 rd = rel[p];
-  const double rcut = a.cutoffs[si * NS + sj];
-  const bool keep = strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+  const int kc = si * NS + sj;
+  T r, x, y, z, r1t, rct;
+  bool keep;
+  if (sizeof(T) == 8) {
+    const dvec4 rd = rel[p];
+    const double rcut = a.cutoffs[kc];
+    keep = strict ? (rsq_exact(rd) < dmul(rcut, rcut)) : (rd.x <= rcut);
+    r = T(rd.x);
+    x = T(rd.y);
+    y = T(rd.z);
+    z = T(rd.w);
+    r1t = T(a.r1);
+    rct = T(rcut);
+  } else {
+    const float4 rf = rel32[p];
+    x = T(rf.x);
+    y = T(rf.y);
+    z = T(rf.z);
+    r = T(rf.w);
+    if (strict) {
+      const dvec4 rd = rel[p];
+      keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
+    } else {
+      keep = keep_pair32(a, kc, rf.w, rel, p);
+    }
+    r1t = T(a.r1f);
+    rct = T(a.cutoffs32[kc]);
+  }
   T f[3] = {T(0), T(0), T(0)};
   if (keep) {
-    T r, x, y, z;
-    if (sizeof(T) == 8) {
-      r = T(rd.x);
-      x = T(rd.y);
-      y = T(rd.z);
-      z = T(rd.w);
-    } else {
-      const float4 rf = rel32[p];
-      x = T(rf.x);
-      y = T(rf.y);
-      z = T(rf.z);
-      r = T(rf.w);
-    }
     T gr[kMaxN], dg[kMaxN];
-    radial_basis_reg<T>(r, T(a.r1), T(rcut), N, a.cutoff_kind, gr, dg);
-    const T *ur = u + (size_t)i * sb + (size_t)sj * N * H;
+    radial_basis_reg<T>(r, r1t, rct, N, a.cutoff_kind, gr, dg);
+    const int NP = u_npad(a);
+    const T *ur = u + (size_t)i * u_row_stride(a) + (size_t)sj * H * NP;
     T fr = T(0);
     harmonics_visit<T>(x, y, z, a.lmax, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
       T ag = T(0), bd = T(0);
+      const T *col = ur + lm * NP;
 #pragma unroll
-      for (int n = 0; n < kMaxN; n++)
-        if (n < N) {
-          const T uv = ur[n * H + lm];
-          ag += uv * gr[n];
-          bd += uv * dg[n];
+      for (int n0 = 0; n0 < kMaxN; n0 += 4)
+        if (n0 < N) {
+          T uv[4];
+          if (sizeof(T) == 4) {
+            const float4 q = *reinterpret_cast<const float4 *>(col + n0);
+            uv[0] = T(q.x);
+            uv[1] = T(q.y);
+            uv[2] = T(q.z);
+            uv[3] = T(q.w);
+          } else {
+            const double2 q0 = *reinterpret_cast<const double2 *>(col + n0);
+            const double2 q1 = *reinterpret_cast<const double2 *>(col + n0 + 2);
+            uv[0] = T(q0.x);
+            uv[1] = T(q0.y);
+            uv[2] = T(q1.x);
+            uv[3] = T(q1.y);
+          }
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (n0 + k < N) {
+              ag += uv[k] * gr[n0 + k];
+              bd += uv[k] * dg[n0 + k];
+            }
         }
       fr += bd * Yv;
       f[0] += ag * Yx;
@@ -690,10 +829,15 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
     f[1] += fr * y * ir;
     f[2] += fr * z * ir;
   }
-  pair_f[(size_t)p * 4 + 0] = f[0];
-  pair_f[(size_t)p * 4 + 1] = f[1];
-  pair_f[(size_t)p * 4 + 2] = f[2];
-  pair_f[(size_t)p * 4 + 3] = T(0);
+  if (sizeof(T) == 4) {
+    reinterpret_cast<float4 *>(pair_f)[p] =
+        make_float4(float(f[0]), float(f[1]), float(f[2]), 0.0f);
+  } else {
+    pair_f[(size_t)p * 4 + 0] = f[0];
+    pair_f[(size_t)p * 4 + 1] = f[1];
+    pair_f[(size_t)p * 4 + 2] = f[2];
+    pair_f[(size_t)p * 4 + 3] = T(0);
+  }
 }
 
 // Stored derivatives of b2.cpp:181-242 for a list of structure pairs (FP64):
@@ -806,7 +950,46 @@ k_gather(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
   __shared__ double sm[10][128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (i < noa) {
+  if (sizeof(T) == 4 && i < noa) {
+    // FP32 pair forces: per-atom sums kept as float-float (exact to ~2^-48)
+    // and the virial compensated, so no FP64 instruction runs per pair
+    float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};
+    float Vs[9], Vc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Vs[k] = Vc[k] = 0.0f;
+    for (int p = offset[i]; p < offset[i + 1]; p++) {
+      const int q = rev[p];
+      const float4 fp = reinterpret_cast<const float4 *>(pair_f)[p];
+      const float4 fq = q >= 0 ? reinterpret_cast<const float4 *>(pair_f)[q]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float fv[3] = {fp.x, fp.y, fp.z}, gv[3] = {fq.x, fq.y, fq.z};
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        float s, e;
+        two_sum(Fh[a], fv[a], s, e);
+        Fl[a] += e;
+        two_sum(s, -gv[a], Fh[a], e);
+        Fl[a] += e;
+      }
+      const float4 r = rel32[p];
+      const float rr[3] = {r.x, r.y, r.z};
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+          const int k = a * 3 + b;
+          const float x = fv[a] * rr[b];
+          const float t = Vs[k] + x;
+          Vc[k] += fabsf(Vs[k]) >= fabsf(x) ? (Vs[k] - t) + x : (x - t) + Vs[k];
+          Vs[k] = t;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) forces[3 * i + a] = double(Fh[a]) + double(Fl[a]);
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[1 + k] = double(Vs[k]) + double(Vc[k]);
+    acc[0] = atom_e[i];
+  } else if (i < noa) {
     double F[3] = {0, 0, 0};
     for (int p = offset[i]; p < offset[i + 1]; p++) {
       const int q = rev[p];
@@ -884,8 +1067,10 @@ size_t forward_smem_per_warp(const B2Args &a, size_t elem) {
 }
 
 size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
-  const int sb = a.n_species * a.N * a.H;
-  size_t b = elem * ((size_t)a.n_d + (size_t)sb);
+  const int sb = a.n_species * a.N * a.H, nr = a.n_species * a.N;
+  const size_t w = nr <= kDenseMaxNR ? (size_t)nr * (a.lmax + 1) * wd_stride(nr)
+                                     : (size_t)a.n_d;
+  size_t b = elem * (w + (size_t)sb);
   return (b + 15) & ~(size_t)15;
 }
 
@@ -938,8 +1123,9 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
-    kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom, c_in,
-                                                           norm_in, atom_e, u_buf);
+    kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom,
+                                                           pair_tab, c_in, norm_in, atom_e,
+                                                           u_buf);
   }
   if (cudaGetLastError() != cudaSuccess) return -1;
   if (n_pairs > 0) {

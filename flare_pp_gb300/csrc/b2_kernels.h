@@ -25,9 +25,23 @@ struct B2Args {
   int strict;       // pair filter rsq < rc^2 (pair style) instead of r <= rc (B2)
   double r1;
   double cutoffs[kMaxSpecies * kMaxSpecies];
+  // FP32 copies for the FP32 kernels, and bounds such that a pair whose
+  // FP32 distance is below cut_lo is surely inside the FP64 cutoff and one
+  // above cut_hi surely outside (only pairs between are decided in FP64)
+  float r1f;
+  float cutoffs32[kMaxSpecies * kMaxSpecies];
+  float cut_lo[kMaxSpecies * kMaxSpecies], cut_hi[kMaxSpecies * kMaxSpecies];
   size_t smem_per_warp;      // filled by the launcher
   size_t smem_per_warp_adj;  // filled by the launcher
 };
+
+// Row of u = dE/dc per atom, laid out [species][lm][n] with n padded to a
+// multiple of 4, so the pair-force kernel reads each (species, lm) column
+// with 16-byte loads.
+inline __host__ __device__ int u_npad(const B2Args &a) { return (a.N + 3) & ~3; }
+inline __host__ __device__ int u_row_stride(const B2Args &a) {
+  return a.n_species * a.H * u_npad(a);
+}
 
 enum WMode { kWFromV2 = 0, kWFromV1 = 1, kWGiven = 2 };
 
@@ -61,6 +75,7 @@ struct Neigh {
 };
 
 int upload_harmonic_tables(cudaStream_t stream);
+void fill_fp32_cutoffs(B2Args &a);  // from r1 and cutoffs
 int upload_descriptor_tables(cudaStream_t stream);  // B3 coupling tables
 int b3_n_ls_host(int lmax);
 size_t forward_smem_per_warp(const B2Args &a, size_t elem);

@@ -110,8 +110,9 @@ inline int upload_b3_tables(cudaStream_t stream) {
             for (int m2 = -l2; m2 <= l2; m2++) {
               const int m3 = -m1 - m2;
               if (std::abs(m3) > l3) continue;
+              // every (m1, m2) with |m3| <= l3 in loop order, zeros included,
+              // so that the term offsets within a triangle are fixed
               const double w = b3_reference_coeff(l1, l2, l3, m1, m2, m3, lmax);
-              if (w == 0.0) continue;  // contributes exactly nothing
               if (nt >= kB3MaxTerms) return -1;
               t.idx[nt] = (unsigned)(l1 * l1 + l1 + m1) |
                           ((unsigned)(l2 * l2 + l2 + m2) << 8) |
@@ -162,7 +163,8 @@ __device__ __forceinline__ void b3_to_complex(const T *__restrict__ c, int nr, i
 }
 
 // p[r * n_ls + t] for every radial triple r (table tri: n1 | n2<<8 | n3<<16)
-// and triangle t; lanes take triples, all lanes walk the same term list.
+// and triangle t; lanes take triples, all lanes walk the same term list (the
+// coefficients and harmonic indices are uniform loads from constant memory).
 template <typename T>
 __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H,
                                             const int *__restrict__ tri,
@@ -173,9 +175,7 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
   const int *beg = c_b3.beg + c_b3.ls_off[lmax];
   for (int t = 0; t < n_ls; t++) {
     const int e0 = beg[t], e1 = beg[t + 1];
-    for (int r0 = 0; r0 < n_tri; r0 += 32) {
-      const int r = r0 + lane;
-      if (r >= n_tri) continue;
+    for (int r = lane; r < n_tri; r += 32) {
       const int tr = tri[r];
       const int o1 = (tr & 0xff) * H1, o2 = ((tr >> 8) & 0xff) * H1, o3 = (tr >> 16) * H1;
       T acc = T(0);
@@ -189,6 +189,46 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
         acc += T(c_b3.w[e]) * (xr * cr - xi * ci);
       }
       p[r * n_ls + t] = acc;
+    }
+  }
+}
+
+// Adjoint of b3_contract: for dE/dp = w, the holomorphic derivative
+// u = dE/dc accumulated per lane into up[(2 k + part) * 32 + lane]
+// (k = n * H + lm: each lane owns a column, so no atomics; the caller sums
+// the 32 columns in a fixed order).
+template <typename T>
+__device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tri, int H,
+                                                    const int *__restrict__ tri,
+                                                    const T *__restrict__ zr,
+                                                    const T *__restrict__ zi,
+                                                    const T *__restrict__ w,
+                                                    T *__restrict__ up, int lane) {
+  const int H1 = H + 1;
+  const int *beg = c_b3.beg + c_b3.ls_off[lmax];
+  for (int t = 0; t < n_ls; t++) {
+    const int e0 = beg[t], e1 = beg[t + 1];
+    for (int r = lane; r < n_tri; r += 32) {
+      const T wq = w[r * n_ls + t];
+      const int tr = tri[r];
+      const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
+      for (int q = e0; q < e1; q++) {
+        const unsigned ix = c_b3.idx[q];
+        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
+        const T f = wq * T(c_b3.w[q]);
+        const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
+        const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
+        const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
+        T *p1 = up + (size_t)(2 * (n1 * H + i1)) * 32 + lane;
+        T *p2 = up + (size_t)(2 * (n2 * H + i2)) * 32 + lane;
+        T *p3 = up + (size_t)(2 * (n3 * H + i3)) * 32 + lane;
+        p1[0] += f * (br * cr - bi * ci);
+        p1[32] += f * (br * ci + bi * cr);
+        p2[0] += f * (ar * cr - ai * ci);
+        p2[32] += f * (ar * ci + ai * cr);
+        p3[0] += f * (ar * br - ai * bi);
+        p3[32] += f * (ar * bi + ai * br);
+      }
     }
   }
 }

@@ -291,6 +291,7 @@ int fpp_b2_create(const char *radial_basis, const char *cutoff_function,
     a.cutoffs[(i / ns) * ns + (i % ns)] = v;
     b->max_cutoff = std::max(b->max_cutoff, v);
   }
+  fill_fp32_cutoffs(a);
   // (n1, n2 >= n1) table in the reference's counter order (b2.cpp:209-231)
   std::vector<int> tab;
   for (int n1 = 0; n1 < nr; n1++)

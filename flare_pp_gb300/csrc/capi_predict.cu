@@ -44,7 +44,7 @@ static int get_cublas(fpp_model *m, cudaStream_t st, cublasHandle_t *out) {
   return FPP_OK;
 }
 
-static int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st) {
+int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st) {
   if (buf.ptr) return FPP_OK;
   FPP_TRY(buf.reserve(sizeof(int) * tab.size()));
   FPP_CUDA(cudaMemcpyAsync(buf.ptr, tab.data(), sizeof(int) * tab.size(),
@@ -100,8 +100,8 @@ static Neigh neigh_of(StructureState &S) {
 }
 
 // FP64 forward: c64, norm64 (atom order), phat64 rows, optional p64 atom order.
-static int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want_p,
-                     cudaStream_t st) {
+int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want_p,
+              cudaStream_t st) {
   StructureState &S = s->st;
   B2Args a = a0;
   a.noa = S.noa;
@@ -383,7 +383,7 @@ static int upload_beta(fpp_model *m, int s, const std::vector<double> &B) {
   for (size_t k = 0; k < pad.size(); k++) {
     const float x = (float)(pad[k] * scale);
     const __half h = __float2half_rn(x);
-    const float rem = (float)((pad[k] * scale - (double)__half2float(h)) * 2048.0);
+    const float rem = (float)(pad[k] * scale - (double)__half2float(h));  // residual
     hi[k] = h;
     lo[k] = __float2half_rn(rem);
   }
@@ -638,7 +638,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     }
     S.mark(4, st);
     g.phat64 = phat;
-    FPP_TRY(adjoint_buffers(S, sizeof(double), a.n_species * a.N * a.H));
+    FPP_TRY(adjoint_buffers(S, sizeof(double), u_row_stride(a)));
     if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
                                   s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
                                   S.c64.as<double>(), S.norm64.as<double>(),
@@ -653,30 +653,32 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     S.mark(3, st);
     if (m->beta_power == 2) {
       FPP_TRY(reserve_zero(S.V, sizeof(float) * (size_t)s->total_rows * ldp, st));
+      GroupedGemmArgs ga;
+      std::memset(&ga, 0, sizeof(ga));
+      ga.a_hi = S.phat_hi.as<__half>();
+      ga.a_lo = S.phat_lo.as<__half>();
+      ga.a_rows = s->total_rows;
+      ga.lda = ldp;
       for (int sp = 0; sp < m->n_species; sp++) {
         if (s->n_rows[sp] == 0) continue;
-        SplitGemmArgs ga;
-        ga.a_hi = S.phat_hi.as<__half>();
-        ga.a_lo = S.phat_lo.as<__half>();
-        ga.a_rows = s->total_rows;
-        ga.lda = ldp;
-        ga.row0 = s->row_off[sp];
-        ga.b_hi = m->sp[sp].beta_hi.as<__half>();
-        ga.b_lo = m->sp[sp].beta_lo.as<__half>();
-        ga.b_rows = nd;
-        ga.ldb = m->ldb;
-        ga.M = s->n_rows[sp];
-        ga.N = nd;
-        ga.K = nd;
-        ga.out_scale = (float)(1.0 / (8192.0 * m->sp[sp].beta_scale));
-        ga.V = S.V.as<float>() + (size_t)s->row_off[sp] * ldp;
-        ga.ldv = ldp;
-        ga.status = S.status.as<DeviceStatus>();
-        int rc = launch_split_gemm(ga, st);
-        if (rc != 0)
-          return fail(FPP_ERR_CUDA, "split-fp16 contraction launch failed (" +
-                                        std::to_string(rc) + ")");
+        GemmGroup &q = ga.group[ga.n_groups++];
+        q.b_hi = m->sp[sp].beta_hi.as<__half>();
+        q.b_lo = m->sp[sp].beta_lo.as<__half>();
+        q.b_rows = nd;
+        q.ldb = m->ldb;
+        q.row0 = s->row_off[sp];
+        q.M = s->n_rows[sp];
+        q.out_scale = (float)(1.0 / (8192.0 * m->sp[sp].beta_scale));
       }
+      ga.N = nd;
+      ga.K = nd;
+      ga.V = S.V.as<float>();
+      ga.ldv = ldp;
+      ga.status = S.status.as<DeviceStatus>();
+      const int rc = launch_split_gemm_grouped(ga, st);
+      if (rc != 0)
+        return fail(FPP_ERR_CUDA,
+                    "split-fp16 contraction launch failed (" + std::to_string(rc) + ")");
       g.V32 = S.V.as<float>();
     }
     S.mark(4, st);
@@ -685,7 +687,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     g.pbar = m->pbar32.as<float>();
     g.gvec = m->g32.as<float>();
     for (int k = 0; k < m->n_species; k++) g.c0[k] = m->c0[k];
-    FPP_TRY(adjoint_buffers(S, sizeof(float), a.n_species * a.N * a.H));
+    FPP_TRY(adjoint_buffers(S, sizeof(float), u_row_stride(a)));
     if (launch_b2_adjoint<float>(a, g, neigh_of(S), S.species.as<int>(),
                                  s->row_of_atom.as<int>(), m->pair_tab.as<int>(),
                                  S.c32.as<float>(), S.pn64.as<double>(),
@@ -803,6 +805,82 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
       return fail(FPP_ERR_CUDA, "envs assembly launch failed");
     FPP_CUDA(cudaStreamSynchronize(st));  // scratch buffers are freed at scope exit
   }
+  return FPP_OK;
+}
+
+}  // extern "C"
+
+namespace fpp {
+// dst[r][col0 + c] = src[r][cols[c]] for r < rows (row-major, leading dims).
+__global__ void k_copy_cols(int rows, int ncols, const double *__restrict__ src, int lds,
+                            const int *__restrict__ cols, double *__restrict__ dst,
+                            long long ldd) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)rows * ncols) return;
+  const int r = (int)(t / ncols), c = (int)(t - (long long)r * ncols);
+  dst[(size_t)r * ldd + c] = src[(size_t)r * lds + cols[c]];
+}
+}  // namespace fpp
+
+extern "C" {
+
+int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures, int32_t n_structures,
+                    const int32_t *label_mask, const int32_t *atom_offsets,
+                    const int32_t *atoms, double *kuf, int64_t n_labels, void *stream) {
+  if (!m || (n_structures > 0 && (!structures || !label_mask)) || !kuf)
+    return fail(FPP_ERR_INVALID, "null argument");
+  if (n_structures < 0 || n_labels < 0) return fail(FPP_ERR_INVALID, "negative count");
+  cudaStream_t st = (cudaStream_t)stream;
+  // label columns of each structure: [E] [F of the listed atoms] [S]
+  std::vector<std::vector<int>> cols(n_structures);
+  int64_t total = 0;
+  for (int k = 0; k < n_structures; k++) {
+    fpp_structure *s = structures[k];
+    if (!s) return fail(FPP_ERR_INVALID, "null structure");
+    const int noa = s->st.noa;
+    std::vector<int> &c = cols[k];
+    if (label_mask[k] & 1) c.push_back(0);
+    if (label_mask[k] & 2) {
+      const int b = atom_offsets ? atom_offsets[k] : 0;
+      const int e = atom_offsets ? atom_offsets[k + 1] : noa;
+      for (int q = b; q < e; q++) {
+        const int a = atom_offsets ? atoms[q] : q;
+        if (a < 0 || a >= noa) return fail(FPP_ERR_INVALID, "force atom index out of range");
+        for (int d = 0; d < 3; d++) c.push_back(1 + 3 * a + d);
+      }
+    }
+    if (label_mask[k] & 4)
+      for (int d = 0; d < 6; d++) c.push_back(1 + 3 * noa + d);
+    total += (int64_t)c.size();
+  }
+  if (total != n_labels)
+    return fail(FPP_ERR_INVALID, "n_labels (" + std::to_string(n_labels) +
+                                     ") differs from the labels of the structures (" +
+                                     std::to_string(total) + ")");
+  const int nst = m->n_sparse_total;
+  DevBuf dK, K, dcols;
+  FPP_TRY(dK.reserve(sizeof(double) * std::max<int64_t>(1, (int64_t)nst * n_labels)));
+  int64_t col0 = 0;
+  for (int k = 0; k < n_structures; k++) {
+    fpp_structure *s = structures[k];
+    FPP_TRY(model_check(m, s));
+    const int n_out = 1 + 3 * s->st.noa + 6;
+    const int nc = (int)cols[k].size();
+    if (nc == 0 || nst == 0) continue;
+    FPP_TRY(envs_struc_device(m, s, st, K));
+    FPP_TRY(dcols.reserve(sizeof(int) * nc));
+    FPP_CUDA(cudaMemcpyAsync(dcols.ptr, cols[k].data(), sizeof(int) * nc,
+                             cudaMemcpyHostToDevice, st));
+    const long long t = (long long)nst * nc;
+    k_copy_cols<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(
+        nst, nc, K.as<double>(), n_out, dcols.as<int>(), dK.as<double>() + col0, n_labels);
+    FPP_CUDA(cudaGetLastError());
+    FPP_CUDA(cudaStreamSynchronize(st));  // dcols / K are reused by the next structure
+    col0 += nc;
+  }
+  if (nst && n_labels)
+    FPP_CUDA(cudaMemcpy(kuf, dK.ptr, sizeof(double) * (size_t)nst * n_labels,
+                        cudaMemcpyDeviceToHost));
   return FPP_OK;
 }
 
@@ -940,7 +1018,7 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
   g.ldp = ldp;
   g.w_given = S.w64.as<double>();
   g.e_given = E.as<double>();
-  FPP_TRY(adjoint_buffers(S, sizeof(double), a.n_species * a.N * a.H));
+  FPP_TRY(adjoint_buffers(S, sizeof(double), u_row_stride(a)));
   FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
   if (launch_b2_adjoint<double>(a, g, neigh_of(S), S.species.as<int>(),
                                 s->row_of_atom.as<int>(), m->pair_tab.as<int>(),

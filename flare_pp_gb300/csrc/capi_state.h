@@ -43,7 +43,7 @@ struct fpp_model {
     fpp::DevBuf d_norms, d_alpha;       // double[n_sparse]
     fpp::DevBuf beta64;                 // double[n_d * ldb] dense symmetric
     fpp::DevBuf beta_hi, beta_lo;       // half[n_d_pad * ldb] split operands
-    double beta_scale = 1;              // beta ~ (hi + lo/2048) / beta_scale
+    double beta_scale = 1;              // beta ~ (hi + lo) / beta_scale, lo the fp16 residual
     std::vector<double> B_host;         // dense beta (n_d x n_d), power 2
   };
   std::vector<Species> sp;
@@ -65,4 +65,9 @@ int prepare_structure(fpp_structure *s, cudaStream_t stream);
 int ensure_layout(fpp_structure *s, int n_species, cudaStream_t stream);
 int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
                 int strict);
+int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st);
+// FP64 forward pass: c64, norm64 (atom order), phat64 rows, p64 (atom order)
+// when want_p.
+int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want_p,
+              cudaStream_t st);
 }  // namespace fpp

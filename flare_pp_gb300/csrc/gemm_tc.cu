@@ -1,22 +1,26 @@
 // Split-fp16 contraction on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
 //   V[m, n] = sum_k P[m, k] B[n, k]
-// with both operands given as power-of-two-scaled fp16 pairs
-//   P ~ (P_hi + P_lo / 2048) / sP,   B ~ (B_hi + B_lo / 2048) / sB,
-// evaluated as three MMAs into two FP32 accumulators held in TMEM:
-//   acc0 += P_hi B_hi^T,   acc1 += P_hi B_lo^T + P_lo B_hi^T,
-//   V = (acc0 + acc1 / 2048) / (sP sB).
+// with both operands given as power-of-two-scaled fp16 pairs, a value and its
+// fp16 residual,
+//   P ~ (P_hi + P_lo) / sP,   B ~ (B_hi + B_lo) / sB,
+// evaluated as three MMAs into one FP32 accumulator held in TMEM:
+//   acc += P_hi B_hi^T + P_hi B_lo^T + P_lo B_hi^T,   V = acc / (sP sB).
 // That keeps about 22 significant bits per operand, which the mapped-beta
-// energy needs (a single fp16 or bf16 term, or a bf16 hi/lo split, does not).
+// energy needs (a single fp16 or bf16 term, or a bf16 hi/lo split, does not);
+// the products of fp16 values are exact in FP32 and the residual terms are
+// 2^-11 of the leading one, so one FP32 accumulator loses nothing against
+// separate ones.
 //
-// One CTA computes a 128 x 256 tile of V:
+// One persistent CTA per SM walks 128 x 256 tiles of all species blocks
+// (each block of P rows against its own B):
 //   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of P_hi, P_lo,
 //                  B_hi, B_lo (64 K-columns per stage) into a 2-stage ring
 //   warp 1 lane 0  MMA issuer: 4 K=16 steps x 3 tcgen05.mma per stage,
-//                  tcgen05.commit frees the stage
-//   warp 2         allocates / frees the 512 TMEM columns
-//   warps 0-3      epilogue: tcgen05.ld of their 32 TMEM lanes, combine,
-//                  scale, store FP32 rows of V
+//                  tcgen05.commit frees the stage; the two 256-column TMEM
+//                  accumulators alternate between tiles
+//   warps 2-5      epilogue: tcgen05.ld of their 32 TMEM lanes, scale, store
+//                  FP32 rows of V, then release the accumulator
 // Every mbarrier wait is bounded; a wait that runs out records
 // FPP_ERR_TIMEOUT in the status word and the CTA skips to its exit.
 #include <cuda.h>
@@ -26,6 +30,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 
 #include "common.cuh"
 #include "gemm_tc.h"
@@ -142,37 +147,62 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ void __launch_bounds__(128, 1)
-k_split_gemm(const __grid_constant__ CUtensorMap map_a_hi,
-             const __grid_constant__ CUtensorMap map_a_lo,
-             const __grid_constant__ CUtensorMap map_b_hi,
-             const __grid_constant__ CUtensorMap map_b_lo, int row0, int M, int N,
-             int K, float out_scale, float *__restrict__ V, int ldv,
-             DeviceStatus *status) {
+// ---------------------------------------------------------------------------
+// Grouped persistent form: every species block of the operand rows against
+// its own B in one launch, one CTA per SM walking the tiles, the two TMEM
+// accumulators of 256 columns used in turn so that the epilogue of one tile
+// overlaps the MMAs of the next.  The lo planes here carry the residual
+// itself (not scaled by 2048), so the three products share one accumulator:
+//   acc = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T,   V = acc * out_scale[g].
+//   warp 0 lane 0  TMA producer (2-stage ring, as above)
+//   warp 1 lane 0  MMA issuer
+//   warps 2..5     epilogue; warp w reads TMEM lanes 32 (w mod 4) ..; warp 2
+//                  also allocates / frees the 512 TMEM columns
+// ---------------------------------------------------------------------------
+struct GroupedParams {
+  CUtensorMap a_hi, a_lo;
+  CUtensorMap b_hi[kGemmMaxGroups], b_lo[kGemmMaxGroups];
+  int row0[kGemmMaxGroups], M[kGemmMaxGroups];
+  float scale[kGemmMaxGroups];
+  int tile_start[kGemmMaxGroups + 1];
+  int n_groups, tiles_n, N, K;
+  float *V;
+  int ldv;
+  DeviceStatus *status;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1)
+k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte aligned operand ring (required by the 128B swizzle)
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   unsigned char *gbase = smem_raw + (base - raw);
   const uint32_t bars = base + STAGES * STAGE_BYTES;
   uint64_t *bar_ptr = reinterpret_cast<uint64_t *>(gbase + STAGES * STAGE_BYTES);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_ptr + 2 * STAGES + 1);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_ptr + 2 * STAGES + 4);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   auto full_bar = [&](int s) { return bars + 8u * s; };
   auto empty_bar = [&](int s) { return bars + 8u * (STAGES + s); };
-  const uint32_t done_bar = bars + 8u * (2 * STAGES);
+  auto accf_bar = [&](int b) { return bars + 8u * (2 * STAGES + b); };
+  auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + 2 + b); };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * BN;
-  const int m0 = blockIdx.y * BM;
-  const int kblocks = (K + BK - 1) / BK;
+  const int n_tiles = p.tile_start[p.n_groups];
+  const int kblocks = (p.K + BK - 1) / BK;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
     }
-    mbar_init(done_bar, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(accf_bar(b), 1);
+      mbar_init(acce_bar(b), 4);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -187,88 +217,125 @@ k_split_gemm(const __grid_constant__ CUtensorMap map_a_hi,
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t acc0 = tmem, acc1 = tmem + BN;
+
+  // tile -> (group, row of the operand block, first column)
+  auto locate = [&](int t, int &g, int &mrow, int &n0) {
+    g = 0;
+    while (g + 1 < p.n_groups && t >= p.tile_start[g + 1]) g++;
+    const int lt = t - p.tile_start[g];
+    mrow = (lt / p.tiles_n) * BM;
+    n0 = (lt % p.tiles_n) * BN;
+  };
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer ----------------
-    for (int kb = 0; kb < kblocks; kb++) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)((kb / STAGES) & 1);
-      if (!mbar_wait(empty_bar(s), ph ^ 1u)) {
-        set_status(status, FPP_ERR_TIMEOUT, 101, kb);
-        *abort_flag = 1;
-        break;
+    int it = 0;
+    for (int t = blockIdx.x; t < n_tiles && !*abort_flag; t += gridDim.x) {
+      int g, mrow, n0;
+      locate(t, g, mrow, n0);
+      const int arow = p.row0[g] + mrow;
+      for (int kb = 0; kb < kblocks; kb++, it++) {
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+        if (!mbar_wait(empty_bar(s), ph ^ 1u)) {
+          set_status(p.status, FPP_ERR_TIMEOUT, 111, t);
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        const uint32_t st = base + s * STAGE_BYTES;
+        mbar_expect_tx(full_bar(s), STAGE_BYTES);
+        const int kc = kb * BK;
+        tma_load_2d(st, &p.a_hi, full_bar(s), kc, arow);
+        tma_load_2d(st + A_TILE, &p.a_lo, full_bar(s), kc, arow);
+        tma_load_2d(st + 2 * A_TILE, &p.b_hi[g], full_bar(s), kc, n0);
+        tma_load_2d(st + 2 * A_TILE + B_TILE, &p.b_lo[g], full_bar(s), kc, n0);
       }
-      if (*abort_flag) break;
-      const uint32_t st = base + s * STAGE_BYTES;
-      mbar_expect_tx(full_bar(s), STAGE_BYTES);
-      const int kc = kb * BK;
-      tma_load_2d(st, &map_a_hi, full_bar(s), kc, row0 + m0);
-      tma_load_2d(st + A_TILE, &map_a_lo, full_bar(s), kc, row0 + m0);
-      tma_load_2d(st + 2 * A_TILE, &map_b_hi, full_bar(s), kc, n0);
-      tma_load_2d(st + 2 * A_TILE + B_TILE, &map_b_lo, full_bar(s), kc, n0);
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
-    for (int kb = 0; kb < kblocks; kb++) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)((kb / STAGES) & 1);
-      if (!mbar_wait(full_bar(s), ph)) {
-        set_status(status, FPP_ERR_TIMEOUT, 102, kb);
+    int it = 0, j = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, j++) {
+      const int buf = j & 1;
+      const uint32_t acc = tmem + (uint32_t)(buf * BN);
+      if (!mbar_wait(acce_bar(buf), (uint32_t)(((j >> 1) & 1) ^ 1))) {
+        set_status(p.status, FPP_ERR_TIMEOUT, 112, t);
         *abort_flag = 1;
+      }
+      if (*abort_flag) {
+        mma_commit(accf_bar(buf));  // release the epilogue of this buffer
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t st = base + s * STAGE_BYTES;
-      const uint32_t a_hi = st, a_lo = st + A_TILE;
-      const uint32_t b_hi = st + 2 * A_TILE, b_lo = st + 2 * A_TILE + B_TILE;
+      bool ok = true;
+      for (int kb = 0; kb < kblocks; kb++, it++) {
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+        if (!mbar_wait(full_bar(s), ph)) {
+          set_status(p.status, FPP_ERR_TIMEOUT, 113, t);
+          *abort_flag = 1;
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = base + s * STAGE_BYTES;
+        const uint32_t a_hi = st, a_lo = st + A_TILE;
+        const uint32_t b_hi = st + 2 * A_TILE, b_lo = st + 2 * A_TILE + B_TILE;
 #pragma unroll
-      for (int ks = 0; ks < BK / 16; ks++) {
-        const uint32_t off = ks * 32;  // 16 fp16 = 32 bytes along K
-        const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-        mma_f16(acc0, smem_desc(a_hi + off), smem_desc(b_hi + off), acc);
-        mma_f16(acc1, smem_desc(a_hi + off), smem_desc(b_lo + off), acc);
-        mma_f16(acc1, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+        for (int ks = 0; ks < BK / 16; ks++) {
+          const uint32_t off = ks * 32;
+          mma_f16(acc, smem_desc(a_hi + off), smem_desc(b_hi + off),
+                  (kb > 0 || ks > 0) ? 1u : 0u);
+          mma_f16(acc, smem_desc(a_hi + off), smem_desc(b_lo + off), 1u);
+          mma_f16(acc, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+        }
+        mma_commit(empty_bar(s));
       }
-      mma_commit(empty_bar(s));
+      mma_commit(accf_bar(buf));
+      if (!ok) break;
     }
-    // signal the epilogue (also on the error path, so nobody waits forever)
-    mma_commit(done_bar);
-  }
-
-  // ---------------- epilogue: all four warps ----------------
-  __syncwarp();
-  bool have = mbar_wait(done_bar, 0);
-  have = __all_sync(0xffffffffu, have) != 0;
-  if (!have && lane == 0) set_status(status, FPP_ERR_TIMEOUT, 103, warp);
-  const int aborted = __shfl_sync(0xffffffffu, *abort_flag, 0);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (have && !aborted) {
-    const int row = m0 + warp * 32 + lane;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  } else if (warp >= 2) {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+    int j = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, j++) {
+      const int buf = j & 1;
+      bool have = mbar_wait(accf_bar(buf), (uint32_t)((j >> 1) & 1));
+      have = __all_sync(0xffffffffu, have) != 0;
+      if (!have) {
+        if (lane == 0) set_status(p.status, FPP_ERR_TIMEOUT, 114, t);
+        *abort_flag = 1;
+        break;
+      }
+      if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      int g, mrow, n0;
+      locate(t, g, mrow, n0);
+      const int r = mrow + q * 32 + lane;  // row within the group
+      const float sc = p.scale[g];
+      const uint32_t acc = tmem + (uint32_t)(buf * BN) + lane_base;
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 32) {
-      float v0[32], v1[32];
-      tmem_ld32(acc0 + lane_base + c, v0);
-      tmem_ld32(acc1 + lane_base + c, v1);
-      if (row < M) {
-        float *dst = V + (size_t)row * ldv + n0 + c;
-        const int ncol = N - (n0 + c);
-        if (ncol >= 32) {
+      for (int c = 0; c < BN; c += 32) {
+        float v[32];
+        tmem_ld32(acc + c, v);
+        if (r < p.M[g]) {
+          float *dst = p.V + (size_t)(p.row0[g] + r) * p.ldv + n0 + c;
+          const int ncol = p.N - (n0 + c);
+          if (ncol >= 32) {
 #pragma unroll
-          for (int i = 0; i < 32; i += 4) {
-            float4 o;
-            o.x = (v0[i + 0] + v1[i + 0] * (1.0f / 2048.0f)) * out_scale;
-            o.y = (v0[i + 1] + v1[i + 1] * (1.0f / 2048.0f)) * out_scale;
-            o.z = (v0[i + 2] + v1[i + 2] * (1.0f / 2048.0f)) * out_scale;
-            o.w = (v0[i + 3] + v1[i + 3] * (1.0f / 2048.0f)) * out_scale;
-            *reinterpret_cast<float4 *>(dst + i) = o;
+            for (int i = 0; i < 32; i += 4)
+              *reinterpret_cast<float4 *>(dst + i) =
+                  make_float4(v[i] * sc, v[i + 1] * sc, v[i + 2] * sc, v[i + 3] * sc);
+          } else {
+            for (int i = 0; i < 32; i++)
+              if (i < ncol) dst[i] = v[i] * sc;
           }
-        } else {
-          for (int i = 0; i < 32; i++)
-            if (i < ncol) dst[i] = (v0[i] + v1[i] * (1.0f / 2048.0f)) * out_scale;
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce_bar(buf));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -315,32 +382,55 @@ static int make_map(CUtensorMap *map, const void *ptr, int inner, int rows,
 
 int split_gemm_smem_bytes() { return SMEM_BYTES; }
 
-int launch_split_gemm(const SplitGemmArgs &g, cudaStream_t stream) {
-  if (g.M <= 0 || g.N <= 0) return 0;
-  // operand rows must start 16-byte aligned and be 16-byte multiples
-  if ((g.lda * 2) % 16 != 0 || (g.ldb * 2) % 16 != 0) return -2;
-  if (((uintptr_t)g.a_hi | (uintptr_t)g.a_lo | (uintptr_t)g.b_hi |
-       (uintptr_t)g.b_lo) % 16 != 0)
-    return -2;
-  if (g.ldv % 4 != 0 || ((uintptr_t)g.V % 16) != 0) return -2;
-  if (g.K > g.lda || g.K > g.ldb) return -2;
-  CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
-  if (make_map(&ma_hi, g.a_hi, g.K, g.a_rows, g.lda, BM) ||
-      make_map(&ma_lo, g.a_lo, g.K, g.a_rows, g.lda, BM) ||
-      make_map(&mb_hi, g.b_hi, g.K, g.b_rows, g.ldb, BN) ||
-      make_map(&mb_lo, g.b_lo, g.K, g.b_rows, g.ldb, BN))
+int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream) {
+  if (g.n_groups <= 0 || g.N <= 0) return 0;
+  if (g.n_groups > kGemmMaxGroups) return -2;
+  if ((g.lda * 2) % 16 != 0 || ((uintptr_t)g.a_hi | (uintptr_t)g.a_lo) % 16 != 0) return -2;
+  if (g.ldv % 4 != 0 || ((uintptr_t)g.V % 16) != 0 || g.K > g.lda) return -2;
+  GroupedParams p;
+  std::memset(&p, 0, sizeof(p));
+  if (make_map(&p.a_hi, g.a_hi, g.K, g.a_rows, g.lda, BM) ||
+      make_map(&p.a_lo, g.a_lo, g.K, g.a_rows, g.lda, BM))
     return -3;
+  const int tiles_n = (g.N + BN - 1) / BN;
+  int tiles = 0;
+  for (int k = 0; k < g.n_groups; k++) {
+    const GemmGroup &q = g.group[k];
+    if ((q.ldb * 2) % 16 != 0 || ((uintptr_t)q.b_hi | (uintptr_t)q.b_lo) % 16 != 0 ||
+        g.K > q.ldb)
+      return -2;
+    if (make_map(&p.b_hi[k], q.b_hi, g.K, q.b_rows, q.ldb, BN) ||
+        make_map(&p.b_lo[k], q.b_lo, g.K, q.b_rows, q.ldb, BN))
+      return -3;
+    p.row0[k] = q.row0;
+    p.M[k] = q.M;
+    p.scale[k] = q.out_scale;
+    p.tile_start[k] = tiles;
+    tiles += ((q.M + BM - 1) / BM) * tiles_n;
+  }
+  p.tile_start[g.n_groups] = tiles;
+  p.n_groups = g.n_groups;
+  p.tiles_n = tiles_n;
+  p.N = g.N;
+  p.K = g.K;
+  p.V = g.V;
+  p.ldv = g.ldv;
+  p.status = g.status;
+  if (tiles == 0) return 0;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_split_gemm_grouped,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
                              SMEM_BYTES) != cudaSuccess)
       return -1;
     attr = true;
   }
-  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
-  k_split_gemm<<<grid, 128, SMEM_BYTES, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, g.row0,
-                                                  g.M, g.N, g.K, g.out_scale, g.V,
-                                                  g.ldv, g.status);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return -1;
+  const int grid = tiles < sms ? tiles : sms;
+  k_split_gemm_grouped<<<grid, 192, SMEM_BYTES, stream>>>(p);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -7,21 +7,27 @@
 
 namespace fpp {
 
-struct SplitGemmArgs {
-  // A operand: a_rows x K (row stride lda elements), tile rows start at row0
-  const __half *a_hi, *a_lo;
-  int a_rows, lda, row0;
-  // B operand: b_rows x K (row stride ldb)
+// Grouped persistent form: operand rows in species blocks (row0, M) of one
+// A, each block against its own B; lo planes hold the unscaled residual
+// (A ~ A_hi + A_lo), V[row0 + r, :] = (A B^T)[r, :] * out_scale.
+constexpr int kGemmMaxGroups = 8;
+struct GemmGroup {
   const __half *b_hi, *b_lo;
   int b_rows, ldb;
-  int M, N, K;          // output tile extent: M rows from row0, N columns
-  float out_scale;      // 1 / (sA sB)
-  float *V;             // output rows row0.. (row stride ldv), already offset
+  int row0, M;
+  float out_scale;
+};
+struct GroupedGemmArgs {
+  const __half *a_hi, *a_lo;
+  int a_rows, lda;
+  int n_groups;
+  GemmGroup group[kGemmMaxGroups];
+  int N, K;
+  float *V;  // rows indexed like A's rows (row stride ldv)
   int ldv;
   DeviceStatus *status;
 };
-
-int launch_split_gemm(const SplitGemmArgs &g, cudaStream_t stream);
+int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream);
 int split_gemm_smem_bytes();
 
 }  // namespace fpp

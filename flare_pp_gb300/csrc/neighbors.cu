@@ -134,16 +134,27 @@ __global__ void k_bin_scatter(int noa, const int *__restrict__ atom_bin,
 
 // Exact FP64 image distance of the reference (structure.cpp:69-77):
 // im = ((diff + s1 c0) + s2 c1) + s3 c2, dist = sqrt((x^2 + y^2) + z^2).
+// dadd(v, dmul(s, c)) bit for bit, with the products by 0 and +-1 (exact)
+// formed without FP64 instructions, which are scarce on this GPU.
+__device__ __forceinline__ double shift_add(double v, int s, double c) {
+  if (s == 0) {
+    if ((__double_as_longlong(v) << 1) != 0) return v;  // v + (+-0) == v unless v is a zero
+    return dadd(v, dmul(0.0, c));
+  }
+  if (s == 1) return dadd(v, c);
+  if (s == -1) return dadd(v, -c);
+  return dadd(v, dmul((double)s, c));
+}
+
 __device__ __forceinline__ double exact_image(const dvec4 &wi, const dvec4 &wj,
                                               const CellDev &cd, int s1, int s2,
                                               int s3, double im[3]) {
   double diff[3] = {dsub(wj.x, wi.x), dsub(wj.y, wi.y), dsub(wj.z, wi.z)};
-  double a = (double)s1, b = (double)s2, c = (double)s3;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    double v = dadd(diff[k], dmul(a, cd.cell[0 * 3 + k]));
-    v = dadd(v, dmul(b, cd.cell[1 * 3 + k]));
-    im[k] = dadd(v, dmul(c, cd.cell[2 * 3 + k]));
+    double v = shift_add(diff[k], s1, cd.cell[0 * 3 + k]);
+    v = shift_add(v, s2, cd.cell[1 * 3 + k]);
+    im[k] = shift_add(v, s3, cd.cell[2 * 3 + k]);
   }
   return __dsqrt_rn(dadd(dadd(dmul(im[0], im[0]), dmul(im[1], im[1])),
                          dmul(im[2], im[2])));
@@ -247,6 +258,7 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
   const float4 pi = wp32[i];
   const float4 fi = frac[i];
   const float fik[3] = {fi.x, fi.y, fi.z};
+  const int center = (cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep;
   int nacc = 0, nr = 0, tot = 0;
   if (lane == 0) s_rpre[w][0] = 0;
   __syncwarp();
@@ -274,6 +286,8 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
         const int sidx = s_rsidx[w][lo];
         if (d2 < cd.in2 && d2 > cd.zero2) {
           ok = true;
+        } else if (j == i && sidx == center) {
+          ok = false;  // the atom itself: its exact distance is 0
         } else if (d2 <= cd.out2) {
           const int s3 = sidx % cd.ns - cd.sweep;
           const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;

@@ -227,6 +227,36 @@ int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream
 int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs,
                 double *variance_efs, void *stream);
 
+/* SparseGP::update_Kuf / stack_Kuf for a batch of training structures
+ * (sparse_gp.cpp:392-462, 464-552, 565-574): the sparse-environment columns
+ * of each structure's labels, [E] [F of the listed atoms] [S], stacked in
+ * structure order into kuf (host, n_sparse_total x n_labels, row-major),
+ * FP64 on the GPU with one device-resident Kuf and one copy out.
+ * label_mask[k]: bit 0 energy, bit 1 forces, bit 2 stress of structure k;
+ * atom_offsets (n_structures + 1) and atoms list the force atoms of each
+ * structure (the reference's atom_indices; NULL: every atom).  n_labels must
+ * equal the total label count (FPP_ERR_INVALID otherwise). */
+int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures,
+                    int32_t n_structures, const int32_t *label_mask,
+                    const int32_t *atom_offsets, const int32_t *atoms, double *kuf,
+                    int64_t n_labels, void *stream);
+
+/* NormalizedDotProduct::struc_struc (normalized_dot_product.cpp:212-444):
+ * the full energy/force/stress covariance of two structures, FP64, from the
+ * descriptor's stored derivatives.  kernel_mat is a host array
+ * (1 + 3 noa1 + 6) x (1 + 3 noa2 + 6), row-major.  FPP_ERR_NUMERIC where the
+ * reference throws (power < 2 and a zero normalized dot product).  Memory
+ * grows with the product of the two structures' pair counts, as in the
+ * reference: meant for small structures. */
+int fpp_struc_struc(const fpp_b2 *descriptor, double sigma, double power,
+                    fpp_structure *s1, fpp_structure *s2, double *kernel_mat,
+                    void *stream);
+
+/* NormalizedDotProduct::self_kernel_struc (:446-578): the diagonal of
+ * struc_struc(s, s), a host array of 1 + 3 noa + 6. */
+int fpp_self_kernel_struc(const fpp_b2 *descriptor, double sigma, double power,
+                          fpp_structure *s, double *kernel_vec, void *stream);
+
 /* Energy, forces and stress of the same model through its mapped
  * coefficients (the pair style's evaluation, pair_flare.cpp:95-180, on the
  * periodic structure), in `precision`.  Outputs are host arrays unless
