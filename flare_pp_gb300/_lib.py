@@ -56,6 +56,7 @@ SIGNATURES = {
     "fpp_model_set_beta": (_c_int, [_vp, _i32, _vp]),
     "fpp_envs_envs": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_envs_struc": (_c_int, [_vp, _vp, _vp, _vp]),
+    "fpp_local_uncertainties": (_c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
     "fpp_kuf_batched": (_c_int, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i64, _vp]),
     "fpp_struc_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp, _vp]),
     "fpp_self_kernel_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp]),

@@ -469,7 +469,9 @@ class SparseGP:
         self.noise_vector = np.zeros(0)
         self.alpha = None
         self.R_inv = None
+        self.L_inv = None
         self.Sigma = None
+        self.Kuu_inverse = None
         self._model = None
         self._mapped = False
 
@@ -572,13 +574,14 @@ class SparseGP:
         self._model = _Model(self.b2, k.sigma, k.power, sd, self.alpha, self.R_inv)
         self._mapped = False
 
-    def set_model(self, b2, sparse_descriptors, alpha, R_inv=None):
+    def set_model(self, b2, sparse_descriptors, alpha, R_inv=None, L_inv=None):
         """Load a trained model: the sparse ClusterDescriptor, alpha and
-        optionally R_inv (the outputs of update_matrices_QR)."""
+        optionally R_inv and L_inv (the outputs of update_matrices_QR)."""
         self.b2 = b2
         self.sparse_descriptors = [sparse_descriptors]
         self.alpha = f64(alpha)
         self.R_inv = None if R_inv is None else f64(R_inv)
+        self.L_inv = None if L_inv is None else f64(L_inv)
         k = self.kernels[0]
         self._model = _Model(b2, k.sigma, k.power, sparse_descriptors, self.alpha,
                              self.R_inv)
@@ -628,6 +631,22 @@ class SparseGP:
         q_self = np.einsum("ij,ij->j", K, self.Kuu_inverse @ K)
         v_sor = np.einsum("ij,ij->j", K, self.Sigma @ K)
         structure.variance_efs = k_self - q_self + v_sor
+
+    def compute_cluster_uncertainties(self, structure, stream=None):
+        """sparse_gp.cpp:93-133: per kernel, the energy variance of every
+        cluster (species by species, atoms in structure order), from the GPU."""
+        if self.L_inv is None:
+            raise ValueError("compute_cluster_uncertainties needs L_inv")
+        L = f64(self.L_inv)
+        v = np.zeros(structure.noa)
+        check(lib().fpp_local_uncertainties(self._model.handle, structure.handle, ptr(L),
+                                            L.shape[0], ptr(v), _stream(stream)))
+        return [v]
+
+    def predict_local_uncertainties(self, structure, stream=None):
+        """sparse_gp.cpp:682-702: mean_efs and local_uncertainties."""
+        self.predict_mean(structure, stream)
+        structure.local_uncertainties = self.compute_cluster_uncertainties(structure, stream)
 
     def predict_mapped(self, structure, precision="mixed", stream=None,
                        atom_energies=False):

@@ -68,6 +68,7 @@ int upload_harmonic_tables(cudaStream_t stream) {
     double d = 1;
     for (int k = 1; k < 2 * m; k += 2) d *= k;
     t.dfact[m] = d;
+    t.dfact_f[m] = (float)d;
   }
   cudaError_t e = cudaMemcpyToSymbolAsync(c_harm, &t, sizeof(t), 0,
                                           cudaMemcpyHostToDevice, stream);
@@ -124,6 +125,36 @@ __device__ __forceinline__ void ff_warp_sum(float &hi, float &lo) {
   }
 }
 
+// Descriptor shape known at compile time for the common settings (N, lmax,
+// n_species), or read from the arguments (the generic instantiation).  With
+// the sizes constant, the radial / harmonic loops unroll and the shared-memory
+// and u indices fold into immediate offsets.
+template <int NT, int LT, int NST> struct Shape {
+  static constexpr int kNR = (NT > 0 && NST > 0) ? NT * NST : 0;  // radial channels
+  static constexpr int kL1 = LT >= 0 ? LT + 1 : 0;
+  static __device__ __forceinline__ int N(const B2Args &a) { return NT > 0 ? NT : a.N; }
+  static __device__ __forceinline__ int lmax(const B2Args &a) { return LT >= 0 ? LT : a.lmax; }
+  static __device__ __forceinline__ int NS(const B2Args &a) {
+    return NST > 0 ? NST : a.n_species;
+  }
+};
+using GenericShape = Shape<0, -1, 0>;
+
+// f(shape) with the compile-time shape matching a, else the generic one.
+// The FP64 (reference-precision) kernels are instantiated generic only.
+template <typename T, typename F>
+int with_shape(const B2Args &a, F &&f) {
+  if constexpr (sizeof(T) == 4) {
+    if (a.kind == kB2) {
+      if (a.n_species == 2 && a.N == 12 && a.lmax == 4) return f(Shape<12, 4, 2>{});
+      if (a.n_species == 2 && a.N == 10 && a.lmax == 4) return f(Shape<10, 4, 2>{});
+      if (a.n_species == 2 && a.N == 8 && a.lmax == 3) return f(Shape<8, 3, 2>{});
+      if (a.n_species == 1 && a.N == 8 && a.lmax == 3) return f(Shape<8, 3, 1>{});
+    }
+  }
+  return f(GenericShape{});
+}
+
 // ---------------------------------------------------------------------------
 // Forward: one warp per atom.
 //   1. stage the bases of up to W neighbors (one neighbor per lane) and list
@@ -146,11 +177,12 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
   FwdLayout<T> L;
   L.W = a.window;
   L.GP = (a.N + 3) & ~3;
-  const int sb = a.n_species * a.N * a.H;
+  // c rows padded to a multiple of 4 entries (16-byte aligned rows)
+  const int sbp = a.n_species * a.N * ((a.H + 3) & ~3);
   size_t st = sizeof(T) * ((size_t)L.W * L.GP + (size_t)a.H * (L.W + 1));
   size_t pb = sizeof(T) * (size_t)a.n_d;
   L.stage = ((st > pb ? st : pb) + 15) & ~(size_t)15;
-  L.csum = (sizeof(T) * 2 * (size_t)sb + 15) & ~(size_t)15;
+  L.csum = (sizeof(T) * 2 * (size_t)sbp + 15) & ~(size_t)15;
   L.lists = (sizeof(int) * ((size_t)a.n_species * L.W + 2 * L.W + a.n_species) + 15) & ~(size_t)15;
   L.cz = a.kind == kB3
              ? (sizeof(T) * 2 * (size_t)a.n_species * a.N * (a.H + 1) + 15) & ~(size_t)15
@@ -159,7 +191,7 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
   return L;
 }
 
-template <typename T>
+template <typename T, typename SH>
 __global__ void __launch_bounds__(128)
 k_b2_forward(B2Args a, const int *__restrict__ offset,
              const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
@@ -174,20 +206,22 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   const int nwarps = blockDim.x >> 5;
   const int atom = blockIdx.x * nwarps + warp;
   const FwdLayout<T> Lay = fwd_layout<T>(a);
-  const int N = a.N, H = a.H, NS = a.n_species, W = Lay.W, GP = Lay.GP;
+  const int N = SH::N(a), LMAX = SH::lmax(a), H = (LMAX + 1) * (LMAX + 1), NS = SH::NS(a);
+  const int W = Lay.W, GP = Lay.GP;
   const int WS = W + 1;
   const int sb = NS * N * H;
+  const int HP = (H + 3) & ~3, sbp = NS * N * HP;     // padded c row stride
   unsigned char *base = smem_raw + Lay.total * warp;
   T *g_s = reinterpret_cast<T *>(base);               // [W][GP]
   T *y_s = g_s + (size_t)W * GP;                      // [H][WS]
   T *p_s = reinterpret_cast<T *>(base);               // [n_d] (after staging)
-  T *c_s = reinterpret_cast<T *>(base + Lay.stage);   // [sb] running sums
-  T *cc_s = c_s + sb;                                 // [sb] compensation
+  T *c_s = reinterpret_cast<T *>(base + Lay.stage);   // [NS N][HP] running sums
+  T *cc_s = c_s + sbp;                                // [NS N][HP] compensation
   int *list = reinterpret_cast<int *>(base + Lay.stage + Lay.csum);  // [NS][W]
   int *cnt_s = list + NS * W;                         // [NS]
   if (atom >= a.noa) return;
 
-  for (int k = lane; k < sb; k += 32) {
+  for (int k = lane; k < sbp; k += 32) {
     c_s[k] = T(0);
     cc_s[k] = T(0);
   }
@@ -237,7 +271,7 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
           sj = sp;
           radial_basis<T>(r, r1t, rct, N, a.cutoff_kind, g_s + (size_t)b * GP,
                           nullptr, 1);
-          real_harmonics<T>(x, y, z, a.lmax, y_s + b, nullptr, WS);
+          real_harmonics<T>(x, y, z, LMAX, y_s + b, nullptr, WS);
         }
       }
       for (int sp = 0; sp < NS; sp++) {
@@ -262,8 +296,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 #pragma unroll
         for (int n = 0; n < kMaxN; n++)
           if (n < N) {
-            sum[n] = c_s[(sp * N + n) * H + lmc];
-            comp[n] = cc_s[(sp * N + n) * H + lmc];
+            sum[n] = c_s[(sp * N + n) * HP + lmc];
+            comp[n] = cc_s[(sp * N + n) * HP + lmc];
           }
         for (int k0 = 0; k0 < ns_; k0 += 16) {
           T chunk[kMaxN];
@@ -291,44 +325,77 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 #pragma unroll
           for (int n = 0; n < kMaxN; n++)
             if (n < N) {
-              c_s[(sp * N + n) * H + lm] = sum[n];
-              cc_s[(sp * N + n) * H + lm] = comp[n];
+              c_s[(sp * N + n) * HP + lm] = sum[n];
+              cc_s[(sp * N + n) * HP + lm] = comp[n];
             }
         }
       }
     }
     __syncwarp();
   }
-  // fold the compensation and publish c
+  // fold the compensation and publish c (unpadded rows in global memory)
   for (int k = lane; k < sb; k += 32) {
-    T v = c_s[k] - cc_s[k];
-    c_s[k] = v;
+    const int r = k / H, lm = k - r * H;
+    const T v = c_s[r * HP + lm] - cc_s[r * HP + lm];
+    c_s[r * HP + lm] = v;
     c_out[(size_t)atom * sb + k] = v;
   }
   __syncwarp();
   // ---- 3. B2 contraction per radial pair q, all l (B3: per radial triple) ----
-  const int L1 = a.lmax + 1;
+  const int L1 = LMAX + 1;
   const int nd = a.n_d;
   const int npair = a.kind == kB3 ? 0 : nd / L1;
   Acc<T> nacc;
   if (a.kind == kB3) {
     T *zr = reinterpret_cast<T *>(base + Lay.stage + Lay.csum + Lay.lists);
     T *zi = zr + (size_t)NS * N * (H + 1);
-    b3_to_complex<T>(c_s, NS * N, H, zr, zi, lane);
+    b3_to_complex<T>(c_s, NS * N, H, zr, zi, lane, HP);
     __syncwarp();
     b3_contract<T>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, zr, zi, p_s, lane);
     __syncwarp();
     for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
   }
-  for (int q = lane; q < npair; q += 32) {
-    const int pr = pair_tab[q];
-    const int n1 = pr & 0xffff, n2 = pr >> 16;
-    const T *c1 = c_s + n1 * H, *c2 = c_s + n2 * H;
-    for (int l = 0; l < L1; l++) {
-      T v = T(0);
-      for (int m = l * l; m < (l + 1) * (l + 1); m++) v += c1[m] * c2[m];
-      p_s[q * L1 + l] = v;
-      nacc.add(v * v);
+  if constexpr (SH::kL1 > 0) {
+    // shape known: both c rows in registers through 16-byte loads
+    constexpr int LL = SH::kL1, HH = LL * LL, H4 = (HH + 3) / 4;
+    for (int q = lane; q < npair; q += 32) {
+      const int pr = pair_tab[q];
+      const int n1 = pr & 0xffff, n2 = pr >> 16;
+      T e[4 * H4];
+#pragma unroll
+      for (int k = 0; k < H4; k++) {
+        if constexpr (sizeof(T) == 4) {
+          const float4 x = reinterpret_cast<const float4 *>(c_s + n1 * HP)[k];
+          const float4 y = reinterpret_cast<const float4 *>(c_s + n2 * HP)[k];
+          e[4 * k + 0] = x.x * y.x;
+          e[4 * k + 1] = x.y * y.y;
+          e[4 * k + 2] = x.z * y.z;
+          e[4 * k + 3] = x.w * y.w;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++) e[4 * k + j] = c_s[n1 * HP + 4 * k + j] * c_s[n2 * HP + 4 * k + j];
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < LL; l++) {
+        T v = T(0);
+#pragma unroll
+        for (int m = l * l; m < (l + 1) * (l + 1); m++) v += e[m];
+        p_s[q * LL + l] = v;
+        nacc.add(v * v);
+      }
+    }
+  } else {
+    for (int q = lane; q < npair; q += 32) {
+      const int pr = pair_tab[q];
+      const int n1 = pr & 0xffff, n2 = pr >> 16;
+      const T *c1 = c_s + n1 * HP, *c2 = c_s + n2 * HP;
+      for (int l = 0; l < L1; l++) {
+        T v = T(0);
+        for (int m = l * l; m < (l + 1) * (l + 1); m++) v += c1[m] * c2[m];
+        p_s[q * L1 + l] = v;
+        nacc.add(v * v);
+      }
     }
   }
   double nrm, inv;
@@ -353,6 +420,31 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   if (lane == 0) norm_out[atom] = nrm;
   __syncwarp();
   const int row = row_of_atom[atom];
+  if (sizeof(T) == 4 && phat_hi && !p_out && !phat64 && (nd & 3) == 0) {
+    // split operand only: four entries per lane, 16-byte reads, 8-byte writes
+    const float4 *P4 = reinterpret_cast<const float4 *>(p_s);
+    const float4 *B4 = reinterpret_cast<const float4 *>(pbar + (size_t)si * nd);
+    uint2 *H4 = reinterpret_cast<uint2 *>(phat_hi + (size_t)row * ldp);
+    uint2 *L4 = reinterpret_cast<uint2 *>(phat_lo + (size_t)row * ldp);
+    for (int q = lane; q < (nd >> 2); q += 32) {
+      const float4 v = P4[q], b = B4[q];
+      const float x[4] = {(v.x * invf - b.x) * 8192.0f, (v.y * invf - b.y) * 8192.0f,
+                          (v.z * invf - b.z) * 8192.0f, (v.w * invf - b.w) * 8192.0f};
+      __half h[4], r[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        h[j] = __float2half_rn(x[j]);
+        r[j] = __float2half_rn((x[j] - __half2float(h[j])) * 2048.0f);
+      }
+      const __half2 h01 = __halves2half2(h[0], h[1]), h23 = __halves2half2(h[2], h[3]);
+      const __half2 r01 = __halves2half2(r[0], r[1]), r23 = __halves2half2(r[2], r[3]);
+      H4[q] = make_uint2(*reinterpret_cast<const unsigned *>(&h01),
+                         *reinterpret_cast<const unsigned *>(&h23));
+      L4[q] = make_uint2(*reinterpret_cast<const unsigned *>(&r01),
+                         *reinterpret_cast<const unsigned *>(&r23));
+    }
+    return;
+  }
   for (int d = lane; d < nd; d += 32) {
     const T v = p_s[d];
     if (p_out) p_out[(size_t)atom * nd + d] = v;
@@ -361,7 +453,7 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       // centred operand: delta = phat - pbar, scaled by 2^13 (|delta| <= 2)
       const float x = (float(v) * invf - pbar[(size_t)si * nd + d]) * 8192.0f;
       const __half h = __float2half_rn(x);
-      const float rem = x - __half2float(h);  // residual (fp16, subnormal when tiny)
+      const float rem = (x - __half2float(h)) * 2048.0f;
       phat_hi[(size_t)row * ldp + d] = h;
       phat_lo[(size_t)row * ldp + d] = __float2half_rn(rem);
     }
@@ -395,6 +487,52 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
       else
         store(d, T((g.beta1[(size_t)si * nd + d] - e * ph) * inv));
     }
+  } else if (g.mode == kWFromV2 && (nd & 3) == 0) {
+    // the mixed power-2 form below, four consecutive entries per lane and
+    // 16-byte (8-byte for the fp16 planes) loads
+    const bool empty = nrm * nrm < g.empty_thresh;
+    const int nq = nd >> 2;
+    const float4 *V4 = reinterpret_cast<const float4 *>(g.V32 + (size_t)row * g.ldv);
+    const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
+    const float4 *B4 = reinterpret_cast<const float4 *>(g.pbar + (size_t)si * nd);
+    const uint2 *H4 = reinterpret_cast<const uint2 *>(g.phat_hi + (size_t)row * g.ldp);
+    const uint2 *L4 = reinterpret_cast<const uint2 *>(g.phat_lo + (size_t)row * g.ldp);
+    auto deltas = [&](int q, float (&dl)[4]) {
+      const uint2 h = H4[q], l = L4[q];
+      const float2 h01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
+      const float2 h23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
+      const float2 l01 = __half22float2(*reinterpret_cast<const __half2 *>(&l.x));
+      const float2 l23 = __half22float2(*reinterpret_cast<const __half2 *>(&l.y));
+      dl[0] = (h01.x + l01.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+      dl[1] = (h01.y + l01.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+      dl[2] = (h23.x + l23.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+      dl[3] = (h23.y + l23.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+    };
+    Acc<float> acc;
+    for (int q = lane; q < nq; q += 32) {
+      float dl[4];
+      deltas(q, dl);
+      const float4 v = V4[q], gg = G4[q];
+      acc.add((2.0f * gg.x + v.x) * dl[0]);
+      acc.add((2.0f * gg.y + v.y) * dl[1]);
+      acc.add((2.0f * gg.z + v.z) * dl[2]);
+      acc.add((2.0f * gg.w + v.w) * dl[3]);
+    }
+    float hi = acc.s, lo = acc.c;
+    ff_warp_sum(hi, lo);
+    const double dot = (double(hi) + double(lo)) + g.c0[si];
+    e = empty ? 0.0 : dot;
+    const float ef = float(e);
+    const float inv = empty ? 0.0f : 1.0f / float(nrm);
+    for (int q = lane; q < nq; q += 32) {
+      float dl[4];
+      deltas(q, dl);
+      const float4 v = V4[q], gg = G4[q], pb = B4[q];
+      store(4 * q + 0, T(2.0f * ((gg.x + v.x) - ef * (pb.x + dl[0])) * inv));
+      store(4 * q + 1, T(2.0f * ((gg.y + v.y) - ef * (pb.y + dl[1])) * inv));
+      store(4 * q + 2, T(2.0f * ((gg.z + v.z) - ef * (pb.z + dl[2])) * inv));
+      store(4 * q + 3, T(2.0f * ((gg.w + v.w) - ef * (pb.w + dl[3])) * inv));
+    }
   } else if (g.mode == kWFromV2 || g.mode == kWFromV1) {
     // mixed form on the centred operand delta = phat - pbar (float):
     //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
@@ -404,7 +542,7 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     Acc<float> acc;
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
-      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o])) *
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
                        (1.0f / 8192.0f);
       if (g.mode == kWFromV2)
         acc.add((2.0f * g.gvec[(size_t)si * nd + d] + g.V32[(size_t)row * g.ldv + d]) * dl);
@@ -419,7 +557,7 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     const float inv = empty ? 0.0f : 1.0f / float(nrm);
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
-      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o])) *
+      const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
                        (1.0f / 8192.0f);
       const float ph = g.pbar[(size_t)si * nd + d] + dl;
       if (g.mode == kWFromV2)
@@ -439,116 +577,74 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
 // Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
 // u = dE/dc = (W + W^T) c per l, written to global memory.
 // ---------------------------------------------------------------------------
-// Dense symmetric form of w per l for the u product: rows of wd are
-// (n2, l) with n1 contiguous, row stride wd_stride(nr) (a multiple of 4 that
-// spreads the five l rows over different banks).
-__host__ __device__ inline int wd_stride(int nr) {
-  const int r4 = (nr + 3) & ~3;
-  return r4 + ((r4 % 8 == 0) ? 4 : 0);
-}
-constexpr int kDenseMaxNR = 32;
-
-template <typename T>
+template <typename T, typename SH>
 __global__ void __launch_bounds__(128)
 k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
         const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
         const T *__restrict__ c_in, const double *__restrict__ norm_in,
         double *__restrict__ atom_e, T *__restrict__ u_out) {
+  (void)pair_tab;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
   const int atom = blockIdx.x * nwarps + warp;
-  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d;
+  const int N = SH::N(a), LMAX = SH::lmax(a), H = (LMAX + 1) * (LMAX + 1), NS = SH::NS(a);
+  const int nd = a.n_d;
   const int sb = NS * N * H, nr = NS * N;
-  const int L1 = a.lmax + 1;
-  const bool dense = nr <= kDenseMaxNR;
-  const int NRP = wd_stride(nr);
+  const int L1 = LMAX + 1;
   unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);  // dense: [nr][L1][NRP]; else packed [nd]
-  T *c_s = w_s + (dense ? nr * L1 * NRP : nd);  // [sb]
+  T *w_s = reinterpret_cast<T *>(base);  // [nd]
+  T *c_s = w_s + nd;                     // [sb]
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
   const double nrm = norm_in[atom];
   for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
 
-  double e;
-  if (dense) {
-    // packed index d = q L1 + l of the pair q = (n1 <= n2): scatter into the
-    // symmetric dense rows, diagonal doubled (the product rule's factor 2)
-    const unsigned magic = 0xFFFFFFFFu / (unsigned)L1 + 1u;  // exact d / L1 for d < 2^16
-    e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) {
-      const int q = L1 == 1 ? d : (int)__umulhi((unsigned)d, magic);
-      const int l = d - q * L1;
-      const int pr = pair_tab[q];
-      const int n1 = pr & 0xffff, n2 = pr >> 16;
-      if (n1 == n2) {
-        w_s[(n2 * L1 + l) * NRP + n1] = T(2) * v;
-      } else {
-        w_s[(n2 * L1 + l) * NRP + n1] = v;
-        w_s[(n1 * L1 + l) * NRP + n2] = v;
-      }
-    }, lane);
-  } else {
-    e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
-  }
+  const double e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
-  const int NP = u_npad(a), usb = u_row_stride(a);
   for (int lm0 = 0; lm0 < H; lm0 += 32) {
     const int lm = lm0 + lane;
     if (lm >= H) continue;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
-    if (dense) {
-      // all n1 in registers; each n2 reads one dense row with 16-byte loads
-      T acc[kDenseMaxNR];
+    if constexpr (SH::kNR > 0 && SH::kL1 > 0) {
+      // shape known: the lane's c column in registers, every w index a constant
+      constexpr int NR = SH::kNR, LL = SH::kL1;
+      T creg[NR];
 #pragma unroll
-      for (int k = 0; k < kDenseMaxNR; k++) acc[k] = T(0);
-      for (int n2 = 0; n2 < nr; n2++) {
-        const T c = c_s[n2 * H + lm];
-        const T *wr = w_s + (n2 * L1 + l) * NRP;
+      for (int n = 0; n < NR; n++) creg[n] = c_s[n * H + lm];
+      const T *wl = w_s + l;
 #pragma unroll
-        for (int k = 0; k < kDenseMaxNR; k += 4)
-          if (k < nr) {
-            T w4[4];
-            if (sizeof(T) == 4) {
-              const float4 q = *reinterpret_cast<const float4 *>(wr + k);
-              w4[0] = T(q.x);
-              w4[1] = T(q.y);
-              w4[2] = T(q.z);
-              w4[3] = T(q.w);
-            } else {
-              const double2 q0 = *reinterpret_cast<const double2 *>(wr + k);
-              const double2 q1 = *reinterpret_cast<const double2 *>(wr + k + 2);
-              w4[0] = T(q0.x);
-              w4[1] = T(q0.y);
-              w4[2] = T(q1.x);
-              w4[3] = T(q1.y);
-            }
+      for (int n1 = 0; n1 < NR; n1++) {
+        T acc = T(0);
 #pragma unroll
-            for (int j = 0; j < 4; j++) acc[k + j] += w4[j] * c;
-          }
+        for (int n2 = 0; n2 < NR; n2++) {
+          const int lo = n1 < n2 ? n1 : n2, hi = n1 < n2 ? n2 : n1;
+          const int q = lo * NR - (lo * (lo - 1)) / 2 + (hi - lo);
+          const T w = wl[q * LL];
+          acc += (n1 == n2 ? T(2) * w : w) * creg[n2];
+        }
+        u_out[(size_t)atom * sb + n1 * H + lm] = acc;
       }
-#pragma unroll
-      for (int n1 = 0; n1 < kDenseMaxNR; n1++)
-        if (n1 < nr) u_out[(size_t)atom * usb + ((n1 / N) * H + lm) * NP + (n1 % N)] = acc[n1];
-      continue;
-    }
-    for (int n1 = 0; n1 < nr; n1++) {
-      T acc = T(0);
-      // n2 < n1: pair (n2, n1), index q = n2 nr - n2 (n2 - 1)/2 + (n1 - n2)
-      int q = n1;  // n2 = 0
-      for (int n2 = 0; n2 < n1; n2++) {
-        acc += w_s[q * L1 + l] * c_s[n2 * H + lm];
-        q += nr - n2 - 1;
+    } else {
+      for (int n1 = 0; n1 < nr; n1++) {
+        T acc = T(0);
+        // n2 < n1: pair (n2, n1), index q = n2 nr - n2 (n2 - 1)/2 + (n1 - n2)
+        int q = n1;  // n2 = 0
+        for (int n2 = 0; n2 < n1; n2++) {
+          acc += w_s[q * L1 + l] * c_s[n2 * H + lm];
+          q += nr - n2 - 1;
+        }
+        // n2 >= n1: pair (n1, n2)
+        q = n1 * nr - (n1 * (n1 - 1)) / 2;
+        acc += T(2) * w_s[q * L1 + l] * c_s[n1 * H + lm];
+        for (int n2 = n1 + 1; n2 < nr; n2++)
+          acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
+        u_out[(size_t)atom * sb + n1 * H + lm] = acc;
       }
-      // n2 >= n1: pair (n1, n2)
-      q = n1 * nr - (n1 * (n1 - 1)) / 2;
-      acc += T(2) * w_s[q * L1 + l] * c_s[n1 * H + lm];
-      for (int n2 = n1 + 1; n2 < nr; n2++) acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
-      u_out[(size_t)atom * usb + ((n1 / N) * H + lm) * NP + (n1 % N)] = acc;
     }
   }
 }
@@ -631,7 +727,7 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
       v = (sg * ur[kp] + ur[km]) * is2;
     else
       v = (ui[km] - sg * ui[kp]) * is2;
-    u_out[(size_t)atom * u_row_stride(a) + ((n / a.N) * H + lm) * u_npad(a) + (n % a.N)] = v;
+    u_out[(size_t)atom * sb + k] = v;
   }
 }
 
@@ -745,7 +841,7 @@ k_b3_dp(B2Args a, int npl, const int *__restrict__ plist, const int *__restrict_
 // with g, g' in registers and the harmonics generated in order and consumed
 // immediately.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, typename SH>
 __global__ void __launch_bounds__(128)
 k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nbr_i,
              const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
@@ -753,7 +849,7 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
              const T *__restrict__ u, T *__restrict__ pair_f) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
-  const int N = a.N, H = a.H, NS = a.n_species;
+  const int N = SH::N(a), LMAX = SH::lmax(a), H = (LMAX + 1) * (LMAX + 1), NS = SH::NS(a);
   const int sb = NS * N * H;
   const int i = nbr_i[p], sj = nbr_s[p], si = species[i];
   const int kc = si * NS + sj;
@@ -788,36 +884,16 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
   if (keep) {
     T gr[kMaxN], dg[kMaxN];
     radial_basis_reg<T>(r, r1t, rct, N, a.cutoff_kind, gr, dg);
-    const int NP = u_npad(a);
-    const T *ur = u + (size_t)i * u_row_stride(a) + (size_t)sj * H * NP;
+    const T *ur = u + (size_t)i * sb + (size_t)sj * N * H;
     T fr = T(0);
-    harmonics_visit<T>(x, y, z, a.lmax, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
+    harmonics_visit<T>(x, y, z, LMAX, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
       T ag = T(0), bd = T(0);
-      const T *col = ur + lm * NP;
 #pragma unroll
-      for (int n0 = 0; n0 < kMaxN; n0 += 4)
-        if (n0 < N) {
-          T uv[4];
-          if (sizeof(T) == 4) {
-            const float4 q = *reinterpret_cast<const float4 *>(col + n0);
-            uv[0] = T(q.x);
-            uv[1] = T(q.y);
-            uv[2] = T(q.z);
-            uv[3] = T(q.w);
-          } else {
-            const double2 q0 = *reinterpret_cast<const double2 *>(col + n0);
-            const double2 q1 = *reinterpret_cast<const double2 *>(col + n0 + 2);
-            uv[0] = T(q0.x);
-            uv[1] = T(q0.y);
-            uv[2] = T(q1.x);
-            uv[3] = T(q1.y);
-          }
-#pragma unroll
-          for (int k = 0; k < 4; k++)
-            if (n0 + k < N) {
-              ag += uv[k] * gr[n0 + k];
-              bd += uv[k] * dg[n0 + k];
-            }
+      for (int n = 0; n < kMaxN; n++)
+        if (n < N) {
+          const T uv = ur[n * H + lm];
+          ag += uv * gr[n];
+          bd += uv * dg[n];
         }
       fr += bd * Yv;
       f[0] += ag * Yx;
@@ -938,6 +1014,65 @@ int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// FP32 pair forces, one warp per atom: lanes take the atom's pairs (f_ij
+// coalesced, f_ji gathered through the reverse index), the warp sums the force
+// and the virial f_ij (x) r_ij as float-float, and each block writes one
+// partial row of energy and virial for k_reduce (fixed order: deterministic).
+// 128 threads = 4 atoms per block.
+__global__ void __launch_bounds__(128)
+k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
+              const float4 *__restrict__ rel32, const float4 *__restrict__ pair_f,
+              const double *__restrict__ atom_e, double *__restrict__ forces,
+              double *__restrict__ partial) {
+  __shared__ double sm[4][10];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + warp;
+  float hi[12], lo[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) hi[k] = lo[k] = 0.0f;
+  if (i < noa) {
+    const int beg = offset[i], end = offset[i + 1];
+    for (int p = beg + lane; p < end; p += 32) {
+      const int q = rev[p];
+      const float4 fp = pair_f[p];
+      const float4 fq = q >= 0 ? pair_f[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 r = rel32[p];
+      const float f[3] = {fp.x, fp.y, fp.z}, g[3] = {fq.x, fq.y, fq.z};
+      const float rr[3] = {r.x, r.y, r.z};
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        float t, e;
+        two_sum(hi[a], f[a], t, e);
+        lo[a] += e;
+        two_sum(t, -g[a], hi[a], e);
+        lo[a] += e;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+          const int k = 3 + 3 * a + b;
+          two_sum(hi[k], f[a] * rr[b], t, e);
+          hi[k] = t;
+          lo[k] += e;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 12; k++) ff_warp_sum(hi[k], lo[k]);
+  if (lane == 0) {
+    if (i < noa) {
+#pragma unroll
+      for (int a = 0; a < 3; a++) forces[3 * i + a] = double(hi[a]) + double(lo[a]);
+    }
+    sm[warp][0] = i < noa ? atom_e[i] : 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) sm[warp][1 + k] = i < noa ? double(hi[3 + k]) + double(lo[3 + k]) : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 10)
+    partial[(size_t)blockIdx.x * 10 + threadIdx.x] =
+        (sm[0][threadIdx.x] + sm[1][threadIdx.x]) + (sm[2][threadIdx.x] + sm[3][threadIdx.x]);
+}
+
 // F_i = sum over pairs of i (f_ij - f_ji); each block also reduces its atoms'
 // energies and virials (sum f_ij (x) r_ij) into one partial row (fixed tree
 // order, so the result is deterministic).  128 threads per block.
@@ -1040,23 +1175,31 @@ k_gather(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
 }
 
 // Sum of the per-block partial rows: out[0] = E, out[1..9] = sum f (x) r.
-__global__ void k_reduce(int nblocks, const double *__restrict__ partial,
-                         double *__restrict__ out) {
-  __shared__ double sm[10][256];
+// One block of 1024 threads: strided per-thread sums, then fixed-order warp
+// and block trees (deterministic).
+__global__ void __launch_bounds__(1024)
+k_reduce(int nblocks, const double *__restrict__ partial, double *__restrict__ out) {
+  __shared__ double sm[32][10];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
 #pragma unroll
     for (int k = 0; k < 10; k++) acc[k] += partial[(size_t)b * 10 + k];
 #pragma unroll
-  for (int k = 0; k < 10; k++) sm[k][threadIdx.x] = acc[k];
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
+  for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
+  if (lane == 0)
 #pragma unroll
-      for (int k = 0; k < 10; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + s];
-    __syncthreads();
+    for (int k = 0; k < 10; k++) sm[warp][k] = acc[k];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      double v = lane < nw ? sm[lane][k] : 0.0;
+      v = warp_sum(v);
+      if (lane == 0) out[k] = v;
+    }
   }
-  if (threadIdx.x < 10) out[threadIdx.x] = sm[threadIdx.x][0];
 }
 
 // ---------------------------------------------------------------------------
@@ -1067,10 +1210,8 @@ size_t forward_smem_per_warp(const B2Args &a, size_t elem) {
 }
 
 size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
-  const int sb = a.n_species * a.N * a.H, nr = a.n_species * a.N;
-  const size_t w = nr <= kDenseMaxNR ? (size_t)nr * (a.lmax + 1) * wd_stride(nr)
-                                     : (size_t)a.n_d;
-  size_t b = elem * (w + (size_t)sb);
+  const int sb = a.n_species * a.N * a.H;
+  size_t b = elem * ((size_t)a.n_d + (size_t)sb);
   return (b + 15) & ~(size_t)15;
 }
 
@@ -1086,14 +1227,16 @@ int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
   while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
   size_t smem = per * wpb;
   if (smem > 227 * 1024) return -1;
-  auto kern = k_b2_forward<T>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return -1;
-  kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
-      a, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom, pair_tab,
-      c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp, pbar);
-  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  return with_shape<T>(a, [&](auto sh) {
+    auto kern = k_b2_forward<T, decltype(sh)>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
+        a, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom, pair_tab,
+        c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp, pbar);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  });
 }
 
 template <typename T>
@@ -1119,26 +1262,41 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                                                             pair_tab, c_in, norm_in, atom_e,
                                                             u_buf);
   } else {
-    auto kern = k_b2_wu<T>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-      return -1;
-    kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom,
-                                                           pair_tab, c_in, norm_in, atom_e,
-                                                           u_buf);
+    const int rc = with_shape<T>(a, [&](auto sh) {
+      auto kern = k_b2_wu<T, decltype(sh)>;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem) != cudaSuccess)
+        return -1;
+      kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(a, g, species, row_of_atom,
+                                                             pair_tab, c_in, norm_in,
+                                                             atom_e, u_buf);
+      return 0;
+    });
+    if (rc != 0) return -1;
   }
   if (cudaGetLastError() != cudaSuccess) return -1;
   if (n_pairs > 0) {
-    k_pair_force<T><<<(unsigned)((n_pairs + 127) / 128), 128, 0, stream>>>(
-        a, g.strict, n_pairs, nbr_i, nb.rel, nb.rel32, nb.nbr_s, species, u_buf, pair_f);
+    with_shape<T>(a, [&](auto sh) {
+      k_pair_force<T, decltype(sh)><<<(unsigned)((n_pairs + 127) / 128), 128, 0, stream>>>(
+          a, g.strict, n_pairs, nbr_i, nb.rel, nb.rel32, nb.nbr_s, species, u_buf, pair_f);
+      return 0;
+    });
     if (cudaGetLastError() != cudaSuccess) return -1;
   }
   if (!gather) return 0;
-  const int nblk = ceil_div(a.noa, 128);
-  k_gather<T><<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32, nb.rel, pair_f,
-                                        atom_e, forces, atom_vir);
+  int nblk;
+  if constexpr (sizeof(T) == 4) {
+    nblk = ceil_div(a.noa, 4);
+    k_gather_warp<<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32,
+                                            reinterpret_cast<const float4 *>(pair_f), atom_e,
+                                            forces, atom_vir);
+  } else {
+    nblk = ceil_div(a.noa, 128);
+    k_gather<T><<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32, nb.rel, pair_f,
+                                          atom_e, forces, atom_vir);
+  }
   if (cudaGetLastError() != cudaSuccess) return -1;
-  k_reduce<<<1, 256, 0, stream>>>(nblk, atom_vir, reduce_out);
+  k_reduce<<<1, 1024, 0, stream>>>(nblk, atom_vir, reduce_out);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -35,12 +35,10 @@ struct B2Args {
   size_t smem_per_warp_adj;  // filled by the launcher
 };
 
-// Row of u = dE/dc per atom, laid out [species][lm][n] with n padded to a
-// multiple of 4, so the pair-force kernel reads each (species, lm) column
-// with 16-byte loads.
-inline __host__ __device__ int u_npad(const B2Args &a) { return (a.N + 3) & ~3; }
+// Row of u = dE/dc per atom, laid out like the single bond c:
+// [species][n][lm].
 inline __host__ __device__ int u_row_stride(const B2Args &a) {
-  return a.n_species * a.H * u_npad(a);
+  return a.n_species * a.N * a.H;
 }
 
 enum WMode { kWFromV2 = 0, kWFromV1 = 1, kWGiven = 2 };

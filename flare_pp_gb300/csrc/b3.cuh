@@ -129,13 +129,14 @@ inline int upload_b3_tables(cudaStream_t stream) {
   return e == cudaSuccess ? 0 : -1;
 }
 
-// Real single-bond block c (nr x H, row stride H) -> complex (zr, zi) with
+// Real single-bond block c (nr x H, row stride ldc, default H) -> complex (zr, zi) with
 // row stride H + 1 (padded so that lanes on different radial rows hit
 // different banks).  Lane-strided; the caller synchronizes the warp.
 template <typename T>
 __device__ __forceinline__ void b3_to_complex(const T *__restrict__ c, int nr, int H,
                                               T *__restrict__ zr, T *__restrict__ zi,
-                                              int lane) {
+                                              int lane, int ldc = -1) {
+  const int HC = ldc < 0 ? H : ldc;  // row stride of c
   const T is2 = T(0.70710678118654752440);
   for (int k = lane; k < nr * H; k += 32) {
     const int n = k / H, lm = k - n * H;
@@ -143,8 +144,8 @@ __device__ __forceinline__ void b3_to_complex(const T *__restrict__ c, int nr, i
     while ((l + 1) * (l + 1) <= lm) l++;
     const int m = lm - l * l - l;
     const int am = m < 0 ? -m : m;
-    const T R = c[n * H + l * l + l + am];
-    const T S = c[n * H + l * l + l - am];
+    const T R = c[n * HC + l * l + l + am];
+    const T S = c[n * HC + l * l + l - am];
     T re, im;
     if (m == 0) {
       re = R;

@@ -29,6 +29,7 @@ struct HarmonicTables {
   float norm_hi[(kMaxL + 1) * (kMaxL + 1)];
   float norm_lo[(kMaxL + 1) * (kMaxL + 1)];
   double dfact[kMaxL + 1];
+  float dfact_f[kMaxL + 1];  // exact in FP32 (at most 15!! = 2027025)
 };
 static __constant__ HarmonicTables c_harm;  // uploaded by upload_harmonic_tables()
 
@@ -152,7 +153,7 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
     for (int l = m; l <= lmax; l++) {
       T q, qz, qr;
       if (l == m) {
-        q = T(c_harm.dfact[m]);
+        q = sizeof(T) == 4 ? T(c_harm.dfact_f[m]) : T(c_harm.dfact[m]);
         qz = T(0);
         qr = T(0);
       } else if (l == m + 1) {
@@ -223,7 +224,7 @@ __device__ __forceinline__ void harmonics_visit(T x, T y, T z, int lmax, Visit v
     for (int l = m; l <= lmax; l++) {
       T q, qz, qr;
       if (l == m) {
-        q = T(c_harm.dfact[m]);
+        q = sizeof(T) == 4 ? T(c_harm.dfact_f[m]) : T(c_harm.dfact[m]);
         qz = T(0);
         qr = T(0);
       } else if (l == m + 1) {

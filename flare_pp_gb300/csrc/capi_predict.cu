@@ -383,7 +383,7 @@ static int upload_beta(fpp_model *m, int s, const std::vector<double> &B) {
   for (size_t k = 0; k < pad.size(); k++) {
     const float x = (float)(pad[k] * scale);
     const __half h = __float2half_rn(x);
-    const float rem = (float)(pad[k] * scale - (double)__half2float(h));  // residual
+    const float rem = (float)((pad[k] * scale - (double)__half2float(h)) * 2048.0);
     hi[k] = h;
     lo[k] = __float2half_rn(rem);
   }
@@ -904,7 +904,7 @@ int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream
     FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, S2, S1, nd, &one,
                            m2->sp[s].d_dhat.as<double>(), nd, m1->sp[s].d_dhat.as<double>(), nd,
                            &zero, Z.as<double>(), S2));
-    if (launch_envs_block(S1, S2, Z.as<double>(), m1->sp[s].d_norms.as<double>(),
+    if (launch_envs_block(S1, S2, Z.as<double>(), S2, m1->sp[s].d_norms.as<double>(),
                           m2->sp[s].d_norms.as<double>(), m1->sigma * m1->sigma, m1->power,
                           K.as<double>() + (size_t)m1->sp[s].sparse_offset * n2 +
                               m2->sp[s].sparse_offset,
@@ -916,6 +916,70 @@ int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream
   if ((size_t)n1 * n2)
     FPP_CUDA(cudaMemcpy(kernel_mat, K.ptr, sizeof(double) * (size_t)n1 * n2,
                         cudaMemcpyDeviceToHost));
+  return FPP_OK;
+}
+
+int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
+                            int32_t n, double *variances, void *stream) {
+  FPP_TRY(model_check(m, s));
+  if (!L_inv || !variances) return fail(FPP_ERR_INVALID, "null argument");
+  if (n != m->n_sparse_total)
+    return fail(FPP_ERR_INVALID, "L_inv size differs from the sparse set");
+  cudaStream_t st = (cudaStream_t)stream;
+  StructureState &S = s->st;
+  const int noa = S.noa, nd = m->n_d, ldp = round_up(nd, 64);
+  if (noa == 0) return FPP_OK;
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  B2Args a = m->args;
+  a.noa = noa;
+  FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+  const int R = s->total_rows;
+  DevBuf rown, K, Q, Ld, q;
+  FPP_TRY(rown.reserve(sizeof(double) * std::max(1, R)));
+  FPP_CUDA(cudaMemsetAsync(rown.ptr, 0, sizeof(double) * R, st));
+  if (launch_gather_rows(noa, s->row_of_atom.as<int>(), S.norm64.as<double>(),
+                         rown.as<double>(), st) != 0)
+    return fail(FPP_ERR_CUDA, "gather launch failed");
+  FPP_TRY(K.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
+  FPP_CUDA(cudaMemsetAsync(K.ptr, 0, sizeof(double) * (size_t)R * n, st));
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m, st, &h));
+  const double one = 1.0, zero = 0.0;
+  // K[cluster][k] = k(cluster, sparse k): block-diagonal in the species
+  for (int sp = 0; sp < m->n_species; sp++) {
+    const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
+    if (Ss == 0 || nsa == 0) continue;
+    double *C = K.as<double>() + (size_t)s->row_off[sp] * n + m->sp[sp].sparse_offset;
+    const double *Ph = S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp;
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one,
+                           m->sp[sp].d_dhat.as<double>(), nd, Ph, ldp, &zero, C, n));
+    if (launch_envs_block(nsa, Ss, C, n, rown.as<double>() + s->row_off[sp],
+                          m->sp[sp].d_norms.as<double>(), m->sigma * m->sigma, m->power, C,
+                          n, st) != 0)
+      return fail(FPP_ERR_CUDA, "local kernel launch failed");
+  }
+  // Q = K L_inv^T; the explained variance of a cluster is |row of Q|^2
+  FPP_TRY(Ld.reserve(sizeof(double) * (size_t)n * n));
+  FPP_CUDA(cudaMemcpyAsync(Ld.ptr, L_inv, sizeof(double) * (size_t)n * n,
+                           cudaMemcpyHostToDevice, st));
+  FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
+  FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, n, R, n, &one, Ld.as<double>(), n,
+                         K.as<double>(), n, &zero, Q.as<double>(), n));
+  FPP_TRY(q.reserve(sizeof(double) * std::max(1, R)));
+  if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
+    return fail(FPP_ERR_CUDA, "row-norm launch failed");
+  std::vector<double> hq(R), hn(R);
+  FPP_CUDA(cudaStreamSynchronize(st));
+  FPP_CUDA(cudaMemcpy(hq.data(), q.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
+  FPP_CUDA(cudaMemcpy(hn.data(), rown.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
+  // clusters in species order, atoms in structure order within a species
+  const double sig2 = m->sigma * m->sigma;
+  int out = 0;
+  for (int sp = 0; sp < m->n_species; sp++)
+    for (int r = 0; r < s->n_rows[sp]; r++) {
+      const int row = s->row_off[sp] + r;
+      variances[out++] = (hn[row] >= 1e-8 ? sig2 : 0.0) - hq[row];
+    }
   return FPP_OK;
 }
 

@@ -43,7 +43,7 @@ struct fpp_model {
     fpp::DevBuf d_norms, d_alpha;       // double[n_sparse]
     fpp::DevBuf beta64;                 // double[n_d * ldb] dense symmetric
     fpp::DevBuf beta_hi, beta_lo;       // half[n_d_pad * ldb] split operands
-    double beta_scale = 1;              // beta ~ (hi + lo) / beta_scale, lo the fp16 residual
+    double beta_scale = 1;              // beta ~ (hi + lo/2048) / beta_scale
     std::vector<double> B_host;         // dense beta (n_d x n_d), power 2
   };
   std::vector<Species> sp;

@@ -1,26 +1,26 @@
 // Split-fp16 contraction on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
 //   V[m, n] = sum_k P[m, k] B[n, k]
-// with both operands given as power-of-two-scaled fp16 pairs, a value and its
-// fp16 residual,
-//   P ~ (P_hi + P_lo) / sP,   B ~ (B_hi + B_lo) / sB,
-// evaluated as three MMAs into one FP32 accumulator held in TMEM:
-//   acc += P_hi B_hi^T + P_hi B_lo^T + P_lo B_hi^T,   V = acc / (sP sB).
+// with both operands given as power-of-two-scaled fp16 pairs
+//   P ~ (P_hi + P_lo / 2048) / sP,   B ~ (B_hi + B_lo / 2048) / sB,
+// evaluated as three MMAs into two FP32 accumulators held in TMEM:
+//   acc0 += P_hi B_hi^T,   acc1 += P_hi B_lo^T + P_lo B_hi^T,
+//   V = (acc0 + acc1 / 2048) / (sP sB).
 // That keeps about 22 significant bits per operand, which the mapped-beta
-// energy needs (a single fp16 or bf16 term, or a bf16 hi/lo split, does not);
-// the products of fp16 values are exact in FP32 and the residual terms are
-// 2^-11 of the leading one, so one FP32 accumulator loses nothing against
-// separate ones.
+// energy needs (a single fp16 or bf16 term, or a bf16 hi/lo split, does not).
+// The cross terms have their own accumulator: added into the leading one they
+// would each round against its magnitude (measured: 1.6x the force error).
 //
-// One persistent CTA per SM walks 128 x 256 tiles of all species blocks
-// (each block of P rows against its own B):
+// One persistent CTA per SM walks the 128 x 128 tiles of all species blocks
+// (each block of P rows against its own B), in one launch:
 //   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of P_hi, P_lo,
-//                  B_hi, B_lo (64 K-columns per stage) into a 2-stage ring
+//                  B_hi, B_lo (64 K-columns per stage) into a 3-stage ring
 //   warp 1 lane 0  MMA issuer: 4 K=16 steps x 3 tcgen05.mma per stage,
-//                  tcgen05.commit frees the stage; the two 256-column TMEM
-//                  accumulators alternate between tiles
-//   warps 2-5      epilogue: tcgen05.ld of their 32 TMEM lanes, scale, store
-//                  FP32 rows of V, then release the accumulator
+//                  tcgen05.commit frees the stage; the two accumulator pairs
+//                  (2 x 2 x 128 TMEM columns) alternate between tiles, so the
+//                  epilogue of one tile overlaps the MMAs of the next
+//   warps 2-5      epilogue: tcgen05.ld of their 32 TMEM lanes, combine,
+//                  scale, store FP32 rows of V, then release the accumulators
 // Every mbarrier wait is bounded; a wait that runs out records
 // FPP_ERR_TIMEOUT in the status word and the CTA skips to its exit.
 #include <cuda.h>
@@ -37,7 +37,7 @@
 
 namespace fpp {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
 constexpr int A_TILE = BM * BK * 2;  // bytes, one fp16 operand tile
 constexpr int B_TILE = BN * BK * 2;
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
@@ -148,16 +148,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
 }
 
 // ---------------------------------------------------------------------------
-// Grouped persistent form: every species block of the operand rows against
-// its own B in one launch, one CTA per SM walking the tiles, the two TMEM
-// accumulators of 256 columns used in turn so that the epilogue of one tile
-// overlaps the MMAs of the next.  The lo planes here carry the residual
-// itself (not scaled by 2048), so the three products share one accumulator:
-//   acc = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T,   V = acc * out_scale[g].
-//   warp 0 lane 0  TMA producer (2-stage ring, as above)
-//   warp 1 lane 0  MMA issuer
-//   warps 2..5     epilogue; warp w reads TMEM lanes 32 (w mod 4) ..; warp 2
-//                  also allocates / frees the 512 TMEM columns
+// Grouped persistent form (see the header comment).
 // ---------------------------------------------------------------------------
 struct GroupedParams {
   CUtensorMap a_hi, a_lo;
@@ -257,7 +248,7 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
     int it = 0, j = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, j++) {
       const int buf = j & 1;
-      const uint32_t acc = tmem + (uint32_t)(buf * BN);
+      const uint32_t acc0 = tmem + (uint32_t)(buf * 2 * BN), acc1 = acc0 + BN;
       if (!mbar_wait(acce_bar(buf), (uint32_t)(((j >> 1) & 1) ^ 1))) {
         set_status(p.status, FPP_ERR_TIMEOUT, 112, t);
         *abort_flag = 1;
@@ -284,10 +275,10 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
 #pragma unroll
         for (int ks = 0; ks < BK / 16; ks++) {
           const uint32_t off = ks * 32;
-          mma_f16(acc, smem_desc(a_hi + off), smem_desc(b_hi + off),
-                  (kb > 0 || ks > 0) ? 1u : 0u);
-          mma_f16(acc, smem_desc(a_hi + off), smem_desc(b_lo + off), 1u);
-          mma_f16(acc, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+          const uint32_t first = (kb > 0 || ks > 0) ? 1u : 0u;
+          mma_f16(acc0, smem_desc(a_hi + off), smem_desc(b_hi + off), first);
+          mma_f16(acc1, smem_desc(a_hi + off), smem_desc(b_lo + off), first);
+          mma_f16(acc1, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
         }
         mma_commit(empty_bar(s));
       }
@@ -314,22 +305,28 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
       locate(t, g, mrow, n0);
       const int r = mrow + q * 32 + lane;  // row within the group
       const float sc = p.scale[g];
-      const uint32_t acc = tmem + (uint32_t)(buf * BN) + lane_base;
+      const uint32_t acc0 = tmem + (uint32_t)(buf * 2 * BN) + lane_base, acc1 = acc0 + BN;
 #pragma unroll 1
       for (int c = 0; c < BN; c += 32) {
-        float v[32];
-        tmem_ld32(acc + c, v);
+        float v0[32], v1[32];
+        tmem_ld32(acc0 + c, v0);
+        tmem_ld32(acc1 + c, v1);
         if (r < p.M[g]) {
           float *dst = p.V + (size_t)(p.row0[g] + r) * p.ldv + n0 + c;
           const int ncol = p.N - (n0 + c);
           if (ncol >= 32) {
 #pragma unroll
-            for (int i = 0; i < 32; i += 4)
-              *reinterpret_cast<float4 *>(dst + i) =
-                  make_float4(v[i] * sc, v[i + 1] * sc, v[i + 2] * sc, v[i + 3] * sc);
+            for (int i = 0; i < 32; i += 4) {
+              float4 o;
+              o.x = (v0[i + 0] + v1[i + 0] * (1.0f / 2048.0f)) * sc;
+              o.y = (v0[i + 1] + v1[i + 1] * (1.0f / 2048.0f)) * sc;
+              o.z = (v0[i + 2] + v1[i + 2] * (1.0f / 2048.0f)) * sc;
+              o.w = (v0[i + 3] + v1[i + 3] * (1.0f / 2048.0f)) * sc;
+              *reinterpret_cast<float4 *>(dst + i) = o;
+            }
           } else {
             for (int i = 0; i < 32; i++)
-              if (i < ncol) dst[i] = v[i] * sc;
+              if (i < ncol) dst[i] = (v0[i] + v1[i] * (1.0f / 2048.0f)) * sc;
           }
         }
       }

@@ -8,8 +8,8 @@
 namespace fpp {
 
 // Grouped persistent form: operand rows in species blocks (row0, M) of one
-// A, each block against its own B; lo planes hold the unscaled residual
-// (A ~ A_hi + A_lo), V[row0 + r, :] = (A B^T)[r, :] * out_scale.
+// A, each block against its own B; lo planes hold the fp16 residual scaled by
+// 2048 (A ~ A_hi + A_lo / 2048), V[row0 + r, :] = (A B^T)[r, :] * out_scale.
 constexpr int kGemmMaxGroups = 8;
 struct GemmGroup {
   const __half *b_hi, *b_lo;

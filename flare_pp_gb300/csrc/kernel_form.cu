@@ -172,23 +172,25 @@ __global__ void k_envs_stress(int S, int nq, const double *__restrict__ fkv, int
 }
 
 // envs_envs block: K[i][j] = sig2 z^p for non-empty environments
-__global__ void k_envs_block(int S1, int S2, const double *__restrict__ Z,
+// (Z may alias K when ldz == ldk: each element is read and written by one thread)
+__global__ void k_envs_block(int S1, int S2, const double *Z, int ldz,
                              const double *__restrict__ n1, const double *__restrict__ n2,
-                             double sig2, double power, double *__restrict__ K, int ldk) {
+                             double sig2, double power, double *K, int ldk) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)S1 * S2) return;
   const int i = (int)(t / S2), j = (int)(t - (long long)i * S2);
   double v = 0.0;
-  if (n1[i] >= 1e-8 && n2[j] >= 1e-8) v = sig2 * powi(Z[t], power);
+  if (n1[i] >= 1e-8 && n2[j] >= 1e-8) v = sig2 * powi(Z[(size_t)i * ldz + j], power);
   K[(size_t)i * ldk + j] = v;
 }
 
-int launch_envs_block(int S1, int S2, const double *Z, const double *n1, const double *n2,
-                      double sig2, double power, double *K, int ldk, cudaStream_t st) {
+int launch_envs_block(int S1, int S2, const double *Z, int ldz, const double *n1,
+                      const double *n2, double sig2, double power, double *K, int ldk,
+                      cudaStream_t st) {
   long long n = (long long)S1 * S2;
   if (n == 0) return 0;
-  k_envs_block<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(S1, S2, Z, n1, n2, sig2, power,
-                                                           K, ldk);
+  k_envs_block<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(S1, S2, Z, ldz, n1, n2, sig2,
+                                                           power, K, ldk);
   return LAUNCH_OK;
 }
 

@@ -25,8 +25,9 @@ int launch_envs_force(int S, int noa, const double *fkv, int ldf, const int *off
 int launch_envs_stress(int S, int nq, const double *fkv, int ldf, const int *q_pair,
                        const dvec4 *rel, double vol_inv, int noa, double *K, int ldk,
                        cudaStream_t st);
-int launch_envs_block(int S1, int S2, const double *Z, const double *n1, const double *n2,
-                      double sig2, double power, double *K, int ldk, cudaStream_t st);
+int launch_envs_block(int S1, int S2, const double *Z, int ldz, const double *n1,
+                      const double *n2, double sig2, double power, double *K, int ldk,
+                      cudaStream_t st);
 int launch_row_sq(int rows, int cols, const double *V, int ldv, double *out,
                   cudaStream_t st);
 }  // namespace fpp

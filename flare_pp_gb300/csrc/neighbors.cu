@@ -58,9 +58,10 @@ static CellDev make_dev(const CellInfo &ci) {
   d.cutoff = ci.cutoff;
   double cmax = 0;
   for (int k = 0; k < 9; k++) cmax = fmax(cmax, fabs(ci.cell[k]));
-  // FP32 positions are within 2^-24 |x| of the FP64 ones; the margin covers
-  // that error many times over for any cell below ~10^4 A
-  double margin = 1e-3 + 1e-5 * (cmax * (2 * ci.sweep + 2) + ci.cutoff);
+  // FP32 positions are within 2^-24 |x| of the FP64 ones; an FP32 image
+  // component then errs by at most ~2^-24 (18 + 12 sweep) cmax, which the
+  // margin covers about five times over
+  double margin = 2e-4 + 4e-6 * (cmax * (2 * ci.sweep + 2) + ci.cutoff);
   d.in2 = (float)((ci.cutoff - margin) * (ci.cutoff - margin));
   if (ci.cutoff <= margin) d.in2 = 0.f;
   d.out2 = (float)((ci.cutoff + margin) * (ci.cutoff + margin));
@@ -309,46 +310,63 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
     tot = 0;
     __syncwarp();
   };
-  for (int s1 = -cd.sweep; s1 <= cd.sweep; s1++)
-    for (int s2 = -cd.sweep; s2 <= cd.sweep; s2++)
-      for (int s3 = -cd.sweep; s3 <= cd.sweep; s3++) {
-        const int sv[3] = {s1, s2, s3};
-        int lo[3], hi[3];
-        bool empty = false;
+  // the shifts' bin ranges are evaluated one shift per lane; the warp then
+  // walks the non-empty ones
+  const unsigned full = 0xffffffffu;
+  for (int s0 = 0; s0 < cd.n_shift; s0 += 32) {
+    const int sidx = s0 + lane;
+    int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
+    float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool nonempty = false;
+    if (sidx < cd.n_shift) {
+      const int s3 = sidx % cd.ns - cd.sweep;
+      const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
+      const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
+      const int sv[3] = {s1, s2, s3};
+      nonempty = true;
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-          const float c = fik[k] - (float)sv[k];
-          int l = (int)floorf((c - cd.delta32[k]) * cd.nb[k]);
-          int h = (int)floorf((c + cd.delta32[k]) * cd.nb[k]);
-          lo[k] = max(l, 0);
-          hi[k] = min(h, cd.nb[k] - 1);
-          if (lo[k] > hi[k]) empty = true;
-        }
-        if (empty) continue;
-        const int sidx = ((s1 + cd.sweep) * cd.ns + (s2 + cd.sweep)) * cd.ns + (s3 + cd.sweep);
-        const float4 sh = make_float4(
-            s1 * cd.cell32[0] + s2 * cd.cell32[3] + s3 * cd.cell32[6],
-            s1 * cd.cell32[1] + s2 * cd.cell32[4] + s3 * cd.cell32[7],
-            s1 * cd.cell32[2] + s2 * cd.cell32[5] + s3 * cd.cell32[8], 0.f);
-        for (int b0 = lo[0]; b0 <= hi[0]; b0++)
-          for (int b1 = lo[1]; b1 <= hi[1]; b1++) {
-            // bins along the last direction are contiguous: one range
-            const int bin_lo = (b0 * cd.nb[1] + b1) * cd.nb[2] + lo[2];
-            const int bin_hi = (b0 * cd.nb[1] + b1) * cd.nb[2] + hi[2];
-            const int st = bin_start[bin_lo], cn = bin_start[bin_hi + 1] - st;
-            if (cn == 0) continue;
-            if (nr == kMaxRanges) flush();
-            if (lane == 0) {
-              s_rstart[w][nr] = st;
-              s_rsidx[w][nr] = sidx;
-              s_rshift[w][nr] = sh;
-              s_rpre[w][nr + 1] = tot + cn;
-            }
-            __syncwarp();
-            tot += cn;
-            nr++;
-          }
+      for (int k = 0; k < 3; k++) {
+        const float c = fik[k] - (float)sv[k];
+        const int l = (int)floorf((c - cd.delta32[k]) * cd.nb[k]);
+        const int h = (int)floorf((c + cd.delta32[k]) * cd.nb[k]);
+        lo[k] = max(l, 0);
+        hi[k] = min(h, cd.nb[k] - 1);
+        if (lo[k] > hi[k]) nonempty = false;
       }
+      sh = make_float4(s1 * cd.cell32[0] + s2 * cd.cell32[3] + s3 * cd.cell32[6],
+                       s1 * cd.cell32[1] + s2 * cd.cell32[4] + s3 * cd.cell32[7],
+                       s1 * cd.cell32[2] + s2 * cd.cell32[5] + s3 * cd.cell32[8], 0.f);
+    }
+    unsigned todo = __ballot_sync(full, nonempty);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int ssrc = __shfl_sync(full, sidx, src);
+      const int l0 = __shfl_sync(full, lo[0], src), h0 = __shfl_sync(full, hi[0], src);
+      const int l1 = __shfl_sync(full, lo[1], src), h1 = __shfl_sync(full, hi[1], src);
+      const int l2 = __shfl_sync(full, lo[2], src), h2 = __shfl_sync(full, hi[2], src);
+      const float4 shs = make_float4(__shfl_sync(full, sh.x, src), __shfl_sync(full, sh.y, src),
+                                     __shfl_sync(full, sh.z, src), 0.f);
+      for (int b0 = l0; b0 <= h0; b0++)
+        for (int b1 = l1; b1 <= h1; b1++) {
+          // bins along the last direction are contiguous: one range
+          const int bin_lo = (b0 * cd.nb[1] + b1) * cd.nb[2] + l2;
+          const int bin_hi = (b0 * cd.nb[1] + b1) * cd.nb[2] + h2;
+          const int st = bin_start[bin_lo], cn = bin_start[bin_hi + 1] - st;
+          if (cn == 0) continue;
+          if (nr == kMaxRanges) flush();
+          if (lane == 0) {
+            s_rstart[w][nr] = st;
+            s_rsidx[w][nr] = ssrc;
+            s_rshift[w][nr] = shs;
+            s_rpre[w][nr + 1] = tot + cn;
+          }
+          __syncwarp();
+          tot += cn;
+          nr++;
+        }
+    }
+  }
   flush();
   if (lane == 0) count[i] = nacc;
   if (nacc > kSlabCap) {
@@ -376,7 +394,28 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
   const int lane = threadIdx.x & 31;
   const int beg = offset[i], n = offset[i + 1] - beg;
   const dvec4 wi = wp[i];
-  for (int e = lane; e < n; e += 32) {
+  // the pair (i, j, s) and its reverse (j, i, -s) have exactly negated images
+  // (IEEE subtraction and addition round symmetrically), so the FP64
+  // geometry is computed for the canonical half only -- keys above
+  // (i, centre shift), a suffix of the sorted list -- and k_mirror copies it
+  const long long thr = ((long long)i << kKeyBits) |
+                        ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
+  int c0 = 0;
+  for (int e0 = 0; e0 < n; e0 += 32) {
+    const int e = e0 + lane;
+    long long key = 0;
+    if (e < n) {
+      key = slab[(size_t)i * kSlabCap + e];
+      const int out = beg + e;
+      const int j = (int)(key >> kKeyBits);
+      keys[out] = key;
+      nbr_i[out] = i;
+      nbr_j[out] = j;
+      nbr_s[out] = species[j];
+    }
+    c0 += __popc(__ballot_sync(0xffffffffu, e < n && key <= thr));
+  }
+  for (int e = c0 + lane; e < n; e += 32) {
     const long long key = slab[(size_t)i * kSlabCap + e];
     const int j = (int)(key >> kKeyBits);
     const int sidx = (int)(key & kKeyMask);
@@ -386,13 +425,26 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
     double im[3];
     const double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
     const int out = beg + e;
-    keys[out] = key;
-    nbr_i[out] = i;
-    nbr_j[out] = j;
-    nbr_s[out] = species[j];
     rel[out] = dvec4{dist, im[0], im[1], im[2]};
     rel32[out] = make_float4((float)im[0], (float)im[1], (float)im[2], (float)dist);
   }
+}
+
+// Geometry of the non-canonical pairs: the negated image of the reverse pair.
+__global__ void k_mirror(long long n_pairs, CellDev cd, const long long *__restrict__ keys,
+                         const int *__restrict__ nbr_i, const int *__restrict__ rev,
+                         dvec4 *__restrict__ rel, float4 *__restrict__ rel32) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const long long thr = ((long long)nbr_i[p] << kKeyBits) |
+                        ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
+  if (keys[p] > thr) return;
+  const int q = rev[p];
+  if (q < 0) return;  // reported by k_reverse
+  const dvec4 r = rel[q];
+  const float4 r32 = rel32[q];
+  rel[p] = dvec4{r.x, -r.y, -r.z, -r.w};
+  rel32[p] = make_float4(-r32.x, -r32.y, -r32.z, r32.w);
 }
 
 __global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
@@ -718,6 +770,12 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
       total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
       st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst);
   FPP_CUDA(cudaGetLastError());
+  if (!overflow) {
+    k_mirror<<<ceil_div(total, tb), tb, 0, stream>>>(
+        total, cd, st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_rev.as<int>(),
+        st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
+    FPP_CUDA(cudaGetLastError());
+  }
   return FPP_OK;
 }
 

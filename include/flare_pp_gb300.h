@@ -227,6 +227,17 @@ int fpp_envs_envs(fpp_model *m1, fpp_model *m2, double *kernel_mat, void *stream
 int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs,
                 double *variance_efs, void *stream);
 
+/* SparseGP::compute_cluster_uncertainties (sparse_gp.cpp:93-133) for the
+ * model's single kernel: per cluster (atom environment) the energy variance
+ * k(c, c) - |L_inv k(sparse, c)|^2, FP64 on the GPU.  L_inv is the host
+ * n x n (row-major) inverse Cholesky factor of Kuu + jitter I (the L_inv of
+ * fpp_update_matrices_QR), n = the model's sparse-set size.  variances (host,
+ * noa) are in cluster order: species by species, atoms in structure order.
+ * This is SparseGP::predict_local_uncertainties' uncertainty
+ * (sparse_gp.cpp:682-702). */
+int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
+                            int32_t n, double *variances, void *stream);
+
 /* SparseGP::update_Kuf / stack_Kuf for a batch of training structures
  * (sparse_gp.cpp:392-462, 464-552, 565-574): the sparse-environment columns
  * of each structure's labels, [E] [F of the listed atoms] [S], stacked in

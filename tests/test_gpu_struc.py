@@ -140,3 +140,33 @@ def test_batched_kuf_training_matches_oracle(gpu_lib):
     np.testing.assert_allclose(ggp.y, ogp.y, rtol=0, atol=0)
     np.testing.assert_allclose(ggp.alpha, ogp.alpha, rtol=0,
                                atol=1e-5 * np.abs(ogp.alpha).max())
+
+
+def test_local_uncertainties_match_oracle(gpu_lib):
+    """SparseGP::compute_cluster_uncertainties / predict_local_uncertainties
+    (sparse_gp.cpp:93-133, 682-702) after a GPU training solve, against the
+    oracle on the same model."""
+    from flare_pp_gb300 import synth
+    from tests import fixtures
+    m = fixtures.config1_model(n_frames=2, n_sparse=20)
+    ogp = m["gp"]
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, 5.0], [], [1, 8, 3])
+    gp = fg.SparseGP([fg.NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
+    frames = []
+    for of in ogp.training_structures:
+        s = fg.Structure(of.cell, of.species, of.positions, 5.0, [b2])
+        s.energy, s.forces, s.stresses = of.energy, of.forces, of.stresses
+        gp.add_training_structure(s)
+        frames.append(s)
+    for k, atoms in enumerate(ogp.sparse_indices[0]):
+        gp.add_specific_environments(frames[k], atoms)
+    gp.update_matrices_QR()
+    cell, sp, pos = synth.fcc_al_108(101, 5)
+    os_ = OStructure(cell, sp, pos, 5.0, [m["b2"]])
+    ref = ogp.compute_cluster_uncertainties(os_)[0]
+    gs = fg.Structure(cell, sp, pos, 5.0)
+    gp.predict_local_uncertainties(gs)
+    got = gs.local_uncertainties[0]
+    # a difference of two O(sigma^2) terms: compare on sigma^2's scale
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-7 * 4.0)
+    assert np.all(got > -1e-8)
