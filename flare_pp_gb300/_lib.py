@@ -62,6 +62,7 @@ SIGNATURES = {
     "fpp_self_kernel_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp]),
     "fpp_predict": (_c_int, [_vp, _vp, _vp, _vp, _vp]),
     "fpp_predict_mapped": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
+    "fpp_model_center_on": (_c_int, [_vp, _vp, _vp]),
     "fpp_update_matrices_QR": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _dbl, _vp, _vp,
                                         _vp, _vp]),
     "fpp_pair_compute": (_c_int, [_vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp,

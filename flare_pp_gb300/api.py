@@ -451,7 +451,7 @@ def update_matrices_QR(Kuu, Kuf, y, noise_vector, jitter=1e-8, stream=None):
 
 class SparseGP:
     """SparseGP (sparse_gp.h:12-112) for one NormalizedDotProduct kernel over
-    one B2 descriptor: training solve and prediction on the GPU."""
+    one B2 or B3 descriptor: training solve and prediction on the GPU."""
 
     def __init__(self, kernels, energy_noise, force_noise, stress_noise):
         self.kernels = list(kernels)
@@ -472,6 +472,7 @@ class SparseGP:
         self.L_inv = None
         self.Sigma = None
         self.Kuu_inverse = None
+        self.b2 = None
         self._model = None
         self._mapped = False
 
@@ -574,6 +575,99 @@ class SparseGP:
         self._model = _Model(self.b2, k.sigma, k.power, sd, self.alpha, self.R_inv)
         self._mapped = False
 
+    # ---- the reference's JSON state (sparse_gp.h:101-111, sparse_gp.cpp:1406-1417)
+    def to_json(self, file_name):
+        """Write the model in the layout of SparseGP::to_json (nlohmann JSON of
+        the NLOHMANN_DEFINE_TYPE_INTRUSIVE fields; Eigen matrices as lists of
+        rows, vectors as lists).  The descriptor settings travel in
+        training_structures[0].descriptor_calculators, as in the reference."""
+        import json
+
+        def mat(a):
+            return None if a is None else np.asarray(a, dtype=np.float64).tolist()
+
+        k = self.kernels[0]
+        sd = self.sparse_descriptors[0]
+        b2 = self.b2 if self.b2 is not None else sd.descriptor_calculator
+        desc = {"radial_basis": b2.radial_basis, "cutoff_function": b2.cutoff_function,
+                "radial_hyps": list(b2.radial_hyps), "cutoff_hyps": list(b2.cutoff_hyps),
+                "descriptor_settings": list(b2.descriptor_settings),
+                "cutoffs": mat(b2.cutoffs),
+                "descriptor_name": "B3" if isinstance(b2, B3) else "B2"}
+        cd = {"descriptors": [mat(d) for d in sd.descriptors],
+              "descriptor_norms": [mat(n) for n in sd.descriptor_norms],
+              "cutoff_values": [mat(c) for c in sd.cutoff_values],
+              "n_clusters_by_type": [int(v) for v in sd.n_clusters_by_type],
+              "cumulative_type_count": [int(v) for v in sd.cumulative_type_count],
+              "n_descriptors": int(sd.n_descriptors), "n_types": int(sd.n_types),
+              "n_clusters": int(sd.n_clusters)}
+        j = {"hyperparameters": [k.sigma, self.energy_noise, self.force_noise,
+                                 self.stress_noise],
+             "kernels": [{"kernel_name": "NormalizedDotProduct", "sigma": k.sigma,
+                          "sig2": k.sigma * k.sigma, "power": k.power,
+                          "kernel_hyperparameters": [k.sigma]}],
+             "n_kernels": 1, "Kuu_jitter": self.Kuu_jitter,
+             "Kuu": mat(getattr(self, "Kuu", None)), "Kuf": mat(getattr(self, "Kuf", None)),
+             "Sigma": mat(self.Sigma), "Kuu_inverse": mat(self.Kuu_inverse),
+             "R_inv": mat(self.R_inv), "L_inv": mat(self.L_inv), "alpha": mat(self.alpha),
+             "sparse_descriptors": [cd], "noise_vector": mat(self.noise_vector),
+             "y": mat(self.y), "n_sparse": int(sd.n_clusters),
+             "energy_noise": self.energy_noise, "force_noise": self.force_noise,
+             "stress_noise": self.stress_noise,
+             "training_structures": [{"descriptor_calculators": [desc]}]}
+        with open(file_name, "w") as f:
+            json.dump(j, f)
+
+    @staticmethod
+    def from_json(file_name):
+        """SparseGP::from_json: a model saved by the reference (or by to_json),
+        loaded for GPU prediction (one NormalizedDotProduct kernel, B2 or B3)."""
+        import json
+        with open(file_name) as f:
+            j = json.load(f)
+
+        def arr(v, shape2=False):
+            if v is None:
+                return np.zeros((0, 0)) if shape2 else np.zeros(0)
+            return np.asarray(v, dtype=np.float64)
+
+        kj = j["kernels"][0]
+        if kj.get("kernel_name") != "NormalizedDotProduct":
+            raise ValueError(f"unsupported kernel {kj.get('kernel_name')}")
+        dj = j["training_structures"][0]["descriptor_calculators"][0]
+        if dj.get("descriptor_name", "B2") == "B3":
+            b2 = B3(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
+                    dj["cutoff_hyps"], dj["descriptor_settings"])
+        else:
+            b2 = B2(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
+                    dj["cutoff_hyps"], dj["descriptor_settings"],
+                    None if dj.get("cutoffs") is None else np.asarray(dj["cutoffs"]))
+        gp = SparseGP([NormalizedDotProduct(kj["sigma"], kj["power"])],
+                      j.get("energy_noise", 1.0), j.get("force_noise", 1.0),
+                      j.get("stress_noise", 1.0))
+        sj = j["sparse_descriptors"][0]
+        cd = ClusterDescriptor()
+        nt, nd = int(sj["n_types"]), int(sj["n_descriptors"])
+        cd.initialize_cluster(nt, nd)
+        cd.descriptors = [arr(d, True).reshape(-1, nd) for d in sj["descriptors"]]
+        cd.descriptor_norms = [arr(v) for v in sj["descriptor_norms"]]
+        cd.cutoff_values = [arr(v) for v in sj["cutoff_values"]]
+        cd.n_clusters_by_type = [int(v) for v in sj["n_clusters_by_type"]]
+        cd.cumulative_type_count = [int(v) for v in sj["cumulative_type_count"]]
+        cd.n_clusters = int(sj["n_clusters"])
+        cd.descriptor_calculator = b2
+        gp.Kuu_jitter = j.get("Kuu_jitter", gp.Kuu_jitter)
+        R_inv = arr(j.get("R_inv"), True)
+        L_inv = arr(j.get("L_inv"), True)
+        gp.set_model(b2, cd, arr(j["alpha"]), R_inv if R_inv.size else None,
+                     L_inv if L_inv.size else None)
+        for key in ("Sigma", "Kuu_inverse"):
+            v = arr(j.get(key), True)
+            setattr(gp, key, v if v.size else None)
+        gp.y = arr(j.get("y"))
+        gp.noise_vector = arr(j.get("noise_vector"))
+        return gp
+
     def set_model(self, b2, sparse_descriptors, alpha, R_inv=None, L_inv=None):
         """Load a trained model: the sparse ClusterDescriptor, alpha and
         optionally R_inv and L_inv (the outputs of update_matrices_QR)."""
@@ -661,6 +755,14 @@ class SparseGP:
                                        PRECISIONS[precision], ptr(e), ptr(f), ptr(s),
                                        ptr(ae), 0, _stream(stream)))
         return (e[0], f, s, ae) if atom_energies else (e[0], f, s)
+
+    def center_mixed_on(self, structure, stream=None):
+        """Centre the mixed-precision mapped form on this structure's mean
+        environment per species (lowers its energy error on structures far
+        from the sparse set's mean; see fpp_model_center_on)."""
+        self._ensure_mapped(stream)
+        check(lib().fpp_model_center_on(self._model.handle, structure.handle,
+                                        _stream(stream)))
 
 
 class PairFLARE:

@@ -18,6 +18,8 @@
 // f_ij and the reverse pair's f_ji, so the result is deterministic.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "basis.cuh"
 #include "b2_kernels.h"
 #include "b3.cuh"
@@ -612,23 +614,30 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
     while ((l + 1) * (l + 1) <= lm) l++;
     if constexpr (SH::kNR > 0 && SH::kL1 > 0) {
       // shape known: the lane's c column in registers, every w index a constant
+      // each packed w (n1 <= n2) is read once and feeds both u[n1] and u[n2]
       constexpr int NR = SH::kNR, LL = SH::kL1;
-      T creg[NR];
+      T creg[NR], acc[NR];
 #pragma unroll
-      for (int n = 0; n < NR; n++) creg[n] = c_s[n * H + lm];
+      for (int n = 0; n < NR; n++) {
+        creg[n] = c_s[n * H + lm];
+        acc[n] = T(0);
+      }
       const T *wl = w_s + l;
 #pragma unroll
-      for (int n1 = 0; n1 < NR; n1++) {
-        T acc = T(0);
+      for (int n1 = 0; n1 < NR; n1++)
 #pragma unroll
-        for (int n2 = 0; n2 < NR; n2++) {
-          const int lo = n1 < n2 ? n1 : n2, hi = n1 < n2 ? n2 : n1;
-          const int q = lo * NR - (lo * (lo - 1)) / 2 + (hi - lo);
+        for (int n2 = n1; n2 < NR; n2++) {
+          const int q = n1 * NR - (n1 * (n1 - 1)) / 2 + (n2 - n1);
           const T w = wl[q * LL];
-          acc += (n1 == n2 ? T(2) * w : w) * creg[n2];
+          if (n1 == n2) {
+            acc[n1] += T(2) * w * creg[n1];
+          } else {
+            acc[n1] += w * creg[n2];
+            acc[n2] += w * creg[n1];
+          }
         }
-        u_out[(size_t)atom * sb + n1 * H + lm] = acc;
-      }
+#pragma unroll
+      for (int n1 = 0; n1 < NR; n1++) u_out[(size_t)atom * sb + n1 * H + lm] = acc[n1];
     } else {
       for (int n1 = 0; n1 < nr; n1++) {
         T acc = T(0);
@@ -1016,21 +1025,26 @@ int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
 
 // FP32 pair forces, one warp per atom: lanes take the atom's pairs (f_ij
 // coalesced, f_ji gathered through the reverse index), the warp sums the force
-// and the virial f_ij (x) r_ij as float-float, and each block writes one
-// partial row of energy and virial for k_reduce (fixed order: deterministic).
-// 128 threads = 4 atoms per block.
-__global__ void __launch_bounds__(128)
+// and the virial f_ij (x) r_ij as float-float.  Warps walk atoms with a grid
+// stride and keep their atoms' energy and virial as float-float sums; each
+// block writes one partial row for k_reduce (fixed order: deterministic).
+constexpr int kGatherWarps = 8;
+
+__global__ void __launch_bounds__(32 * kGatherWarps)
 k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
               const float4 *__restrict__ rel32, const float4 *__restrict__ pair_f,
               const double *__restrict__ atom_e, double *__restrict__ forces,
               double *__restrict__ partial) {
-  __shared__ double sm[4][10];
+  __shared__ double sm[kGatherWarps][10];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 4 + warp;
-  float hi[12], lo[12];
+  float th[9], tl[9];  // this warp's virial, float-float
 #pragma unroll
-  for (int k = 0; k < 12; k++) hi[k] = lo[k] = 0.0f;
-  if (i < noa) {
+  for (int k = 0; k < 9; k++) th[k] = tl[k] = 0.0f;
+  double esum = 0.0;  // lane 0: this warp's energy
+  for (int i = blockIdx.x * kGatherWarps + warp; i < noa; i += gridDim.x * kGatherWarps) {
+    float hi[12], lo[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) hi[k] = lo[k] = 0.0f;
     const int beg = offset[i], end = offset[i + 1];
     for (int p = beg + lane; p < end; p += 32) {
       const int q = rev[p];
@@ -1055,22 +1069,33 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
         }
       }
     }
-  }
 #pragma unroll
-  for (int k = 0; k < 12; k++) ff_warp_sum(hi[k], lo[k]);
-  if (lane == 0) {
-    if (i < noa) {
+    for (int k = 0; k < 12; k++) ff_warp_sum(hi[k], lo[k]);
+    if (lane == 0) {
 #pragma unroll
       for (int a = 0; a < 3; a++) forces[3 * i + a] = double(hi[a]) + double(lo[a]);
+      esum += atom_e[i];
     }
-    sm[warp][0] = i < noa ? atom_e[i] : 0.0;
 #pragma unroll
-    for (int k = 0; k < 9; k++) sm[warp][1 + k] = i < noa ? double(hi[3 + k]) + double(lo[3 + k]) : 0.0;
+    for (int k = 0; k < 9; k++) {
+      float t, e;
+      two_sum(th[k], hi[3 + k], t, e);
+      th[k] = t;
+      tl[k] += e + lo[3 + k];
+    }
+  }
+  if (lane == 0) {
+    sm[warp][0] = esum;
+#pragma unroll
+    for (int k = 0; k < 9; k++) sm[warp][1 + k] = double(th[k]) + double(tl[k]);
   }
   __syncthreads();
-  if (threadIdx.x < 10)
-    partial[(size_t)blockIdx.x * 10 + threadIdx.x] =
-        (sm[0][threadIdx.x] + sm[1][threadIdx.x]) + (sm[2][threadIdx.x] + sm[3][threadIdx.x]);
+  if (threadIdx.x < 10) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kGatherWarps; w++) v += sm[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * 10 + threadIdx.x] = v;
+  }
 }
 
 // F_i = sum over pairs of i (f_ij - f_ji); each block also reduces its atoms'
@@ -1175,31 +1200,21 @@ k_gather(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
 }
 
 // Sum of the per-block partial rows: out[0] = E, out[1..9] = sum f (x) r.
-// One block of 1024 threads: strided per-thread sums, then fixed-order warp
-// and block trees (deterministic).
-__global__ void __launch_bounds__(1024)
+// Block k sums column k (ten blocks on ten SMs: FP64 adds are scarce on one
+// SM): strided per-thread sums, then a fixed shared-memory tree.
+__global__ void __launch_bounds__(128)
 k_reduce(int nblocks, const double *__restrict__ partial, double *__restrict__ out) {
-  __shared__ double sm[32][10];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < 10; k++) acc[k] += partial[(size_t)b * 10 + k];
-#pragma unroll
-  for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < 10; k++) sm[warp][k] = acc[k];
+  __shared__ double sm[128];
+  const int k = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partial[(size_t)b * 10 + k];
+  sm[threadIdx.x] = acc;
   __syncthreads();
-  if (warp == 0) {
-    const int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 10; k++) {
-      double v = lane < nw ? sm[lane][k] : 0.0;
-      v = warp_sum(v);
-      if (lane == 0) out[k] = v;
-    }
+  for (int st = 64; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) sm[threadIdx.x] += sm[threadIdx.x + st];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) out[k] = sm[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -1286,17 +1301,18 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
   if (!gather) return 0;
   int nblk;
   if constexpr (sizeof(T) == 4) {
-    nblk = ceil_div(a.noa, 4);
-    k_gather_warp<<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32,
-                                            reinterpret_cast<const float4 *>(pair_f), atom_e,
-                                            forces, atom_vir);
+    // a few resident blocks per SM, each walking many atoms
+    nblk = std::min(ceil_div(a.noa, kGatherWarps), 152 * 8);
+    k_gather_warp<<<nblk, 32 * kGatherWarps, 0, stream>>>(
+        a.noa, nb.offset, nb.rev, nb.rel32, reinterpret_cast<const float4 *>(pair_f), atom_e,
+        forces, atom_vir);
   } else {
     nblk = ceil_div(a.noa, 128);
     k_gather<T><<<nblk, 128, 0, stream>>>(a.noa, nb.offset, nb.rev, nb.rel32, nb.rel, pair_f,
                                           atom_e, forces, atom_vir);
   }
   if (cudaGetLastError() != cudaSuccess) return -1;
-  k_reduce<<<1, 1024, 0, stream>>>(nblk, atom_vir, reduce_out);
+  k_reduce<<<10, 128, 0, stream>>>(nblk, atom_vir, reduce_out);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

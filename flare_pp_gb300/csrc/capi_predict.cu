@@ -145,10 +145,41 @@ static int forward32(fpp_structure *s, const B2Args &a0, const int *pair_tab,
   return FPP_OK;
 }
 
+// energy and the flare-order stress -(1/V) sum f_a r_b from the reduced row
+__global__ void k_finish(const double *__restrict__ red, double vi, double *energy,
+                         double *stress) {
+  if (threadIdx.x != 0) return;
+  if (energy) energy[0] = red[0];
+  if (stress) {
+    stress[0] = -red[1] * vi;
+    stress[1] = -red[2] * vi;
+    stress[2] = -red[3] * vi;
+    stress[3] = -red[5] * vi;
+    stress[4] = -red[6] * vi;
+    stress[5] = -red[9] * vi;
+  }
+}
+
 static int finish_outputs(fpp_structure *s, cudaStream_t st, double *energy,
                           double *forces, double *stress, double *atom_energies,
                           int on_device) {
   StructureState &S = s->st;
+  if (on_device) {
+    // stays asynchronous: the outputs are written in stream order, and a
+    // device-side error of this call is reported by the next synchronizing
+    // call on the structure (the status word is only cleared once read)
+    if (energy || stress) {
+      k_finish<<<1, 32, 0, st>>>(S.reduce_out.as<double>(), 1.0 / S.ci.volume, energy, stress);
+      FPP_CUDA(cudaGetLastError());
+    }
+    if (forces && S.noa)
+      FPP_CUDA(cudaMemcpyAsync(forces, S.forces.ptr, sizeof(double) * 3 * S.noa,
+                               cudaMemcpyDeviceToDevice, st));
+    if (atom_energies && S.noa)
+      FPP_CUDA(cudaMemcpyAsync(atom_energies, S.atom_e.ptr, sizeof(double) * S.noa,
+                               cudaMemcpyDeviceToDevice, st));
+    return FPP_OK;
+  }
   double red[10];
   FPP_CUDA(cudaMemcpyAsync(red, S.reduce_out.ptr, sizeof(red), cudaMemcpyDeviceToHost, st));
   FPP_CUDA(cudaStreamSynchronize(st));
@@ -558,8 +589,10 @@ static int center_from_sparse(fpp_model *m) {
 }
 
 // pbar from a structure: the normalised mean of its atoms' unit descriptors
-// (FP64 forward pass), for species the sparse set does not cover.
-static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st) {
+// (FP64 forward pass), for species the sparse set does not cover, or (with
+// every_species) for every species that has atoms in the structure.
+static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st,
+                                 bool every_species = false) {
   StructureState &S = s->st;
   const int nd = m->n_d, ldp = round_up(nd, 64);
   B2Args a = m->args;
@@ -578,7 +611,8 @@ static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st
       pbar[sp][d] = old[(size_t)sp * nd + d];
       n0 += pbar[sp][d] * pbar[sp][d];
     }
-    if (n0 > 0 || s->n_rows[sp] == 0) continue;  // already centred, or no atoms
+    if (s->n_rows[sp] == 0 || (n0 > 0 && !every_species)) continue;
+    for (int d = 0; d < nd; d++) pbar[sp][d] = 0.0;
     std::vector<double> rows((size_t)s->n_rows[sp] * ldp);
     FPP_CUDA(cudaMemcpy(rows.data(), S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp,
                         sizeof(double) * rows.size(), cudaMemcpyDeviceToHost));
@@ -617,7 +651,6 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
   g.ldp = ldp;
   g.ldv = ldp;
   g.beta1 = m->beta1.as<double>();
-  if (!strict) FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
   S.mark(2, st);
   if (precision == FPP_PREC_FP64) {
     FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
@@ -712,6 +745,15 @@ int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision, double *en
   cudaStream_t st = (cudaStream_t)stream;
   FPP_TRY(mapped_core(m, s, precision, st, 0));
   return finish_outputs(s, st, energy, forces, stress, atom_energies, outputs_on_device);
+}
+
+int fpp_model_center_on(fpp_model *m, fpp_structure *s, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  FPP_TRY(model_check(m, s));
+  if (m->beta_power == 0)
+    return fail(FPP_ERR_INVALID, "mapped coefficients not set (fpp_model_compute_beta)");
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  return center_from_structure(m, s, st, true);
 }
 
 // Full FP64 kernel matrix on the device: K (n_sparse_total x n_out) row-major.

@@ -397,7 +397,7 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
   // the pair (i, j, s) and its reverse (j, i, -s) have exactly negated images
   // (IEEE subtraction and addition round symmetrically), so the FP64
   // geometry is computed for the canonical half only -- keys above
-  // (i, centre shift), a suffix of the sorted list -- and k_mirror copies it
+  // (i, centre shift), a suffix of the sorted list -- and k_reverse copies it
   const long long thr = ((long long)i << kKeyBits) |
                         ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
   int c0 = 0;
@@ -430,22 +430,6 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
   }
 }
 
-// Geometry of the non-canonical pairs: the negated image of the reverse pair.
-__global__ void k_mirror(long long n_pairs, CellDev cd, const long long *__restrict__ keys,
-                         const int *__restrict__ nbr_i, const int *__restrict__ rev,
-                         dvec4 *__restrict__ rel, float4 *__restrict__ rel32) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n_pairs) return;
-  const long long thr = ((long long)nbr_i[p] << kKeyBits) |
-                        ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
-  if (keys[p] > thr) return;
-  const int q = rev[p];
-  if (q < 0) return;  // reported by k_reverse
-  const dvec4 r = rel[q];
-  const float4 r32 = rel32[q];
-  rel[p] = dvec4{r.x, -r.y, -r.z, -r.w};
-  rel32[p] = make_float4(-r32.x, -r32.y, -r32.z, r32.w);
-}
 
 __global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
                         const float4 *__restrict__ wp32,
@@ -527,9 +511,10 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
                           const long long *__restrict__ keys,
                           const int *__restrict__ nbr_i,
                           const int *__restrict__ nbr_j, int *__restrict__ rev,
-                          DeviceStatus *st) {
+                          DeviceStatus *st, int mirror, dvec4 *rel, float4 *rel32) {
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
+  const int center = (cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep;
   int i = nbr_i[p], j = nbr_j[p];
   int sidx = (int)(keys[p] & kKeyMask);
   long long want = ((long long)i << kKeyBits) | (cd.n_shift - 1 - sidx);
@@ -548,6 +533,14 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
   }
   if (found < 0) set_status(st, FPP_ERR_NUMERIC, 6, (int)p);
   rev[p] = found;
+  // pairs below the canonical half take the negated image of their reverse
+  // pair (computed by k_compact_geom; the other builds compute both, equal)
+  if (found >= 0 && mirror && keys[p] <= (((long long)i << kKeyBits) | center)) {
+    const dvec4 r = rel[found];
+    const float4 r32 = rel32[found];
+    rel[p] = dvec4{r.x, -r.y, -r.z, -r.w};
+    rel32[p] = make_float4(-r32.x, -r32.y, -r32.z, r32.w);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -637,6 +630,9 @@ int check_status(StructureState &st, cudaStream_t stream, const char *what) {
                            stream));
   FPP_CUDA(cudaStreamSynchronize(stream));
   if (h.code != 0) {
+    // cleared once reported (an asynchronous call leaves its errors here for
+    // the next synchronizing call)
+    FPP_CUDA(cudaMemsetAsync(st.status.ptr, 0, sizeof(DeviceStatus), stream));
     char buf[256];
     snprintf(buf, sizeof(buf), "%s: device status %d at %d (index %d)", what,
              h.code, h.where, h.info);
@@ -649,8 +645,10 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   const int noa = st.noa;
   CellDev cd = make_dev(st.ci);
   const int nbins = st.ci.nb[0] * st.ci.nb[1] * st.ci.nb[2];
-  FPP_TRY(st.status.reserve(sizeof(DeviceStatus)));
-  FPP_CUDA(cudaMemsetAsync(st.status.ptr, 0, sizeof(DeviceStatus), stream));
+  if (!st.status.ptr) {
+    FPP_TRY(st.status.reserve(sizeof(DeviceStatus)));
+    FPP_CUDA(cudaMemsetAsync(st.status.ptr, 0, sizeof(DeviceStatus), stream));
+  }
   FPP_TRY(st.nbr_count.reserve(sizeof(int) * (noa + 1)));
   FPP_TRY(st.nbr_offset.reserve(sizeof(int) * (noa + 1)));
   if (noa == 0) {
@@ -715,7 +713,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_CUDA(cudaMemcpyAsync(&hinfo[1], st.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost,
                            stream));
   FPP_CUDA(cudaStreamSynchronize(stream));
-  FPP_TRY(check_status(st, stream, "neighbor wrap"));
+  FPP_TRY(check_status(st, stream, "neighbor build or an earlier asynchronous call"));
   const bool overflow = hinfo[1] != 0;
   int total = hinfo[0];
   if (overflow) {
@@ -768,14 +766,9 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   }
   k_reverse<<<ceil_div(total, tb), tb, 0, stream>>>(
       total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
-      st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst);
+      st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst, overflow ? 0 : 1,
+      st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
   FPP_CUDA(cudaGetLastError());
-  if (!overflow) {
-    k_mirror<<<ceil_div(total, tb), tb, 0, stream>>>(
-        total, cd, st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_rev.as<int>(),
-        st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
-    FPP_CUDA(cudaGetLastError());
-  }
   return FPP_OK;
 }
 

@@ -273,11 +273,29 @@ int fpp_self_kernel_struc(const fpp_b2 *descriptor, double sigma, double power,
  * periodic structure), in `precision`.  Outputs are host arrays unless
  * outputs_on_device != 0: energy (1), forces (noa x 3), stress (6, flare
  * order), atom_energies (noa, optional).  Requires fpp_model_compute_beta
- * or fpp_model_set_beta. */
+ * or fpp_model_set_beta.  With device outputs the call returns without
+ * synchronizing the stream (outputs are written in stream order); a
+ * device-side error of such a call is reported by the next call that
+ * synchronizes on the structure (fpp_structure_set_positions included).
+ *
+ * FPP_PREC_MIXED evaluates E_i = c0 + 2 g.delta + delta.(beta delta) on the
+ * offset delta = phat - pbar from a per-species centre pbar (g = beta pbar,
+ * c0 = pbar.g in FP64).  The tensor cores accumulate beta delta in FP32 with
+ * truncation, so the energy error grows with |delta| |beta delta|: it is
+ * smallest when pbar is the mean environment of the structures predicted.
+ * The centre defaults to the mean of the sparse set (or, for species without
+ * sparse environments, of the first structure predicted). */
 int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
                        double *energy, double *forces, double *stress,
                        double *atom_energies, int outputs_on_device,
                        void *stream);
+
+/* Recentre the mixed form on a structure: pbar of every species with atoms in
+ * s becomes the normalised mean of their unit descriptors (FP64 forward pass,
+ * synchronizes the stream).  Deterministic: later predictions depend only on
+ * the model and the structure it was centred on.  No reference counterpart
+ * (pair_flare.cpp evaluates in FP64 throughout). */
+int fpp_model_center_on(fpp_model *m, fpp_structure *s, void *stream);
 
 /* ------------------------------------------------------------------------
  * SparseGP::update_matrices_QR (src/flare_pp/bffs/sparse_gp.cpp:576-610) in
