@@ -338,8 +338,12 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
         for (int ks = 0; ks < BK / 16; ks++) {
           const uint32_t off = ks * 32;
           const uint32_t first = (kb > 0 || ks > 0) ? 1u : 0u;
-          mma_f16<BN>(acc0, smem_desc(a_hi + off), smem_desc(b_hi + off), first);
-          mma_f16<BN>(acc1, smem_desc(a_hi + off), smem_desc(b_hi + B_TILE + off), first);
+          // B_hi and B_lo are one 256-row operand in shared memory and acc0,
+          // acc1 adjacent TMEM columns: [acc0 | acc1] = A_hi [B_hi ; B_lo]^T
+          // in one N = 256 MMA, then acc1 += A_lo B_hi^T.  Shared-memory
+          // reads per K step fall from 24 KB to 20 KB (the operand reads and
+          // the TMA writes share the SM's shared-memory bandwidth).
+          mma_f16<2 * BN>(acc0, smem_desc(a_hi + off), smem_desc(b_hi + off), first);
           mma_f16<BN>(acc1, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
         }
         mma_commit_mc(empty_bar(s), (uint16_t)3);  // frees the stage in both CTAs
