@@ -237,7 +237,8 @@ def run_ours(args):
     # ---- end-to-end through the public API with host buffers ----
     pinned = torch.from_numpy(np.stack(disp[:K])).pin_memory()
     he = np.zeros(1)
-    hf = np.zeros((noa, 3))
+    hf_t = torch.zeros((noa, 3), dtype=torch.float64).pin_memory()  # pinned host forces
+    hf = hf_t.numpy()
     hs = np.zeros(6)
     for k in range(min(2, K)):   # warm
         check(L.fpp_structure_set_positions(sh, pinned[k].data_ptr(), 0, stream))
@@ -319,11 +320,11 @@ def run_ours(args):
 
 
 def launches_per_step(n_species):
-    # neighbors: wrap_bin, bin_scatter, enum, compact_geom, reverse and two
-    # CUB exclusive scans of two kernels each (compiled into the library);
-    # descriptors: forward; contraction: one grouped split GEMM; adjoint: wu,
-    # pair_force, gather, reduce
-    return 9 + 1 + 1 + 4
+    # neighbors: wrap_bin, bin_scatter, enum, nb_readback, compact_geom,
+    # reverse and two CUB exclusive scans of two kernels each (compiled into
+    # the library); descriptors: forward; contraction: one grouped split GEMM;
+    # adjoint: wu, pair_force, gather, reduce; outputs: finish
+    return 10 + 1 + 1 + 4 + 1
 
 
 def cpu_baseline(w, seconds=15.0):

@@ -37,16 +37,22 @@ void fill_fp32_cutoffs(B2Args &a) {
     // fl32(r) < cut_lo  =>  r <= fl32(r) (1 + 2^-24) < rc, and symmetrically
     a.cut_lo[k] = nextafterf((float)(rc * (1.0 - 1e-6)), 0.0f);
     a.cut_hi[k] = nextafterf((float)(rc * (1.0 + 1e-6)), 3.0e38f);
+    const double ci = rc > a.r1 ? 1.0 / (rc - a.r1) : 0.0;
+    a.cinv_hi[k] = (float)ci;
+    a.cinv_lo[k] = (float)(ci - (double)a.cinv_hi[k]);
   }
 }
 
-// Descriptor filter r <= rc of b2.cpp:277 / b3.cpp:258 for a pair, FP32
-// first: only pairs within the band around rc read the FP64 distance.
+// Descriptor filter r <= rc of b2.cpp:277 / b3.cpp:258 for pair p of atom i,
+// FP32 first: only pairs within the band around rc use the FP64 distance,
+// recomputed from the positions (or read from the caller's FP64 table).
 __device__ __forceinline__ bool keep_pair32(const B2Args &a, int k, float rf,
-                                            const dvec4 *__restrict__ rel, long long p) {
+                                            const dvec4 *__restrict__ rel,
+                                            const NbGeom &geom, int i, long long p) {
   if (rf < a.cut_lo[k]) return true;
   if (rf > a.cut_hi[k]) return false;
-  return rel[p].x <= a.cutoffs[k];
+  const double r = geom.wp ? exact_pair_dist(geom, i, p) : rel[p].x;
+  return r <= a.cutoffs[k];
 }
 int b3_n_ls_host(int lmax) { return b3_n_ls(lmax); }
 
@@ -63,8 +69,11 @@ int upload_harmonic_tables(cudaStream_t stream) {
         if (m > 0) v *= sqrt(2.0);
       }
       t.norm[l * (kMaxL + 1) + m] = v;
-      t.norm_hi[l * (kMaxL + 1) + m] = (float)v;
-      t.norm_lo[l * (kMaxL + 1) + m] = (float)(v - (double)(float)v);
+      double dl = 1;  // D_lm of the division-free FP32 recurrence
+      for (int k = m + 2; k <= l; k++) dl *= k - m;
+      const double vf = v / dl;
+      t.norm_hi[l * (kMaxL + 1) + m] = (float)vf;
+      t.norm_lo[l * (kMaxL + 1) + m] = (float)(vf - (double)(float)vf);
     }
   for (int m = 0; m <= kMaxL; m++) {
     double d = 1;
@@ -132,6 +141,7 @@ __device__ __forceinline__ void ff_warp_sum(float &hi, float &lo) {
 // the sizes constant, the radial / harmonic loops unroll and the shared-memory
 // and u indices fold into immediate offsets.
 template <int NT, int LT, int NST> struct Shape {
+  static constexpr int kN = NT > 0 ? NT : 0;
   static constexpr int kNR = (NT > 0 && NST > 0) ? NT * NST : 0;  // radial channels
   static constexpr int kL1 = LT >= 0 ? LT + 1 : 0;
   static __device__ __forceinline__ int N(const B2Args &a) { return NT > 0 ? NT : a.N; }
@@ -196,7 +206,7 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
 template <typename T, typename SH>
 __global__ void __launch_bounds__(128)
 k_b2_forward(B2Args a, const int *__restrict__ offset,
-             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
+             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32, NbGeom geom,
              const int *__restrict__ nbr_s, const int *__restrict__ species,
              const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
              T *__restrict__ c_out, T *__restrict__ p_out,
@@ -264,15 +274,17 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
             const dvec4 rd = rel[p];
             keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
           } else {
-            keep = keep_pair32(a, kc, rf.w, rel, p);
+            keep = keep_pair32(a, kc, rf.w, rel, geom, atom, p);
           }
           r1t = T(a.r1f);
           rct = T(a.cutoffs32[kc]);
         }
         if (keep) {
           sj = sp;
+          // FP32: hi/lo reciprocal of (rc - r1); FP64: the division
           radial_basis<T>(r, r1t, rct, N, a.cutoff_kind, g_s + (size_t)b * GP,
-                          nullptr, 1);
+                          nullptr, 1, sizeof(T) == 4 ? T(a.cinv_hi[kc]) : T(0),
+                          sizeof(T) == 4 ? T(a.cinv_lo[kc]) : T(0));
           real_harmonics<T>(x, y, z, LMAX, y_s + b, nullptr, WS);
         }
       }
@@ -306,13 +318,38 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 #pragma unroll
           for (int n = 0; n < kMaxN; n++) chunk[n] = T(0);
           const int k1 = min(ns_, k0 + 16);
-          for (int k = k0; k < k1; k++) {
-            const int b = ls[k];
-            const T yv = y_s[lmc * WS + b];
-            const T *gb = g_s + (size_t)b * GP;
+          if constexpr (SH::kN > 0 && sizeof(T) == 4) {
+            // radial row of the neighbor in 16-byte loads (GP = N rounded up to 4)
+            constexpr int G4 = (SH::kN + 3) / 4;
+            auto accum = [&](int b) {
+              const T yv = y_s[lmc * WS + b];
+              const float4 *gb4 = reinterpret_cast<const float4 *>(g_s + (size_t)b * (4 * G4));
 #pragma unroll
-            for (int n = 0; n < kMaxN; n++)
-              if (n < N) chunk[n] += gb[n] * yv;
+              for (int j = 0; j < G4; j++) {
+                const float4 gv = gb4[j];
+                if (4 * j + 0 < SH::kN) chunk[4 * j + 0] += gv.x * yv;
+                if (4 * j + 1 < SH::kN) chunk[4 * j + 1] += gv.y * yv;
+                if (4 * j + 2 < SH::kN) chunk[4 * j + 2] += gv.z * yv;
+                if (4 * j + 3 < SH::kN) chunk[4 * j + 3] += gv.w * yv;
+              }
+            };
+            // two neighbors per iteration (same summation order)
+            int k = k0;
+            for (; k + 1 < k1; k += 2) {
+              const int b0 = ls[k], b1 = ls[k + 1];
+              accum(b0);
+              accum(b1);
+            }
+            if (k < k1) accum(ls[k]);
+          } else {
+            for (int k = k0; k < k1; k++) {
+              const int b = ls[k];
+              const T yv = y_s[lmc * WS + b];
+              const T *gb = g_s + (size_t)b * GP;
+#pragma unroll
+              for (int n = 0; n < kMaxN; n++)
+                if (n < N) chunk[n] += gb[n] * yv;
+            }
           }
 #pragma unroll
           for (int n = 0; n < kMaxN; n++)
@@ -363,29 +400,40 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     for (int q = lane; q < npair; q += 32) {
       const int pr = pair_tab[q];
       const int n1 = pr & 0xffff, n2 = pr >> 16;
-      T e[4 * H4];
+      T x[4 * H4], y[4 * H4];
 #pragma unroll
       for (int k = 0; k < H4; k++) {
         if constexpr (sizeof(T) == 4) {
-          const float4 x = reinterpret_cast<const float4 *>(c_s + n1 * HP)[k];
-          const float4 y = reinterpret_cast<const float4 *>(c_s + n2 * HP)[k];
-          e[4 * k + 0] = x.x * y.x;
-          e[4 * k + 1] = x.y * y.y;
-          e[4 * k + 2] = x.z * y.z;
-          e[4 * k + 3] = x.w * y.w;
+          const float4 u = reinterpret_cast<const float4 *>(c_s + n1 * HP)[k];
+          const float4 w = reinterpret_cast<const float4 *>(c_s + n2 * HP)[k];
+          x[4 * k + 0] = u.x;
+          x[4 * k + 1] = u.y;
+          x[4 * k + 2] = u.z;
+          x[4 * k + 3] = u.w;
+          y[4 * k + 0] = w.x;
+          y[4 * k + 1] = w.y;
+          y[4 * k + 2] = w.z;
+          y[4 * k + 3] = w.w;
         } else {
 #pragma unroll
-          for (int j = 0; j < 4; j++) e[4 * k + j] = c_s[n1 * HP + 4 * k + j] * c_s[n2 * HP + 4 * k + j];
+          for (int j = 0; j < 4; j++) {
+            x[4 * k + j] = c_s[n1 * HP + 4 * k + j];
+            y[4 * k + j] = c_s[n2 * HP + 4 * k + j];
+          }
         }
       }
+      // p per l as a chain of multiply-adds; the pair's squared entries are
+      // summed first and enter the compensated norm sum once per pair
+      T sq = T(0);
 #pragma unroll
       for (int l = 0; l < LL; l++) {
-        T v = T(0);
+        T v = x[l * l] * y[l * l];
 #pragma unroll
-        for (int m = l * l; m < (l + 1) * (l + 1); m++) v += e[m];
+        for (int m = l * l + 1; m < (l + 1) * (l + 1); m++) v = fma(x[m], y[m], v);
         p_s[q * LL + l] = v;
-        nacc.add(v * v);
+        sq = fma(v, v, sq);
       }
+      nacc.add(sq);
     }
   } else {
     for (int q = lane; q < npair; q += 32) {
@@ -400,8 +448,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       }
     }
   }
-  double nrm, inv;
-  float invf;
+  double nrm = 0.0, inv = 0.0;
+  float invf, nrm_hi = 0.0f, nrm_lo = 0.0f;
   if (sizeof(T) == 8) {
     const double nsq = warp_sum(double(nacc.s) + double(nacc.c));
     nrm = sqrt(nsq);
@@ -409,17 +457,22 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     invf = float(inv);
   } else {
     // |p|^2 as float-float; sqrt and 1/sqrt by one correction step of the
-    // FP32 values (relative error ~1 ulp of FP32), no FP64 division or sqrt
+    // FP32 values (relative error ~1 ulp of FP32), no FP64 arithmetic
     float hi = float(nacc.s), lo = float(nacc.c);
     ff_warp_sum(hi, lo);
     const float r0 = sqrtf(hi);
     const float rc = r0 > 0.0f ? (fmaf(-r0, r0, hi) + lo) / (2.0f * r0) : 0.0f;
     const float y0 = r0 > 0.0f ? 1.0f / r0 : 0.0f;
     invf = fmaf(-y0 * y0, rc, y0);
-    nrm = double(r0) + double(rc);
-    inv = double(invf);
+    nrm_hi = r0;
+    nrm_lo = rc;
   }
-  if (lane == 0) norm_out[atom] = nrm;
+  if (lane == 0) {
+    if (sizeof(T) == 4)  // FP32 kernels: |p| as a float-float pair in the 8-byte slot
+      reinterpret_cast<float2 *>(norm_out)[atom] = make_float2(nrm_hi, nrm_lo);
+    else
+      norm_out[atom] = nrm;
+  }
   __syncwarp();
   const int row = row_of_atom[atom];
   if (sizeof(T) == 4 && phat_hi && !p_out && !phat64 && (nd & 3) == 0) {
@@ -430,16 +483,16 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     uint2 *L4 = reinterpret_cast<uint2 *>(phat_lo + (size_t)row * ldp);
     for (int q = lane; q < (nd >> 2); q += 32) {
       const float4 v = P4[q], b = B4[q];
-      const float x[4] = {(v.x * invf - b.x) * 8192.0f, (v.y * invf - b.y) * 8192.0f,
-                          (v.z * invf - b.z) * 8192.0f, (v.w * invf - b.w) * 8192.0f};
-      __half h[4], r[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        h[j] = __float2half_rn(x[j]);
-        r[j] = __float2half_rn((x[j] - __half2float(h[j])) * 2048.0f);
-      }
-      const __half2 h01 = __halves2half2(h[0], h[1]), h23 = __halves2half2(h[2], h[3]);
-      const __half2 r01 = __halves2half2(r[0], r[1]), r23 = __halves2half2(r[2], r[3]);
+      const float2 x01 = make_float2((v.x * invf - b.x) * 8192.0f, (v.y * invf - b.y) * 8192.0f);
+      const float2 x23 = make_float2((v.z * invf - b.z) * 8192.0f, (v.w * invf - b.w) * 8192.0f);
+      // paired conversions (round to nearest); the residual of each entry
+      // scaled by 2^11 is the lo plane
+      const __half2 h01 = __float22half2_rn(x01), h23 = __float22half2_rn(x23);
+      const float2 g01 = __half22float2(h01), g23 = __half22float2(h23);
+      const __half2 r01 = __float22half2_rn(
+          make_float2((x01.x - g01.x) * 2048.0f, (x01.y - g01.y) * 2048.0f));
+      const __half2 r23 = __float22half2_rn(
+          make_float2((x23.x - g23.x) * 2048.0f, (x23.y - g23.y) * 2048.0f));
       H4[q] = make_uint2(*reinterpret_cast<const unsigned *>(&h01),
                          *reinterpret_cast<const unsigned *>(&h23));
       L4[q] = make_uint2(*reinterpret_cast<const unsigned *>(&r01),
@@ -450,7 +503,7 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   for (int d = lane; d < nd; d += 32) {
     const T v = p_s[d];
     if (p_out) p_out[(size_t)atom * nd + d] = v;
-    if (phat64) phat64[(size_t)row * ldp + d] = double(v) * inv;
+    if (phat64) phat64[(size_t)row * ldp + d] = double(v) * (sizeof(T) == 8 ? inv : double(invf));
     if (phat_hi) {
       // centred operand: delta = phat - pbar, scaled by 2^13 (|delta| <= 2)
       const float x = (float(v) * invf - pbar[(size_t)si * nd + d]) * 8192.0f;
@@ -467,7 +520,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 // given per operand row (kernel form).
 template <typename T, typename Store>
 __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, int si,
-                                            int row, double nrm, Store store, int lane) {
+                                            int row, double nrm, float2 nrm32, Store store,
+                                            int lane) {
   const int nd = a.n_d;
   double e = 0.0;
   if ((g.mode == kWFromV2 || g.mode == kWFromV1) && g.phat64) {
@@ -491,16 +545,15 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     }
   } else if (g.mode == kWFromV2 && (nd & 3) == 0) {
     // the mixed power-2 form below, four consecutive entries per lane and
-    // 16-byte (8-byte for the fp16 planes) loads
-    const bool empty = nrm * nrm < g.empty_thresh;
+    // 16-byte (8-byte for the fp16 planes) loads; |p| and E as float-float
+    const bool empty = nrm32.x * nrm32.x < float(g.empty_thresh);
     const int nq = nd >> 2;
     const float4 *V4 = reinterpret_cast<const float4 *>(g.V32 + (size_t)row * g.ldv);
     const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
     const float4 *B4 = reinterpret_cast<const float4 *>(g.pbar + (size_t)si * nd);
     const uint2 *H4 = reinterpret_cast<const uint2 *>(g.phat_hi + (size_t)row * g.ldp);
     const uint2 *L4 = reinterpret_cast<const uint2 *>(g.phat_lo + (size_t)row * g.ldp);
-    auto deltas = [&](int q, float (&dl)[4]) {
-      const uint2 h = H4[q], l = L4[q];
+    auto deltas = [&](uint2 h, uint2 l, float (&dl)[4]) {
       const float2 h01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
       const float2 h23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
       const float2 l01 = __half22float2(*reinterpret_cast<const __half2 *>(&l.x));
@@ -510,37 +563,74 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
       dl[2] = (h23.x + l23.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
       dl[3] = (h23.y + l23.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
     };
+    // loads of kU iterations are issued before any of them is used (one atom's
+    // rows are a few KB: the loop is latency-bound without this)
+    constexpr int kU = 4;
     Acc<float> acc;
-    for (int q = lane; q < nq; q += 32) {
-      float dl[4];
-      deltas(q, dl);
-      const float4 v = V4[q], gg = G4[q];
-      acc.add((2.0f * gg.x + v.x) * dl[0]);
-      acc.add((2.0f * gg.y + v.y) * dl[1]);
-      acc.add((2.0f * gg.z + v.z) * dl[2]);
-      acc.add((2.0f * gg.w + v.w) * dl[3]);
+    for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
+      uint2 h[kU], l[kU];
+      float4 v[kU], gg[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int q = q0 + 32 * u;
+        if (q < nq) {
+          h[u] = H4[q];
+          l[u] = L4[q];
+          v[u] = V4[q];
+          gg[u] = G4[q];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        if (q0 + 32 * u < nq) {
+          float dl[4];
+          deltas(h[u], l[u], dl);
+          acc.add((2.0f * gg[u].x + v[u].x) * dl[0]);
+          acc.add((2.0f * gg[u].y + v[u].y) * dl[1]);
+          acc.add((2.0f * gg[u].z + v[u].z) * dl[2]);
+          acc.add((2.0f * gg[u].w + v[u].w) * dl[3]);
+        }
+      }
     }
     float hi = acc.s, lo = acc.c;
     ff_warp_sum(hi, lo);
-    const double dot = (double(hi) + double(lo)) + g.c0[si];
-    e = empty ? 0.0 : dot;
-    const float ef = float(e);
-    const float inv = empty ? 0.0f : 1.0f / float(nrm);
-    for (int q = lane; q < nq; q += 32) {
-      float dl[4];
-      deltas(q, dl);
-      const float4 v = V4[q], gg = G4[q], pb = B4[q];
-      store(4 * q + 0, T(2.0f * ((gg.x + v.x) - ef * (pb.x + dl[0])) * inv));
-      store(4 * q + 1, T(2.0f * ((gg.y + v.y) - ef * (pb.y + dl[1])) * inv));
-      store(4 * q + 2, T(2.0f * ((gg.z + v.z) - ef * (pb.z + dl[2])) * inv));
-      store(4 * q + 3, T(2.0f * ((gg.w + v.w) - ef * (pb.w + dl[3])) * inv));
+    const ff et = ff_add(ff_norm(hi, lo), ff{g.c0_hi[si], g.c0_lo[si]});
+    const float ef = empty ? 0.0f : et.hi + et.lo;
+    const float inv = empty ? 0.0f : 1.0f / nrm32.x;
+    e = empty ? 0.0 : double(et.hi) + double(et.lo);
+    for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
+      uint2 h[kU], l[kU];
+      float4 v[kU], gg[kU], pb[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int q = q0 + 32 * u;
+        if (q < nq) {
+          h[u] = H4[q];
+          l[u] = L4[q];
+          v[u] = V4[q];
+          gg[u] = G4[q];
+          pb[u] = B4[q];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int q = q0 + 32 * u;
+        if (q < nq) {
+          float dl[4];
+          deltas(h[u], l[u], dl);
+          store(4 * q + 0, T(2.0f * ((gg[u].x + v[u].x) - ef * (pb[u].x + dl[0])) * inv));
+          store(4 * q + 1, T(2.0f * ((gg[u].y + v[u].y) - ef * (pb[u].y + dl[1])) * inv));
+          store(4 * q + 2, T(2.0f * ((gg[u].z + v[u].z) - ef * (pb[u].z + dl[2])) * inv));
+          store(4 * q + 3, T(2.0f * ((gg[u].w + v[u].w) - ef * (pb[u].w + dl[3])) * inv));
+        }
+      }
     }
   } else if (g.mode == kWFromV2 || g.mode == kWFromV1) {
     // mixed form on the centred operand delta = phat - pbar (float):
     //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
     //            g = beta pbar, c0 = pbar^T beta pbar;  dE/dp = 2 (g + V - E phat)/|p|
     //   power 1: E = phat . beta1,                      dE/dp = (beta1 - E phat)/|p|
-    const bool empty = nrm * nrm < g.empty_thresh;
+    const bool empty = nrm32.x * nrm32.x < float(g.empty_thresh);
     Acc<float> acc;
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
@@ -553,10 +643,11 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     }
     float hi = acc.s, lo = acc.c;
     ff_warp_sum(hi, lo);
-    const double dot = (double(hi) + double(lo)) + (g.mode == kWFromV2 ? g.c0[si] : 0.0);
-    e = empty ? 0.0 : dot;
-    const float ef = float(e);
-    const float inv = empty ? 0.0f : 1.0f / float(nrm);
+    const ff et = g.mode == kWFromV2 ? ff_add(ff_norm(hi, lo), ff{g.c0_hi[si], g.c0_lo[si]})
+                                     : ff_norm(hi, lo);
+    const float ef = empty ? 0.0f : et.hi + et.lo;
+    const float inv = empty ? 0.0f : 1.0f / nrm32.x;
+    e = empty ? 0.0 : double(et.hi) + double(et.lo);
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
       const float dl = (__half2float(g.phat_hi[o]) + __half2float(g.phat_lo[o]) * (1.0f / 2048.0f)) *
@@ -600,10 +691,15 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
-  const double nrm = norm_in[atom];
+  // FP32 kernels: the forward stored |p| as a float-float pair
+  const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
+  const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
+                                      : make_float2(0.0f, 0.0f);
+#pragma unroll 4
   for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
 
-  const double e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
+  const double e =
+      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
@@ -696,10 +792,14 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
-  const double nrm = norm_in[atom];
+  // FP32 kernels: the forward stored |p| as a float-float pair
+  const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
+  const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
+                                      : make_float2(0.0f, 0.0f);
   // real c staged through ur (free until the reduction below)
   for (int k = lane; k < sb; k += 32) ur[k] = c_in[(size_t)atom * sb + k];
-  const double e = adjoint_w<T>(a, g, si, row, nrm, [&](int d, T v) { w_s[d] = v; }, lane);
+  const double e =
+      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   b3_to_complex<T>(ur, nr, H, zr, zi, lane);
@@ -853,7 +953,7 @@ k_b3_dp(B2Args a, int npl, const int *__restrict__ plist, const int *__restrict_
 template <typename T, typename SH>
 __global__ void __launch_bounds__(128)
 k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nbr_i,
-             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
+             const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32, NbGeom geom,
              const int *__restrict__ nbr_s, const int *__restrict__ species,
              const T *__restrict__ u, T *__restrict__ pair_f) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -884,7 +984,7 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
       const dvec4 rd = rel[p];
       keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
     } else {
-      keep = keep_pair32(a, kc, rf.w, rel, p);
+      keep = keep_pair32(a, kc, rf.w, rel, geom, i, p);
     }
     r1t = T(a.r1f);
     rct = T(a.cutoffs32[kc]);
@@ -892,7 +992,9 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
   T f[3] = {T(0), T(0), T(0)};
   if (keep) {
     T gr[kMaxN], dg[kMaxN];
-    radial_basis_reg<T>(r, r1t, rct, N, a.cutoff_kind, gr, dg);
+    radial_basis_reg<T>(r, r1t, rct, N, a.cutoff_kind, gr, dg,
+                        sizeof(T) == 4 ? T(a.cinv_hi[kc]) : T(0),
+                        sizeof(T) == 4 ? T(a.cinv_lo[kc]) : T(0));
     const T *ur = u + (size_t)i * sb + (size_t)sj * N * H;
     T fr = T(0);
     harmonics_visit<T>(x, y, z, LMAX, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
@@ -1071,11 +1173,14 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
     }
 #pragma unroll
     for (int k = 0; k < 12; k++) ff_warp_sum(hi[k], lo[k]);
-    if (lane == 0) {
-#pragma unroll
-      for (int a = 0; a < 3; a++) forces[3 * i + a] = double(hi[a]) + double(lo[a]);
-      esum += atom_e[i];
+    // lanes 0..2 convert one force component each (FP64 instructions are
+    // scarce: one conversion pass per atom instead of three)
+    {
+      const float fh = lane == 0 ? hi[0] : (lane == 1 ? hi[1] : hi[2]);
+      const float fl = lane == 0 ? lo[0] : (lane == 1 ? lo[1] : lo[2]);
+      if (lane < 3) forces[3 * i + lane] = double(fh) + double(fl);
     }
+    if (lane == 0) esum += atom_e[i];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       float t, e;
@@ -1248,7 +1353,7 @@ int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
                              (int)smem) != cudaSuccess)
       return -1;
     kern<<<ceil_div(a.noa, wpb), 32 * wpb, smem, stream>>>(
-        a, nb.offset, nb.rel, nb.rel32, nb.nbr_s, species, row_of_atom, pair_tab,
+        a, nb.offset, nb.rel, nb.rel32, nb.geom, nb.nbr_s, species, row_of_atom, pair_tab,
         c_out, p_out, norm_out, phat64, phat_hi, phat_lo, ldp, pbar);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
   });
@@ -1293,7 +1398,8 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
   if (n_pairs > 0) {
     with_shape<T>(a, [&](auto sh) {
       k_pair_force<T, decltype(sh)><<<(unsigned)((n_pairs + 127) / 128), 128, 0, stream>>>(
-          a, g.strict, n_pairs, nbr_i, nb.rel, nb.rel32, nb.nbr_s, species, u_buf, pair_f);
+          a, g.strict, n_pairs, nbr_i, nb.rel, nb.rel32, nb.geom, nb.nbr_s, species, u_buf,
+          pair_f);
       return 0;
     });
     if (cudaGetLastError() != cudaSuccess) return -1;

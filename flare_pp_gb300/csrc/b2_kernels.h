@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "geom.cuh"
 
 #include <cstddef>
 
@@ -31,6 +32,9 @@ struct B2Args {
   float r1f;
   float cutoffs32[kMaxSpecies * kMaxSpecies];
   float cut_lo[kMaxSpecies * kMaxSpecies], cut_hi[kMaxSpecies * kMaxSpecies];
+  // 1 / (rc - r1) per species pair as an FP32 hi/lo split (the Chebyshev
+  // argument without a per-pair division or a rounded reciprocal)
+  float cinv_hi[kMaxSpecies * kMaxSpecies], cinv_lo[kMaxSpecies * kMaxSpecies];
   size_t smem_per_warp;      // filled by the launcher
   size_t smem_per_warp_adj;  // filled by the launcher
 };
@@ -57,6 +61,7 @@ struct AdjArgs {
   const float *pbar;                // [n_species][n_d] centre of the mixed operand
   const float *gvec;                // [n_species][n_d] beta pbar
   double c0[kMaxSpecies];           // pbar^T beta pbar
+  float c0_hi[kMaxSpecies], c0_lo[kMaxSpecies];  // the same as float-float
   // mapped power 1: beta vector per species [n_species][n_d]
   const double *beta1;
   // given dE/dp and energies per operand row (row stride ldp)
@@ -66,10 +71,11 @@ struct AdjArgs {
 
 struct Neigh {
   const int *offset;
-  const dvec4 *rel;
+  const dvec4 *rel;     // FP64 pairs (valid unless geom.wp is set)
   const float4 *rel32;
   const int *nbr_s;
   const int *rev;
+  NbGeom geom;          // exact distances on demand (geom.wp == nullptr: use rel)
 };
 
 int upload_harmonic_tables(cudaStream_t stream);

@@ -21,9 +21,11 @@
 
 namespace fpp {
 
-// Normalisation N_lm * (sqrt 2 if m > 0) at [l*(kMaxL+1) + m] (with an FP32
-// hi/lo split, so FP32 evaluation carries no systematic rounding of the
-// constants), and the double factorials (2m-1)!! at [m].
+// Normalisation N_lm * (sqrt 2 if m > 0) at [l*(kMaxL+1) + m]; its FP32
+// hi/lo split (so FP32 evaluation carries no systematic rounding of the
+// constants) is further divided by D_lm = prod_{k=m+2..l} (k - m), the factor
+// the division-free FP32 recurrence leaves in Q_l^m.  Double factorials
+// (2m-1)!! at [m].
 struct HarmonicTables {
   double norm[(kMaxL + 1) * (kMaxL + 1)];
   float norm_hi[(kMaxL + 1) * (kMaxL + 1)];
@@ -33,16 +35,19 @@ struct HarmonicTables {
 };
 static __constant__ HarmonicTables c_harm;  // uploaded by upload_harmonic_tables()
 
-// N_lm * v, with the constant kept to ~48 bits in FP32
+// N_lm * v (FP32: N_lm / D_lm * v), with the constant kept to ~48 bits in FP32
 __device__ __forceinline__ double norm_scale(int k, double v) { return c_harm.norm[k] * v; }
 __device__ __forceinline__ float norm_scale(int k, float v) {
   return fmaf(c_harm.norm_hi[k], v, c_harm.norm_lo[k] * v);
 }
 
 // g_n and dg_n/dr into out_g[n * stride], out_dg[n * stride].
+// FP32: the argument is (r - r1) (cinv_hi + cinv_lo) with the reciprocal
+// 1 / (rc - r1) split hi/lo in FP64 (when cinv_hi is given, else divided).
 template <typename T>
 __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_kind,
-                                             T *out_g, T *out_dg, int stride) {
+                                             T *out_g, T *out_dg, int stride,
+                                             T cinv_hi = T(0), T cinv_lo = T(0)) {
   T fc, dfc;
   if (r > rc) {
     fc = T(0);
@@ -57,10 +62,17 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
     dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
   }
   const bool inside = !(r < r1 || r > rc);
-  // x by a correctly rounded division: a rounded reciprocal would shift every
-  // pair's argument the same way and bias the descriptors in FP32
-  const T c = T(1) / (rc - r1);
-  const T x = (r - r1) / (rc - r1);
+  // x by a correctly rounded division or the hi/lo reciprocal: a rounded
+  // reciprocal alone would shift every pair's argument the same way and bias
+  // the descriptors in FP32
+  T c, x;
+  if (cinv_hi != T(0)) {
+    c = cinv_hi;
+    x = fma(r - r1, cinv_hi, (r - r1) * cinv_lo);
+  } else {
+    c = T(1) / (rc - r1);
+    x = (r - r1) / (rc - r1);
+  }
   T tm2 = 0, tm1 = 0, dm2 = 0, dm1 = 0;
   for (int n = 0; n < N; n++) {
     T t, dt;
@@ -87,7 +99,8 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
 // Register version: g[n], dg[n] for n < N in fully unrolled arrays.
 template <typename T>
 __device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cutoff_kind,
-                                                 T (&g)[kMaxN], T (&dg)[kMaxN]) {
+                                                 T (&g)[kMaxN], T (&dg)[kMaxN],
+                                                 T cinv_hi = T(0), T cinv_lo = T(0)) {
   T fc, dfc;
   if (r > rc) {
     fc = T(0);
@@ -102,8 +115,14 @@ __device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cut
     dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
   }
   const bool inside = !(r < r1 || r > rc);
-  const T c = T(1) / (rc - r1);
-  const T x = (r - r1) / (rc - r1);
+  T c, x;
+  if (cinv_hi != T(0)) {
+    c = cinv_hi;
+    x = fma(r - r1, cinv_hi, (r - r1) * cinv_lo);
+  } else {
+    c = T(1) / (rc - r1);
+    x = (r - r1) / (rc - r1);
+  }
   T tm2 = 0, tm1 = 0, dm2 = 0, dm1 = 0;
 #pragma unroll
   for (int n = 0; n < kMaxN; n++) {
@@ -160,6 +179,15 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
         q = T(2 * m + 1) * uz * q1;
         qz = T(2 * m + 1) * q1;
         qr = T(0);
+      } else if constexpr (sizeof(T) == 4) {
+        // division-free: q carries the factor D_l = prod_{k=m+2..l} (k - m),
+        // which the FP32 normalisation table divides out (no per-pair
+        // divisions, and no rounded reciprocal of l - m)
+        const T a = T(2 * l - 1);
+        const T bc = T((l + m - 1) * (l - 1 >= m + 2 ? l - 1 - m : 1));
+        q = a * uz * q1 - bc * q2;
+        qz = a * (q1 + uz * qz1) - bc * qz2;
+        qr = a * uz * qr1 - bc * (q2 + qr2);
       } else {
         const T a = T(2 * l - 1), b = T(l + m - 1), dv = T(l - m);
         q = (a * uz * q1 - b * q2) / dv;
@@ -231,6 +259,15 @@ __device__ __forceinline__ void harmonics_visit(T x, T y, T z, int lmax, Visit v
         q = T(2 * m + 1) * uz * q1;
         qz = T(2 * m + 1) * q1;
         qr = T(0);
+      } else if constexpr (sizeof(T) == 4) {
+        // division-free: q carries the factor D_l = prod_{k=m+2..l} (k - m),
+        // which the FP32 normalisation table divides out (no per-pair
+        // divisions, and no rounded reciprocal of l - m)
+        const T a = T(2 * l - 1);
+        const T bc = T((l + m - 1) * (l - 1 >= m + 2 ? l - 1 - m : 1));
+        q = a * uz * q1 - bc * q2;
+        qz = a * (q1 + uz * qz1) - bc * qz2;
+        qr = a * uz * qr1 - bc * (q2 + qr2);
       } else {
         const T a = T(2 * l - 1), b = T(l + m - 1), dv = T(l - m);
         q = (a * uz * q1 - b * q2) / dv;

@@ -207,6 +207,7 @@ int fpp_structure_get_neighbors(const fpp_structure *s, int32_t *neighbor_count,
   const StructureState &st = s->st;
   const int noa = st.noa;
   const int64_t np = st.n_pairs;
+  FPP_TRY(ensure_rel64(const_cast<StructureState &>(st), nullptr));
   FPP_CUDA(cudaDeviceSynchronize());
   std::vector<int> off(noa + 1, 0);
   if (noa > 0)

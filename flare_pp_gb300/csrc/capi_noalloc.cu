@@ -11,6 +11,8 @@
 // loads this library holds until the process exits.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include <cstdint>
 #include <string>
 
@@ -115,6 +117,7 @@ extern "C" int fpp_b2_descriptors_noalloc(const fpp_b2 *b2, int32_t n_atoms,
   a.noa = n_atoms;
   a.strict = 0;
   Neigh nb;
+  std::memset(&nb, 0, sizeof(nb));  // geom.wp == nullptr: rel is the FP64 table
   nb.offset = offsets;
   nb.rel = reinterpret_cast<const dvec4 *>(rel);
   nb.rel32 = nullptr;  // read only by the FP32 instantiation

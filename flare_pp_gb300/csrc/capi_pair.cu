@@ -206,6 +206,7 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                                            S.status.as<DeviceStatus>());
     FPP_CUDA(cudaGetLastError());
   }
+  S.rel64_valid = true;  // the FP64 pair table comes from LAMMPS's arrays
   // same kernels as fpp_predict_mapped, with the pair style's strict filter
   FPP_TRY(mapped_core(m, s, precision, st, /*strict=*/1));
   if (np) {

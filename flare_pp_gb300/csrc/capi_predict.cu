@@ -55,10 +55,12 @@ int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st) {
 
 int ensure_layout(fpp_structure *s, int ns, cudaStream_t st) {
   StructureState &S = s->st;
+  // species are fixed once the structure exists (the pair path resets
+  // layout_species when it replaces them), so the check below runs once
+  if (s->layout_species == ns && s->row_of_atom.ptr) return FPP_OK;
   for (int i = 0; i < S.noa; i++)
     if (S.species_host[i] >= ns)
       return fail(FPP_ERR_INVALID, "structure species exceeds the descriptor's n_species");
-  if (s->layout_species == ns && s->row_of_atom.ptr) return FPP_OK;
   s->n_rows.assign(ns, 0);
   s->row_off.assign(ns, 0);
   for (int i = 0; i < S.noa; i++) s->n_rows[S.species_host[i]]++;
@@ -96,6 +98,12 @@ static Neigh neigh_of(StructureState &S) {
   nb.rel32 = S.nbr_rel32.as<float4>();
   nb.nbr_s = S.nbr_s.as<int>();
   nb.rev = S.nbr_rev.as<int>();
+  // without the FP64 table, exact distances near a cutoff are recomputed
+  // from the positions (the FP32 kernels need them for a few pairs only)
+  if (S.rel64_valid)
+    std::memset(&nb.geom, 0, sizeof(nb.geom));
+  else
+    nb.geom = nb_geom(S);
   return nb;
 }
 
@@ -108,6 +116,7 @@ int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want
   const int ldp = round_up(a.n_d, 64);
   const int sb = a.n_species * a.N * a.H;
   FPP_TRY(ensure_layout(s, a.n_species, st));
+  FPP_TRY(ensure_rel64(S, st));
   FPP_TRY(S.c64.reserve(sizeof(double) * std::max(1, S.noa) * sb));
   FPP_TRY(S.norm64.reserve(sizeof(double) * std::max(1, S.noa)));
   FPP_TRY(reserve_zero(S.p64, want_p ? sizeof(double) * std::max(1, S.noa) * a.n_d : 8, st));
@@ -123,7 +132,8 @@ int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want
   return FPP_OK;
 }
 
-// Mixed forward: c32, pn64 (atom order), split fp16 phat rows.
+// Mixed forward: c32, norms (atom order; FP32 hi/lo pairs in pn64's 8-byte
+// slots), split fp16 phat rows.
 static int forward32(fpp_structure *s, const B2Args &a0, const int *pair_tab,
                      const float *pbar, cudaStream_t st) {
   StructureState &S = s->st;
@@ -180,23 +190,28 @@ static int finish_outputs(fpp_structure *s, cudaStream_t st, double *energy,
                                cudaMemcpyDeviceToDevice, st));
     return FPP_OK;
   }
-  double red[10];
-  FPP_CUDA(cudaMemcpyAsync(red, S.reduce_out.ptr, sizeof(red), cudaMemcpyDeviceToHost, st));
+  // every device-to-host copy of the call, then one synchronization
+  FPP_TRY(ensure_readback(S));
+  FPP_CUDA(cudaMemcpyAsync(S.rb->red, S.reduce_out.ptr, sizeof(double) * 10,
+                           cudaMemcpyDeviceToHost, st));
+  FPP_CUDA(cudaMemcpyAsync(S.rb->status, S.status.ptr, sizeof(DeviceStatus),
+                           cudaMemcpyDeviceToHost, st));
+  if (forces && S.noa)
+    FPP_CUDA(cudaMemcpyAsync(forces, S.forces.ptr, sizeof(double) * 3 * S.noa,
+                             cudaMemcpyDeviceToHost, st));
+  if (atom_energies && S.noa)
+    FPP_CUDA(cudaMemcpyAsync(atom_energies, S.atom_e.ptr, sizeof(double) * S.noa,
+                             cudaMemcpyDeviceToHost, st));
   FPP_CUDA(cudaStreamSynchronize(st));
-  FPP_TRY(check_status(S, st, "prediction"));
+  FPP_TRY(status_from_readback(S, st, "prediction"));
+  const double *red = S.rb->red;
   const double vi = 1.0 / S.ci.volume;
   // -(1/V) sum f_a r_b, order xx xy xz yy yz zz
   double sv[6] = {-red[1] * vi, -red[2] * vi, -red[3] * vi,
                   -red[5] * vi, -red[6] * vi, -red[9] * vi};
-  cudaMemcpyKind k = on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
-  cudaMemcpyKind kd = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  if (energy) FPP_CUDA(cudaMemcpyAsync(energy, &red[0], sizeof(double), k, st));
-  if (stress) FPP_CUDA(cudaMemcpyAsync(stress, sv, sizeof(sv), k, st));
-  if (forces && S.noa)
-    FPP_CUDA(cudaMemcpyAsync(forces, S.forces.ptr, sizeof(double) * 3 * S.noa, kd, st));
-  if (atom_energies && S.noa)
-    FPP_CUDA(cudaMemcpyAsync(atom_energies, S.atom_e.ptr, sizeof(double) * S.noa, kd, st));
-  FPP_CUDA(cudaStreamSynchronize(st));
+  if (energy) energy[0] = red[0];
+  if (stress)
+    for (int k = 0; k < 6; k++) stress[k] = sv[k];
   return FPP_OK;
 }
 
@@ -226,10 +241,10 @@ extern "C" {
 
 int fpp_b2_pair_count(const fpp_b2 *b2, fpp_structure *s, int64_t *n_desc_pairs,
                       void *stream) {
-  (void)stream;
   if (!b2 || !s || !n_desc_pairs) return fail(FPP_ERR_INVALID, "null argument");
   StructureState &S = s->st;
   const int ns = b2->args.n_species;
+  FPP_TRY(ensure_rel64(S, (cudaStream_t)stream));
   for (int i = 0; i < S.noa; i++)
     if (S.species_host[i] >= ns)
       return fail(FPP_ERR_INVALID, "structure species exceeds the descriptor's n_species");
@@ -719,7 +734,11 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
     g.phat_lo = S.phat_lo.as<__half>();
     g.pbar = m->pbar32.as<float>();
     g.gvec = m->g32.as<float>();
-    for (int k = 0; k < m->n_species; k++) g.c0[k] = m->c0[k];
+    for (int k = 0; k < m->n_species; k++) {
+      g.c0[k] = m->c0[k];
+      g.c0_hi[k] = (float)m->c0[k];
+      g.c0_lo[k] = (float)(m->c0[k] - (double)g.c0_hi[k]);
+    }
     FPP_TRY(adjoint_buffers(S, sizeof(float), u_row_stride(a)));
     if (launch_b2_adjoint<float>(a, g, neigh_of(S), S.species.as<int>(),
                                  s->row_of_atom.as<int>(), m->pair_tab.as<int>(),

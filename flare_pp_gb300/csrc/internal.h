@@ -56,8 +56,21 @@ struct CellInfo {
 
 int make_cell_info(const double *cell, double cutoff, CellInfo *ci);
 
+// Small host-visible block (pinned, mapped) that kernels and copies fill
+// with the values the host must read after a step: one synchronization
+// instead of one per value.
+struct HostReadback {
+  int total_pairs;
+  int overflow;
+  int pad[2];
+  int status[4];   // DeviceStatus
+  double red[16];  // reduction outputs (energy, virial sums)
+};
+
 struct StructureState {
   int noa = 0;
+  HostReadback *rb = nullptr;      // host pointer (nullptr until first use)
+  HostReadback *rb_dev = nullptr;  // the same block as a device pointer
   int n_species_max = 0;
   CellInfo ci{};
   std::vector<int32_t> species_host;
@@ -65,7 +78,8 @@ struct StructureState {
   DevBuf positions;      // double[noa*3]
   DevBuf species;        // int32[noa]
   DevBuf wrapped;        // dvec4[noa] (x, y, z, unused)
-  DevBuf wrapped32;      // float4[noa]
+  DevBuf wrapped32;      // float4[noa] (leading float of each coordinate)
+  DevBuf wrapped_lo;     // float4[noa] (wrapped - wrapped32, the float-float tail)
   DevBuf frac;           // dvec4[noa] wrapped fractional coordinates
   DevBuf atom_bin;       // int32[noa]
   DevBuf bin_count;      // int32[n_bins]
@@ -84,7 +98,8 @@ struct StructureState {
   DevBuf nbr_i;          // int32[n_pairs]  central atom
   DevBuf nbr_j;          // int32[n_pairs]  neighbor atom (structure index)
   DevBuf nbr_s;          // int32[n_pairs]  neighbor species
-  DevBuf nbr_rel;        // dvec4[n_pairs] (r, x, y, z)
+  DevBuf nbr_rel;        // dvec4[n_pairs] (r, x, y, z); valid when rel64_valid
+  bool rel64_valid = false;  // filled on demand by ensure_rel64
   DevBuf nbr_rel32;      // float4[n_pairs]  (x, y, z, r)
   DevBuf nbr_rev;        // int32[n_pairs]  index of the reverse pair
   DevBuf scan_tmp;       // CUB scratch
@@ -114,10 +129,20 @@ struct StructureState {
   ~StructureState() {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
+    if (rb) cudaFreeHost(rb);
   }
 };
 
 int build_neighbors(StructureState &st, cudaStream_t stream);
+// the FP64 pair table for the callers that return or consume FP64 geometry
+int ensure_rel64(StructureState &st, cudaStream_t stream);
+// exact-distance geometry of the structure's neighbor list (geom.cuh)
+struct NbGeom;
+NbGeom nb_geom(const StructureState &st);
 int check_status(StructureState &st, cudaStream_t stream, const char *what);
+// allocate the readback block on first use
+int ensure_readback(StructureState &st);
+// report (and clear) a device status already copied into st.rb->status
+int status_from_readback(StructureState &st, cudaStream_t stream, const char *what);
 
 }  // namespace fpp

@@ -16,25 +16,29 @@
 //   6. reverse     index of the (j, i, -s) pair for the deterministic force
 //                  gather
 // All FP64 arithmetic that decides membership or is returned uses explicitly
-// rounded operations, so results equal the oracle bit for bit.
+// rounded operations, so results equal the oracle bit for bit.  The fast
+// build (one-pass enumeration into per-atom slabs) decides candidates near
+// the cutoff in float-float and computes the FP32 pair vectors the same way;
+// the FP64 pair table is filled on demand (ensure_rel64) for the callers
+// that return or consume FP64 geometry.
 #include <cub/cub.cuh>
+#include <cstring>
 
 #include <cmath>
 #include <cstdio>
 
 #include "common.cuh"
+#include "geom.cuh"
 #include "internal.h"
 
 namespace fpp {
 
-// Neighbor keys (j << kKeyBits) | shift index: ordered by j, then shift, as
-// the reference lists them; decoded with shifts (n_shift <= 2^kKeyBits).
-constexpr int kKeyBits = 20;
-constexpr long long kKeyMask = (1LL << kKeyBits) - 1;
-
 struct CellDev {
   double cell[9], ct[9], ct_inv[9], cdot[9], cdot_inv[9];
   float cell32[9];
+  CellFF cff;               // lattice vectors as float-float
+  float cut2_hi, cut2_lo;   // cutoff^2 as float-float
+  float ff_eps;             // |r^2_ff - cutoff^2| above this decides without FP64
   double cutoff;
   float in2, out2, zero2;  // FP32 squared-distance bands: surely inside below
                            // in2, surely outside above out2, and distances
@@ -54,8 +58,15 @@ static CellDev make_dev(const CellInfo &ci) {
     d.cdot[k] = ci.cdot[k];
     d.cdot_inv[k] = ci.cdot_inv[k];
     d.cell32[k] = (float)ci.cell[k];
+    d.cff.hi[k] = (float)ci.cell[k];
+    d.cff.lo[k] = (float)(ci.cell[k] - (double)d.cff.hi[k]);
   }
   d.cutoff = ci.cutoff;
+  {
+    const double c2 = ci.cutoff * ci.cutoff;
+    d.cut2_hi = (float)c2;
+    d.cut2_lo = (float)(c2 - (double)d.cut2_hi);
+  }
   double cmax = 0;
   for (int k = 0; k < 9; k++) cmax = fmax(cmax, fabs(ci.cell[k]));
   // FP32 positions are within 2^-24 |x| of the FP64 ones; an FP32 image
@@ -72,7 +83,27 @@ static CellDev make_dev(const CellInfo &ci) {
   d.ns = 2 * ci.sweep + 1;
   d.n_shift = d.ns * d.ns * d.ns;
   for (int k = 0; k < 3; k++) d.nb[k] = ci.nb[k];
+  // float-float image error: positions split hi + lo carry ~2^-48 |x|, and
+  // each float-float operation errs by ~2^-44 of its operands' magnitude;
+  // with about ten operations on magnitudes below scale = cmax (2 sweep + 2)
+  // + rc, a component errs by < 2^-40 scale and r^2 by 2 r times that.  The
+  // margin is 2^-30 scale (2 rc + 1): a thousand times more, and still far
+  // below the FP32 rounding of any distance.
+  {
+    const double scale = cmax * (2 * ci.sweep + 2) + ci.cutoff;
+    d.ff_eps = (float)(std::ldexp(1.0, -30) * scale * (2.0 * ci.cutoff + 1.0) + 1e-30);
+  }
   return d;
+}
+
+NbGeom nb_geom(const StructureState &st) {
+  NbGeom g;
+  g.wp = st.wrapped.as<dvec4>();
+  g.keys = st.nbr_key.as<long long>();
+  for (int k = 0; k < 9; k++) g.cell[k] = st.ci.cell[k];
+  g.sweep = st.ci.sweep;
+  g.ns = 2 * st.ci.sweep + 1;
+  return g;
 }
 
 // (n,3) x (3,3) row with the sum order ((a0 b0 + a1 b1) + a2 b2).
@@ -87,6 +118,7 @@ __device__ __forceinline__ void mm3(const double a[3], const double *m,
 // Structure::wrap_positions (structure.cpp:120-133) plus binning.
 __global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
                            dvec4 *__restrict__ wp, float4 *__restrict__ wp32,
+                           float4 *__restrict__ wp_lo,
                            float4 *__restrict__ frac, int *__restrict__ atom_bin,
                            int *__restrict__ bin_count, DeviceStatus *st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -104,7 +136,10 @@ __global__ void k_wrap_bin(int noa, const double *__restrict__ pos, CellDev cd,
   mm3(rw, cd.cdot, t);
   mm3(t, cd.ct_inv, w);
   wp[i] = dvec4{w[0], w[1], w[2], 0.0};
-  wp32[i] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+  const float4 h = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+  wp32[i] = h;
+  wp_lo[i] = make_float4((float)(w[0] - (double)h.x), (float)(w[1] - (double)h.y),
+                         (float)(w[2] - (double)h.z), 0.f);
   frac[i] = make_float4((float)rw[0], (float)rw[1], (float)rw[2], 0.f);
   int b[3];
 #pragma unroll
@@ -137,28 +172,38 @@ __global__ void k_bin_scatter(int noa, const int *__restrict__ atom_bin,
 // im = ((diff + s1 c0) + s2 c1) + s3 c2, dist = sqrt((x^2 + y^2) + z^2).
 // dadd(v, dmul(s, c)) bit for bit, with the products by 0 and +-1 (exact)
 // formed without FP64 instructions, which are scarce on this GPU.
-__device__ __forceinline__ double shift_add(double v, int s, double c) {
-  if (s == 0) {
-    if ((__double_as_longlong(v) << 1) != 0) return v;  // v + (+-0) == v unless v is a zero
-    return dadd(v, dmul(0.0, c));
-  }
-  if (s == 1) return dadd(v, c);
-  if (s == -1) return dadd(v, -c);
-  return dadd(v, dmul((double)s, c));
-}
-
 __device__ __forceinline__ double exact_image(const dvec4 &wi, const dvec4 &wj,
                                               const CellDev &cd, int s1, int s2,
                                               int s3, double im[3]) {
-  double diff[3] = {dsub(wj.x, wi.x), dsub(wj.y, wi.y), dsub(wj.z, wi.z)};
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    double v = shift_add(diff[k], s1, cd.cell[0 * 3 + k]);
-    v = shift_add(v, s2, cd.cell[1 * 3 + k]);
-    im[k] = shift_add(v, s3, cd.cell[2 * 3 + k]);
+  return exact_image_cell(wi, wj, cd.cell, s1, s2, s3, im);
+}
+
+// The exact FP64 decision, out of line: it is rarely reached, and kept out
+// of the callers' instruction stream and registers.
+static __device__ __noinline__ bool member_fp64(const dvec4 *__restrict__ wp, int i, int j,
+                                         const CellDev &cd, int s1, int s2, int s3) {
+  double imd[3];
+  const double dist = exact_image(wp[i], wp[j], cd, s1, s2, s3, imd);
+  return (dist < cd.cutoff) && (dist != 0.0);
+}
+
+// Membership of a candidate whose FP32 distance fell in the band around the
+// cutoff (or near zero): float-float first, the exact FP64 distance only if
+// that is within ff_eps of the cutoff or of zero.
+__device__ __forceinline__ bool band_member(int i, int j, const CellDev &cd,
+                                            const dvec4 *__restrict__ wp,
+                                            const float4 *__restrict__ wp32,
+                                            const float4 *__restrict__ wp_lo, int s1,
+                                            int s2, int s3) {
+  ff im[3], r2;
+  image_ff(wp32[i], wp_lo[i], wp32[j], wp_lo[j], cd.cff, s1, s2, s3, im, r2);
+  const ff d = ff_add(r2, ff{-cd.cut2_hi, -cd.cut2_lo});
+  const float dv = d.hi + d.lo;
+  if (r2.hi > cd.ff_eps) {
+    if (dv < -cd.ff_eps) return true;
+    if (dv > cd.ff_eps) return false;
   }
-  return __dsqrt_rn(dadd(dadd(dmul(im[0], im[0]), dmul(im[1], im[1])),
-                         dmul(im[2], im[2])));
+  return member_fp64(wp, i, j, cd, s1, s2, s3);
 }
 
 // Enumerate the candidate (j, s) pairs of atom i; `emit` is called by each
@@ -245,6 +290,7 @@ constexpr int kEnumWarps = 4;
 
 __global__ void __launch_bounds__(32 * kEnumWarps)
 k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restrict__ wp32,
+       const float4 *__restrict__ wp_lo,
        const float4 *__restrict__ frac, const int *__restrict__ bin_start,
        const float4 *__restrict__ binned, int *__restrict__ count,
        long long *__restrict__ slab, int *__restrict__ overflow) {
@@ -290,12 +336,9 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
         } else if (j == i && sidx == center) {
           ok = false;  // the atom itself: its exact distance is 0
         } else if (d2 <= cd.out2) {
-          const int s3 = sidx % cd.ns - cd.sweep;
-          const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
-          const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
-          double im[3];
-          const double dist = exact_image(wp[i], wp[j], cd, s1, s2, s3, im);
-          ok = (dist < cd.cutoff) && (dist != 0.0);
+          int s1, s2, s3;
+          decode_shift(sidx, cd.ns, cd.sweep, s1, s2, s3);
+          ok = band_member(i, j, cd, wp, wp32, wp_lo, s1, s2, s3);
         }
         key = ((long long)j << kKeyBits) | sidx;
       }
@@ -373,6 +416,32 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
     if (lane == 0) atomicExch(overflow, 1);
     return;
   }
+  if (nacc <= 64) {
+    // bitonic sort across the warp, key e in lane e % 32, register e / 32
+    // (the keys are unique; the padding sorts last)
+    const long long pad = 0x7fffffffffffffffLL;
+    long long k0 = lane < nacc ? s_keys[w][lane] : pad;
+    long long k1 = lane + 32 < nacc ? s_keys[w][lane + 32] : pad;
+    auto step = [&](long long v, int e, int stride, int size) {
+      const long long o = __shfl_xor_sync(0xffffffffu, v, stride);
+      const bool keep_min = ((e & stride) == 0) == ((e & size) == 0);
+      return keep_min ? (v < o ? v : o) : (v < o ? o : v);
+    };
+    for (int size = 2; size <= 64; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        if (stride == 32) {  // partners in the same lane; size 64 ascends everywhere
+          const long long lo = k0 < k1 ? k0 : k1, hi = k0 < k1 ? k1 : k0;
+          k0 = lo;
+          k1 = hi;
+        } else {
+          k0 = step(k0, lane, stride, size);
+          k1 = step(k1, lane + 32, stride, size);
+        }
+      }
+    if (lane < nacc) slab[(size_t)i * kSlabCap + lane] = k0;
+    if (lane + 32 < nacc) slab[(size_t)i * kSlabCap + lane + 32] = k1;
+    return;
+  }
   for (int e = lane; e < nacc; e += 32) {
     const long long key = s_keys[w][e];
     int rank = 0;
@@ -382,22 +451,23 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
 }
 
 // Slab -> CSR in reference order, with the FP64 geometry of every pair.
-__global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp,
+__global__ void k_compact_geom(int noa, CellDev cd, const float4 *__restrict__ wp32,
+                               const float4 *__restrict__ wp_lo,
                                const int *__restrict__ species,
                                const int *__restrict__ offset,
                                const long long *__restrict__ slab,
                                long long *__restrict__ keys, int *__restrict__ nbr_i,
                                int *__restrict__ nbr_j, int *__restrict__ nbr_s,
-                               dvec4 *__restrict__ rel, float4 *__restrict__ rel32) {
+                               float4 *__restrict__ rel32) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= noa) return;
   const int lane = threadIdx.x & 31;
   const int beg = offset[i], n = offset[i + 1] - beg;
-  const dvec4 wi = wp[i];
-  // the pair (i, j, s) and its reverse (j, i, -s) have exactly negated images
-  // (IEEE subtraction and addition round symmetrically), so the FP64
-  // geometry is computed for the canonical half only -- keys above
-  // (i, centre shift), a suffix of the sorted list -- and k_reverse copies it
+  const float4 hi_i = wp32[i], lo_i = wp_lo[i];
+  // the pair (i, j, s) and its reverse (j, i, -s) have exactly negated
+  // images, so the geometry is computed for the canonical half only -- keys
+  // above (i, centre shift), a suffix of the sorted list -- and k_reverse
+  // copies it; FP32 vectors from the float-float image (no FP64 here)
   const long long thr = ((long long)i << kKeyBits) |
                         ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
   int c0 = 0;
@@ -418,18 +488,28 @@ __global__ void k_compact_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp
   for (int e = c0 + lane; e < n; e += 32) {
     const long long key = slab[(size_t)i * kSlabCap + e];
     const int j = (int)(key >> kKeyBits);
-    const int sidx = (int)(key & kKeyMask);
-    const int s3 = sidx % cd.ns - cd.sweep;
-    const int s2 = (sidx / cd.ns) % cd.ns - cd.sweep;
-    const int s1 = sidx / (cd.ns * cd.ns) - cd.sweep;
-    double im[3];
-    const double dist = exact_image(wi, wp[j], cd, s1, s2, s3, im);
-    const int out = beg + e;
-    rel[out] = dvec4{dist, im[0], im[1], im[2]};
-    rel32[out] = make_float4((float)im[0], (float)im[1], (float)im[2], (float)dist);
+    int s1, s2, s3;
+    decode_shift((int)(key & kKeyMask), cd.ns, cd.sweep, s1, s2, s3);
+    ff im[3], r2;
+    image_ff(hi_i, lo_i, wp32[j], wp_lo[j], cd.cff, s1, s2, s3, im, r2);
+    rel32[beg + e] = make_float4(im[0].hi + im[0].lo, im[1].hi + im[1].lo,
+                                 im[2].hi + im[2].lo, ff_sqrt_f(r2));
   }
 }
 
+// The FP64 pair table (r, x, y, z) of every pair, by the reference's formula.
+__global__ void k_rel64(long long n_pairs, CellDev cd, const dvec4 *__restrict__ wp,
+                        const long long *__restrict__ keys, const int *__restrict__ nbr_i,
+                        dvec4 *__restrict__ rel) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const long long key = keys[p];
+  int s1, s2, s3;
+  decode_shift((int)(key & kKeyMask), cd.ns, cd.sweep, s1, s2, s3);
+  double im[3];
+  const double dist = exact_image(wp[nbr_i[p]], wp[(int)(key >> kKeyBits)], cd, s1, s2, s3, im);
+  rel[p] = dvec4{dist, im[0], im[1], im[2]};
+}
 
 __global__ void k_count(int noa, CellDev cd, const dvec4 *__restrict__ wp,
                         const float4 *__restrict__ wp32,
@@ -511,7 +591,7 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
                           const long long *__restrict__ keys,
                           const int *__restrict__ nbr_i,
                           const int *__restrict__ nbr_j, int *__restrict__ rev,
-                          DeviceStatus *st, int mirror, dvec4 *rel, float4 *rel32) {
+                          DeviceStatus *st, int mirror, float4 *rel32) {
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
   const int center = (cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep;
@@ -536,9 +616,7 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
   // pairs below the canonical half take the negated image of their reverse
   // pair (computed by k_compact_geom; the other builds compute both, equal)
   if (found >= 0 && mirror && keys[p] <= (((long long)i << kKeyBits) | center)) {
-    const dvec4 r = rel[found];
     const float4 r32 = rel32[found];
-    rel[p] = dvec4{r.x, -r.y, -r.z, -r.w};
     rel32[p] = make_float4(-r32.x, -r32.y, -r32.z, r32.w);
   }
 }
@@ -613,7 +691,9 @@ int make_cell_info(const double *cell, double cutoff, CellInfo *ci) {
     double cy = p[2] * q[0] - p[0] * q[2];
     double cz = p[0] * q[1] - p[1] * q[0];
     ci->height[k] = ci->volume / std::sqrt(cx * cx + cy * cy + cz * cz);
-    int nb = (int)std::floor(ci->height[k] / (cutoff * (1 + 1e-6) + 1e-6));
+    // bins of about half the cutoff: an atom's reach then spans ~5 bins per
+    // direction instead of 3 whole-cutoff bins, ~40% fewer candidates
+    int nb = (int)std::floor(ci->height[k] / (0.5 * cutoff * (1 + 1e-6) + 1e-6));
     ci->nb[k] = std::min(std::max(nb, 1), 1024);
   }
   long long nbins = (long long)ci->nb[0] * ci->nb[1] * ci->nb[2];
@@ -624,11 +704,23 @@ int make_cell_info(const double *cell, double cutoff, CellInfo *ci) {
   return FPP_OK;
 }
 
-int check_status(StructureState &st, cudaStream_t stream, const char *what) {
-  DeviceStatus h{};
-  FPP_CUDA(cudaMemcpyAsync(&h, st.status.ptr, sizeof(h), cudaMemcpyDeviceToHost,
-                           stream));
-  FPP_CUDA(cudaStreamSynchronize(stream));
+int ensure_readback(StructureState &st) {
+  if (st.rb) return FPP_OK;
+  void *h = nullptr, *d = nullptr;
+  FPP_CUDA(cudaHostAlloc(&h, sizeof(HostReadback), cudaHostAllocMapped));
+  const cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+  if (e != cudaSuccess) {
+    cudaFreeHost(h);
+    return cuda_fail(e, "cudaHostGetDevicePointer");
+  }
+  std::memset(h, 0, sizeof(HostReadback));
+  st.rb = static_cast<HostReadback *>(h);
+  st.rb_dev = static_cast<HostReadback *>(d);
+  return FPP_OK;
+}
+
+int status_from_readback(StructureState &st, cudaStream_t stream, const char *what) {
+  const DeviceStatus h = *reinterpret_cast<const DeviceStatus *>(st.rb->status);
   if (h.code != 0) {
     // cleared once reported (an asynchronous call leaves its errors here for
     // the next synchronizing call)
@@ -639,6 +731,28 @@ int check_status(StructureState &st, cudaStream_t stream, const char *what) {
     return fail(h.code, buf);
   }
   return FPP_OK;
+}
+
+int check_status(StructureState &st, cudaStream_t stream, const char *what) {
+  FPP_TRY(ensure_readback(st));
+  FPP_CUDA(cudaMemcpyAsync(st.rb->status, st.status.ptr, sizeof(DeviceStatus),
+                           cudaMemcpyDeviceToHost, stream));
+  FPP_CUDA(cudaStreamSynchronize(stream));
+  return status_from_readback(st, stream, what);
+}
+
+// The pair total, the slab overflow flag and the status word into the
+// host-visible readback block (one thread).
+__global__ void k_nb_readback(const int *__restrict__ total, const int *__restrict__ flags,
+                              const DeviceStatus *__restrict__ status,
+                              HostReadback *__restrict__ rb) {
+  if (threadIdx.x != 0) return;
+  rb->total_pairs = *total;
+  rb->overflow = flags[0];
+  rb->status[0] = status->code;
+  rb->status[1] = status->where;
+  rb->status[2] = status->info;
+  rb->status[3] = status->pad;
 }
 
 int build_neighbors(StructureState &st, cudaStream_t stream) {
@@ -658,6 +772,8 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   }
   FPP_TRY(st.wrapped.reserve(sizeof(dvec4) * noa));
   FPP_TRY(st.wrapped32.reserve(sizeof(float4) * noa));
+  FPP_TRY(st.wrapped_lo.reserve(sizeof(float4) * noa));
+  st.rel64_valid = false;
   FPP_TRY(st.frac.reserve(sizeof(float4) * noa));
   FPP_TRY(st.atom_bin.reserve(sizeof(int) * noa));
   FPP_TRY(st.bin_atoms.reserve(sizeof(int) * noa));
@@ -671,7 +787,8 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   const int tb = 256;
   k_wrap_bin<<<ceil_div(noa, tb), tb, 0, stream>>>(
       noa, st.positions.as<double>(), cd, st.wrapped.as<dvec4>(),
-      st.wrapped32.as<float4>(), st.frac.as<float4>(), st.atom_bin.as<int>(),
+      st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.frac.as<float4>(),
+      st.atom_bin.as<int>(),
       st.bin_count.as<int>(), dst);
   FPP_CUDA(cudaGetLastError());
 
@@ -699,23 +816,23 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_TRY(st.flags.reserve(sizeof(int) * 4));
   FPP_CUDA(cudaMemsetAsync(st.flags.ptr, 0, sizeof(int) * 4, stream));
   k_enum<<<ceil_div(noa, kEnumWarps), 32 * kEnumWarps, 0, stream>>>(
-      noa, cd, st.wrapped.as<dvec4>(), st.wrapped32.as<float4>(), st.frac.as<float4>(),
-      st.bin_start.as<int>(), st.binned.as<float4>(), st.nbr_count.as<int>(),
+      noa, cd, st.wrapped.as<dvec4>(), st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(),
+      st.frac.as<float4>(), st.bin_start.as<int>(), st.binned.as<float4>(),
+      st.nbr_count.as<int>(),
       st.slab.as<long long>(), st.flags.as<int>());
   FPP_CUDA(cudaGetLastError());
   tmp_bytes = st.scan_tmp.bytes;
   FPP_CUDA(cub::DeviceScan::ExclusiveSum(st.scan_tmp.ptr, tmp_bytes,
                                          st.nbr_count.as<int>(),
                                          st.nbr_offset.as<int>(), noa + 1, stream));
-  int hinfo[2] = {0, 0};
-  FPP_CUDA(cudaMemcpyAsync(&hinfo[0], st.nbr_offset.as<int>() + noa, sizeof(int),
-                           cudaMemcpyDeviceToHost, stream));
-  FPP_CUDA(cudaMemcpyAsync(&hinfo[1], st.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost,
-                           stream));
+  FPP_TRY(ensure_readback(st));
+  k_nb_readback<<<1, 32, 0, stream>>>(st.nbr_offset.as<int>() + noa, st.flags.as<int>(),
+                                      st.status.as<DeviceStatus>(), st.rb_dev);
+  FPP_CUDA(cudaGetLastError());
   FPP_CUDA(cudaStreamSynchronize(stream));
-  FPP_TRY(check_status(st, stream, "neighbor build or an earlier asynchronous call"));
-  const bool overflow = hinfo[1] != 0;
-  int total = hinfo[0];
+  FPP_TRY(status_from_readback(st, stream, "neighbor build or an earlier asynchronous call"));
+  const bool overflow = st.rb->overflow != 0;
+  int total = st.rb->total_pairs;
   if (overflow) {
     // some atom has more than kSlabCap neighbors: two-pass count / fill
     k_count<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
@@ -744,9 +861,9 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   if (total == 0) return FPP_OK;
   if (!overflow) {
     k_compact_geom<<<grid, block, 0, stream>>>(
-        noa, cd, st.wrapped.as<dvec4>(), st.species.as<int>(), st.nbr_offset.as<int>(),
-        st.slab.as<long long>(), st.nbr_key.as<long long>(), st.nbr_i.as<int>(),
-        st.nbr_j.as<int>(), st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(),
+        noa, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.species.as<int>(),
+        st.nbr_offset.as<int>(), st.slab.as<long long>(), st.nbr_key.as<long long>(),
+        st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_s.as<int>(),
         st.nbr_rel32.as<float4>());
     FPP_CUDA(cudaGetLastError());
   } else {
@@ -763,12 +880,27 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
         st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_j.as<int>(),
         st.nbr_s.as<int>(), st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
     FPP_CUDA(cudaGetLastError());
+    st.rel64_valid = true;  // this build computes the FP64 table for every pair
   }
   k_reverse<<<ceil_div(total, tb), tb, 0, stream>>>(
       total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
       st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst, overflow ? 0 : 1,
-      st.nbr_rel.as<dvec4>(), st.nbr_rel32.as<float4>());
+      st.nbr_rel32.as<float4>());
   FPP_CUDA(cudaGetLastError());
+  return FPP_OK;
+}
+
+int ensure_rel64(StructureState &st, cudaStream_t stream) {
+  if (st.rel64_valid || st.n_pairs == 0) {
+    st.rel64_valid = true;
+    return FPP_OK;
+  }
+  const CellDev cd = make_dev(st.ci);
+  k_rel64<<<ceil_div((int)st.n_pairs, 256), 256, 0, stream>>>(
+      st.n_pairs, cd, st.wrapped.as<dvec4>(), st.nbr_key.as<long long>(),
+      st.nbr_i.as<int>(), st.nbr_rel.as<dvec4>());
+  FPP_CUDA(cudaGetLastError());
+  st.rel64_valid = true;
   return FPP_OK;
 }
 
