@@ -320,11 +320,11 @@ def run_ours(args):
 
 
 def launches_per_step(n_species):
-    # neighbors: wrap_bin, bin_scatter, enum, nb_readback, compact_geom,
-    # reverse and two CUB exclusive scans of two kernels each (compiled into
-    # the library); descriptors: forward; contraction: one grouped split GEMM;
-    # adjoint: wu, pair_force, gather, reduce; outputs: finish
-    return 10 + 1 + 1 + 4 + 1
+    # neighbors: wrap_bin, bin_scatter, enum, nb_readback, compact_geom (which
+    # also links reverse pairs) and two CUB exclusive scans of two kernels each
+    # (compiled into the library); descriptors: forward; contraction: one
+    # grouped split GEMM; adjoint: wu, pair_force, gather, reduce; outputs: finish
+    return 9 + 1 + 1 + 4 + 1
 
 
 def cpu_baseline(w, seconds=15.0):

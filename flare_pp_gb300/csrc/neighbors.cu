@@ -458,7 +458,8 @@ __global__ void k_compact_geom(int noa, CellDev cd, const float4 *__restrict__ w
                                const long long *__restrict__ slab,
                                long long *__restrict__ keys, int *__restrict__ nbr_i,
                                int *__restrict__ nbr_j, int *__restrict__ nbr_s,
-                               float4 *__restrict__ rel32) {
+                               float4 *__restrict__ rel32, int *__restrict__ rev,
+                               DeviceStatus *st) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= noa) return;
   const int lane = threadIdx.x & 31;
@@ -466,8 +467,10 @@ __global__ void k_compact_geom(int noa, CellDev cd, const float4 *__restrict__ w
   const float4 hi_i = wp32[i], lo_i = wp_lo[i];
   // the pair (i, j, s) and its reverse (j, i, -s) have exactly negated
   // images, so the geometry is computed for the canonical half only -- keys
-  // above (i, centre shift), a suffix of the sorted list -- and k_reverse
-  // copies it; FP32 vectors from the float-float image (no FP64 here)
+  // above (i, centre shift), a suffix of the sorted list -- and written to
+  // both; the canonical pair also finds its reverse (binary search in j's
+  // sorted slab row) and links the two.  FP32 vectors come from the
+  // float-float image (no FP64 here).
   const long long thr = ((long long)i << kKeyBits) |
                         ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
   int c0 = 0;
@@ -488,12 +491,40 @@ __global__ void k_compact_geom(int noa, CellDev cd, const float4 *__restrict__ w
   for (int e = c0 + lane; e < n; e += 32) {
     const long long key = slab[(size_t)i * kSlabCap + e];
     const int j = (int)(key >> kKeyBits);
+    const int sidx = (int)(key & kKeyMask);
     int s1, s2, s3;
-    decode_shift((int)(key & kKeyMask), cd.ns, cd.sweep, s1, s2, s3);
+    decode_shift(sidx, cd.ns, cd.sweep, s1, s2, s3);
     ff im[3], r2;
     image_ff(hi_i, lo_i, wp32[j], wp_lo[j], cd.cff, s1, s2, s3, im, r2);
-    rel32[beg + e] = make_float4(im[0].hi + im[0].lo, im[1].hi + im[1].lo,
+    const float4 v = make_float4(im[0].hi + im[0].lo, im[1].hi + im[1].lo,
                                  im[2].hi + im[2].lo, ff_sqrt_f(r2));
+    const int out = beg + e;
+    rel32[out] = v;
+    // reverse pair (j, i, -s) in j's sorted row
+    const long long want = ((long long)i << kKeyBits) | (cd.n_shift - 1 - sidx);
+    const long long *row = slab + (size_t)j * kSlabCap;
+    int lo = 0, hi = offset[j + 1] - offset[j] - 1, found = -1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      const long long k = row[mid];
+      if (k == want) {
+        found = mid;
+        break;
+      }
+      if (k < want)
+        lo = mid + 1;
+      else
+        hi = mid - 1;
+    }
+    if (found < 0) {
+      set_status(st, FPP_ERR_NUMERIC, 7, out);
+      rev[out] = -1;
+      continue;
+    }
+    const int orev = offset[j] + found;
+    rev[out] = orev;
+    rev[orev] = out;
+    rel32[orev] = make_float4(-v.x, -v.y, -v.z, v.w);
   }
 }
 
@@ -864,8 +895,9 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
         noa, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.species.as<int>(),
         st.nbr_offset.as<int>(), st.slab.as<long long>(), st.nbr_key.as<long long>(),
         st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_s.as<int>(),
-        st.nbr_rel32.as<float4>());
+        st.nbr_rel32.as<float4>(), st.nbr_rev.as<int>(), dst);
     FPP_CUDA(cudaGetLastError());
+    return FPP_OK;  // reverse links and mirrored geometry written above
   } else {
     FPP_TRY(st.nbr_key_tmp.reserve(sizeof(long long) * np));
     k_fill<<<grid, block, 0, stream>>>(noa, cd, st.wrapped.as<dvec4>(),
