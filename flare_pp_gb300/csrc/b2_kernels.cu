@@ -1132,6 +1132,22 @@ int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
 // block writes one partial row for k_reduce (fixed order: deterministic).
 constexpr int kGatherWarps = 8;
 
+// Float-float sum over the kGatherLanes lanes of a group (xor offsets stay
+// inside the group), every lane of the group ends with the total.
+constexpr int kGatherLanes = 8;  // lanes per atom (four atoms per warp)
+__device__ __forceinline__ void ff_group_sum(float &hi, float &lo) {
+#pragma unroll
+  for (int o = kGatherLanes / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e += lo + l2;
+    hi = s + e;
+    lo = e - (hi - s);
+  }
+}
+
 __global__ void __launch_bounds__(32 * kGatherWarps)
 k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
               const float4 *__restrict__ rel32, const float4 *__restrict__ pair_f,
@@ -1139,28 +1155,35 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
               double *__restrict__ partial) {
   __shared__ double sm[kGatherWarps][10];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float th[9], tl[9];  // this warp's virial, float-float
+  const int g = lane / kGatherLanes, gl = lane % kGatherLanes;  // group, lane in group
+  constexpr int kGroups = 32 / kGatherLanes;
+  float th[9], tl[9];  // this lane's share of the virial, float-float
 #pragma unroll
   for (int k = 0; k < 9; k++) th[k] = tl[k] = 0.0f;
-  double esum = 0.0;  // lane 0: this warp's energy
-  for (int i = blockIdx.x * kGatherWarps + warp; i < noa; i += gridDim.x * kGatherWarps) {
+  double esum = 0.0;  // group leaders: their atoms' energies
+  // atoms in rounds of kGroups per warp; all lanes run the same number of
+  // rounds (the group shuffles need the whole warp)
+  const int stride = gridDim.x * kGatherWarps * kGroups;
+  for (int i0 = (blockIdx.x * kGatherWarps + warp) * kGroups; i0 < noa; i0 += stride) {
+    const int i = i0 + g;
+    const bool live = i < noa;
     float hi[12], lo[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) hi[k] = lo[k] = 0.0f;
-    const int beg = offset[i], end = offset[i + 1];
-    for (int p = beg + lane; p < end; p += 32) {
+    const int beg = live ? offset[i] : 0, end = live ? offset[i + 1] : 0;
+    for (int p = beg + gl; p < end; p += kGatherLanes) {
       const int q = rev[p];
       const float4 fp = pair_f[p];
       const float4 fq = q >= 0 ? pair_f[q] : make_float4(0.f, 0.f, 0.f, 0.f);
       const float4 r = rel32[p];
-      const float f[3] = {fp.x, fp.y, fp.z}, g[3] = {fq.x, fq.y, fq.z};
+      const float f[3] = {fp.x, fp.y, fp.z}, gq[3] = {fq.x, fq.y, fq.z};
       const float rr[3] = {r.x, r.y, r.z};
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         float t, e;
         two_sum(hi[a], f[a], t, e);
         lo[a] += e;
-        two_sum(t, -g[a], hi[a], e);
+        two_sum(t, -gq[a], hi[a], e);
         lo[a] += e;
 #pragma unroll
         for (int b = 0; b < 3; b++) {
@@ -1172,23 +1195,29 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
       }
     }
 #pragma unroll
-    for (int k = 0; k < 12; k++) ff_warp_sum(hi[k], lo[k]);
-    // lanes 0..2 convert one force component each (FP64 instructions are
-    // scarce: one conversion pass per atom instead of three)
-    {
-      const float fh = lane == 0 ? hi[0] : (lane == 1 ? hi[1] : hi[2]);
-      const float fl = lane == 0 ? lo[0] : (lane == 1 ? lo[1] : lo[2]);
-      if (lane < 3) forces[3 * i + lane] = double(fh) + double(fl);
-    }
-    if (lane == 0) esum += atom_e[i];
+    for (int k = 0; k < 12; k++) ff_group_sum(hi[k], lo[k]);
+    if (live) {
+      // lanes 0..2 of the group convert one force component each
+      const float fh = gl == 0 ? hi[0] : (gl == 1 ? hi[1] : hi[2]);
+      const float fl = gl == 0 ? lo[0] : (gl == 1 ? lo[1] : lo[2]);
+      if (gl < 3) forces[3 * i + gl] = double(fh) + double(fl);
+      if (gl == 0) esum += atom_e[i];
+      if (gl == 0) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-      float t, e;
-      two_sum(th[k], hi[3 + k], t, e);
-      th[k] = t;
-      tl[k] += e + lo[3 + k];
+        for (int k = 0; k < 9; k++) {
+          float t, e;
+          two_sum(th[k], hi[3 + k], t, e);
+          th[k] = t;
+          tl[k] += e + lo[3 + k];
+        }
+      }
     }
   }
+  // the group leaders' virial (other lanes hold zeros) and energies, summed
+  // over the warp in a fixed order
+#pragma unroll
+  for (int k = 0; k < 9; k++) ff_warp_sum(th[k], tl[k]);
+  esum = warp_sum(esum);
   if (lane == 0) {
     sm[warp][0] = esum;
 #pragma unroll
@@ -1408,7 +1437,7 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
   int nblk;
   if constexpr (sizeof(T) == 4) {
     // a few resident blocks per SM, each walking many atoms
-    nblk = std::min(ceil_div(a.noa, kGatherWarps), 152 * 8);
+    nblk = std::min(ceil_div(a.noa, kGatherWarps * (32 / kGatherLanes)), 152 * 8);
     k_gather_warp<<<nblk, 32 * kGatherWarps, 0, stream>>>(
         a.noa, nb.offset, nb.rev, nb.rel32, reinterpret_cast<const float4 *>(pair_f), atom_e,
         forces, atom_vir);
