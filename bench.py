@@ -62,6 +62,23 @@ def dist_env():
     return rank, world, local
 
 
+def replica_time(ms_total, world, device=None):
+    """Timed-region length of an N-replica run: the maximum over ranks (every
+    rank processes its own copy of the workload; no data-path collective)."""
+    if world <= 1:
+        return ms_total
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_total], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_atoms, steps, ms_total, world):
+    """Whole-job atoms/s: all replicas' atoms over the slowest rank's time."""
+    return world * n_atoms * steps / (ms_total / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -216,13 +233,9 @@ def run_ours(args):
     torch.cuda.profiler.stop()
     clocks.mark_end()
     clk = clocks.stop()
-    ms_total = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = replica_time(ev0.elapsed_time(ev1), world, dev)
     ms_step = ms_total / K
-    value = world * noa * K / (ms_total / 1e3)
+    value = replica_value(noa, K, ms_total, world)
     # ---- per-stage device times (separate pass: the event reads synchronize) ----
     check(L.fpp_structure_set_profiling(sh, 1))
     stage = np.zeros(4)
