@@ -75,7 +75,7 @@ struct Neigh {
   const float4 *rel32;
   const int *nbr_s;
   const int *rev;
-  NbGeom geom;          // exact distances on demand (geom.wp == nullptr: use rel)
+  const NbGeom *geom;   // exact distances on demand (nullptr: rel is the FP64 table)
 };
 
 int upload_harmonic_tables(cudaStream_t stream);

@@ -100,10 +100,7 @@ static Neigh neigh_of(StructureState &S) {
   nb.rev = S.nbr_rev.as<int>();
   // without the FP64 table, exact distances near a cutoff are recomputed
   // from the positions (the FP32 kernels need them for a few pairs only)
-  if (S.rel64_valid)
-    std::memset(&nb.geom, 0, sizeof(nb.geom));
-  else
-    nb.geom = nb_geom(S);
+  nb.geom = (S.rel64_valid || !S.rb_dev) ? nullptr : &S.rb_dev->geom;
   return nb;
 }
 

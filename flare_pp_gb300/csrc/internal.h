@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/flare_pp_gb300.h"
+#include "geom.cuh"
 
 namespace fpp {
 
@@ -65,6 +66,10 @@ struct HostReadback {
   int pad[2];
   int status[4];   // DeviceStatus
   double red[16];  // reduction outputs (energy, virial sums)
+  // exact-distance geometry of the current neighbor list, read by the FP32
+  // kernels (through the mapped pointer) only for pairs next to a cutoff;
+  // written by the host after the neighbor build's synchronization
+  NbGeom geom;
 };
 
 struct StructureState {
@@ -137,7 +142,6 @@ int build_neighbors(StructureState &st, cudaStream_t stream);
 // the FP64 pair table for the callers that return or consume FP64 geometry
 int ensure_rel64(StructureState &st, cudaStream_t stream);
 // exact-distance geometry of the structure's neighbor list (geom.cuh)
-struct NbGeom;
 NbGeom nb_geom(const StructureState &st);
 int check_status(StructureState &st, cudaStream_t stream, const char *what);
 // allocate the readback block on first use

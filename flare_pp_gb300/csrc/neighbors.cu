@@ -889,6 +889,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   FPP_TRY(st.nbr_rel.reserve(sizeof(dvec4) * np));
   FPP_TRY(st.nbr_rel32.reserve(sizeof(float4) * np));
   FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
+  st.rb->geom = nb_geom(st);  // the stream is idle here (synchronized above)
   if (total == 0) return FPP_OK;
   if (!overflow) {
     k_compact_geom<<<grid, block, 0, stream>>>(
