@@ -390,24 +390,40 @@ k_enum(int noa, CellDev cd, const dvec4 *__restrict__ wp, const float4 *__restri
       const int l2 = __shfl_sync(full, lo[2], src), h2 = __shfl_sync(full, hi[2], src);
       const float4 shs = make_float4(__shfl_sync(full, sh.x, src), __shfl_sync(full, sh.y, src),
                                      __shfl_sync(full, sh.z, src), 0.f);
-      for (int b0 = l0; b0 <= h0; b0++)
-        for (int b1 = l1; b1 <= h1; b1++) {
-          // bins along the last direction are contiguous: one range
+      // bins along the last direction are contiguous: one range per (b0, b1),
+      // looked up by the lanes in parallel, appended in (b0, b1) order
+      const int w1 = h1 - l1 + 1, ncomb = (h0 - l0 + 1) * w1;
+      for (int c0 = 0; c0 < ncomb; c0 += 32) {
+        const int c = c0 + lane;
+        int st = 0, cn = 0;
+        if (c < ncomb) {
+          const int b0 = l0 + c / w1, b1 = l1 + c % w1;
           const int bin_lo = (b0 * cd.nb[1] + b1) * cd.nb[2] + l2;
           const int bin_hi = (b0 * cd.nb[1] + b1) * cd.nb[2] + h2;
-          const int st = bin_start[bin_lo], cn = bin_start[bin_hi + 1] - st;
-          if (cn == 0) continue;
-          if (nr == kMaxRanges) flush();
-          if (lane == 0) {
-            s_rstart[w][nr] = st;
-            s_rsidx[w][nr] = ssrc;
-            s_rshift[w][nr] = shs;
-            s_rpre[w][nr + 1] = tot + cn;
-          }
-          __syncwarp();
-          tot += cn;
-          nr++;
+          st = bin_start[bin_lo];
+          cn = bin_start[bin_hi + 1] - st;
         }
+        const unsigned nz = __ballot_sync(full, cn > 0);
+        const int k = __popc(nz);
+        if (k == 0) continue;
+        if (nr + k > kMaxRanges) flush();
+        int incl = cn;  // inclusive scan of the counts in lane order
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(full, incl, o);
+          if (lane >= o) incl += v;
+        }
+        if (cn > 0) {
+          const int idx = nr + __popc(nz & ((1u << lane) - 1u));
+          s_rstart[w][idx] = st;
+          s_rsidx[w][idx] = ssrc;
+          s_rshift[w][idx] = shs;
+          s_rpre[w][idx + 1] = tot + incl;
+        }
+        __syncwarp();
+        tot += __shfl_sync(full, incl, 31);
+        nr += k;
+      }
     }
   }
   flush();
