@@ -86,16 +86,6 @@ int upload_harmonic_tables(cudaStream_t stream) {
   return e == cudaSuccess ? 0 : -1;
 }
 
-// 16-byte asynchronous global -> shared copy (completion: cp_async_wait_all
-// by the issuing thread, then a warp barrier for the other lanes' copies).
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;" ::: "memory");
-}
-
 // Running sum; compensated (Neumaier) when T is float.
 template <typename T> struct Acc {
   T s = T(0), c = T(0);
@@ -705,73 +695,10 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
   const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
                                       : make_float2(0.0f, 0.0f);
-  double e;
-  if (sizeof(T) == 4 && SH::kNR > 0 && g.mode == kWFromV2 && g.phat_hi && (nd & 3) == 0 &&
-      (sb & 3) == 0) {
-    // staged mixed form: the atom's V row, delta planes and c row are copied
-    // into shared memory with 16-byte asynchronous copies, all in flight at
-    // once, then w is formed in place of V
-    const int nh = ((nd * 2 + 15) & ~15) / 2;  // halves per staged delta row
-    __half *dh_s = reinterpret_cast<__half *>(c_s + sb);
-    __half *dl_s = dh_s + nh;
-    const char *vsrc = reinterpret_cast<const char *>(g.V32 + (size_t)row * g.ldv);
-    const char *hsrc = reinterpret_cast<const char *>(g.phat_hi + (size_t)row * g.ldp);
-    const char *lsrc = reinterpret_cast<const char *>(g.phat_lo + (size_t)row * g.ldp);
-    const char *csrc = reinterpret_cast<const char *>(c_in + (size_t)atom * sb);
-    for (int q = lane; q < nd / 4; q += 32) cp_async16(w_s + 4 * q, vsrc + 16 * q);
-    for (int q = lane; q < nh / 8; q += 32) {
-      cp_async16(dh_s + 8 * q, hsrc + 16 * q);
-      cp_async16(dl_s + 8 * q, lsrc + 16 * q);
-    }
-    for (int q = lane; q < sb / 4; q += 32) cp_async16(c_s + 4 * q, csrc + 16 * q);
-    cp_async_wait_all();
-    __syncwarp();
-    const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
-    const float4 *B4 = reinterpret_cast<const float4 *>(g.pbar + (size_t)si * nd);
-    float4 *W4 = reinterpret_cast<float4 *>(w_s);
-    const uint2 *H4 = reinterpret_cast<const uint2 *>(dh_s);
-    const uint2 *L4 = reinterpret_cast<const uint2 *>(dl_s);
-    auto deltas = [&](uint2 h, uint2 l, float (&dl)[4]) {
-      const float2 h01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
-      const float2 h23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
-      const float2 l01 = __half22float2(*reinterpret_cast<const __half2 *>(&l.x));
-      const float2 l23 = __half22float2(*reinterpret_cast<const __half2 *>(&l.y));
-      dl[0] = (h01.x + l01.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[1] = (h01.y + l01.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[2] = (h23.x + l23.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[3] = (h23.y + l23.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-    };
-    const bool empty = nrm32.x * nrm32.x < float(g.empty_thresh);
-    Acc<float> acc;
-    for (int q = lane; q < nd / 4; q += 32) {
-      float dl[4];
-      deltas(H4[q], L4[q], dl);
-      const float4 v = W4[q], gg = G4[q];
-      acc.add((2.0f * gg.x + v.x) * dl[0]);
-      acc.add((2.0f * gg.y + v.y) * dl[1]);
-      acc.add((2.0f * gg.z + v.z) * dl[2]);
-      acc.add((2.0f * gg.w + v.w) * dl[3]);
-    }
-    float hi = acc.s, lo = acc.c;
-    ff_warp_sum(hi, lo);
-    const ff et = ff_add(ff_norm(hi, lo), ff{g.c0_hi[si], g.c0_lo[si]});
-    const float ef = empty ? 0.0f : et.hi + et.lo;
-    const float inv = empty ? 0.0f : 1.0f / nrm32.x;
-    e = empty ? 0.0 : double(et.hi) + double(et.lo);
-    for (int q = lane; q < nd / 4; q += 32) {
-      float dl[4];
-      deltas(H4[q], L4[q], dl);
-      const float4 v = W4[q], gg = G4[q], pb = B4[q];
-      W4[q] = make_float4(2.0f * ((gg.x + v.x) - ef * (pb.x + dl[0])) * inv,
-                          2.0f * ((gg.y + v.y) - ef * (pb.y + dl[1])) * inv,
-                          2.0f * ((gg.z + v.z) - ef * (pb.z + dl[2])) * inv,
-                          2.0f * ((gg.w + v.w) - ef * (pb.w + dl[3])) * inv);
-    }
-  } else {
 #pragma unroll 4
-    for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
-    e = adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
-  }
+  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
+  const double e =
+      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
@@ -1433,8 +1360,6 @@ size_t forward_smem_per_warp(const B2Args &a, size_t elem) {
 size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
   const int sb = a.n_species * a.N * a.H;
   size_t b = elem * ((size_t)a.n_d + (size_t)sb);
-  // FP32: room for the staged fp16 delta planes of the mixed form
-  if (elem == 4) b += 2 * (((size_t)a.n_d * 2 + 15) & ~(size_t)15);
   return (b + 15) & ~(size_t)15;
 }
 
