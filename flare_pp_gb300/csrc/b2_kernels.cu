@@ -764,8 +764,9 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
 template <typename T>
 __host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a) {
   const size_t nr = (size_t)a.n_species * a.N;
+  // w, complex c, summed u, and per-lane private rows of the lane's triple
   size_t b = sizeof(T) * ((size_t)a.n_d + 2 * nr * (a.H + 1) + 2 * nr * a.H +
-                          2 * nr * a.H * 32);
+                          6 * (size_t)a.H * 32);
   return (b + 15) & ~(size_t)15;
 }
 
@@ -787,7 +788,7 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   T *zi = zr + (size_t)nr * H1;
   T *ur = zi + (size_t)nr * H1;          // [sb] summed u (re)
   T *ui = ur + sb;                       // [sb] (im)
-  T *up = ui + sb;                       // [sb][2][32] per-lane partial u
+  T *up = ui + sb;                       // [3][H][2][32] per-lane private rows
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
@@ -802,21 +803,10 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   b3_to_complex<T>(ur, nr, H, zr, zi, lane);
-  for (int k = 0; k < 2 * sb; k++) up[(size_t)k * 32 + lane] = T(0);
   __syncwarp();
-  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, tri, zr, zi, w_s, up, lane);
+  for (int k = lane; k < sb; k += 32) ur[k] = ui[k] = T(0);
   __syncwarp();
-  for (int k = lane; k < sb; k += 32) {
-    T sr = T(0), sm = T(0);
-    for (int j = 0; j < 32; j++) {
-      const int jj = (j + lane) & 31;  // rotated: the lanes read different banks
-      sr += up[(size_t)(2 * k) * 32 + jj];
-      sm += up[(size_t)(2 * k + 1) * 32 + jj];
-    }
-    ur[k] = sr;
-    ui[k] = sm;
-  }
-  __syncwarp();
+  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, zr, zi, w_s, up, ur, ui, lane);
   // dE/dc_real: for m > 0 with u+ = u[l, m], u- = u[l, -m], s = (-1)^m:
   //   dE/dR = (s Re u+ + Re u-) / sqrt 2,  dE/dS = (Im u- - s Im u+) / sqrt 2
   const T is2 = T(0.70710678118654752440);

@@ -195,42 +195,73 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
 }
 
 // Adjoint of b3_contract: for dE/dp = w, the holomorphic derivative
-// u = dE/dc accumulated per lane into up[(2 k + part) * 32 + lane]
-// (k = n * H + lm: each lane owns a column, so no atomics; the caller sums
-// the 32 columns in a fixed order).
+// u = dE/dc summed into (ur, ui)[n * H + lm].  Lanes take radial triples in
+// rounds of 32; within a round lane r only updates the rows n1(r), n2(r),
+// n3(r) of its own triple, so it accumulates into three private rows in
+// shared memory, priv[((pos * H + lm) * 2 + part) * 32 + lane] (conflict-free
+// banks, no atomics).  After each round the private rows are summed into
+// (ur, ui) by output entry, over lanes in a fixed rotated order.  The caller
+// zeroes (ur, ui) and synchronizes the warp before and after.
 template <typename T>
 __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tri, int H,
-                                                    const int *__restrict__ tri,
+                                                    int nr, const int *__restrict__ tri,
                                                     const T *__restrict__ zr,
                                                     const T *__restrict__ zi,
                                                     const T *__restrict__ w,
-                                                    T *__restrict__ up, int lane) {
+                                                    T *__restrict__ priv, T *__restrict__ ur,
+                                                    T *__restrict__ ui, int lane) {
   const int H1 = H + 1;
   const int *beg = c_b3.beg + c_b3.ls_off[lmax];
-  for (int t = 0; t < n_ls; t++) {
-    const int e0 = beg[t], e1 = beg[t + 1];
-    for (int r = lane; r < n_tri; r += 32) {
-      const T wq = w[r * n_ls + t];
-      const int tr = tri[r];
+  for (int r0 = 0; r0 < n_tri; r0 += 32) {
+    const int r = r0 + lane;
+    const bool live = r < n_tri;
+    const int tr = live ? tri[r] : 0;
+    for (int k = 0; k < 6 * H; k++) priv[k * 32 + lane] = T(0);
+    if (live) {
       const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
-      for (int q = e0; q < e1; q++) {
-        const unsigned ix = c_b3.idx[q];
-        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
-        const T f = wq * T(c_b3.w[q]);
-        const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
-        const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
-        const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
-        T *p1 = up + (size_t)(2 * (n1 * H + i1)) * 32 + lane;
-        T *p2 = up + (size_t)(2 * (n2 * H + i2)) * 32 + lane;
-        T *p3 = up + (size_t)(2 * (n3 * H + i3)) * 32 + lane;
-        p1[0] += f * (br * cr - bi * ci);
-        p1[32] += f * (br * ci + bi * cr);
-        p2[0] += f * (ar * cr - ai * ci);
-        p2[32] += f * (ar * ci + ai * cr);
-        p3[0] += f * (ar * br - ai * bi);
-        p3[32] += f * (ar * bi + ai * br);
+      T *p1 = priv + lane;
+      T *p2 = priv + (size_t)(2 * H) * 32 + lane;
+      T *p3 = priv + (size_t)(4 * H) * 32 + lane;
+      for (int t = 0; t < n_ls; t++) {
+        const int e0 = beg[t], e1 = beg[t + 1];
+        const T wq = w[r * n_ls + t];
+        for (int q = e0; q < e1; q++) {
+          const unsigned ix = c_b3.idx[q];
+          const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
+          const T f = wq * T(c_b3.w[q]);
+          const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
+          const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
+          const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
+          p1[(2 * i1) * 32] += f * (br * cr - bi * ci);
+          p1[(2 * i1 + 1) * 32] += f * (br * ci + bi * cr);
+          p2[(2 * i2) * 32] += f * (ar * cr - ai * ci);
+          p2[(2 * i2 + 1) * 32] += f * (ar * ci + ai * cr);
+          p3[(2 * i3) * 32] += f * (ar * br - ai * bi);
+          p3[(2 * i3 + 1) * 32] += f * (ar * bi + ai * br);
+        }
       }
     }
+    __syncwarp();
+    // (ur, ui)[n, lm] += sum over lanes j and positions with n_pos(j) == n
+    for (int k = lane; k < 2 * nr * H; k += 32) {
+      const int part = k & 1, nl = k >> 1;
+      const int n = nl / H, lm = nl - n * H;
+      T acc = T(0);
+      for (int j0 = 0; j0 < 32; j0++) {
+        const int j = (j0 + lane) & 31;  // rotated: lanes read different banks
+        if (r0 + j >= n_tri) continue;
+        const int tj = tri[r0 + j];
+        const T *col = priv + (size_t)((lm * 2 + part) * 32) + j;
+        if ((tj & 0xff) == n) acc += col[0];
+        if (((tj >> 8) & 0xff) == n) acc += col[(2 * H) * 32];
+        if ((tj >> 16) == n) acc += col[(4 * H) * 32];
+      }
+      if (part == 0)
+        ur[nl] += acc;
+      else
+        ui[nl] += acc;
+    }
+    __syncwarp();
   }
 }
 

@@ -5,22 +5,25 @@
 // dist != 0, and orders each atom's list by j, then s1, s2, s3.  Here the
 // same (j, s) pairs are found through bins in fractional coordinates:
 //   1. wrap_bin    wrapped positions (reference formula, exact FP64 order),
-//                  fractional coordinates and a bin per atom
+//                  their float-float split, fractional coordinates, a bin
+//                  (bins are about half the cutoff wide)
 //   2. bin sort    counting sort of atoms into bins
-//   3. count       warp per atom; candidates from the bins reachable for each
-//                  shift, an FP32 pre-filter with a safety margin, then the
-//                  reference's FP64 distance for the survivors
-//   4. fill        same enumeration, writes the keys j * n_shift + shift
-//   5. sort_geom   per atom, ranks the keys (unique) into reference order and
-//                  recomputes the FP64 geometry of each pair
-//   6. reverse     index of the (j, i, -s) pair for the deterministic force
-//                  gather
-// All FP64 arithmetic that decides membership or is returned uses explicitly
-// rounded operations, so results equal the oracle bit for bit.  The fast
-// build (one-pass enumeration into per-atom slabs) decides candidates near
-// the cutoff in float-float and computes the FP32 pair vectors the same way;
-// the FP64 pair table is filled on demand (ensure_rel64) for the callers
-// that return or consume FP64 geometry.
+//   3. enum        warp per atom: the bin ranges reachable for each shift
+//                  (looked up across the lanes), candidates tested in FP32
+//                  with a safety margin, the ones near the cutoff decided in
+//                  float-float and, within ~1e-6 A of it, by the reference's
+//                  FP64 distance; accepted keys (j << 20 | shift) sorted into
+//                  reference order (warp bitonic sort) in a per-atom slab
+//   4. compact     CSR arrays from the slabs; the FP32 pair vector of the
+//                  canonical half from the float-float image, written to the
+//                  pair and (negated) to its reverse (j, i, -s), whose index
+//                  it finds and links for the deterministic force gather
+// An atom with more than 256 neighbors sends the build through the two-pass
+// path (count, fill, sort_geom with FP64 geometry, reverse).  All FP64
+// arithmetic that decides membership or is returned uses explicitly rounded
+// operations, so results equal the oracle bit for bit; the FP64 pair table is
+// filled on demand (ensure_rel64) for the callers that return or consume FP64
+// geometry.
 #include <cub/cub.cuh>
 #include <cstring>
 
