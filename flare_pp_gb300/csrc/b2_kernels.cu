@@ -1353,6 +1353,25 @@ size_t adjoint_smem_per_warp(const B2Args &a, size_t elem) {
   return (b + 15) & ~(size_t)15;
 }
 
+// Warps per block (4, 2 or 1) for a warp-per-atom kernel with `per` bytes of
+// shared memory per warp: the most resident warps per SM (228 KB of shared
+// memory per SM, 1 KB reserved per block, at most 32 blocks), ties to the
+// larger block.  0 if one warp does not fit in a block.
+static int warps_per_block(size_t per) {
+  int best = 0, best_warps = 0;
+  for (int wpb = 4; wpb >= 1; wpb >>= 1) {
+    const size_t blk = per * wpb;
+    if (blk > 227 * 1024) continue;
+    int blocks = (int)((228 * 1024) / (blk + 1024));
+    if (blocks > 32) blocks = 32;
+    if (blocks * wpb > best_warps) {
+      best_warps = blocks * wpb;
+      best = wpb;
+    }
+  }
+  return best;
+}
+
 template <typename T>
 int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
                       const int *row_of_atom, const int *pair_tab, T *c_out,
@@ -1361,10 +1380,9 @@ int launch_b2_forward(B2Args a, const Neigh &nb, const int *species,
   if (a.noa == 0) return 0;
   a.window = 32;
   const size_t per = fwd_layout<T>(a).total;
-  int wpb = 4;
-  while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
+  const int wpb = warps_per_block(per);
+  if (wpb == 0) return -1;
   size_t smem = per * wpb;
-  if (smem > 227 * 1024) return -1;
   return with_shape<T>(a, [&](auto sh) {
     auto kern = k_b2_forward<T, decltype(sh)>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1387,10 +1405,9 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
   if (a.noa == 0) return 0;
   a.smem_per_warp_adj = a.kind == kB3 ? b3_adjoint_smem_per_warp<T>(a)
                                       : adjoint_smem_per_warp(a, sizeof(T));
-  int wpb = 4;
-  while (wpb > 1 && a.smem_per_warp_adj * wpb > 200 * 1024) wpb >>= 1;
+  const int wpb = warps_per_block(a.smem_per_warp_adj);
+  if (wpb == 0) return -1;
   size_t smem = a.smem_per_warp_adj * wpb;
-  if (smem > 227 * 1024) return -1;
   if (a.kind == kB3) {
     auto kern3 = k_b3_wu<T>;
     if (cudaFuncSetAttribute(kern3, cudaFuncAttributeMaxDynamicSharedMemorySize,
