@@ -173,7 +173,8 @@ int with_shape(const B2Args &a, F &&f) {
 //      the staged neighbors by species (warp ballots);
 //   2. lane = (l, m) column: for each species, run over its listed neighbors
 //      accumulating the N radial channels in registers (plain sums over 16
-//      neighbors, folded into compensated per-channel sums in shared memory);
+//      neighbors, Kahan-folded into per-channel sums within the window; the
+//      folded sum carries over to the next window in shared memory);
 //   3. B2 contraction per radial pair (n1, n2 >= n1) into shared memory with
 //      a compensated norm, then the normalized / split outputs.
 // ---------------------------------------------------------------------------
@@ -194,7 +195,9 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
   size_t st = sizeof(T) * ((size_t)L.W * L.GP + (size_t)a.H * (L.W + 1));
   size_t pb = sizeof(T) * (size_t)a.n_d;
   L.stage = ((st > pb ? st : pb) + 15) & ~(size_t)15;
-  L.csum = (sizeof(T) * 2 * (size_t)sbp + 15) & ~(size_t)15;
+  // FP32: running sums only (compensated within a window); FP64: running
+  // sums and their compensation terms across windows
+  L.csum = (sizeof(T) * (sizeof(T) == 8 ? 2 : 1) * (size_t)sbp + 15) & ~(size_t)15;
   L.lists = (sizeof(int) * ((size_t)a.n_species * L.W + 2 * L.W + a.n_species) + 15) & ~(size_t)15;
   L.cz = a.kind == kB3
              ? (sizeof(T) * 2 * (size_t)a.n_species * a.N * (a.H + 1) + 15) & ~(size_t)15
@@ -228,14 +231,14 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   T *y_s = g_s + (size_t)W * GP;                      // [H][WS]
   T *p_s = reinterpret_cast<T *>(base);               // [n_d] (after staging)
   T *c_s = reinterpret_cast<T *>(base + Lay.stage);   // [NS N][HP] running sums
-  T *cc_s = c_s + sbp;                                // [NS N][HP] compensation
+  T *cc_s = c_s + sbp;  // FP64 only: [NS N][HP] compensation
   int *list = reinterpret_cast<int *>(base + Lay.stage + Lay.csum);  // [NS][W]
   int *cnt_s = list + NS * W;                         // [NS]
   if (atom >= a.noa) return;
 
   for (int k = lane; k < sbp; k += 32) {
     c_s[k] = T(0);
-    cc_s[k] = T(0);
+    if (sizeof(T) == 8) cc_s[k] = T(0);
   }
   const int si = species[atom];
   const int beg = offset[atom], end = offset[atom + 1];
@@ -311,7 +314,8 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
         for (int n = 0; n < kMaxN; n++)
           if (n < N) {
             sum[n] = c_s[(sp * N + n) * HP + lmc];
-            comp[n] = cc_s[(sp * N + n) * HP + lmc];
+            // FP32: compensated within the window and folded at its end
+            comp[n] = sizeof(T) == 8 ? cc_s[(sp * N + n) * HP + lmc] : T(0);
           }
         for (int k0 = 0; k0 < ns_; k0 += 16) {
           T chunk[kMaxN];
@@ -364,19 +368,26 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
 #pragma unroll
           for (int n = 0; n < kMaxN; n++)
             if (n < N) {
-              c_s[(sp * N + n) * HP + lm] = sum[n];
-              cc_s[(sp * N + n) * HP + lm] = comp[n];
+              if (sizeof(T) == 8) {
+                c_s[(sp * N + n) * HP + lm] = sum[n];
+                cc_s[(sp * N + n) * HP + lm] = comp[n];
+              } else {
+                c_s[(sp * N + n) * HP + lm] = sum[n] - comp[n];
+              }
             }
         }
       }
     }
     __syncwarp();
   }
-  // fold the compensation and publish c (unpadded rows in global memory)
+  // (FP64: fold the compensation) publish c (unpadded rows in global memory)
   for (int k = lane; k < sb; k += 32) {
     const int r = k / H, lm = k - r * H;
-    const T v = c_s[r * HP + lm] - cc_s[r * HP + lm];
-    c_s[r * HP + lm] = v;
+    T v = c_s[r * HP + lm];
+    if (sizeof(T) == 8) {
+      v -= cc_s[r * HP + lm];
+      c_s[r * HP + lm] = v;
+    }
     c_out[(size_t)atom * sb + k] = v;
   }
   __syncwarp();
