@@ -323,18 +323,22 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
           for (int n = 0; n < kMaxN; n++) chunk[n] = T(0);
           const int k1 = min(ns_, k0 + 16);
           if constexpr (SH::kN > 0 && sizeof(T) == 4) {
-            // radial row of the neighbor in 16-byte loads (GP = N rounded up to 4)
+            // radial row of the neighbor in 16-byte loads (GP = N rounded up
+            // to 4), channels accumulated in pairs with paired multiply-adds
+            // (pad channels past N are computed and discarded)
             constexpr int G4 = (SH::kN + 3) / 4;
+            float2 c2[2 * G4];
+#pragma unroll
+            for (int j = 0; j < 2 * G4; j++) c2[j] = make_float2(0.f, 0.f);
             auto accum = [&](int b) {
-              const T yv = y_s[lmc * WS + b];
+              const float yv = y_s[lmc * WS + b];
+              const float2 y2 = make_float2(yv, yv);
               const float4 *gb4 = reinterpret_cast<const float4 *>(g_s + (size_t)b * (4 * G4));
 #pragma unroll
               for (int j = 0; j < G4; j++) {
                 const float4 gv = gb4[j];
-                if (4 * j + 0 < SH::kN) chunk[4 * j + 0] += gv.x * yv;
-                if (4 * j + 1 < SH::kN) chunk[4 * j + 1] += gv.y * yv;
-                if (4 * j + 2 < SH::kN) chunk[4 * j + 2] += gv.z * yv;
-                if (4 * j + 3 < SH::kN) chunk[4 * j + 3] += gv.w * yv;
+                c2[2 * j] = ffma2(make_float2(gv.x, gv.y), y2, c2[2 * j]);
+                c2[2 * j + 1] = ffma2(make_float2(gv.z, gv.w), y2, c2[2 * j + 1]);
               }
             };
             // two neighbors per iteration (same summation order)
@@ -345,6 +349,11 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
               accum(b1);
             }
             if (k < k1) accum(ls[k]);
+#pragma unroll
+            for (int j = 0; j < 2 * G4; j++) {
+              if (2 * j < SH::kN) chunk[2 * j] = c2[j].x;
+              if (2 * j + 1 < SH::kN) chunk[2 * j + 1] = c2[j].y;
+            }
           } else {
             for (int k = k0; k < k1; k++) {
               const int b = ls[k];
@@ -997,20 +1006,44 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
                         sizeof(T) == 4 ? T(a.cinv_lo[kc]) : T(0));
     const T *ur = u + (size_t)i * sb + (size_t)sj * N * H;
     T fr = T(0);
-    harmonics_visit<T>(x, y, z, LMAX, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
-      T ag = T(0), bd = T(0);
+    if constexpr (sizeof(T) == 4) {
+      // paired FP32 multiply-adds: (ag, bd) and (f0, f1), (f2, fr) advance
+      // together (each component is the same chain of fmaf as unpaired)
+      float2 gd[kMaxN];
 #pragma unroll
-      for (int n = 0; n < kMaxN; n++)
-        if (n < N) {
-          const T uv = ur[n * H + lm];
-          ag += uv * gr[n];
-          bd += uv * dg[n];
-        }
-      fr += bd * Yv;
-      f[0] += ag * Yx;
-      f[1] += ag * Yy;
-      f[2] += ag * Yz;
-    });
+      for (int n = 0; n < kMaxN; n++) gd[n] = make_float2(gr[n], dg[n]);
+      float2 f01 = make_float2(0.f, 0.f), f2r = make_float2(0.f, 0.f);
+      harmonics_visit_f2(x, y, z, LMAX, [&](int lm, float Yv, float2 Yxy, float Yz) {
+        float2 ab = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int n = 0; n < kMaxN; n++)
+          if (n < N) {
+            const float uv = ur[n * H + lm];
+            ab = ffma2(make_float2(uv, uv), gd[n], ab);
+          }
+        f01 = ffma2(make_float2(ab.x, ab.x), Yxy, f01);
+        f2r = ffma2(ab, make_float2(Yz, Yv), f2r);
+      });
+      f[0] = f01.x;
+      f[1] = f01.y;
+      f[2] = f2r.x;
+      fr = f2r.y;
+    } else {
+      harmonics_visit<T>(x, y, z, LMAX, [&](int lm, T Yv, T Yx, T Yy, T Yz) {
+        T ag = T(0), bd = T(0);
+#pragma unroll
+        for (int n = 0; n < kMaxN; n++)
+          if (n < N) {
+            const T uv = ur[n * H + lm];
+            ag += uv * gr[n];
+            bd += uv * dg[n];
+          }
+        fr += bd * Yv;
+        f[0] += ag * Yx;
+        f[1] += ag * Yy;
+        f[2] += ag * Yz;
+      });
+    }
     const T ir = T(1) / r;
     f[0] += fr * x * ir;
     f[1] += fr * y * ir;

@@ -301,4 +301,76 @@ __device__ __forceinline__ void harmonics_visit(T x, T y, T z, int lmax, Visit v
   }
 }
 
+// FP32 harmonics with gradients handed to visit(lm, Y, (dY/dx, dY/dy), dY/dz)
+// with the x and y components formed together by paired FP32 instructions
+// (the same recurrence and normalisation as harmonics_visit<float>).
+template <typename Visit>
+__device__ __forceinline__ void harmonics_visit_f2(float x, float y, float z, int lmax,
+                                                   Visit visit) {
+  const float r = sqrtf(x * x + y * y + z * z);
+  const float ir = 1.0f / r;
+  const float ux = x * ir, uy = y * ir, uz = z * ir;
+  const float2 uxy = make_float2(ux, uy), ir2 = make_float2(ir, ir);
+  float A = 1.0f, B = 0.0f, Aprev = 1.0f, Bprev = 0.0f;
+#pragma unroll
+  for (int m = 0; m <= lmax; m++) {
+    if (m > 0) {
+      Aprev = A;
+      Bprev = B;
+      const float a2 = ux * A - uy * B;
+      const float b2 = uy * A + ux * B;
+      A = a2;
+      B = b2;
+    }
+    const float2 Axy = make_float2(float(m) * Aprev, -float(m) * Bprev);
+    const float2 Bxy = make_float2(float(m) * Bprev, float(m) * Aprev);
+    float q2 = 0, q1 = 0, qz2 = 0, qz1 = 0, qr2 = 0, qr1 = 0;
+#pragma unroll
+    for (int l = m; l <= lmax; l++) {
+      float q, qz, qr;
+      if (l == m) {
+        q = c_harm.dfact_f[m];
+        qz = 0.0f;
+        qr = 0.0f;
+      } else if (l == m + 1) {
+        q = float(2 * m + 1) * uz * q1;
+        qz = float(2 * m + 1) * q1;
+        qr = 0.0f;
+      } else {
+        // division-free: the D_lm factor is divided out by the normalisation
+        const float a = float(2 * l - 1);
+        const float bc = float((l + m - 1) * (l - 1 >= m + 2 ? l - 1 - m : 1));
+        q = a * uz * q1 - bc * q2;
+        qz = a * (q1 + uz * qz1) - bc * qz2;
+        qr = a * uz * qr1 - bc * (q2 + qr2);
+      }
+      q2 = q1;
+      q1 = q;
+      qz2 = qz1;
+      qz1 = qz;
+      qr2 = qr1;
+      qr1 = qr;
+      const int kn = l * (kMaxL + 1) + m;
+      const float nh = c_harm.norm_hi[kn], nl = c_harm.norm_lo[kn];
+      const float2 nh2 = make_float2(nh, nh), nl2 = make_float2(nl, nl);
+      const float2 q2v = make_float2(q, q);
+      const float tq = qr * 2.0f;
+      auto emit = [&](int lm, float C, float2 Cxy) {
+        const float qc = q * C;
+        const float R = fmaf(nh, qc, nl * qc);
+        const float t = tq * C;
+        const float2 sxy = ffma2(make_float2(t, t), uxy, fmul2(q2v, Cxy));
+        const float2 Rxy = ffma2(nh2, sxy, fmul2(nl2, sxy));
+        const float sz = (qz + tq * uz) * C;
+        const float Rz = fmaf(nh, sz, nl * sz);
+        const float lR = float(l) * R;
+        const float2 gxy = fmul2(ffma2(make_float2(-lR, -lR), uxy, Rxy), ir2);
+        visit(lm, R, gxy, (Rz - lR * uz) * ir);
+      };
+      emit(l * l + l + m, A, Axy);
+      if (m > 0) emit(l * l + l - m, B, Bxy);
+    }
+  }
+}
+
 }  // namespace fpp

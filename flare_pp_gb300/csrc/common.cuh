@@ -42,6 +42,27 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
+// Two independent fused multiply-adds (round to nearest) in one paired FP32
+// instruction: d = a * b + c lane by lane, the same results as two fmaf.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const unsigned long long *>(&a)),
+        "l"(*reinterpret_cast<const unsigned long long *>(&b)),
+        "l"(*reinterpret_cast<const unsigned long long *>(&c)));
+  return *reinterpret_cast<const float2 *>(&d);
+}
+
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const unsigned long long *>(&a)),
+        "l"(*reinterpret_cast<const unsigned long long *>(&b)));
+  return *reinterpret_cast<const float2 *>(&d);
+}
+
 // Kahan-Babuska (Neumaier) compensated accumulator in FP32.
 struct CompSum {
   float s, c;
