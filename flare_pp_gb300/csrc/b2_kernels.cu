@@ -738,19 +738,55 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
         acc[n] = T(0);
       }
       const T *wl = w_s + l;
+      auto wq = [&](int n1, int n2) {  // packed w of the pair n1 <= n2
+        return wl[(n1 * NR - (n1 * (n1 - 1)) / 2 + (n2 - n1)) * LL];
+      };
+      if constexpr (sizeof(T) == 4 && (NR % 2) == 0) {
+        // 2 x 2 blocks of (n1, n2) with paired multiply-adds: rows 2a, 2a+1
+        // of u advance together
+        float2 a2[NR / 2], c2[NR / 2];
 #pragma unroll
-      for (int n1 = 0; n1 < NR; n1++)
+        for (int a = 0; a < NR / 2; a++) {
+          a2[a] = make_float2(0.f, 0.f);
+          c2[a] = make_float2(creg[2 * a], creg[2 * a + 1]);
+        }
 #pragma unroll
-        for (int n2 = n1; n2 < NR; n2++) {
-          const int q = n1 * NR - (n1 * (n1 - 1)) / 2 + (n2 - n1);
-          const T w = wl[q * LL];
-          if (n1 == n2) {
-            acc[n1] += T(2) * w * creg[n1];
-          } else {
-            acc[n1] += w * creg[n2];
-            acc[n2] += w * creg[n1];
+        for (int a = 0; a < NR / 2; a++) {
+          {  // diagonal block: (2a, 2a), (2a, 2a+1), (2a+1, 2a+1)
+            const float w00 = wq(2 * a, 2 * a), w01 = wq(2 * a, 2 * a + 1);
+            const float w11 = wq(2 * a + 1, 2 * a + 1);
+            a2[a] = ffma2(make_float2(2.0f * w00, w01), make_float2(c2[a].x, c2[a].x), a2[a]);
+            a2[a] = ffma2(make_float2(w01, 2.0f * w11), make_float2(c2[a].y, c2[a].y), a2[a]);
+          }
+#pragma unroll
+          for (int b = a + 1; b < NR / 2; b++) {
+            const float w00 = wq(2 * a, 2 * b), w01 = wq(2 * a, 2 * b + 1);
+            const float w10 = wq(2 * a + 1, 2 * b), w11 = wq(2 * a + 1, 2 * b + 1);
+            a2[a] = ffma2(make_float2(w00, w10), make_float2(c2[b].x, c2[b].x), a2[a]);
+            a2[a] = ffma2(make_float2(w01, w11), make_float2(c2[b].y, c2[b].y), a2[a]);
+            a2[b] = ffma2(make_float2(w00, w01), make_float2(c2[a].x, c2[a].x), a2[b]);
+            a2[b] = ffma2(make_float2(w10, w11), make_float2(c2[a].y, c2[a].y), a2[b]);
           }
         }
+#pragma unroll
+        for (int a = 0; a < NR / 2; a++) {
+          acc[2 * a] = a2[a].x;
+          acc[2 * a + 1] = a2[a].y;
+        }
+      } else {
+#pragma unroll
+        for (int n1 = 0; n1 < NR; n1++)
+#pragma unroll
+          for (int n2 = n1; n2 < NR; n2++) {
+            const T w = wq(n1, n2);
+            if (n1 == n2) {
+              acc[n1] += T(2) * w * creg[n1];
+            } else {
+              acc[n1] += w * creg[n2];
+              acc[n2] += w * creg[n1];
+            }
+          }
+      }
 #pragma unroll
       for (int n1 = 0; n1 < NR; n1++) u_out[(size_t)atom * sb + n1 * H + lm] = acc[n1];
     } else {
