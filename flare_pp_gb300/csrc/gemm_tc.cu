@@ -381,14 +381,17 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
           float *dst = p.V + (size_t)(p.row0[g] + r) * p.ldv + n0 + c;
           const int ncol = p.N - (n0 + c);
           if (ncol >= 32) {
+            // 32-byte stores: each lane writes whole sectors of its row
 #pragma unroll
-            for (int i = 0; i < 32; i += 4) {
-              float4 o;
-              o.x = (v0[i + 0] + v1[i + 0] * (1.0f / 2048.0f)) * sc;
-              o.y = (v0[i + 1] + v1[i + 1] * (1.0f / 2048.0f)) * sc;
-              o.z = (v0[i + 2] + v1[i + 2] * (1.0f / 2048.0f)) * sc;
-              o.w = (v0[i + 3] + v1[i + 3] * (1.0f / 2048.0f)) * sc;
-              *reinterpret_cast<float4 *>(dst + i) = o;
+            for (int i = 0; i < 32; i += 8) {
+              float o[8];
+#pragma unroll
+              for (int j = 0; j < 8; j++) o[j] = (v0[i + j] + v1[i + j] * (1.0f / 2048.0f)) * sc;
+              asm volatile(
+                  "st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst + i),
+                  "f"(o[0]), "f"(o[1]), "f"(o[2]), "f"(o[3]), "f"(o[4]), "f"(o[5]), "f"(o[6]),
+                  "f"(o[7])
+                  : "memory");
             }
           } else {
             for (int i = 0; i < 32; i++)
@@ -450,7 +453,8 @@ int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream) {
   if (g.n_groups <= 0 || g.N <= 0) return 0;
   if (g.n_groups > kGemmMaxGroups) return -2;
   if ((g.lda * 2) % 16 != 0 || ((uintptr_t)g.a_hi | (uintptr_t)g.a_lo) % 16 != 0) return -2;
-  if (g.ldv % 4 != 0 || ((uintptr_t)g.V % 16) != 0 || g.K > g.lda) return -2;
+  // V rows take 32-byte stores: 32-byte aligned rows
+  if (g.ldv % 8 != 0 || ((uintptr_t)g.V % 32) != 0 || g.K > g.lda) return -2;
   GroupedParams p;
   std::memset(&p, 0, sizeof(p));
   if (make_map(&p.a_hi, g.a_hi, g.K, g.a_rows, g.lda, BM) ||
