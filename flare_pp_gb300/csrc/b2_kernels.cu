@@ -92,7 +92,7 @@ template <typename T> struct Acc {
   __device__ __forceinline__ void add(T x) {
     if (sizeof(T) == 4) {
       T t = s + x;
-      if (fabs(s) >= fabs(x))
+      if (fabs_t(s) >= fabs_t(x))
         c += (s - t) + x;
       else
         c += (x - t) + s;
@@ -449,9 +449,9 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
       for (int l = 0; l < LL; l++) {
         T v = x[l * l] * y[l * l];
 #pragma unroll
-        for (int m = l * l + 1; m < (l + 1) * (l + 1); m++) v = fma(x[m], y[m], v);
+        for (int m = l * l + 1; m < (l + 1) * (l + 1); m++) v = fma_t(x[m], y[m], v);
         p_s[q * LL + l] = v;
-        sq = fma(v, v, sq);
+        sq = fma_t(v, v, sq);
       }
       nacc.add(sq);
     }
@@ -1222,7 +1222,8 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
               const float4 *__restrict__ rel32, const float4 *__restrict__ pair_f,
               const double *__restrict__ atom_e, double *__restrict__ forces,
               double *__restrict__ partial) {
-  __shared__ double sm[kGatherWarps][10];
+  __shared__ double sm_e[kGatherWarps];
+  __shared__ float2 sm_v[kGatherWarps][9];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / kGatherLanes, gl = lane % kGatherLanes;  // group, lane in group
   constexpr int kGroups = 32 / kGatherLanes;
@@ -1283,21 +1284,28 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
     }
   }
   // the group leaders' virial (other lanes hold zeros) and energies, summed
-  // over the warp in a fixed order
+  // over the warp and then the block in a fixed order; the virial stays
+  // float-float until one conversion per block (FP64 instructions are scarce)
 #pragma unroll
   for (int k = 0; k < 9; k++) ff_warp_sum(th[k], tl[k]);
   esum = warp_sum(esum);
   if (lane == 0) {
-    sm[warp][0] = esum;
+    sm_e[warp] = esum;
 #pragma unroll
-    for (int k = 0; k < 9; k++) sm[warp][1 + k] = double(th[k]) + double(tl[k]);
+    for (int k = 0; k < 9; k++) sm_v[warp][k] = make_float2(th[k], tl[k]);
   }
   __syncthreads();
-  if (threadIdx.x < 10) {
+  if (threadIdx.x == 0) {
     double v = 0.0;
 #pragma unroll
-    for (int w = 0; w < kGatherWarps; w++) v += sm[w][threadIdx.x];
-    partial[(size_t)blockIdx.x * 10 + threadIdx.x] = v;
+    for (int w = 0; w < kGatherWarps; w++) v += sm_e[w];
+    partial[(size_t)blockIdx.x * 10] = v;
+  } else if (threadIdx.x < 10) {
+    const int k = threadIdx.x - 1;
+    ff t = ff{sm_v[0][k].x, sm_v[0][k].y};
+#pragma unroll
+    for (int w = 1; w < kGatherWarps; w++) t = ff_add(t, ff{sm_v[w][k].x, sm_v[w][k].y});
+    partial[(size_t)blockIdx.x * 10 + threadIdx.x] = double(t.hi) + double(t.lo);
   }
 }
 

@@ -42,6 +42,16 @@ __device__ __forceinline__ float norm_scale(int k, float v) {
 }
 
 // g_n and dg_n/dr into out_g[n * stride], out_dg[n * stride].
+// (cos(pi r / rc) + 1) / 2 and its derivative, out of line: the quadratic
+// cutoff is the common case, and the trigonometric code (whose range reduction
+// has FP64 steps) stays off its instruction stream.
+template <typename T>
+static __device__ __noinline__ void cosine_cutoff(T r, T rc, T &fc, T &dfc) {
+  const T pi = T(3.14159265358979323846);
+  fc = T(0.5) * (cos_t(pi * r / rc) + T(1));
+  dfc = -pi * sin_t(pi * r / rc) / (T(2) * rc);
+}
+
 // FP32: the argument is (r - r1) (cinv_hi + cinv_lo) with the reciprocal
 // 1 / (rc - r1) split hi/lo in FP64 (when cinv_hi is given, else divided).
 template <typename T>
@@ -57,9 +67,7 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
     fc = d * d;
     dfc = T(2) * d;
   } else {
-    const T pi = T(3.14159265358979323846);
-    fc = T(0.5) * (cos(pi * r / rc) + T(1));
-    dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
+    cosine_cutoff(r, rc, fc, dfc);
   }
   const bool inside = !(r < r1 || r > rc);
   // x by a correctly rounded division or the hi/lo reciprocal: a rounded
@@ -68,7 +76,7 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
   T c, x;
   if (cinv_hi != T(0)) {
     c = cinv_hi;
-    x = fma(r - r1, cinv_hi, (r - r1) * cinv_lo);
+    x = fma_t(r - r1, cinv_hi, (r - r1) * cinv_lo);
   } else {
     c = T(1) / (rc - r1);
     x = (r - r1) / (rc - r1);
@@ -110,15 +118,13 @@ __device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cut
     fc = d * d;
     dfc = T(2) * d;
   } else {
-    const T pi = T(3.14159265358979323846);
-    fc = T(0.5) * (cos(pi * r / rc) + T(1));
-    dfc = -pi * sin(pi * r / rc) / (T(2) * rc);
+    cosine_cutoff(r, rc, fc, dfc);
   }
   const bool inside = !(r < r1 || r > rc);
   T c, x;
   if (cinv_hi != T(0)) {
     c = cinv_hi;
-    x = fma(r - r1, cinv_hi, (r - r1) * cinv_lo);
+    x = fma_t(r - r1, cinv_hi, (r - r1) * cinv_lo);
   } else {
     c = T(1) / (rc - r1);
     x = (r - r1) / (rc - r1);
@@ -152,7 +158,7 @@ __device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cut
 template <typename T>
 __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
                                                T *grad, int stride) {
-  const T r = sqrt(x * x + y * y + z * z);
+  const T r = sqrt_t(x * x + y * y + z * z);
   const T ir = T(1) / r;
   const T ux = x * ir, uy = y * ir, uz = z * ir;
   T A = T(1), B = T(0), Aprev = T(1), Bprev = T(0);
@@ -233,7 +239,7 @@ __device__ __forceinline__ void real_harmonics(T x, T y, T z, int lmax, T *out,
 // dY/dz) one by one as the recurrence produces them (nothing is stored).
 template <typename T, typename Visit>
 __device__ __forceinline__ void harmonics_visit(T x, T y, T z, int lmax, Visit visit) {
-  const T r = sqrt(x * x + y * y + z * z);
+  const T r = sqrt_t(x * x + y * y + z * z);
   const T ir = T(1) / r;
   const T ux = x * ir, uy = y * ir, uz = z * ir;
   T A = T(1), B = T(0), Aprev = T(1), Bprev = T(0);

@@ -42,6 +42,22 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
+// Fused multiply-add in the argument's own precision (an unqualified fma on
+// floats can resolve to the double overload, i.e. FP64 instructions).
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) {
+  return __fma_rn(a, b, c);
+}
+
+__device__ __forceinline__ float sqrt_t(float a) { return sqrtf(a); }
+__device__ __forceinline__ double sqrt_t(double a) { return sqrt(a); }
+__device__ __forceinline__ float fabs_t(float a) { return fabsf(a); }
+__device__ __forceinline__ double fabs_t(double a) { return fabs(a); }
+__device__ __forceinline__ float cos_t(float a) { return cosf(a); }
+__device__ __forceinline__ double cos_t(double a) { return cos(a); }
+__device__ __forceinline__ float sin_t(float a) { return sinf(a); }
+__device__ __forceinline__ double sin_t(double a) { return sin(a); }
+
 // Two independent fused multiply-adds (round to nearest) in one paired FP32
 // instruction: d = a * b + c lane by lane, the same results as two fmaf.
 __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
