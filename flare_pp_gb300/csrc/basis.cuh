@@ -53,7 +53,8 @@ static __device__ __noinline__ void cosine_cutoff(T r, T rc, T &fc, T &dfc) {
 }
 
 // FP32: the argument is (r - r1) (cinv_hi + cinv_lo) with the reciprocal
-// 1 / (rc - r1) split hi/lo in FP64 (when cinv_hi is given, else divided).
+// 1 / (rc - r1) split hi/lo in FP64 (FP32 callers always pass it); FP64: the
+// correctly rounded division.
 template <typename T>
 __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_kind,
                                              T *out_g, T *out_dg, int stride,
@@ -70,11 +71,13 @@ __device__ __forceinline__ void radial_basis(T r, T r1, T rc, int N, int cutoff_
     cosine_cutoff(r, rc, fc, dfc);
   }
   const bool inside = !(r < r1 || r > rc);
-  // x by a correctly rounded division or the hi/lo reciprocal: a rounded
-  // reciprocal alone would shift every pair's argument the same way and bias
-  // the descriptors in FP32
+  // x by the hi/lo reciprocal (FP32) or a correctly rounded division (FP64):
+  // a rounded reciprocal alone would shift every pair's argument the same way
+  // and bias the descriptors in FP32.  FP32 has no division fallback: the
+  // divide's special-case handling issued FP64-pipe instructions even where
+  // a branch around it was never taken.
   T c, x;
-  if (cinv_hi != T(0)) {
+  if constexpr (sizeof(T) == 4) {
     c = cinv_hi;
     x = fma_t(r - r1, cinv_hi, (r - r1) * cinv_lo);
   } else {
@@ -122,7 +125,7 @@ __device__ __forceinline__ void radial_basis_reg(T r, T r1, T rc, int N, int cut
   }
   const bool inside = !(r < r1 || r > rc);
   T c, x;
-  if (cinv_hi != T(0)) {
+  if constexpr (sizeof(T) == 4) {  // split reciprocal, as in radial_basis
     c = cinv_hi;
     x = fma_t(r - r1, cinv_hi, (r - r1) * cinv_lo);
   } else {

@@ -635,16 +635,16 @@ __global__ void k_sort_geom(int noa, CellDev cd, const dvec4 *__restrict__ wp,
   }
 }
 
-// Reverse pair: (i, j, s) -> (j, i, -s), found by binary search in j's list.
+// Reverse pair: (i, j, s) -> (j, i, -s), found by binary search in j's list
+// (the two-pass build; the one-pass build links pairs in k_compact_geom).
 __global__ void k_reverse(long long n_pairs, CellDev cd,
                           const int *__restrict__ offset,
                           const long long *__restrict__ keys,
                           const int *__restrict__ nbr_i,
                           const int *__restrict__ nbr_j, int *__restrict__ rev,
-                          DeviceStatus *st, int mirror, float4 *rel32) {
+                          DeviceStatus *st) {
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_pairs) return;
-  const int center = (cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep;
   int i = nbr_i[p], j = nbr_j[p];
   int sidx = (int)(keys[p] & kKeyMask);
   long long want = ((long long)i << kKeyBits) | (cd.n_shift - 1 - sidx);
@@ -663,12 +663,6 @@ __global__ void k_reverse(long long n_pairs, CellDev cd,
   }
   if (found < 0) set_status(st, FPP_ERR_NUMERIC, 6, (int)p);
   rev[p] = found;
-  // pairs below the canonical half take the negated image of their reverse
-  // pair (computed by k_compact_geom; the other builds compute both, equal)
-  if (found >= 0 && mirror && keys[p] <= (((long long)i << kKeyBits) | center)) {
-    const float4 r32 = rel32[found];
-    rel32[p] = make_float4(-r32.x, -r32.y, -r32.z, r32.w);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -936,8 +930,7 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   }
   k_reverse<<<ceil_div(total, tb), tb, 0, stream>>>(
       total, cd, st.nbr_offset.as<int>(), st.nbr_key.as<long long>(),
-      st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst, overflow ? 0 : 1,
-      st.nbr_rel32.as<float4>());
+      st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_rev.as<int>(), dst);
   FPP_CUDA(cudaGetLastError());
   return FPP_OK;
 }

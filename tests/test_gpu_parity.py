@@ -35,6 +35,11 @@ def _cases():
                 np.array([[0.2, 0.3, 0.4]]), 5.0))
     cell, sp, pos = synth.bcc_alloy((10, 10, 10), 202)
     out.append(("bcc2000", cell, sp, pos, 5.5))
+    # ~320 neighbors per atom: more than the one-pass build's 256-key slab,
+    # so the list comes from the two-pass (count / fill / sort) build
+    dense = np.array([[0.0, 0.0, 0.0], [1.5, 1.5, 0.0], [1.5, 0.0, 1.5], [0.0, 1.5, 1.5]])
+    out.append(("dense_two_pass", np.eye(3) * 3.0, np.array([0, 1, 0, 1]),
+                dense + rng.uniform(-0.05, 0.05, size=(4, 3)), 8.0))
     return out
 
 
