@@ -46,13 +46,19 @@ void fill_fp32_cutoffs(B2Args &a) {
 // Descriptor filter r <= rc of b2.cpp:277 / b3.cpp:258 for pair p of atom i,
 // FP32 first: only pairs within the band around rc use the FP64 distance,
 // recomputed from the positions (or read from the caller's FP64 table).
+static __device__ __noinline__ bool band_keep(const dvec4 *__restrict__ rel,
+                                              const NbGeom *geom, int i, long long p,
+                                              double rc) {
+  const double r = geom ? exact_pair_dist(*geom, i, p) : rel[p].x;
+  return r <= rc;
+}
+
 __device__ __forceinline__ bool keep_pair32(const B2Args &a, int k, float rf,
                                             const dvec4 *__restrict__ rel,
                                             const NbGeom *geom, int i, long long p) {
   if (rf < a.cut_lo[k]) return true;
   if (rf > a.cut_hi[k]) return false;
-  const double r = geom ? exact_pair_dist(*geom, i, p) : rel[p].x;
-  return r <= a.cutoffs[k];
+  return band_keep(rel, geom, i, p, a.cutoffs[k]);  // out of line: FP64
 }
 int b3_n_ls_host(int lmax) { return b3_n_ls(lmax); }
 
@@ -106,6 +112,14 @@ template <typename T> struct Acc {
 // x^2 + y^2 + z^2 of a pair vector, rounded as the host computes it.
 __device__ __forceinline__ double rsq_exact(const dvec4 &r) {
   return dadd(dadd(dmul(r.y, r.y), dmul(r.z, r.z)), dmul(r.w, r.w));
+}
+
+// The pair style's filter rsq < rc^2 (pair_flare.cpp:150) for the FP32
+// kernels, out of line: inline, its FP64 instructions were issued (predicated
+// off) for every pair of the non-strict default as well.
+static __device__ __noinline__ bool strict_keep(const dvec4 *__restrict__ rel, long long p,
+                                                double rc) {
+  return rsq_exact(rel[p]) < dmul(rc, rc);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -273,12 +287,10 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
           y = T(rf.y);
           z = T(rf.z);
           r = T(rf.w);
-          if (a.strict) {
-            const dvec4 rd = rel[p];
-            keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
-          } else {
+          if (a.strict)
+            keep = strict_keep(rel, p, a.cutoffs[kc]);
+          else
             keep = keep_pair32(a, kc, rf.w, rel, geom, atom, p);
-          }
           r1t = T(a.r1f);
           rct = T(a.cutoffs32[kc]);
         }
@@ -566,7 +578,7 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
   } else if (g.mode == kWFromV2 && (nd & 3) == 0) {
     // the mixed power-2 form below, four consecutive entries per lane and
     // 16-byte (8-byte for the fp16 planes) loads; |p| and E as float-float
-    const bool empty = nrm32.x * nrm32.x < float(g.empty_thresh);
+    const bool empty = nrm32.x * nrm32.x < g.empty_thresh_f;
     const int nq = nd >> 2;
     const float4 *V4 = reinterpret_cast<const float4 *>(g.V32 + (size_t)row * g.ldv);
     const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
@@ -650,7 +662,7 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
     //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
     //            g = beta pbar, c0 = pbar^T beta pbar;  dE/dp = 2 (g + V - E phat)/|p|
     //   power 1: E = phat . beta1,                      dE/dp = (beta1 - E phat)/|p|
-    const bool empty = nrm32.x * nrm32.x < float(g.empty_thresh);
+    const bool empty = nrm32.x * nrm32.x < g.empty_thresh_f;
     Acc<float> acc;
     for (int d = lane; d < nd; d += 32) {
       const size_t o = (size_t)row * g.ldp + d;
@@ -1025,12 +1037,10 @@ k_pair_force(B2Args a, int strict, long long n_pairs, const int *__restrict__ nb
     y = T(rf.y);
     z = T(rf.z);
     r = T(rf.w);
-    if (strict) {
-      const dvec4 rd = rel[p];
-      keep = rsq_exact(rd) < dmul(a.cutoffs[kc], a.cutoffs[kc]);
-    } else {
+    if (strict)
+      keep = strict_keep(rel, p, a.cutoffs[kc]);
+    else
       keep = keep_pair32(a, kc, rf.w, rel, geom, i, p);
-    }
     r1t = T(a.r1f);
     rct = T(a.cutoffs32[kc]);
   }

@@ -51,6 +51,7 @@ struct AdjArgs {
   int mode;              // WMode
   int strict;            // pair filter rsq < rc^2 (pair style) instead of r <= rc
   double empty_thresh;   // on |p|^2 for the mapped forms
+  float empty_thresh_f;  // the same for the FP32 kernels
   // mapped power 2: V = beta phat rows (one of V32 / V64), phat operands
   const float *V32;
   const double *V64;

@@ -660,6 +660,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
   g.mode = m->beta_power == 2 ? kWFromV2 : kWFromV1;
   g.strict = strict;
   g.empty_thresh = 1e-8;
+  g.empty_thresh_f = 1e-8f;
   g.ldp = ldp;
   g.ldv = ldp;
   g.beta1 = m->beta1.as<double>();
