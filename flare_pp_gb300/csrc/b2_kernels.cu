@@ -220,8 +220,10 @@ __host__ __device__ inline FwdLayout<T> fwd_layout(const B2Args &a) {
   return L;
 }
 
+// FP32: registers capped for six blocks of four warps per SM (the shared
+// memory allows six); FP64: no cap (it would spill)
 template <typename T, typename SH>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 1)
 k_b2_forward(B2Args a, const int *__restrict__ offset,
              const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32, const NbGeom *geom,
              const int *__restrict__ nbr_s, const int *__restrict__ species,
@@ -426,7 +428,49 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     __syncwarp();
     for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
   }
-  if constexpr (SH::kL1 > 0) {
+  if constexpr (SH::kL1 > 0 && sizeof(T) == 4) {
+    // shape known, FP32: the lane's pairs q and q + 32 advance together with
+    // paired multiply-adds; the c rows stream through 16-byte loads and each
+    // entry m feeds the chain of its l, so every p value is the same chain of
+    // fmaf as for one pair at a time
+    constexpr int LL = SH::kL1, HH = LL * LL, H4 = (HH + 3) / 4;
+    auto l_of = [](int m) { int l = 0; while ((l + 1) * (l + 1) <= m) l++; return l; };
+    for (int q = lane; q < npair; q += 64) {
+      const int qb = q + 32;
+      const bool has_b = qb < npair;
+      const int pa = pair_tab[q], pb = has_b ? pair_tab[qb] : pa;
+      const float4 *xa = reinterpret_cast<const float4 *>(c_s + (pa & 0xffff) * HP);
+      const float4 *ya = reinterpret_cast<const float4 *>(c_s + (pa >> 16) * HP);
+      const float4 *xb = reinterpret_cast<const float4 *>(c_s + (pb & 0xffff) * HP);
+      const float4 *yb = reinterpret_cast<const float4 *>(c_s + (pb >> 16) * HP);
+      float2 v[LL];
+#pragma unroll
+      for (int l = 0; l < LL; l++) v[l] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < H4; k++) {
+        const float4 ua = xa[k], wa = ya[k], ub = xb[k], wb = yb[k];
+        const float au[4] = {ua.x, ua.y, ua.z, ua.w}, aw[4] = {wa.x, wa.y, wa.z, wa.w};
+        const float bu[4] = {ub.x, ub.y, ub.z, ub.w}, bw[4] = {wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int m = 4 * k + j;
+          if (m < HH) {
+            const int l = l_of(m);
+            v[l] = ffma2(make_float2(au[j], bu[j]), make_float2(aw[j], bw[j]), v[l]);
+          }
+        }
+      }
+      float2 sq = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int l = 0; l < LL; l++) {
+        p_s[q * LL + l] = v[l].x;
+        if (has_b) p_s[qb * LL + l] = v[l].y;
+        sq = ffma2(v[l], v[l], sq);
+      }
+      nacc.add(sq.x);
+      if (has_b) nacc.add(sq.y);
+    }
+  } else if constexpr (SH::kL1 > 0) {
     // shape known: both c rows in registers through 16-byte loads
     constexpr int LL = SH::kL1, HH = LL * LL, H4 = (HH + 3) / 4;
     for (int q = lane; q < npair; q += 32) {
