@@ -420,11 +420,10 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   const int npair = a.kind == kB3 ? 0 : nd / L1;
   Acc<T> nacc;
   if (a.kind == kB3) {
-    T *zr = reinterpret_cast<T *>(base + Lay.stage + Lay.csum + Lay.lists);
-    T *zi = zr + (size_t)NS * N * (H + 1);
-    b3_to_complex<T>(c_s, NS * N, H, zr, zi, lane, HP);
+    V2<T> *z = reinterpret_cast<V2<T> *>(base + Lay.stage + Lay.csum + Lay.lists);
+    b3_to_complex2<T>(c_s, NS * N, H, z, lane, HP);
     __syncwarp();
-    b3_contract<T>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, zr, zi, p_s, lane);
+    b3_contract<T>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, z, p_s, lane);
     __syncwarp();
     for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
   }
@@ -876,8 +875,9 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
 template <typename T>
 __host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a) {
   const size_t nr = (size_t)a.n_species * a.N;
-  // w, complex c, summed u, and per-lane private rows of the lane's triple
-  size_t b = sizeof(T) * ((size_t)a.n_d + 2 * nr * (a.H + 1) + 2 * nr * a.H +
+  // w (padded to 4 entries), complex c, summed u, and per-lane private rows of
+  // the lane's triple (complex entries interleaved)
+  size_t b = sizeof(T) * ((size_t)((a.n_d + 3) & ~3) + 2 * nr * (a.H + 1) + 2 * nr * a.H +
                           6 * (size_t)a.H * 32);
   return (b + 15) & ~(size_t)15;
 }
@@ -895,12 +895,10 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const int H = a.H, H1 = a.H + 1, nd = a.n_d;
   const int nr = a.n_species * a.N, sb = nr * H;
   unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);  // [nd]
-  T *zr = w_s + nd;                      // [nr][H+1]
-  T *zi = zr + (size_t)nr * H1;
-  T *ur = zi + (size_t)nr * H1;          // [sb] summed u (re)
-  T *ui = ur + sb;                       // [sb] (im)
-  T *up = ui + sb;                       // [3][H][2][32] per-lane private rows
+  T *w_s = reinterpret_cast<T *>(base);                        // [nd]
+  V2<T> *z = reinterpret_cast<V2<T> *>(w_s + ((nd + 3) & ~3));  // [nr][H+1] complex c
+  V2<T> *u2 = z + (size_t)nr * H1;                             // [sb] summed u
+  V2<T> *up = u2 + sb;                                         // [3 H][32] private rows
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
@@ -908,17 +906,18 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
   const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
                                       : make_float2(0.0f, 0.0f);
-  // real c staged through ur (free until the reduction below)
-  for (int k = lane; k < sb; k += 32) ur[k] = c_in[(size_t)atom * sb + k];
+  // real c staged through u2 (free until the accumulation below)
+  T *cst = reinterpret_cast<T *>(u2);
+  for (int k = lane; k < sb; k += 32) cst[k] = c_in[(size_t)atom * sb + k];
   const double e =
       adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
-  b3_to_complex<T>(ur, nr, H, zr, zi, lane);
+  b3_to_complex2<T>(cst, nr, H, z, lane);
   __syncwarp();
-  for (int k = lane; k < sb; k += 32) ur[k] = ui[k] = T(0);
+  for (int k = lane; k < sb; k += 32) u2[k] = V2<T>{T(0), T(0)};
   __syncwarp();
-  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, zr, zi, w_s, up, ur, ui, lane);
+  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, z, w_s, up, u2, lane);
   // dE/dc_real: for m > 0 with u+ = u[l, m], u- = u[l, -m], s = (-1)^m:
   //   dE/dR = (s Re u+ + Re u-) / sqrt 2,  dE/dS = (Im u- - s Im u+) / sqrt 2
   const T is2 = T(0.70710678118654752440);
@@ -932,11 +931,11 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
     const T sg = (am & 1) ? T(-1) : T(1);
     T v;
     if (m == 0)
-      v = ur[k];
+      v = u2[k].x;
     else if (m > 0)
-      v = (sg * ur[kp] + ur[km]) * is2;
+      v = (sg * u2[kp].x + u2[km].x) * is2;
     else
-      v = (ui[km] - sg * ui[kp]) * is2;
+      v = (u2[km].y - sg * u2[kp].y) * is2;
     u_out[(size_t)atom * sb + k] = v;
   }
 }

@@ -163,31 +163,65 @@ __device__ __forceinline__ void b3_to_complex(const T *__restrict__ c, int nr, i
   }
 }
 
+// (re, im) pairs for 8-byte (FP32) / 16-byte (FP64) shared-memory accesses.
+template <typename T> struct V2T;
+template <> struct V2T<float> { using type = float2; };
+template <> struct V2T<double> { using type = double2; };
+template <typename T> using V2 = typename V2T<T>::type;
+
+// b3_to_complex with the complex block interleaved: z[n * (H + 1) + lm] = (re, im).
+template <typename T>
+__device__ __forceinline__ void b3_to_complex2(const T *__restrict__ c, int nr, int H,
+                                               V2<T> *__restrict__ z, int lane, int ldc = -1) {
+  const int HC = ldc < 0 ? H : ldc;
+  const T is2 = T(0.70710678118654752440);
+  for (int k = lane; k < nr * H; k += 32) {
+    const int n = k / H, lm = k - n * H;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) l++;
+    const int m = lm - l * l - l;
+    const int am = m < 0 ? -m : m;
+    const T R = c[n * HC + l * l + l + am];
+    const T S = c[n * HC + l * l + l - am];
+    V2<T> v;
+    if (m == 0) {
+      v.x = R;
+      v.y = T(0);
+    } else if (m > 0) {
+      const T sg = (am & 1) ? T(-1) : T(1);
+      v.x = sg * R * is2;
+      v.y = sg * S * is2;
+    } else {
+      v.x = R * is2;
+      v.y = -S * is2;
+    }
+    z[n * (H + 1) + lm] = v;
+  }
+}
+
 // p[r * n_ls + t] for every radial triple r (table tri: n1 | n2<<8 | n3<<16)
-// and triangle t; lanes take triples, all lanes walk the same term list (the
-// coefficients and harmonic indices are uniform loads from constant memory).
+// and triangle t, from the interleaved complex block; lanes take triples, all
+// lanes walk the same term list (the coefficients and harmonic indices are
+// uniform loads from constant memory).
 template <typename T>
 __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H,
-                                            const int *__restrict__ tri,
-                                            const T *__restrict__ zr,
-                                            const T *__restrict__ zi, T *__restrict__ p,
-                                            int lane) {
+                                             const int *__restrict__ tri,
+                                             const V2<T> *__restrict__ z, T *__restrict__ p,
+                                             int lane) {
   const int H1 = H + 1;
   const int *beg = c_b3.beg + c_b3.ls_off[lmax];
   for (int t = 0; t < n_ls; t++) {
     const int e0 = beg[t], e1 = beg[t + 1];
     for (int r = lane; r < n_tri; r += 32) {
       const int tr = tri[r];
-      const int o1 = (tr & 0xff) * H1, o2 = ((tr >> 8) & 0xff) * H1, o3 = (tr >> 16) * H1;
+      const V2<T> *z1 = z + (tr & 0xff) * H1, *z2 = z + ((tr >> 8) & 0xff) * H1;
+      const V2<T> *z3 = z + (tr >> 16) * H1;
       T acc = T(0);
       for (int e = e0; e < e1; e++) {
         const unsigned ix = c_b3.idx[e];
-        const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
-        const T ar = zr[o1 + i1], ai = zi[o1 + i1];
-        const T br = zr[o2 + i2], bi = zi[o2 + i2];
-        const T cr = zr[o3 + i3], ci = zi[o3 + i3];
-        const T xr = ar * br - ai * bi, xi = ar * bi + ai * br;
-        acc += T(c_b3.w[e]) * (xr * cr - xi * ci);
+        const V2<T> a = z1[ix & 0xff], b = z2[(ix >> 8) & 0xff], c = z3[ix >> 16];
+        const T xr = a.x * b.x - a.y * b.y, xi = a.x * b.y + a.y * b.x;
+        acc += T(c_b3.w[e]) * (xr * c.x - xi * c.y);
       }
       p[r * n_ls + t] = acc;
     }
@@ -195,33 +229,33 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
 }
 
 // Adjoint of b3_contract: for dE/dp = w, the holomorphic derivative
-// u = dE/dc summed into (ur, ui)[n * H + lm].  Lanes take radial triples in
-// rounds of 32; within a round lane r only updates the rows n1(r), n2(r),
+// u = dE/dc summed into u2[n * H + lm] = (re, im).  Lanes take radial triples
+// in rounds of 32; within a round lane r only updates the rows n1(r), n2(r),
 // n3(r) of its own triple, so it accumulates into three private rows in
-// shared memory, priv[((pos * H + lm) * 2 + part) * 32 + lane] (conflict-free
-// banks, no atomics).  After each round the private rows are summed into
-// (ur, ui) by output entry, over lanes in a fixed rotated order.  The caller
-// zeroes (ur, ui) and synchronizes the warp before and after.
+// shared memory, priv[(pos * H + lm) * 32 + lane] (conflict-free banks, no
+// atomics).  After each round the private rows are summed into u2 by output
+// entry, over lanes in a fixed rotated order.  The caller zeroes u2 and
+// synchronizes the warp before and after.
 template <typename T>
 __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tri, int H,
                                                     int nr, const int *__restrict__ tri,
-                                                    const T *__restrict__ zr,
-                                                    const T *__restrict__ zi,
+                                                    const V2<T> *__restrict__ z,
                                                     const T *__restrict__ w,
-                                                    T *__restrict__ priv, T *__restrict__ ur,
-                                                    T *__restrict__ ui, int lane) {
+                                                    V2<T> *__restrict__ priv,
+                                                    V2<T> *__restrict__ u2, int lane) {
   const int H1 = H + 1;
   const int *beg = c_b3.beg + c_b3.ls_off[lmax];
   for (int r0 = 0; r0 < n_tri; r0 += 32) {
     const int r = r0 + lane;
     const bool live = r < n_tri;
     const int tr = live ? tri[r] : 0;
-    for (int k = 0; k < 6 * H; k++) priv[k * 32 + lane] = T(0);
+    for (int k = 0; k < 3 * H; k++) priv[k * 32 + lane] = V2<T>{T(0), T(0)};
     if (live) {
       const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
-      T *p1 = priv + lane;
-      T *p2 = priv + (size_t)(2 * H) * 32 + lane;
-      T *p3 = priv + (size_t)(4 * H) * 32 + lane;
+      const V2<T> *z1 = z + n1 * H1, *z2 = z + n2 * H1, *z3 = z + n3 * H1;
+      V2<T> *p1 = priv + lane;
+      V2<T> *p2 = priv + (size_t)H * 32 + lane;
+      V2<T> *p3 = priv + (size_t)(2 * H) * 32 + lane;
       for (int t = 0; t < n_ls; t++) {
         const int e0 = beg[t], e1 = beg[t + 1];
         const T wq = w[r * n_ls + t];
@@ -229,37 +263,48 @@ __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tr
           const unsigned ix = c_b3.idx[q];
           const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
           const T f = wq * T(c_b3.w[q]);
-          const T ar = zr[n1 * H1 + i1], ai = zi[n1 * H1 + i1];
-          const T br = zr[n2 * H1 + i2], bi = zi[n2 * H1 + i2];
-          const T cr = zr[n3 * H1 + i3], ci = zi[n3 * H1 + i3];
-          p1[(2 * i1) * 32] += f * (br * cr - bi * ci);
-          p1[(2 * i1 + 1) * 32] += f * (br * ci + bi * cr);
-          p2[(2 * i2) * 32] += f * (ar * cr - ai * ci);
-          p2[(2 * i2 + 1) * 32] += f * (ar * ci + ai * cr);
-          p3[(2 * i3) * 32] += f * (ar * br - ai * bi);
-          p3[(2 * i3 + 1) * 32] += f * (ar * bi + ai * br);
+          const V2<T> a = z1[i1], b = z2[i2], c = z3[i3];
+          V2<T> s1 = p1[i1 * 32], s2 = p2[i2 * 32], s3 = p3[i3 * 32];
+          s1.x += f * (b.x * c.x - b.y * c.y);
+          s1.y += f * (b.x * c.y + b.y * c.x);
+          s2.x += f * (a.x * c.x - a.y * c.y);
+          s2.y += f * (a.x * c.y + a.y * c.x);
+          s3.x += f * (a.x * b.x - a.y * b.y);
+          s3.y += f * (a.x * b.y + a.y * b.x);
+          p1[i1 * 32] = s1;
+          p2[i2 * 32] = s2;
+          p3[i3 * 32] = s3;
         }
       }
     }
     __syncwarp();
-    // (ur, ui)[n, lm] += sum over lanes j and positions with n_pos(j) == n
-    for (int k = lane; k < 2 * nr * H; k += 32) {
-      const int part = k & 1, nl = k >> 1;
-      const int n = nl / H, lm = nl - n * H;
-      T acc = T(0);
+    // u2[n, lm] += sum over lanes j and positions with n_pos(j) == n
+    for (int k = lane; k < nr * H; k += 32) {
+      const int n = k / H, lm = k - n * H;
+      V2<T> acc{T(0), T(0)};
       for (int j0 = 0; j0 < 32; j0++) {
         const int j = (j0 + lane) & 31;  // rotated: lanes read different banks
         if (r0 + j >= n_tri) continue;
         const int tj = tri[r0 + j];
-        const T *col = priv + (size_t)((lm * 2 + part) * 32) + j;
-        if ((tj & 0xff) == n) acc += col[0];
-        if (((tj >> 8) & 0xff) == n) acc += col[(2 * H) * 32];
-        if ((tj >> 16) == n) acc += col[(4 * H) * 32];
+        const V2<T> *col = priv + (size_t)lm * 32 + j;
+        if ((tj & 0xff) == n) {
+          const V2<T> v = col[0];
+          acc.x += v.x;
+          acc.y += v.y;
+        }
+        if (((tj >> 8) & 0xff) == n) {
+          const V2<T> v = col[H * 32];
+          acc.x += v.x;
+          acc.y += v.y;
+        }
+        if ((tj >> 16) == n) {
+          const V2<T> v = col[(2 * H) * 32];
+          acc.x += v.x;
+          acc.y += v.y;
+        }
       }
-      if (part == 0)
-        ur[nl] += acc;
-      else
-        ui[nl] += acc;
+      u2[k].x += acc.x;
+      u2[k].y += acc.y;
     }
     __syncwarp();
   }
