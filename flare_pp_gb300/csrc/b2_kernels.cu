@@ -176,6 +176,10 @@ int with_shape(const B2Args &a, F &&f) {
       if (a.n_species == 2 && a.N == 10 && a.lmax == 4) return f(Shape<10, 4, 2>{});
       if (a.n_species == 2 && a.N == 8 && a.lmax == 3) return f(Shape<8, 3, 2>{});
       if (a.n_species == 1 && a.N == 8 && a.lmax == 3) return f(Shape<8, 3, 1>{});
+    } else if (a.kind == kB3) {
+      // the shape-specialised single-bond and pair stages; the bispectrum
+      // contraction and its adjoint keep runtime loops
+      if (a.n_species == 1 && a.N == 6 && a.lmax == 3) return f(Shape<6, 3, 1>{});
     }
   }
   return f(GenericShape{});

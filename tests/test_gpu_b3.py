@@ -112,3 +112,24 @@ def test_b3_mapped_fp64_and_mixed(gpu_lib, b3m):
           f"stress err {np.abs(s - bf['stress']).max():.3e}")
     assert err_e < E_GATE
     assert err_f < F_GATE
+
+
+def test_b3_mixed_n6_lmax3(gpu_lib):
+    """The settings of the 1M-atom B3 workload (N=6, lmax=3, one species),
+    whose FP32 single-bond and pair stages are compiled for that shape: the
+    mixed mapped form against the oracle's beta form on 108 atoms."""
+    rc = 5.0
+    ob = OB3("chebyshev", "quadratic", [0, rc], [], [1, 6, 3])
+    frames = [synth.fcc_al_108(505, k) for k in range(2)]
+    fit = fixtures.site_energy_model(ob, frames, 40, sigma=2.0, power=2)
+    ggp, _ = fixtures.to_gpu_model((1, 6, 3, rc), fit["sparse"], fit["alpha"], 2.0, 2,
+                                   fit["R_inv"], kind="B3")
+    cell, sp, pos = synth.fcc_al_108(505, 5)
+    st = fixtures.settings_b3(1, 6, 3, rc)
+    beta = ONDP(2.0, 2).compute_map_coeff_pow2(fit["sparse"], fit["alpha"])
+    B = opred.unpack_beta(beta, fit["sparse"].n_descriptors)
+    bf = opred.beta_form(OStructure(cell, sp, pos, rc), st, B)
+    gs = fg.Structure(cell, sp, pos, rc)
+    e, f, s = ggp.predict_mapped(gs, "mixed")
+    assert abs(e - bf["energy"]) / len(sp) < E_GATE
+    assert np.abs(f - bf["forces"]).max() < F_GATE
