@@ -39,9 +39,14 @@ struct B3Tables {
   int beg[kB3MaxLs];          // per triangle: first term (absolute index)
   unsigned idx[kB3MaxTerms];  // i1 | i2 << 8 | i3 << 16 (harmonic index l*l+l+m)
   double w[kB3MaxTerms];
+  float wf[kB3MaxTerms];      // w rounded to FP32 (the FP32 kernels convert nothing)
 };
 
 static __constant__ B3Tables c_b3;
+// The coupling coefficient of term e in the kernel's precision.
+template <typename T> __device__ __forceinline__ T b3_w(int e);
+template <> __device__ __forceinline__ float b3_w<float>(int e) { return c_b3.wf[e]; }
+template <> __device__ __forceinline__ double b3_w<double>(int e) { return c_b3.w[e]; }
 
 inline double b3_factorial(int n) {
   double f = 1.0;
@@ -118,6 +123,7 @@ inline int upload_b3_tables(cudaStream_t stream) {
                           ((unsigned)(l2 * l2 + l2 + m2) << 8) |
                           ((unsigned)(l3 * l3 + l3 + m3) << 16);
               t.w[nt] = w;
+              t.wf[nt] = (float)w;
               nt++;
             }
         }
@@ -221,7 +227,7 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
         const unsigned ix = c_b3.idx[e];
         const V2<T> a = z1[ix & 0xff], b = z2[(ix >> 8) & 0xff], c = z3[ix >> 16];
         const T xr = a.x * b.x - a.y * b.y, xi = a.x * b.y + a.y * b.x;
-        acc += T(c_b3.w[e]) * (xr * c.x - xi * c.y);
+        acc += b3_w<T>(e) * (xr * c.x - xi * c.y);
       }
       p[r * n_ls + t] = acc;
     }
@@ -262,7 +268,7 @@ __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tr
         for (int q = e0; q < e1; q++) {
           const unsigned ix = c_b3.idx[q];
           const int i1 = ix & 0xff, i2 = (ix >> 8) & 0xff, i3 = ix >> 16;
-          const T f = wq * T(c_b3.w[q]);
+          const T f = wq * b3_w<T>(q);
           const V2<T> a = z1[i1], b = z2[i2], c = z3[i3];
           V2<T> s1 = p1[i1 * 32], s2 = p2[i2 * 32], s3 = p3[i3 * 32];
           s1.x += f * (b.x * c.x - b.y * c.y);
