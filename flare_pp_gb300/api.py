@@ -429,6 +429,21 @@ class _Model(_Handle):
         b = f64(beta_packed)
         check(lib().fpp_model_set_beta(self._h, int(power), ptr(b)))
 
+    def set_L_inv(self, L_inv):
+        L = f64(L_inv)
+        check(lib().fpp_model_set_L_inv(self._h, L.shape[0], ptr(L)))
+
+    def compute_varmap(self, stream=None):
+        """compute_varmap_coefficients -> (n_species, n_d^2)."""
+        nd, ns = self.n_descriptors, self.n_species
+        out = np.zeros((ns, nd * nd))
+        check(lib().fpp_model_compute_varmap(self._h, ptr(out), _stream(stream)))
+        return out
+
+    def set_varmap(self, varmap):
+        v = f64(varmap)
+        check(lib().fpp_model_set_varmap(self._h, ptr(v)))
+
 
 # --------------------------------------------------------------------------
 def update_matrices_QR(Kuu, Kuf, y, noise_vector, jitter=1e-8, stream=None):
@@ -742,6 +757,53 @@ class SparseGP:
         self.predict_mean(structure, stream)
         structure.local_uncertainties = self.compute_cluster_uncertainties(structure, stream)
 
+    # ---- coefficient files (sparse_gp.cpp:1142-1404) ----------------------
+    @property
+    def hyperparameters(self):
+        k = self.kernels[0]
+        return np.array([k.sigma, self.energy_noise, self.force_noise, self.stress_noise])
+
+    def _file_header(self):
+        ns, N, lmax = self.b2.descriptor_settings
+        return dict(n_species=ns, n_max=N, l_max=lmax, cutoffs=self.b2.cutoffs,
+                    cutoff_function=self.b2.cutoff_function, radial=self.b2.radial_basis)
+
+    def write_mapping_coefficients(self, file_name, contributor, kernel_index=0,
+                                   stream=None):
+        """SparseGP::write_mapping_coefficients (sparse_gp.cpp:1142-1206)."""
+        from .potential import write_potential
+        self._ensure_mapped(stream)
+        write_potential(file_name, self.mapping_coefficients, self.kernels[0].power,
+                        contributor=contributor, **self._file_header())
+
+    def write_varmap_coefficients(self, file_name, contributor, kernel_index=0,
+                                  stream=None):
+        """SparseGP::write_varmap_coefficients (sparse_gp.cpp:1208-1281):
+        the variance map of a power-1 model, computed on the GPU."""
+        from .potential import write_varmap
+        if self.L_inv is None:
+            raise ValueError("write_varmap_coefficients needs L_inv")
+        self._model.set_L_inv(self.L_inv)
+        self.varmap_coeffs = self._model.compute_varmap(stream)
+        write_varmap(file_name, self.varmap_coeffs, self.hyperparameters,
+                     contributor=contributor, **self._file_header())
+
+    def write_L_inverse(self, file_name, contributor):
+        """SparseGP::write_L_inverse (sparse_gp.cpp:1283-1344)."""
+        from .potential import write_L_inverse
+        if self.L_inv is None:
+            raise ValueError("write_L_inverse needs L_inv")
+        write_L_inverse(file_name, self.L_inv, self.kernels[0].power,
+                        self.hyperparameters, contributor=contributor,
+                        **self._file_header())
+
+    def write_sparse_descriptors(self, file_name, contributor):
+        """SparseGP::write_sparse_descriptors (sparse_gp.cpp:1346-1404)."""
+        from .potential import write_sparse_descriptors
+        sd = self.sparse_descriptors[0]
+        write_sparse_descriptors(file_name, sd.descriptors, sd.descriptor_norms,
+                                 contributor=contributor)
+
     def predict_mapped(self, structure, precision="mixed", stream=None,
                        atom_energies=False):
         """Energy, forces and stress through the mapped coefficients (the pair
@@ -813,3 +875,74 @@ class PairFLARE:
                                      len(il), ptr(il), ptr(nn), ptr(nb), prec, ptr(f),
                                      ptr(e), ptr(v), ptr(ea), _stream(stream)))
         return (f, e[0], v, ea) if eatom else (f, e[0], v)
+
+
+class ComputeFlareStdAtom:
+    """The LAMMPS compute flare/std/atom (lammps_plugins/compute_flare_std_atom.h):
+    per-atom uncertainty from a variance-map file (one file), or from an
+    L_inverse file and a sparse-descriptor file (two files), evaluated on the
+    GPU on LAMMPS-shaped arrays."""
+
+    def __init__(self, *files):
+        self.use_map = False
+        if files:
+            self.coeff(*files)
+
+    def coeff(self, *files):
+        """ComputeFlareStdAtom::coeff (compute_flare_std_atom.cpp:287-307)."""
+        from .potential import read_L_inverse, read_sparse_descriptors, read_varmap
+        if len(files) == 1:
+            hdr = read_varmap(files[0])
+            self.use_map = True
+        elif len(files) == 2:
+            hdr = read_L_inverse(files[0])
+            self.use_map = False
+        else:
+            raise ValueError("Incorrect args for compute coefficients")
+        ns, N, lmax = hdr["n_species"], hdr["n_max"], hdr["l_max"]
+        self.hyperparameters = hdr["hyps"]
+        self.cutoff_matrix = hdr["cutoffs"]
+        self.cutoff = float(self.cutoff_matrix.max())
+        b2 = B2(hdr["radial"], hdr["cutoff_function"], [0.0, self.cutoff], [],
+                [ns, N, lmax], self.cutoff_matrix)
+        self.b2 = b2
+        envs = ClusterDescriptor()
+        envs.initialize_cluster(ns, b2.n_descriptors)
+        sigma = float(self.hyperparameters[0])
+        if self.use_map:
+            self.model = _Model(b2, sigma, 2, envs)
+            self.model.set_varmap(hdr["varmap"].reshape(ns, -1))
+            return
+        self.power = hdr["power"]
+        rows = read_sparse_descriptors(files[1], b2.n_descriptors, hdr["n_clusters"])
+        if len(rows) != ns:
+            raise ValueError("sparse descriptors hold a different species count")
+        envs.n_clusters_by_type = [len(r) for r in rows]
+        envs.cumulative_type_count = [int(v) for v in np.concatenate(
+            [[0], np.cumsum(envs.n_clusters_by_type)[:-1]])]
+        envs.n_clusters = int(sum(envs.n_clusters_by_type))
+        envs.descriptors = [f64(r) for r in rows]
+        # the file's rows are normalized already: unit norms (0 for the zero
+        # rows of empty environments) keep them as they are
+        envs.descriptor_norms = [np.where(np.abs(r).max(axis=1, initial=0.0) > 0, 1.0, 0.0)
+                                 for r in rows]
+        self.model = _Model(b2, sigma, self.power, envs)
+        self.model.set_L_inv(hdr["L_inv"])
+
+    def compute_peratom(self, x, type_, ilist, numneigh, neighbors, nlocal=None,
+                        stream=None):
+        """ComputeFlareStdAtom::compute_peratom (compute_flare_std_atom.cpp:98-207):
+        stds (nall), 0 for atoms outside ilist and for empty environments."""
+        x = f64(x).reshape(-1, 3)
+        t = i32(type_)
+        il = i32(ilist)
+        nn = i32(numneigh)
+        nb = i32(neighbors)
+        nall = len(x)
+        nlocal = len(il) if nlocal is None else int(nlocal)
+        out = np.zeros(nall)
+        check(lib().fpp_std_atom_compute(self.model.handle, nlocal, nall, ptr(x), ptr(t),
+                                         len(il), ptr(il), ptr(nn), ptr(nb),
+                                         1 if self.use_map else 0, ptr(out),
+                                         _stream(stream)))
+        return out

@@ -113,27 +113,13 @@ __global__ void k_energy_sum(int inum, const double *__restrict__ e, double *out
   if (threadIdx.x == 0) out[0] = sm[0];
 }
 
-}  // namespace fpp
-
-using namespace fpp;
-
-extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
-                                const double *x, const int32_t *type, int32_t inum,
-                                const int32_t *ilist, const int32_t *numneigh,
-                                const int32_t *neighbors, int precision, double *f,
-                                double *eng_vdwl, double *virial, double *eatom,
-                                void *stream) {
-  if (!m) return fail(FPP_ERR_INVALID, "null model");
-  if (m->args.kind != kB2)
-    return fail(FPP_ERR_UNSUPPORTED, "the pair style maps B2 models only (pair_flare.cpp)");
+int lammps_load(fpp_model *m, int32_t nlocal, int32_t nall, const double *x,
+                const int32_t *type, int32_t inum, const int32_t *ilist,
+                const int32_t *numneigh, const int32_t *neighbors, cudaStream_t st) {
   if (nall < nlocal || nlocal < 0 || inum < 0 || inum > nall)
     return fail(FPP_ERR_INVALID, "bad atom counts");
-  if (inum > 0 && (!x || !type || !ilist || !numneigh || !f))
+  if (inum > 0 && (!x || !type || !ilist || !numneigh))
     return fail(FPP_ERR_INVALID, "null argument");
-  if (m->beta_power == 0)
-    return fail(FPP_ERR_INVALID, "mapped coefficients not set");
-  if (precision != FPP_PREC_FP64 && precision != FPP_PREC_MIXED)
-    return fail(FPP_ERR_INVALID, "bad precision");
   for (int k = 0; k < nall; k++)
     if (type[k] < 1 || type[k] > m->n_species)
       return fail(FPP_ERR_INVALID, "atom type outside 1..n_species");
@@ -149,16 +135,9 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
       if (neighbors[p] < 0 || neighbors[p] >= nall)
         return fail(FPP_ERR_INVALID, "neighbor index outside 0..nall-1");
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  // Reuse a structure-shaped workspace owned by the model.
-  static thread_local fpp_structure *ws_cache = nullptr;
-  static thread_local fpp_model *ws_owner = nullptr;
-  if (ws_owner != m) {
-    delete ws_cache;
-    ws_cache = new fpp_structure();
-    ws_owner = m;
-  }
-  fpp_structure *s = ws_cache;
+  if (!m->lammps) m->lammps = new fpp_lammps_ws();
+  fpp_lammps_ws &w = *m->lammps;
+  fpp_structure *s = &w.s;
   StructureState &S = s->st;
   std::vector<int> off(inum + 1, 0);
   for (int ii = 0; ii < inum; ii++) off[ii + 1] = off[ii] + numneigh[ii];
@@ -169,14 +148,10 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
   for (int ii = 0; ii < inum; ii++) S.species_host[ii] = type[ilist[ii]] - 1;
   s->layout_species = -1;  // species can change between calls
   S.ci.volume = 1.0;
-  DevBuf d_x, d_type, d_ilist, d_nbrs, d_f, d_vir, d_e;
-  FPP_TRY(d_x.reserve(sizeof(double) * 3 * std::max(nall, 1)));
-  FPP_TRY(d_type.reserve(sizeof(int) * std::max(nall, 1)));
-  FPP_TRY(d_ilist.reserve(sizeof(int) * std::max(inum, 1)));
-  FPP_TRY(d_nbrs.reserve(sizeof(int) * std::max(np, 1)));
-  FPP_TRY(d_f.reserve(sizeof(double) * 3 * std::max(nall, 1)));
-  FPP_TRY(d_vir.reserve(sizeof(double) * 8));
-  FPP_TRY(d_e.reserve(sizeof(double) * 8));
+  FPP_TRY(w.d_x.reserve(sizeof(double) * 3 * std::max(nall, 1)));
+  FPP_TRY(w.d_type.reserve(sizeof(int) * std::max(nall, 1)));
+  FPP_TRY(w.d_ilist.reserve(sizeof(int) * std::max(inum, 1)));
+  FPP_TRY(w.d_nbrs.reserve(sizeof(int) * std::max(np, 1)));
   FPP_TRY(S.nbr_offset.reserve(sizeof(int) * (inum + 1)));
   FPP_TRY(S.species.reserve(sizeof(int) * std::max(inum, 1)));
   const size_t npp = std::max(np, 1);
@@ -188,50 +163,80 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
   FPP_TRY(S.status.reserve(sizeof(DeviceStatus)));
   FPP_CUDA(cudaMemsetAsync(S.status.ptr, 0, sizeof(DeviceStatus), st));
   if (nall) {
-    FPP_CUDA(cudaMemcpyAsync(d_x.ptr, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, st));
-    FPP_CUDA(cudaMemcpyAsync(d_type.ptr, type, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
-    FPP_CUDA(cudaMemsetAsync(d_f.ptr, 0, sizeof(double) * 3 * nall, st));
+    FPP_CUDA(cudaMemcpyAsync(w.d_x.ptr, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, st));
+    FPP_CUDA(cudaMemcpyAsync(w.d_type.ptr, type, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
   }
-  if (inum) FPP_CUDA(cudaMemcpyAsync(d_ilist.ptr, ilist, sizeof(int) * inum, cudaMemcpyHostToDevice, st));
-  if (np) FPP_CUDA(cudaMemcpyAsync(d_nbrs.ptr, neighbors, sizeof(int) * np, cudaMemcpyHostToDevice, st));
+  if (inum) FPP_CUDA(cudaMemcpyAsync(w.d_ilist.ptr, ilist, sizeof(int) * inum, cudaMemcpyHostToDevice, st));
+  if (np) FPP_CUDA(cudaMemcpyAsync(w.d_nbrs.ptr, neighbors, sizeof(int) * np, cudaMemcpyHostToDevice, st));
   FPP_CUDA(cudaMemcpyAsync(S.nbr_offset.ptr, off.data(), sizeof(int) * (inum + 1),
                            cudaMemcpyHostToDevice, st));
-  FPP_CUDA(cudaMemsetAsync(d_vir.ptr, 0, sizeof(double) * 8, st));
   if (inum) {
-    k_pairs_from_list<<<inum, 64, 0, st>>>(inum, d_ilist.as<int>(), S.nbr_offset.as<int>(),
-                                           d_nbrs.as<int>(), d_x.as<double>(),
-                                           d_type.as<int>(), nall, S.nbr_i.as<int>(),
+    k_pairs_from_list<<<inum, 64, 0, st>>>(inum, w.d_ilist.as<int>(), S.nbr_offset.as<int>(),
+                                           w.d_nbrs.as<int>(), w.d_x.as<double>(),
+                                           w.d_type.as<int>(), nall, S.nbr_i.as<int>(),
                                            S.nbr_s.as<int>(), S.nbr_rel.as<dvec4>(),
                                            S.nbr_rel32.as<float4>(), S.species.as<int>(),
                                            S.status.as<DeviceStatus>());
     FPP_CUDA(cudaGetLastError());
   }
   S.rel64_valid = true;  // the FP64 pair table comes from LAMMPS's arrays
+  return FPP_OK;
+}
+
+}  // namespace fpp
+
+using namespace fpp;
+
+extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
+                                const double *x, const int32_t *type, int32_t inum,
+                                const int32_t *ilist, const int32_t *numneigh,
+                                const int32_t *neighbors, int precision, double *f,
+                                double *eng_vdwl, double *virial, double *eatom,
+                                void *stream) {
+  if (!m) return fail(FPP_ERR_INVALID, "null model");
+  if (m->args.kind != kB2)
+    return fail(FPP_ERR_UNSUPPORTED, "the pair style maps B2 models only (pair_flare.cpp)");
+  if (inum > 0 && !f) return fail(FPP_ERR_INVALID, "null argument");
+  if (m->beta_power == 0)
+    return fail(FPP_ERR_INVALID, "mapped coefficients not set");
+  if (precision != FPP_PREC_FP64 && precision != FPP_PREC_MIXED)
+    return fail(FPP_ERR_INVALID, "bad precision");
+  cudaStream_t st = (cudaStream_t)stream;
+  FPP_TRY(lammps_load(m, nlocal, nall, x, type, inum, ilist, numneigh, neighbors, st));
+  fpp_lammps_ws &w = *m->lammps;
+  fpp_structure *s = &w.s;
+  StructureState &S = s->st;
+  const int np = (int)S.n_pairs;
+  FPP_TRY(w.d_f.reserve(sizeof(double) * 3 * std::max(nall, 1)));
+  FPP_TRY(w.d_vir.reserve(sizeof(double) * 8));
+  FPP_TRY(w.d_e.reserve(sizeof(double) * 8));
+  if (nall) FPP_CUDA(cudaMemsetAsync(w.d_f.ptr, 0, sizeof(double) * 3 * nall, st));
+  FPP_CUDA(cudaMemsetAsync(w.d_vir.ptr, 0, sizeof(double) * 8, st));
   // same kernels as fpp_predict_mapped, with the pair style's strict filter
   FPP_TRY(mapped_core(m, s, precision, st, /*strict=*/1));
   if (np) {
     if (precision == FPP_PREC_FP64)
       k_pair_scatter<double><<<(np + 127) / 128, 128, 0, st>>>(
-          np, d_ilist.as<int>(), S.nbr_i.as<int>(), d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
-          S.pair_f.as<double>(), d_f.as<double>(), d_vir.as<double>());
+          np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
+          S.pair_f.as<double>(), w.d_f.as<double>(), w.d_vir.as<double>());
     else
       k_pair_scatter<float><<<(np + 127) / 128, 128, 0, st>>>(
-          np, d_ilist.as<int>(), S.nbr_i.as<int>(), d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
-          S.pair_f.as<float>(), d_f.as<double>(), d_vir.as<double>());
+          np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
+          S.pair_f.as<float>(), w.d_f.as<double>(), w.d_vir.as<double>());
     FPP_CUDA(cudaGetLastError());
   }
-  if (inum) k_energy_sum<<<1, 256, 0, st>>>(inum, S.atom_e.as<double>(), d_e.as<double>());
+  if (inum) k_energy_sum<<<1, 256, 0, st>>>(inum, S.atom_e.as<double>(), w.d_e.as<double>());
   FPP_CUDA(cudaGetLastError());
   std::vector<double> hf(3 * (size_t)nall), he(inum);
   double vir[6] = {0, 0, 0, 0, 0, 0}, etot = 0;
   FPP_CUDA(cudaStreamSynchronize(st));
   FPP_TRY(check_status(S, st, "pair compute"));
-  if (nall) FPP_CUDA(cudaMemcpy(hf.data(), d_f.ptr, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost));
+  if (nall) FPP_CUDA(cudaMemcpy(hf.data(), w.d_f.ptr, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost));
   if (inum) {
     FPP_CUDA(cudaMemcpy(he.data(), S.atom_e.ptr, sizeof(double) * inum, cudaMemcpyDeviceToHost));
-    FPP_CUDA(cudaMemcpy(&etot, d_e.ptr, sizeof(double), cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(&etot, w.d_e.ptr, sizeof(double), cudaMemcpyDeviceToHost));
   }
-  FPP_CUDA(cudaMemcpy(vir, d_vir.ptr, sizeof(vir), cudaMemcpyDeviceToHost));
+  FPP_CUDA(cudaMemcpy(vir, w.d_vir.ptr, sizeof(vir), cudaMemcpyDeviceToHost));
   for (size_t k = 0; k < hf.size(); k++) f[k] += hf[k];
   if (eng_vdwl) *eng_vdwl += etot;
   if (virial)

@@ -29,7 +29,7 @@ static int center_from_sparse(fpp_model *m);
                                     std::to_string((int)_s));                \
   } while (0)
 
-static int get_cublas(fpp_model *m, cudaStream_t st, cublasHandle_t *out) {
+int get_cublas(fpp_model *m, cudaStream_t st, cublasHandle_t *out) {
   if (!m->cublas) {
     cublasHandle_t h;
     if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS)
@@ -354,6 +354,7 @@ int fpp_model_create(const fpp_b2 *b2, double sigma, double power, fpp_model **o
 
 int fpp_model_destroy(fpp_model *m) {
   if (m && m->cublas) cublasDestroy((cublasHandle_t)m->cublas);
+  if (m) delete m->lammps;
   delete m;
   return FPP_OK;
 }

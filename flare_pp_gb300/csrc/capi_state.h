@@ -1,5 +1,6 @@
 // Definitions of the opaque C ABI handles.
 #pragma once
+#include <cublas_v2.h>
 #include <cuda_fp16.h>
 
 #include <vector>
@@ -16,6 +17,13 @@ struct fpp_structure {
   std::vector<int> n_rows;      // per species, atom count
   int total_rows = 0;
   fpp::DevBuf row_of_atom;      // int32[noa]
+};
+
+// Device copies of LAMMPS-shaped arrays and the structure-shaped workspace
+// the pair style and the uncertainty compute run on (owned by a model).
+struct fpp_lammps_ws {
+  fpp_structure s;
+  fpp::DevBuf d_x, d_type, d_ilist, d_nbrs, d_f, d_vir, d_e;
 };
 
 struct fpp_b2 {
@@ -57,6 +65,13 @@ struct fpp_model {
   int n_sparse_total = 0;
   fpp::DevBuf R_inv;                    // double[n * n]
   bool has_R_inv = false;
+  // ComputeFlareStdAtom coefficients: L_inv (n x n, row-major lower
+  // triangle) and the variance map (per species n_d x n_d, row-major)
+  fpp::DevBuf L_inv;
+  bool has_L_inv = false;
+  fpp::DevBuf varmap;
+  bool has_varmap = false;
+  fpp_lammps_ws *lammps = nullptr;      // LAMMPS-array workspace
   void *cublas = nullptr;               // cublasHandle_t
 };
 
@@ -65,6 +80,13 @@ int prepare_structure(fpp_structure *s, cudaStream_t stream);
 int ensure_layout(fpp_structure *s, int n_species, cudaStream_t stream);
 int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
                 int strict);
+// Validates LAMMPS-shaped arrays (pair_flare.cpp:68-100: x, 1-based type,
+// full neighbor list in ilist order) and loads them into m->lammps: pair
+// list with the FP64 pair geometry, species per listed atom.
+int lammps_load(fpp_model *m, int32_t nlocal, int32_t nall, const double *x,
+                const int32_t *type, int32_t inum, const int32_t *ilist,
+                const int32_t *numneigh, const int32_t *neighbors, cudaStream_t st);
+int get_cublas(fpp_model *m, cudaStream_t st, cublasHandle_t *out);
 int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st);
 // FP64 forward pass: c64, norm64 (atom order), phat64 rows, p64 (atom order)
 // when want_p.

@@ -330,6 +330,38 @@ int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                      double *eng_vdwl, double *virial, double *eatom,
                      void *stream);
 
+/* ------------------------------------------------------------------------
+ * ComputeFlareStdAtom (lammps_plugins/compute_flare_std_atom.cpp): the
+ * per-atom uncertainty of the LAMMPS compute flare/std/atom.
+ * ---------------------------------------------------------------------- */
+/* L_inv of the sparse set (the L_inverse file's block, read by
+ * ComputeFlareStdAtom::read_L_inverse, compute_flare_std_atom.cpp:456-568):
+ * host n x n row-major lower triangle, n = the model's sparse-set size. */
+int fpp_model_set_L_inv(fpp_model *m, int32_t n, const double *L_inv);
+/* NormalizedDotProduct::compute_varmap_coefficients
+ * (normalized_dot_product.cpp:761-850) on the GPU in FP64 from the sparse
+ * set, sigma and L_inv (Kuu^-1 = L_inv^T L_inv); power-1 models only
+ * (FPP_ERR_UNSUPPORTED otherwise, with the reference's message).  varmap
+ * (host, optional): n_species x n_d^2, row-major, the layout
+ * SparseGP::write_varmap_coefficients writes (sparse_gp.cpp:1208-1281).
+ * The map is kept on the model for fpp_std_atom_compute. */
+int fpp_model_compute_varmap(fpp_model *m, double *varmap, void *stream);
+/* Load a variance map (ComputeFlareStdAtom::read_file,
+ * compute_flare_std_atom.cpp:345-454): n_species x n_d^2, row-major. */
+int fpp_model_set_varmap(fpp_model *m, const double *varmap);
+/* ComputeFlareStdAtom::compute_peratom (compute_flare_std_atom.cpp:98-207)
+ * with the LAMMPS-shaped arrays of fpp_pair_compute.  use_map = 1: the
+ * variance-map form, var = p.(M p) / |p|^2 / sigma^2; use_map = 0: the
+ * L_inv form, var = 1 - sigma^2 |L_inv k|^2 with k_j = (dhat_j . phat)^power
+ * over the sparse set of the atom's species.  stds (host, nall) receives
+ * sqrt(var) (-sqrt(-var) when var < 0) at the listed atoms and 0 elsewhere
+ * and for empty environments (|p|^2 < 1e-8).  FP64 on the GPU. */
+int fpp_std_atom_compute(fpp_model *m, int32_t nlocal, int32_t nall,
+                         const double *x, const int32_t *type, int32_t inum,
+                         const int32_t *ilist, const int32_t *numneigh,
+                         const int32_t *neighbors, int32_t use_map,
+                         double *stds, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

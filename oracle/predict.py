@@ -219,3 +219,72 @@ def unpack_beta(packed, n_d, power=2):
         B[iu[1][off], iu[0][off]] = row[off] / 2
         out.append(B)
     return out
+
+
+def varmap_coefficients(sparse_descriptors, Kuu_inverse, sigma, power, alpha_ind=0):
+    """NormalizedDotProduct::compute_varmap_coefficients
+    (normalized_dot_product.cpp:761-850): per species s the n_d x n_d map
+    sum_ij -sigma^4 Kuu^-1_ij dhat_i dhat_j^T, plus sigma^2 on the diagonal
+    while visiting the pair (0, 0); empty environments are skipped.  Returns
+    (n_species, n_d^2) row-major, or None for power != 1 (the reference
+    prints a message and returns an empty matrix)."""
+    if power != 1:
+        return None
+    sd = sparse_descriptors
+    nd = sd.n_descriptors
+    sig2 = sigma * sigma
+    out = np.zeros((sd.n_types, nd * nd))
+    diag = np.arange(nd) * (nd + 1)
+    for s in range(sd.n_types):
+        n_t = sd.n_clusters_by_type[s]
+        K_ind = alpha_ind + sd.cumulative_type_count[s]
+        for i in range(n_t):
+            pi = sd.descriptors[s][i]
+            ni = sd.descriptor_norms[s][i]
+            if ni < EMPTY_THRESH:
+                continue
+            for j in range(n_t):
+                pj = sd.descriptors[s][j]
+                nj = sd.descriptor_norms[s][j]
+                if nj < EMPTY_THRESH:
+                    continue
+                kn = Kuu_inverse[K_ind + i, K_ind + j] / ni / nj
+                out[s] += (sig2 * sig2 * np.outer(pi, pj) * (-kn)).ravel()
+                if i == 0 and j == 0:
+                    out[s][diag] += sig2
+    return out
+
+
+def std_atom(structure, settings, sigma, power=None, L_inv=None, sparse_normed=None,
+             varmap=None):
+    """ComputeFlareStdAtom::compute_peratom (compute_flare_std_atom.cpp:98-207)
+    on a periodic structure, per atom in structure order.
+
+    Map form (varmap: (n_species, n_d, n_d)): var = p.(M p) / |p|^2 / sigma^2
+    (compute_energy_and_u with power 2).  L_inv form: k over all sparse
+    clusters, (dhat . phat)^power in the block of the atom's species and 0
+    elsewhere, var = 1 - sigma^2 |L_inv k|^2.  std = sqrt(var), -sqrt(-var)
+    for var < 0, 0 for |p|^2 < 1e-8."""
+    _, p, norms = descriptors(structure, settings)
+    sig2 = sigma * sigma
+    out = np.zeros(structure.noa)
+    for i in range(structure.noa):
+        nsq = float(p[i] @ p[i])
+        if nsq < EMPTY_THRESH:
+            continue
+        s = int(structure.species[i])
+        if varmap is not None:
+            B = np.asarray(varmap[s]).reshape(p.shape[1], p.shape[1])
+            var = float(p[i] @ (B @ p[i])) / nsq / sig2
+        else:
+            ph = p[i] / nsq ** 0.5
+            kv = np.zeros(L_inv.shape[0])
+            cum = 0
+            for t, D in enumerate(sparse_normed):
+                if t == s:
+                    kv[cum:cum + len(D)] = (D @ ph) ** power
+                cum += len(D)
+            v = L_inv @ kv
+            var = 1.0 - sig2 * float(v @ v)
+        out[i] = var ** 0.5 if var >= 0.0 else -abs(var) ** 0.5
+    return out

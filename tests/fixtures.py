@@ -115,3 +115,59 @@ def to_gpu_model(b2_settings_list, oracle_sparse, alpha, sigma, power, R_inv=Non
     gp = fg.SparseGP([fg.NormalizedDotProduct(sigma, power)], 0.001, 0.05, 0.006)
     gp.set_model(b2, cd, alpha, R_inv)
     return gp, b2
+
+
+def lammps_arrays(cell, sp, pos, rc):
+    """Full neighbor list with ghost atoms from the periodic structure."""
+    o = OStructure(cell, sp, pos, rc)
+    wp = o.wrapped_positions
+    noa = o.noa
+    x = [wp[i] for i in range(noa)]
+    types = [int(s) + 1 for s in sp]
+    owner = list(range(noa))
+    ghost_of = {}
+    numneigh, nbrs = [], []
+    off = o.cumulative_neighbor_count
+    for i in range(noa):
+        numneigh.append(int(off[i + 1] - off[i]))
+        for p in range(off[i], off[i + 1]):
+            j = int(o.structure_indices[p])
+            img = wp[i] + o.relative_positions[p, 1:]
+            key = (j, tuple(np.round(img - wp[j], 6)))
+            if np.allclose(img, wp[j]):
+                nbrs.append(j)
+                continue
+            if key not in ghost_of:
+                ghost_of[key] = len(x)
+                x.append(img)
+                types.append(int(sp[j]) + 1)
+                owner.append(j)
+            nbrs.append(ghost_of[key])
+    return (np.array(x), np.array(types), np.arange(noa), np.array(numneigh),
+            np.array(nbrs), np.array(owner))
+
+
+def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
+    """Two-species sparse set (10 environments per species of a 54-atom BCC
+    alloy frame, per-pair cutoffs) and the inverse Cholesky factor of its
+    Kuu + 1e-8 I: the coefficients of the compute flare/std/atom."""
+    import scipy.linalg as sla
+    rc = 4.5
+    cut = np.array([[4.5, 4.0], [4.0, 4.2]])
+    b2 = OB2("chebyshev", "quadratic", [0, rc], [], [2, 4, 2], cut)
+    cell, sp, pos = synth.bcc_alloy((3, 3, 3), seed)
+    frame = OStructure(cell, sp, pos, rc, [b2])
+    dv = frame.descriptors[0]
+    rng = np.random.default_rng(seed)
+    clusters = [sorted(int(v) for v in rng.choice(dv.n_clusters_by_type[s],
+                                                   n_per_species, replace=False))
+                for s in range(2)]
+    sd = OCD(dv, clusters)
+    Kuu = ONDP(sigma, power).envs_envs(sd, sd)
+    n = Kuu.shape[0]
+    L = np.linalg.cholesky(Kuu + 1e-8 * np.eye(n))
+    L_inv = sla.solve_triangular(L, np.eye(n), lower=True)
+    sparse_normed = [sd.descriptors[s] / sd.descriptor_norms[s][:, None] for s in range(2)]
+    return dict(b2=b2, sd=sd, L_inv=L_inv, Kuu_inverse=L_inv.T @ L_inv, sigma=sigma,
+                power=power, cutoffs=cut, rc=rc, sparse_normed=sparse_normed,
+                settings=settings(2, 4, 2, rc, cut))

@@ -93,3 +93,33 @@ def test_potential_file_round_trip(tmp_path):
     write_potential(bad, beta[:, :-1], 2, ns, N, lmax, np.full((ns, ns), 4.5))
     with pytest.raises(ValueError):
         read_potential(bad)
+
+
+def test_std_atom_argument_errors(lib):
+    """The compute flare/std/atom entry points check their arguments before
+    any device work: a model without coefficients, the power-1 restriction of
+    the variance map, a missing output."""
+    from flare_pp_gb300 import _lib
+    h = ctypes.c_void_p()
+    rh = np.array([0.0, 5.0])
+    ds = np.array([1, 4, 2], dtype=np.int32)
+    assert lib.fpp_b2_create(b"chebyshev", b"quadratic", rh.ctypes.data, 2, None, 0,
+                             ds.ctypes.data, None, ctypes.byref(h)) == 0
+    m = ctypes.c_void_p()
+    assert lib.fpp_model_create(h, 1.5, 2.0, ctypes.byref(m)) == 0
+    x = np.zeros((1, 3))
+    t = np.ones(1, dtype=np.int32)
+    il = np.zeros(1, dtype=np.int32)
+    nn = np.zeros(1, dtype=np.int32)
+    out = np.zeros(1)
+    for use_map, msg in ((1, b"variance map"), (0, b"L_inv")):
+        rc = lib.fpp_std_atom_compute(m, 1, 1, x.ctypes.data, t.ctypes.data, 1,
+                                      il.ctypes.data, nn.ctypes.data, None, use_map,
+                                      out.ctypes.data, None)
+        assert rc == _lib.FPP_ERR_INVALID and msg in lib.fpp_last_error()
+    assert lib.fpp_model_compute_varmap(m, None, None) == _lib.FPP_ERR_UNSUPPORTED
+    assert b"power 1 only" in lib.fpp_last_error()
+    assert lib.fpp_model_set_L_inv(m, 3, out.ctypes.data) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_model_set_varmap(m, None) == _lib.FPP_ERR_INVALID
+    lib.fpp_model_destroy(m)
+    lib.fpp_b2_destroy(h)

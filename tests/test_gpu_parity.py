@@ -202,36 +202,6 @@ def test_mapped_config2_mixed_gates(gpu_lib, c2):
     assert err_f < F_GATE
 
 
-def _lammps_arrays(cell, sp, pos, rc):
-    """Full neighbor list with ghost atoms from the periodic structure."""
-    o = OStructure(cell, sp, pos, rc)
-    wp = o.wrapped_positions
-    noa = o.noa
-    x = [wp[i] for i in range(noa)]
-    types = [int(s) + 1 for s in sp]
-    owner = list(range(noa))
-    ghost_of = {}
-    numneigh, nbrs = [], []
-    off = o.cumulative_neighbor_count
-    for i in range(noa):
-        numneigh.append(int(off[i + 1] - off[i]))
-        for p in range(off[i], off[i + 1]):
-            j = int(o.structure_indices[p])
-            img = wp[i] + o.relative_positions[p, 1:]
-            key = (j, tuple(np.round(img - wp[j], 6)))
-            if np.allclose(img, wp[j]):
-                nbrs.append(j)
-                continue
-            if key not in ghost_of:
-                ghost_of[key] = len(x)
-                x.append(img)
-                types.append(int(sp[j]) + 1)
-                owner.append(j)
-            nbrs.append(ghost_of[key])
-    return (np.array(x), np.array(types), np.arange(noa), np.array(numneigh),
-            np.array(nbrs), np.array(owner))
-
-
 def test_pair_compute_matches_mapped(gpu_lib, c1, tmp_path):
     from flare_pp_gb300.potential import write_potential
     m, ggp = c1["m"], c1["ggp"]
@@ -239,7 +209,7 @@ def test_pair_compute_matches_mapped(gpu_lib, c1, tmp_path):
     fn = tmp_path / "Al.txt"
     write_potential(fn, ggp.mapping_coefficients, 2, 1, 8, 3, np.array([[5.0]]))
     pair = fg.PairFLARE(str(fn))
-    x, t, il, nn, nb, owner = _lammps_arrays(c1["cell"], c1["sp"], c1["pos"], 5.0)
+    x, t, il, nn, nb, owner = fixtures.lammps_arrays(c1["cell"], c1["sp"], c1["pos"], 5.0)
     for prec, tol in (("fp64", 1e-9), ("mixed", F_GATE)):
         f, e, vir, ea = pair.compute(x, t, il, nn, nb, precision=prec, eatom=True)
         F = np.zeros((c1["gs"].noa, 3))
