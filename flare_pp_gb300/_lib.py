@@ -68,6 +68,8 @@ SIGNATURES = {
     "fpp_pair_compute": (_c_int, [_vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp,
                                   _c_int, _vp, _vp, _vp, _vp, _vp]),
     "fpp_model_set_L_inv": (_c_int, [_vp, _i32, _vp]),
+    "fpp_likelihood_gradient_stable": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "fpp_model_compute_varmap": (_c_int, [_vp, _vp, _vp]),
     "fpp_model_set_varmap": (_c_int, [_vp, _vp]),
     "fpp_std_atom_compute": (_c_int, [_vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp,

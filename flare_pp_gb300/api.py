@@ -482,6 +482,7 @@ class SparseGP:
         self.training_atom_indices = []
         self.y = np.zeros(0)
         self.noise_vector = np.zeros(0)
+        self.label_kind = np.zeros(0, dtype=np.int32)  # 0 energy, 1 force, 2 stress
         self.alpha = None
         self.R_inv = None
         self.L_inv = None
@@ -536,6 +537,9 @@ class SparseGP:
             self.noise_vector, np.full(n_e, 1 / self.energy_noise ** 2),
             np.full(n_force, 1 / self.force_noise ** 2),
             np.full(n_s, 1 / self.stress_noise ** 2)])
+        self.label_kind = np.concatenate([
+            self.label_kind, np.zeros(n_e, np.int32), np.ones(n_force, np.int32),
+            np.full(n_s, 2, np.int32)])
         self.training_structures.append(structure)
         self.training_atom_indices.append(atoms)
 
@@ -582,13 +586,83 @@ class SparseGP:
         k = self.kernels[0]
         self.Kuu = k.envs_envs(sd, sd)
         self.Kuf = self._kuf_batched(sd, k)
+        self._solve()
+
+    def _solve(self):
+        sd = self.sparse_descriptors[0]
+        k = self.kernels[0]
         self.alpha, self.R_inv, self.L_inv = update_matrices_QR(
             self.Kuu, self.Kuf, self.y, self.noise_vector, self.Kuu_jitter)
         self.Sigma = self.R_inv @ self.R_inv.T
         self.Kuu_inverse = self.L_inv.T @ self.L_inv
+        self.L_diag = np.diag(self.L_inv).copy()
+        self.R_inv_diag = np.diag(self.R_inv).copy()
         self.b2 = sd.descriptor_calculator
         self._model = _Model(self.b2, k.sigma, k.power, sd, self.alpha, self.R_inv)
         self._mapped = False
+
+    # ---- hyperparameters and likelihood (sparse_gp.cpp:704-922, 1105-1140)
+    def set_hyperparameters(self, hyps):
+        """sparse_gp.cpp:1105-1140: Kuu and Kuf rescaled to the new sigma
+        (normalized_dot_product.cpp:581-615), the noise vector rebuilt from the
+        new noises, and the QR solve repeated on the GPU."""
+        hyps = f64(hyps)
+        k = self.kernels[0]
+        scale = hyps[0] * hyps[0] / (k.sigma * k.sigma)
+        self.Kuu = self.Kuu * scale
+        self.Kuf = self.Kuf * scale
+        k.sigma = float(hyps[0])
+        k.kernel_hyperparameters = np.array([k.sigma])
+        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[1:4])
+        inv_var = np.array([1 / self.energy_noise ** 2, 1 / self.force_noise ** 2,
+                            1 / self.stress_noise ** 2])
+        self.noise_vector = inv_var[self.label_kind]
+        self._solve()
+
+    def _likelihood(self, want_gradient, KnK=None, stream=None):
+        n, m = self.Kuf.shape
+        out = np.zeros(8)
+        Kuf, Kuu, y = f64(self.Kuf), f64(self.Kuu), f64(self.y)
+        kinds = i32(self.label_kind)
+        a, S = f64(self.alpha), f64(self.Sigma)
+        Ld, Rd = f64(self.L_diag), f64(self.R_inv_diag)
+        hyps = f64(self.hyperparameters)
+        check(lib().fpp_likelihood_gradient_stable(
+            n, m, ptr(Kuf), ptr(Kuu), ptr(y), ptr(kinds), ptr(a), ptr(S), ptr(Ld), ptr(Rd),
+            ptr(hyps), 1 if want_gradient else 0, ptr(out), ptr(KnK), _stream(stream)))
+        (self.log_marginal_likelihood, self.data_fit, self.complexity_penalty,
+         self.constant_term) = out[:4]
+        if want_gradient:
+            self.likelihood_gradient = out[4:8].copy()
+        return self.log_marginal_likelihood
+
+    def compute_likelihood_stable(self, stream=None):
+        """sparse_gp.cpp:704-732, on the GPU."""
+        return self._likelihood(False, stream=stream)
+
+    def compute_likelihood_gradient_stable(self, precomputed_KnK=False, stream=None):
+        """sparse_gp.cpp:734-862, on the GPU: returns the log marginal
+        likelihood and sets likelihood_gradient (sigma, sigma_e, sigma_f,
+        sigma_s).  The traces it needs come from one GEMM per call, so the
+        precomputed and direct forms of the reference give the same numbers."""
+        return self._likelihood(True, stream=stream)
+
+    def compute_KnK(self, precomputed=False, stream=None):
+        """sparse_gp.cpp:888-922: KnK_e, KnK_f, KnK_s = Kuf one_x Kuf^T."""
+        n = self.Kuf.shape[0]
+        KnK = np.zeros((3, n, n))
+        self._likelihood(False, KnK=KnK, stream=stream)
+        self.KnK_e, self.KnK_f, self.KnK_s = KnK
+        return KnK
+
+    def precompute_KnK(self, stream=None):
+        """sparse_gp.cpp:864-886: Kuf one_x Kuf^T / sigma^4 for later
+        hyperparameter changes."""
+        sig4 = self.kernels[0].sigma ** 4
+        KnK = self.compute_KnK(stream=stream)
+        self.Kuf_e_noise_Kfu = [KnK[0] / sig4]
+        self.Kuf_f_noise_Kfu = [KnK[1] / sig4]
+        self.Kuf_s_noise_Kfu = [KnK[2] / sig4]
 
     # ---- the reference's JSON state (sparse_gp.h:101-111, sparse_gp.cpp:1406-1417)
     def to_json(self, file_name):

@@ -331,6 +331,30 @@ int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                      void *stream);
 
 /* ------------------------------------------------------------------------
+ * Training side: the log marginal likelihood and its hyperparameter gradient
+ * for one NormalizedDotProduct kernel, FP64 on the GPU.
+ * SparseGP::compute_likelihood_stable (sparse_gp.cpp:704-732) and, with
+ * want_gradient, compute_likelihood_gradient_stable (sparse_gp.cpp:734-862).
+ * Host inputs: Kuf n x m (row-major), Kuu n x n (the kernel matrix without
+ * jitter), y m, label_kind m (0 energy, 1 force, 2 stress), alpha n,
+ * Sigma n x n (= R_inv R_inv^T), L_diag n and R_inv_diag n (diagonals of
+ * L_inv and R_inv from fpp_update_matrices_QR), hyps[4] = sigma, sigma_e,
+ * sigma_f, sigma_s.  out[4] = log marginal likelihood, data fit, complexity
+ * penalty, constant term; with want_gradient also out[4..7] = d/d hyps
+ * (Kuu and Sigma are then required).  KnK (host, optional): 3 x n x n,
+ * Kuf one_x Kuf^T for x = energy, force, stress (SparseGP::compute_KnK,
+ * sparse_gp.cpp:888-922).  FPP_ERR_NUMERIC for a zero or non-finite
+ * hyperparameter or a singular Kuu.
+ * ---------------------------------------------------------------------- */
+int fpp_likelihood_gradient_stable(int32_t n, int32_t m, const double *Kuf,
+                                   const double *Kuu, const double *y,
+                                   const int32_t *label_kind, const double *alpha,
+                                   const double *Sigma, const double *L_diag,
+                                   const double *R_inv_diag, const double *hyps,
+                                   int32_t want_gradient, double *out, double *KnK,
+                                   void *stream);
+
+/* ------------------------------------------------------------------------
  * ComputeFlareStdAtom (lammps_plugins/compute_flare_std_atom.cpp): the
  * per-atom uncertainty of the LAMMPS compute flare/std/atom.
  * ---------------------------------------------------------------------- */

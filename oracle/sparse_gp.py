@@ -28,6 +28,7 @@ class SparseGP:
         self.training_atom_indices = []
         self.y = np.zeros(0)
         self.noise_vector = np.zeros(0)
+        self.label_kind = np.zeros(0, dtype=np.int32)   # 0 energy, 1 force, 2 stress
 
     # ------------------------------------------------------------------
     def _init_sparse(self, structure):
@@ -83,6 +84,9 @@ class SparseGP:
             np.full(n_energy, 1 / self.energy_noise ** 2),
             np.full(n_force, 1 / self.force_noise ** 2),
             np.full(n_stress, 1 / self.stress_noise ** 2)])
+        self.label_kind = np.concatenate([
+            self.label_kind, np.zeros(n_energy, np.int32), np.ones(n_force, np.int32),
+            np.full(n_stress, 2, np.int32)])
         self.training_structures.append(structure)
         self.training_atom_indices.append(atoms)
 
@@ -121,9 +125,11 @@ class SparseGP:
 
     def update_matrices_QR(self):
         """sparse_gp.cpp:576-610."""
-        Kuu = self.Kuu()
-        Kuf = self.Kuf()
-        self.Kuu_mat, self.Kuf_mat = Kuu, Kuf
+        self.Kuu_mat, self.Kuf_mat = self.Kuu(), self.Kuf()
+        self._solve()
+
+    def _solve(self):
+        Kuu, Kuf = self.Kuu_mat, self.Kuf_mat
         n = Kuu.shape[0]
         L = np.linalg.cholesky(Kuu + self.Kuu_jitter * np.eye(n))
         self.L_inv = sla.solve_triangular(L, np.eye(n), lower=True)
@@ -135,6 +141,97 @@ class SparseGP:
         self.R_inv = sla.solve_triangular(R, np.eye(n), lower=False)
         self.alpha = self.R_inv @ (Q.T @ b)
         self.Sigma = self.R_inv @ self.R_inv.T
+        self.L_diag = np.diag(self.L_inv).copy()
+        self.R_inv_diag = np.diag(self.R_inv).copy()
+
+    # ---- likelihood (sparse_gp.cpp:704-992, 1105-1140) -------------------
+    @property
+    def hyperparameters(self):
+        return np.array([self.kernels[0].sigma, self.energy_noise, self.force_noise,
+                         self.stress_noise])
+
+    def set_hyperparameters(self, hyps):
+        """sparse_gp.cpp:1105-1140 for one NormalizedDotProduct kernel: Kuu and
+        Kuf rescaled by (sigma_new / sigma)^2 (Kuu_grad / Kuf_grad [0],
+        normalized_dot_product.cpp:581-615), the noise vector rebuilt, and
+        the QR solve repeated."""
+        k = self.kernels[0]
+        scale = hyps[0] * hyps[0] / k.sig2
+        self.Kuu_mat = self.Kuu_mat * scale
+        self.Kuf_mat = self.Kuf_mat * scale
+        k.sigma = float(hyps[0])
+        k.sig2 = k.sigma * k.sigma
+        k.kernel_hyperparameters = np.array([k.sigma])
+        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[1:4])
+        one = [self.label_kind == t for t in range(3)]
+        self.noise_vector = (one[0] / self.energy_noise ** 2 + one[1] / self.force_noise ** 2
+                             + one[2] / self.stress_noise ** 2)
+        self._solve()
+
+    def compute_likelihood(self):
+        """sparse_gp.cpp:959-992: Qff + Lambda through a column-pivoted QR."""
+        noise = 1 / self.noise_vector
+        Kuu_inverse = self.L_inv.T @ self.L_inv
+        Q = self.Kuf_mat.T @ Kuu_inverse @ self.Kuf_mat + np.diag(noise)
+        _, R, _ = sla.qr(Q, pivoting=True)
+        q_inv_y = np.linalg.solve(Q, self.y)
+        self.complexity_penalty = -np.sum(np.log(np.abs(np.diag(R)))) / 2
+        self.data_fit = -0.5 * self.y @ q_inv_y
+        self.constant_term = -0.5 * len(self.y) * np.log(2 * np.pi)
+        self.log_marginal_likelihood = (self.complexity_penalty + self.data_fit
+                                        + self.constant_term)
+        return self.log_marginal_likelihood
+
+    def compute_likelihood_stable(self):
+        """sparse_gp.cpp:704-732."""
+        nv = self.noise_vector
+        self.data_fit = -0.5 * self.y @ (nv * (self.y - self.Kuf_mat.T @ self.alpha))
+        self.constant_term = -0.5 * len(self.y) * np.log(2 * np.pi)
+        noise_det = np.sum(np.log(nv))
+        kuu_inv_det = -2 * np.sum(np.log(np.abs(self.L_diag)))
+        sigma_inv_det = 2 * np.sum(np.log(np.abs(self.R_inv_diag)))
+        self.complexity_penalty = 0.5 * (noise_det + kuu_inv_det + sigma_inv_det)
+        self.log_marginal_likelihood = (self.complexity_penalty + self.data_fit
+                                        + self.constant_term)
+        return self.log_marginal_likelihood
+
+    def compute_likelihood_gradient_stable(self):
+        """sparse_gp.cpp:734-862 (the form without precomputed KnK) for one
+        NormalizedDotProduct kernel: dKuu/dsigma = 2 Kuu / sigma and
+        dKuf/dsigma = 2 Kuf / sigma (normalized_dot_product.cpp:581-615).
+        Sets likelihood_gradient (sigma, sigma_e, sigma_f, sigma_s) and
+        returns the log marginal likelihood."""
+        sig = self.kernels[0].sigma
+        Kuf, Kuu, S, a, y = self.Kuf_mat, self.Kuu_mat, self.Sigma, self.alpha, self.y
+        nv = self.noise_vector
+        r = y - Kuf.T @ a
+        self.data_fit = -0.5 * y @ (nv * r)
+        self.constant_term = -0.5 * len(y) * np.log(2 * np.pi)
+        one = [(self.label_kind == t).astype(np.float64) for t in range(3)]
+        noises = [self.energy_noise, self.force_noise, self.stress_noise]
+        noise_det = -2 * sum(o.sum() * np.log(abs(s)) for o, s in zip(one, noises))
+        kuu_inv_det = -2 * np.sum(np.log(np.abs(self.L_diag)))
+        sigma_inv_det = 2 * np.sum(np.log(np.abs(self.R_inv_diag)))
+        self.complexity_penalty = 0.5 * (noise_det + kuu_inv_det + sigma_inv_det)
+        self.log_marginal_likelihood = (self.complexity_penalty + self.data_fit
+                                        + self.constant_term)
+        grad = np.zeros(4)
+        Kuu_grad = Kuu * (2 / sig)
+        Kuf_grad = Kuf * (2 / sig)
+        dKnK = Kuf_grad @ (nv[:, None] * Kuf.T)
+        Pi = dKnK + dKnK.T + Kuu_grad
+        cg = 0.5 * np.trace(np.linalg.inv(Kuu) @ Kuu_grad) - 0.5 * np.trace(Pi @ S)
+        dK_alpha = Kuf_grad.T @ a
+        dg = dK_alpha @ (nv * r) - 0.5 * a @ Kuu_grad @ a
+        grad[0] = cg + dg
+        for t in range(3):
+            KnK = Kuf @ (one[t][:, None] * Kuf.T)
+            s3 = noises[t] ** 3
+            cg = -one[t].sum() / noises[t] + np.trace(KnK @ S) / s3
+            dg = (r @ (one[t] * r)) / s3
+            grad[1 + t] = cg + dg
+        self.likelihood_gradient = grad
+        return self.log_marginal_likelihood
 
     # ------------------------------------------------------------------
     def kernel_mat(self, structure):

@@ -171,3 +171,27 @@ def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
     return dict(b2=b2, sd=sd, L_inv=L_inv, Kuu_inverse=L_inv.T @ L_inv, sigma=sigma,
                 power=power, cutoffs=cut, rc=rc, sparse_normed=sparse_normed,
                 settings=settings(2, 4, 2, rc, cut))
+
+
+def likelihood_model(seed=808, sigma=2.0, noises=(1.0, 2.0, 3.0), power=2):
+    """Two-species model for the likelihood tests: three 16-atom BCC alloy
+    frames (a = 3.6 A) rattled by 0.2 A (E, F, S labels from Lennard-Jones;
+    the second frame labels the forces of three atoms only) and 5 sparse
+    environments per frame, so that Kuu is well conditioned."""
+    rc = 4.0
+    b2 = OB2("chebyshev", "quadratic", [0, rc], [], [2, 4, 2])
+    gp = OSGP([ONDP(sigma, power)], *noises)
+    frames = []
+    for k in range(3):
+        cell, sp, pos = synth.bcc_alloy((2, 2, 2), seed + k, sigma=0.2, a=3.6)
+        s = OStructure(cell, sp, pos, rc, [b2])
+        e, f, st, _ = synth.lennard_jones(cell, pos)
+        s.energy = np.array([e])
+        s.forces = f.reshape(-1)
+        s.stresses = st
+        gp.add_training_structure(s, [0, 3, 5] if k == 1 else (-1,))
+        frames.append(s)
+    for k in range(3):
+        gp.add_specific_environments(frames[k], [(3 * k + 5 * j) % 16 for j in range(5)])
+    gp.update_matrices_QR()
+    return dict(b2=b2, gp=gp, frames=frames, rc=rc)
