@@ -282,10 +282,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     e64 = out_e.item()
     f64_forces = out_f.clone()
+    s64 = out_s.clone()
     step(0, _lib.FPP_PREC_MIXED)
     torch.cuda.synchronize()
     err_e = abs(out_e.item() - e64) / noa
     err_f = (out_f - f64_forces).abs().max().item()
+    err_s = (out_s - s64).abs().max().item()
     # ---- roofline of the dominant kernel (the contraction) ----
     peaks, peak_src = measured_peaks()
     nd = gp._model.n_descriptors
@@ -321,7 +323,8 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(noa * 3 * 8 + 8 + 6 * 8)},
         "fp64_gpu": {"value": round(world * noa / (fp64_ms / 1e3), 1), "unit": UNIT,
                      "ms_per_step": round(fp64_ms, 3)},
-        "errors_vs_fp64": {"energy_per_atom_eV": err_e, "force_max_eV_per_A": err_f},
+        "errors_vs_fp64": {"energy_per_atom_eV": err_e, "force_max_eV_per_A": err_f,
+                           "stress_max_eV_per_A3": err_s},
         "gpu_launches": int(K * launches_per_step(SETTINGS["n_species"])),
         "clocks": clk,
         "cpu_baseline": cpu,
