@@ -427,7 +427,9 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     V2<T> *z = reinterpret_cast<V2<T> *>(base + Lay.stage + Lay.csum + Lay.lists);
     b3_to_complex2<T>(c_s, NS * N, H, z, lane, HP);
     __syncwarp();
-    b3_contract<T>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, z, p_s, lane);
+    // FP32 at lmax 3 (the B3 workload shape): the contraction unrolled
+    constexpr int kB3L = (sizeof(T) == 4 && SH::kL1 == 4) ? 3 : -1;
+    b3_contract<T, kB3L>(a.lmax, a.n_ls, a.n_tri, H, pair_tab, z, p_s, lane);
     __syncwarp();
     for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
   }
@@ -886,7 +888,8 @@ __host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a) {
   return (b + 15) & ~(size_t)15;
 }
 
-template <typename T>
+// LM >= 0: the adjoint's terms unrolled for lmax = LM (a.lmax must equal it)
+template <typename T, int LM = -1>
 __global__ void __launch_bounds__(128)
 k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
         const int *__restrict__ row_of_atom, const int *__restrict__ tri,
@@ -921,7 +924,7 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   __syncwarp();
   for (int k = lane; k < sb; k += 32) u2[k] = V2<T>{T(0), T(0)};
   __syncwarp();
-  b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, z, w_s, up, u2, lane);
+  b3_contract_adjoint<T, LM>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, z, w_s, up, u2, lane);
   // dE/dc_real: for m > 0 with u+ = u[l, m], u- = u[l, -m], s = (-1)^m:
   //   dE/dR = (s Re u+ + Re u-) / sqrt 2,  dE/dS = (Im u- - s Im u+) / sqrt 2
   const T is2 = T(0.70710678118654752440);
@@ -1554,7 +1557,10 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
   if (wpb == 0) return -1;
   size_t smem = a.smem_per_warp_adj * wpb;
   if (a.kind == kB3) {
-    auto kern3 = k_b3_wu<T>;
+    // FP32 at lmax 3 (the B3 workload shape): the unrolled adjoint
+    auto kern3 = k_b3_wu<T, -1>;
+    if constexpr (sizeof(T) == 4)
+      if (a.lmax == 3) kern3 = k_b3_wu<T, 3>;
     if (cudaFuncSetAttribute(kern3, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;

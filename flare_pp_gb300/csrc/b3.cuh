@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -209,12 +210,27 @@ __device__ __forceinline__ void b3_to_complex2(const T *__restrict__ c, int nr, 
 // and triangle t, from the interleaved complex block; lanes take triples, all
 // lanes walk the same term list (the coefficients and harmonic indices are
 // uniform loads from constant memory).
-template <typename T>
+template <int LM, typename T>
+__device__ __forceinline__ void b3_contract_fixed(const V2<T> *__restrict__ z1,
+                                                  const V2<T> *__restrict__ z2,
+                                                  const V2<T> *__restrict__ z3,
+                                                  T *__restrict__ prow);
+
+template <typename T, int LM = -1>
 __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H,
                                              const int *__restrict__ tri,
                                              const V2<T> *__restrict__ z, T *__restrict__ p,
                                              int lane) {
   const int H1 = H + 1;
+  if constexpr (LM >= 0) {
+    // lmax = LM: every term unrolled (the same terms in the same order)
+    for (int r = lane; r < n_tri; r += 32) {
+      const int tr = tri[r];
+      b3_contract_fixed<LM, T>(z + (tr & 0xff) * H1, z + ((tr >> 8) & 0xff) * H1,
+                               z + (tr >> 16) * H1, p + r * n_ls);
+    }
+    return;
+  }
   const int *beg = c_b3.beg + c_b3.ls_off[lmax];
   for (int t = 0; t < n_ls; t++) {
     const int e0 = beg[t], e1 = beg[t + 1];
@@ -234,6 +250,185 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
   }
 }
 
+// ---------------------------------------------------------------------------
+// The term tables at compile time, in upload_b3_tables' order (lmax blocks,
+// triangles l1, l2, l3 in loop order, then m1, m2): for a fixed lmax the
+// adjoint below unrolls every term, so indices and coefficient addresses are
+// constants and the per-term sums stay in registers.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int b3_iabs(int v) { return v < 0 ? -v : v; }
+__host__ __device__ constexpr bool b3_tri_ok(int l1, int l2, int l3) {
+  return !(b3_iabs(l1 - l2) > l3 || l3 > l1 + l2);
+}
+__host__ __device__ constexpr int b3_tri_terms(int l1, int l2, int l3) {
+  int n = 0;
+  for (int m1 = -l1; m1 <= l1; m1++)
+    for (int m2 = -l2; m2 <= l2; m2++)
+      if (b3_iabs(m1 + m2) <= l3) n++;
+  return n;
+}
+// absolute index of the first term of triangle (L1, L2, L3) of block LM
+__host__ __device__ constexpr int b3_tri_first(int LM, int L1, int L2, int L3) {
+  int nt = 0;
+  for (int lm = 0; lm <= LM; lm++)
+    for (int l1 = 0; l1 <= lm; l1++)
+      for (int l2 = 0; l2 <= lm; l2++)
+        for (int l3 = 0; l3 <= lm; l3++) {
+          if (!b3_tri_ok(l1, l2, l3)) continue;
+          if (lm == LM && l1 == L1 && l2 == L2 && l3 == L3) return nt;
+          nt += b3_tri_terms(l1, l2, l3);
+        }
+  return -1;
+}
+// index of triangle (L1, L2, L3) within block LM (the column of w)
+__host__ __device__ constexpr int b3_tri_index(int LM, int L1, int L2, int L3) {
+  int t = 0;
+  for (int l1 = 0; l1 <= LM; l1++)
+    for (int l2 = 0; l2 <= LM; l2++)
+      for (int l3 = 0; l3 <= LM; l3++) {
+        if (!b3_tri_ok(l1, l2, l3)) continue;
+        if (l1 == L1 && l2 == L2 && l3 == L3) return t;
+        t++;
+      }
+  return -1;
+}
+// offset of term (M1, M2) within its triangle
+__host__ __device__ constexpr int b3_term_offset(int L1, int L2, int L3, int M1, int M2) {
+  int n = 0;
+  for (int m1 = -L1; m1 <= L1; m1++)
+    for (int m2 = -L2; m2 <= L2; m2++) {
+      if (b3_iabs(m1 + m2) > L3) continue;
+      if (m1 == M1 && m2 == M2) return n;
+      n++;
+    }
+  return -1;
+}
+
+template <int B, int E, typename F>
+__device__ __forceinline__ void b3_static_for(F &&f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    b3_static_for<B + 1, E>(f);
+  }
+}
+
+// One triangle of the adjoint for lane-private rows p1, p2, p3 (stride 32):
+// the terms of each m1 sum into a register pair before the one update of
+// p1[l1 m1]; the rows of positions 2 and 3 sum in registers over the whole
+// triangle.
+template <int LM, int L1, int L2, int L3, typename T>
+__device__ __forceinline__ void b3_adjoint_triangle(const V2<T> *__restrict__ z1,
+                                                    const V2<T> *__restrict__ z2,
+                                                    const V2<T> *__restrict__ z3,
+                                                    const T *__restrict__ wrow, V2<T> *p1,
+                                                    V2<T> *p2, V2<T> *p3) {
+  constexpr int t = b3_tri_index(LM, L1, L2, L3);
+  constexpr int q0 = b3_tri_first(LM, L1, L2, L3);
+  static_assert(t >= 0 && q0 >= 0, "triangle outside the tables");
+  const T wq = wrow[t];
+  V2<T> s2[2 * L2 + 1], s3[2 * L3 + 1];
+#pragma unroll
+  for (int j = 0; j < 2 * L2 + 1; j++) s2[j] = V2<T>{T(0), T(0)};
+#pragma unroll
+  for (int j = 0; j < 2 * L3 + 1; j++) s3[j] = V2<T>{T(0), T(0)};
+  b3_static_for<0, 2 * L1 + 1>([&](auto j1) {
+    constexpr int m1 = decltype(j1)::value - L1;
+    const V2<T> a = z1[L1 * L1 + L1 + m1];
+    V2<T> s1{T(0), T(0)};
+    b3_static_for<0, 2 * L2 + 1>([&](auto j2) {
+      constexpr int m2 = decltype(j2)::value - L2;
+      constexpr int m3 = -m1 - m2;
+      if constexpr (b3_iabs(m3) <= L3) {
+        constexpr int q = q0 + b3_term_offset(L1, L2, L3, m1, m2);
+        const T f = wq * b3_w<T>(q);
+        const V2<T> b = z2[L2 * L2 + L2 + m2], c = z3[L3 * L3 + L3 + m3];
+        s1.x += f * (b.x * c.x - b.y * c.y);
+        s1.y += f * (b.x * c.y + b.y * c.x);
+        s2[m2 + L2].x += f * (a.x * c.x - a.y * c.y);
+        s2[m2 + L2].y += f * (a.x * c.y + a.y * c.x);
+        s3[m3 + L3].x += f * (a.x * b.x - a.y * b.y);
+        s3[m3 + L3].y += f * (a.x * b.y + a.y * b.x);
+      }
+    });
+    V2<T> &d = p1[(L1 * L1 + L1 + m1) * 32];
+    d.x += s1.x;
+    d.y += s1.y;
+  });
+#pragma unroll
+  for (int j = 0; j < 2 * L2 + 1; j++) {
+    V2<T> &d = p2[(L2 * L2 + j) * 32];
+    d.x += s2[j].x;
+    d.y += s2[j].y;
+  }
+#pragma unroll
+  for (int j = 0; j < 2 * L3 + 1; j++) {
+    V2<T> &d = p3[(L3 * L3 + j) * 32];
+    d.x += s3[j].x;
+    d.y += s3[j].y;
+  }
+}
+
+// The forward sum of one triangle for one radial triple, terms in table order.
+template <int LM, int L1, int L2, int L3, typename T>
+__device__ __forceinline__ T b3_contract_triangle(const V2<T> *__restrict__ z1,
+                                                  const V2<T> *__restrict__ z2,
+                                                  const V2<T> *__restrict__ z3) {
+  constexpr int q0 = b3_tri_first(LM, L1, L2, L3);
+  static_assert(q0 >= 0, "triangle outside the tables");
+  T acc = T(0);
+  b3_static_for<0, 2 * L1 + 1>([&](auto j1) {
+    constexpr int m1 = decltype(j1)::value - L1;
+    const V2<T> a = z1[L1 * L1 + L1 + m1];
+    b3_static_for<0, 2 * L2 + 1>([&](auto j2) {
+      constexpr int m2 = decltype(j2)::value - L2;
+      constexpr int m3 = -m1 - m2;
+      if constexpr (b3_iabs(m3) <= L3) {
+        constexpr int q = q0 + b3_term_offset(L1, L2, L3, m1, m2);
+        const V2<T> b = z2[L2 * L2 + L2 + m2], c = z3[L3 * L3 + L3 + m3];
+        const T xr = a.x * b.x - a.y * b.y, xi = a.x * b.y + a.y * b.x;
+        acc += b3_w<T>(q) * (xr * c.x - xi * c.y);
+      }
+    });
+  });
+  return acc;
+}
+
+template <int LM, typename T>
+__device__ __forceinline__ void b3_contract_fixed(const V2<T> *__restrict__ z1,
+                                                  const V2<T> *__restrict__ z2,
+                                                  const V2<T> *__restrict__ z3,
+                                                  T *__restrict__ prow) {
+  b3_static_for<0, LM + 1>([&](auto i1) {
+    b3_static_for<0, LM + 1>([&](auto i2) {
+      b3_static_for<0, LM + 1>([&](auto i3) {
+        constexpr int l1 = decltype(i1)::value, l2 = decltype(i2)::value,
+                      l3 = decltype(i3)::value;
+        if constexpr (b3_tri_ok(l1, l2, l3))
+          prow[b3_tri_index(LM, l1, l2, l3)] = b3_contract_triangle<LM, l1, l2, l3, T>(z1, z2, z3);
+      });
+    });
+  });
+}
+
+// Every triangle of block LM, in table order.
+template <int LM, typename T>
+__device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
+                                                 const V2<T> *__restrict__ z2,
+                                                 const V2<T> *__restrict__ z3,
+                                                 const T *__restrict__ wrow, V2<T> *p1,
+                                                 V2<T> *p2, V2<T> *p3) {
+  b3_static_for<0, LM + 1>([&](auto i1) {
+    b3_static_for<0, LM + 1>([&](auto i2) {
+      b3_static_for<0, LM + 1>([&](auto i3) {
+        constexpr int l1 = decltype(i1)::value, l2 = decltype(i2)::value,
+                      l3 = decltype(i3)::value;
+        if constexpr (b3_tri_ok(l1, l2, l3))
+          b3_adjoint_triangle<LM, l1, l2, l3, T>(z1, z2, z3, wrow, p1, p2, p3);
+      });
+    });
+  });
+}
+
 // Adjoint of b3_contract: for dE/dp = w, the holomorphic derivative
 // u = dE/dc summed into u2[n * H + lm] = (re, im).  Lanes take radial triples
 // in rounds of 32; within a round lane r only updates the rows n1(r), n2(r),
@@ -242,7 +437,7 @@ __device__ __forceinline__ void b3_contract(int lmax, int n_ls, int n_tri, int H
 // atomics).  After each round the private rows are summed into u2 by output
 // entry, over lanes in a fixed rotated order.  The caller zeroes u2 and
 // synchronizes the warp before and after.
-template <typename T>
+template <typename T, int LM = -1>
 __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tri, int H,
                                                     int nr, const int *__restrict__ tri,
                                                     const V2<T> *__restrict__ z,
@@ -262,6 +457,9 @@ __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tr
       V2<T> *p1 = priv + lane;
       V2<T> *p2 = priv + (size_t)H * 32 + lane;
       V2<T> *p3 = priv + (size_t)(2 * H) * 32 + lane;
+      if constexpr (LM >= 0) {
+        b3_adjoint_fixed<LM, T>(z1, z2, z3, w + r * n_ls, p1, p2, p3);
+      } else
       for (int t = 0; t < n_ls; t++) {
         const int e0 = beg[t], e1 = beg[t + 1];
         const T wq = w[r * n_ls + t];
