@@ -879,12 +879,21 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
 // (the inverse of b3_to_complex's linear map), written to global memory.
 // ---------------------------------------------------------------------------
 template <typename T>
-__host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a) {
+__host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a, bool fixed = false) {
   const size_t nr = (size_t)a.n_species * a.N;
-  // w (padded to 4 entries), complex c, summed u, and per-lane private rows of
-  // the lane's triple (complex entries interleaved)
-  size_t b = sizeof(T) * ((size_t)((a.n_d + 3) & ~3) + 2 * nr * (a.H + 1) + 2 * nr * a.H +
-                          6 * (size_t)a.H * 32);
+  const size_t priv = 6 * (size_t)a.H * 32;
+  size_t b;
+  if (fixed) {
+    // the private rows share memory with the w rows of the first round
+    const size_t rows_a = (size_t)(a.n_tri < 32 ? a.n_tri : 32) * a.n_ls;
+    const size_t rows_b = (size_t)(a.n_tri > 32 ? a.n_tri - 32 : 0) * a.n_ls;
+    b = sizeof(T) * ((priv > rows_a ? priv : rows_a) + ((rows_b + 3) & ~(size_t)3) +
+                     2 * nr * (a.H + 1) + 2 * nr * a.H);
+  } else {
+    // w (padded to 4 entries), complex c, summed u, and per-lane private rows
+    // of the lane's triple (complex entries interleaved)
+    b = sizeof(T) * ((size_t)((a.n_d + 3) & ~3) + 2 * nr * (a.H + 1) + 2 * nr * a.H + priv);
+  }
   return (b + 15) & ~(size_t)15;
 }
 
@@ -902,10 +911,23 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   const int H = a.H, H1 = a.H + 1, nd = a.n_d;
   const int nr = a.n_species * a.N, sb = nr * H;
   unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);                        // [nd]
-  V2<T> *z = reinterpret_cast<V2<T> *>(w_s + ((nd + 3) & ~3));  // [nr][H+1] complex c
-  V2<T> *u2 = z + (size_t)nr * H1;                             // [sb] summed u
-  V2<T> *up = u2 + sb;                                         // [3 H][32] private rows
+  T *w_s = reinterpret_cast<T *>(base);  // [nd] (fixed: rows of triples < 32)
+  T *w_b = nullptr;                      // fixed: rows of triples >= 32
+  V2<T> *z, *u2, *up;                    // [nr][H+1] complex c, [sb] summed u,
+                                         // [3 H][32] private rows
+  const int rows_a = a.n_tri < 32 ? a.n_tri : 32;
+  if constexpr (LM >= 0) {
+    const size_t priv = 6 * (size_t)H * 32, wa = (size_t)rows_a * a.n_ls;
+    const size_t wbn = (size_t)(a.n_tri - rows_a) * a.n_ls;
+    w_b = w_s + (priv > wa ? priv : wa);
+    z = reinterpret_cast<V2<T> *>(w_b + ((wbn + 3) & ~(size_t)3));
+    u2 = z + (size_t)nr * H1;
+    up = reinterpret_cast<V2<T> *>(w_s);
+  } else {
+    z = reinterpret_cast<V2<T> *>(w_s + ((nd + 3) & ~3));
+    u2 = z + (size_t)nr * H1;
+    up = u2 + sb;
+  }
   if (atom >= a.noa) return;
   const int si = species[atom];
   const int row = row_of_atom[atom];
@@ -916,15 +938,26 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
   // real c staged through u2 (free until the accumulation below)
   T *cst = reinterpret_cast<T *>(u2);
   for (int k = lane; k < sb; k += 32) cst[k] = c_in[(size_t)atom * sb + k];
-  const double e =
-      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
+  const int split = rows_a * a.n_ls;
+  const double e = adjoint_w<T>(
+      a, g, si, row, nrm, nrm32,
+      [&](int d, T v) {
+        if (LM >= 0 && d >= split)
+          w_b[d - split] = v;
+        else
+          w_s[d] = v;
+      },
+      lane);
   if (lane == 0) atom_e[atom] = e;
   __syncwarp();
   b3_to_complex2<T>(cst, nr, H, z, lane);
   __syncwarp();
   for (int k = lane; k < sb; k += 32) u2[k] = V2<T>{T(0), T(0)};
   __syncwarp();
-  b3_contract_adjoint<T, LM>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, z, w_s, up, u2, lane);
+  if constexpr (LM >= 0)
+    b3_contract_adjoint_fixed<T, LM>(a.n_tri, H, nr, tri, z, w_s, w_b, up, u2, lane);
+  else
+    b3_contract_adjoint<T>(a.lmax, a.n_ls, a.n_tri, H, nr, tri, z, w_s, up, u2, lane);
   // dE/dc_real: for m > 0 with u+ = u[l, m], u- = u[l, -m], s = (-1)^m:
   //   dE/dR = (s Re u+ + Re u-) / sqrt 2,  dE/dS = (Im u- - s Im u+) / sqrt 2
   const T is2 = T(0.70710678118654752440);
@@ -1551,16 +1584,17 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                       double *reduce_out, bool gather, T *u_buf, long long n_pairs,
                       const int *nbr_i, cudaStream_t stream) {
   if (a.noa == 0) return 0;
-  a.smem_per_warp_adj = a.kind == kB3 ? b3_adjoint_smem_per_warp<T>(a)
+  // FP32 at lmax 3 (the B3 workload shape): the unrolled adjoint
+  const bool b3_fixed = a.kind == kB3 && sizeof(T) == 4 && a.lmax == 3;
+  a.smem_per_warp_adj = a.kind == kB3 ? b3_adjoint_smem_per_warp<T>(a, b3_fixed)
                                       : adjoint_smem_per_warp(a, sizeof(T));
   const int wpb = warps_per_block(a.smem_per_warp_adj);
   if (wpb == 0) return -1;
   size_t smem = a.smem_per_warp_adj * wpb;
   if (a.kind == kB3) {
-    // FP32 at lmax 3 (the B3 workload shape): the unrolled adjoint
     auto kern3 = k_b3_wu<T, -1>;
     if constexpr (sizeof(T) == 4)
-      if (a.lmax == 3) kern3 = k_b3_wu<T, 3>;
+      if (b3_fixed) kern3 = k_b3_wu<T, 3>;
     if (cudaFuncSetAttribute(kern3, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;

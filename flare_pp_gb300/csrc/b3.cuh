@@ -316,16 +316,16 @@ __device__ __forceinline__ void b3_static_for(F &&f) {
 // the terms of each m1 sum into a register pair before the one update of
 // p1[l1 m1]; the rows of positions 2 and 3 sum in registers over the whole
 // triangle.
-template <int LM, int L1, int L2, int L3, typename T>
+template <int LM, int L1, int L2, int L3, typename T, int NLS>
 __device__ __forceinline__ void b3_adjoint_triangle(const V2<T> *__restrict__ z1,
                                                     const V2<T> *__restrict__ z2,
                                                     const V2<T> *__restrict__ z3,
-                                                    const T *__restrict__ wrow, V2<T> *p1,
+                                                    const T (&wr)[NLS], V2<T> *p1,
                                                     V2<T> *p2, V2<T> *p3) {
   constexpr int t = b3_tri_index(LM, L1, L2, L3);
   constexpr int q0 = b3_tri_first(LM, L1, L2, L3);
-  static_assert(t >= 0 && q0 >= 0, "triangle outside the tables");
-  const T wq = wrow[t];
+  static_assert(t >= 0 && t < NLS && q0 >= 0, "triangle outside the tables");
+  const T wq = wr[t];
   V2<T> s2[2 * L2 + 1], s3[2 * L3 + 1];
 #pragma unroll
   for (int j = 0; j < 2 * L2 + 1; j++) s2[j] = V2<T>{T(0), T(0)};
@@ -411,11 +411,21 @@ __device__ __forceinline__ void b3_contract_fixed(const V2<T> *__restrict__ z1,
 }
 
 // Every triangle of block LM, in table order.
-template <int LM, typename T>
+// triangles of block LM (b3_n_ls at compile time)
+__host__ __device__ constexpr int b3_n_triangles(int LM) {
+  int t = 0;
+  for (int l1 = 0; l1 <= LM; l1++)
+    for (int l2 = 0; l2 <= LM; l2++)
+      for (int l3 = 0; l3 <= LM; l3++)
+        if (b3_tri_ok(l1, l2, l3)) t++;
+  return t;
+}
+
+template <int LM, typename T, int NLS>
 __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
                                                  const V2<T> *__restrict__ z2,
                                                  const V2<T> *__restrict__ z3,
-                                                 const T *__restrict__ wrow, V2<T> *p1,
+                                                 const T (&wr)[NLS], V2<T> *p1,
                                                  V2<T> *p2, V2<T> *p3) {
   b3_static_for<0, LM + 1>([&](auto i1) {
     b3_static_for<0, LM + 1>([&](auto i2) {
@@ -423,7 +433,7 @@ __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
         constexpr int l1 = decltype(i1)::value, l2 = decltype(i2)::value,
                       l3 = decltype(i3)::value;
         if constexpr (b3_tri_ok(l1, l2, l3))
-          b3_adjoint_triangle<LM, l1, l2, l3, T>(z1, z2, z3, wrow, p1, p2, p3);
+          b3_adjoint_triangle<LM, l1, l2, l3, T, NLS>(z1, z2, z3, wr, p1, p2, p3);
       });
     });
   });
@@ -437,7 +447,78 @@ __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
 // atomics).  After each round the private rows are summed into u2 by output
 // entry, over lanes in a fixed rotated order.  The caller zeroes u2 and
 // synchronizes the warp before and after.
-template <typename T, int LM = -1>
+// u2[n, lm] += the private rows of one round, over lanes j in a fixed rotated
+// order (lanes read different banks) and positions with n_pos(j) == n.
+template <typename T>
+__device__ __forceinline__ void b3_reduce_private(int r0, int n_tri, int H, int nr,
+                                                  const int *__restrict__ tri,
+                                                  const V2<T> *__restrict__ priv,
+                                                  V2<T> *__restrict__ u2, int lane) {
+  for (int k = lane; k < nr * H; k += 32) {
+    const int n = k / H, lm = k - n * H;
+    V2<T> acc{T(0), T(0)};
+    for (int j0 = 0; j0 < 32; j0++) {
+      const int j = (j0 + lane) & 31;
+      if (r0 + j >= n_tri) continue;
+      const int tj = tri[r0 + j];
+      const V2<T> *col = priv + (size_t)lm * 32 + j;
+      if ((tj & 0xff) == n) {
+        const V2<T> v = col[0];
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+      if (((tj >> 8) & 0xff) == n) {
+        const V2<T> v = col[H * 32];
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+      if ((tj >> 16) == n) {
+        const V2<T> v = col[(2 * H) * 32];
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+    }
+    u2[k].x += acc.x;
+    u2[k].y += acc.y;
+  }
+}
+
+// The adjoint with every term unrolled for lmax = LM.  Each lane first copies
+// its triple's row of w into registers, so the rows of the first round (wa)
+// may share memory with the private rows; the rows of later rounds (wb, triple
+// r >= 32 at wb + (r - 32) n_ls) are kept apart.
+template <typename T, int LM>
+__device__ __forceinline__ void b3_contract_adjoint_fixed(int n_tri, int H, int nr,
+                                                          const int *__restrict__ tri,
+                                                          const V2<T> *__restrict__ z,
+                                                          const T *wa, const T *wb,
+                                                          V2<T> *priv, V2<T> *__restrict__ u2,
+                                                          int lane) {
+  constexpr int NLS = b3_n_triangles(LM);
+  const int H1 = H + 1;
+  for (int r0 = 0; r0 < n_tri; r0 += 32) {
+    const int r = r0 + lane;
+    const bool live = r < n_tri;
+    const int tr = live ? tri[r] : 0;
+    T wr[NLS];
+    const T *wrow = r < 32 ? wa + r * NLS : wb + (r - 32) * NLS;
+#pragma unroll
+    for (int t = 0; t < NLS; t++) wr[t] = live ? wrow[t] : T(0);
+    __syncwarp();  // every row is in registers before the private rows are zeroed
+    for (int k = 0; k < 3 * H; k++) priv[k * 32 + lane] = V2<T>{T(0), T(0)};
+    if (live) {
+      const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
+      b3_adjoint_fixed<LM, T, NLS>(z + n1 * H1, z + n2 * H1, z + n3 * H1, wr, priv + lane,
+                                   priv + (size_t)H * 32 + lane,
+                                   priv + (size_t)(2 * H) * 32 + lane);
+    }
+    __syncwarp();
+    b3_reduce_private<T>(r0, n_tri, H, nr, tri, priv, u2, lane);
+    __syncwarp();
+  }
+}
+
+template <typename T>
 __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tri, int H,
                                                     int nr, const int *__restrict__ tri,
                                                     const V2<T> *__restrict__ z,
@@ -457,9 +538,6 @@ __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tr
       V2<T> *p1 = priv + lane;
       V2<T> *p2 = priv + (size_t)H * 32 + lane;
       V2<T> *p3 = priv + (size_t)(2 * H) * 32 + lane;
-      if constexpr (LM >= 0) {
-        b3_adjoint_fixed<LM, T>(z1, z2, z3, w + r * n_ls, p1, p2, p3);
-      } else
       for (int t = 0; t < n_ls; t++) {
         const int e0 = beg[t], e1 = beg[t + 1];
         const T wq = w[r * n_ls + t];
@@ -482,34 +560,7 @@ __device__ __forceinline__ void b3_contract_adjoint(int lmax, int n_ls, int n_tr
       }
     }
     __syncwarp();
-    // u2[n, lm] += sum over lanes j and positions with n_pos(j) == n
-    for (int k = lane; k < nr * H; k += 32) {
-      const int n = k / H, lm = k - n * H;
-      V2<T> acc{T(0), T(0)};
-      for (int j0 = 0; j0 < 32; j0++) {
-        const int j = (j0 + lane) & 31;  // rotated: lanes read different banks
-        if (r0 + j >= n_tri) continue;
-        const int tj = tri[r0 + j];
-        const V2<T> *col = priv + (size_t)lm * 32 + j;
-        if ((tj & 0xff) == n) {
-          const V2<T> v = col[0];
-          acc.x += v.x;
-          acc.y += v.y;
-        }
-        if (((tj >> 8) & 0xff) == n) {
-          const V2<T> v = col[H * 32];
-          acc.x += v.x;
-          acc.y += v.y;
-        }
-        if ((tj >> 16) == n) {
-          const V2<T> v = col[(2 * H) * 32];
-          acc.x += v.x;
-          acc.y += v.y;
-        }
-      }
-      u2[k].x += acc.x;
-      u2[k].y += acc.y;
-    }
+    b3_reduce_private<T>(r0, n_tri, H, nr, tri, priv, u2, lane);
     __syncwarp();
   }
 }
