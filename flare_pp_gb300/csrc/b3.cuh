@@ -448,19 +448,26 @@ __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
 // entry, over lanes in a fixed rotated order.  The caller zeroes u2 and
 // synchronizes the warp before and after.
 // u2[n, lm] += the private rows of one round, over lanes j in a fixed rotated
-// order (lanes read different banks) and positions with n_pos(j) == n.
+// order (lanes read different banks) and positions with n_pos(j) == n.  Each
+// lane reads its own triple once; the others come by shuffle, in loops whose
+// trip counts are the same for every lane.
 template <typename T>
 __device__ __forceinline__ void b3_reduce_private(int r0, int n_tri, int H, int nr,
                                                   const int *__restrict__ tri,
                                                   const V2<T> *__restrict__ priv,
                                                   V2<T> *__restrict__ u2, int lane) {
-  for (int k = lane; k < nr * H; k += 32) {
-    const int n = k / H, lm = k - n * H;
+  const int own = r0 + lane < n_tri ? tri[r0 + lane] : -1;
+  const int total = nr * H;
+  for (int k0 = 0; k0 < total; k0 += 32) {
+    const int k = k0 + lane;
+    const bool act = k < total;
+    const int n = act ? k / H : -1;
+    const int lm = act ? k - n * H : 0;
     V2<T> acc{T(0), T(0)};
     for (int j0 = 0; j0 < 32; j0++) {
       const int j = (j0 + lane) & 31;
-      if (r0 + j >= n_tri) continue;
-      const int tj = tri[r0 + j];
+      const int tj = __shfl_sync(0xffffffffu, own, j);
+      if (tj < 0) continue;  // no triple in this round's slot j
       const V2<T> *col = priv + (size_t)lm * 32 + j;
       if ((tj & 0xff) == n) {
         const V2<T> v = col[0];
@@ -478,8 +485,10 @@ __device__ __forceinline__ void b3_reduce_private(int r0, int n_tri, int H, int 
         acc.y += v.y;
       }
     }
-    u2[k].x += acc.x;
-    u2[k].y += acc.y;
+    if (act) {
+      u2[k].x += acc.x;
+      u2[k].y += acc.y;
+    }
   }
 }
 
