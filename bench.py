@@ -414,6 +414,46 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def measure_matmul_peaks(n=8192, seconds=4.0):
+    """FP64 and TF32 matmul peaks of this GPU, the way the bf16 peak is
+    measured: torch.matmul of n^3 (2 n^3 FLOP), best of 10 (burst) and back to
+    back for `seconds` (sustained), CUDA events.  The FP64 figures bound the
+    FP64 path (cuBLAS DGEMM contraction, training solve, uncertainties)."""
+    import torch
+    dev = torch.device("cuda", 0)
+    out = {}
+    for name, dtype, tf32 in (("fp64", torch.float64, False), ("tf32", torch.float32, True)):
+        torch.backends.cuda.matmul.allow_tf32 = tf32
+        a = torch.randn(n, n, dtype=dtype, device=dev)
+        b = torch.randn(n, n, dtype=dtype, device=dev)
+        c = torch.empty(n, n, dtype=dtype, device=dev)
+        for _ in range(3):
+            torch.matmul(a, b, out=c)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        reps = max(1, int(seconds / best))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        sus = e0.elapsed_time(e1) * 1e-3 / reps
+        flop = 2.0 * n ** 3
+        out[name] = {"tflops_burst": flop / best / 1e12, "tflops_sustained": flop / sus / 1e12,
+                     "n": n, "sustained_reps": reps}
+        del a, b, c
+    torch.backends.cuda.matmul.allow_tf32 = False
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,7 +464,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-atoms", type=int, default=2048)
     ap.add_argument("--workload", default="bcc_alloy_32k", choices=sorted(WORKLOADS))
+    ap.add_argument("--measure-peaks", action="store_true",
+                    help="print the FP64 and TF32 matmul peaks and exit")
     args = ap.parse_args()
+    if args.measure_peaks:
+        print(json.dumps(measure_matmul_peaks()))
+        return
     select_workload(args.workload)
     if args.warmup < 3:
         args.warmup = 3
