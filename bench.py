@@ -130,9 +130,16 @@ class ClockSampler:
         # on each side: nvidia-smi prints a sample up to 100 ms after taking it)
         b = getattr(self, "t_begin", -1e30)
         e = getattr(self, "t_end", 1e30) + 0.1
-        for t, ln in self.lines:
-            if t < b or t > e:
-                continue
+        inside = [(t, ln) for t, ln in self.lines if b <= t <= e]
+        window = "timed steps"
+        if not inside and self.lines:
+            # timed steps shorter than the sample period: the samples just
+            # before and just after them
+            before = [x for x in self.lines if x[0] < b][-1:]
+            after = [x for x in self.lines if x[0] > e][:1]
+            inside = before + after
+            window = "adjacent to the timed steps (shorter than a sample period)"
+        for t, ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -146,7 +153,7 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window}
 
 
 def measured_peaks():
