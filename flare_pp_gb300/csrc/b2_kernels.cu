@@ -1296,7 +1296,7 @@ constexpr int kGatherWarps = 8;
 
 // Float-float sum over the kGatherLanes lanes of a group (xor offsets stay
 // inside the group), every lane of the group ends with the total.
-constexpr int kGatherLanes = 8;  // lanes per atom (four atoms per warp)
+constexpr int kGatherLanes = 4;  // lanes per atom (eight atoms per warp)
 __device__ __forceinline__ void ff_group_sum(float &hi, float &lo) {
 #pragma unroll
   for (int o = kGatherLanes / 2; o > 0; o >>= 1) {
