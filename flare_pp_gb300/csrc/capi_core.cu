@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -50,18 +51,23 @@ int DevBuf::reserve(size_t n) {
 
 static int ensure_tables(cudaStream_t stream) {
   // the harmonic normalisation and B3 coupling tables live in constant memory
-  // of this module; upload them once per device
-  static int uploaded_mask = 0;
+  // of this module; upload them once per device (under a lock: host threads
+  // may make their first call on a device at the same time)
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static bool uploaded[kMaxDev] = {false};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(FPP_ERR_CUDA, "no CUDA device");
-  if (dev < 31 && (uploaded_mask >> dev) & 1) return FPP_OK;
+  if (dev < 0 || dev >= kMaxDev) return fail(FPP_ERR_UNSUPPORTED, "device index beyond 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (uploaded[dev]) return FPP_OK;
   if (upload_harmonic_tables(stream) != 0)
     return fail(FPP_ERR_CUDA, "upload of harmonic tables failed");
   if (upload_descriptor_tables(stream) != 0)
     return fail(FPP_ERR_CUDA, "upload of B3 coupling tables failed");
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_fail(e, "upload of harmonic tables");
-  if (dev < 31) uploaded_mask |= 1 << dev;
+  uploaded[dev] = true;
   return FPP_OK;
 }
 

@@ -2,18 +2,23 @@
 //
 // Some callers cannot allocate device memory at the point where they need
 // descriptors: an MD engine that owns all device memory through its own pool
-// (nothing may be cudaMalloc'd behind its back), code that runs while a
-// stream is being captured into a CUDA graph, or a real-time loop with a fixed
-// memory budget.  fpp_b2_descriptors_noalloc serves them: the caller passes
-// the pair geometry and the output buffers, and the only scratch the forward
-// kernel needs (the single-bond coefficients, an identity row map and the
-// radial-pair table) lives in the fixed arrays below, which every GPU that
-// loads this library holds until the process exits.
+// (nothing may be cudaMalloc'd behind its back), or a real-time loop with a
+// fixed memory budget decided up front.  fpp_b2_descriptors_noalloc serves
+// them: the caller passes the pair geometry and the output buffers, and the
+// only scratch the forward kernel needs (the single-bond coefficients, an
+// identity row map and the radial-pair table) lives in the fixed arrays below,
+// which every GPU that loads this library holds until the process exits.
+//
+// The first call on a device does a one-time set-up with that device current:
+// it resolves the arrays' device addresses (cudaGetSymbolAddress), uploads the
+// harmonic normalisation table and synchronizes the stream.  Make that first
+// call before any stream capture begins.
 #include <cuda_runtime.h>
 
-#include <cstring>
-
+#include <atomic>
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 #include <string>
 
 #include "b2_kernels.h"
@@ -33,29 +38,34 @@ static __device__ __align__(256) double g_noalloc_c[kNoAllocC];
 static __device__ __align__(256) int g_noalloc_rows[kNoAllocAtoms];
 static __device__ __align__(256) int g_noalloc_tab[kNoAllocPairTab];
 
-// Device addresses of the arrays above, resolved once per device.
+// Device addresses of the arrays above, resolved once per device.  In host
+// code the arrays' names stand for host-side shadows, never device addresses.
 struct NoAllocSlot {
-  bool ready = false;
+  std::atomic<bool> ready{false};
   double *c = nullptr;
   int *rows = nullptr;
   int *tab = nullptr;
 };
 static NoAllocSlot g_slots[64];
+static std::mutex g_setup_mu;  // serialises first calls from several host threads
 
 static int noalloc_setup(NoAllocSlot **out, cudaStream_t st) {
   int dev = 0;
   FPP_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(FPP_ERR_UNSUPPORTED, "device index beyond 63");
   NoAllocSlot &s = g_slots[dev];
-  if (!s.ready) {
-    // host code must not use the arrays' names as device addresses
-    FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.c), g_noalloc_c));
-    FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.rows), g_noalloc_rows));
-    FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.tab), g_noalloc_tab));
-    if (upload_harmonic_tables(st) != 0)
-      return fail(FPP_ERR_CUDA, "upload of harmonic tables failed");
-    FPP_CUDA(cudaStreamSynchronize(st));
-    s.ready = true;
+  if (!s.ready.load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!s.ready.load(std::memory_order_relaxed)) {
+      FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.c), g_noalloc_c));
+      FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.rows), g_noalloc_rows));
+      FPP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&s.tab), g_noalloc_tab));
+      if (upload_harmonic_tables(st) != 0)
+        return fail(FPP_ERR_CUDA, "upload of harmonic tables failed");
+      FPP_CUDA(cudaStreamSynchronize(st));
+      // the addresses above become visible to other threads with the flag
+      s.ready.store(true, std::memory_order_release);
+    }
   }
   *out = &s;
   return FPP_OK;

@@ -12,7 +12,8 @@
 // would each round against its magnitude (measured: 1.6x the force error).
 //
 // One persistent CTA per SM walks the 128 x 128 tiles of all species blocks
-// (each block of P rows against its own B), in one launch:
+// (each block of P rows against its own B), in one launch; every CTA loads
+// all four operand planes of its own tile (no clusters):
 //   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of P_hi, P_lo,
 //                  B_hi, B_lo (64 K-columns per stage) into a 3-stage ring
 //   warp 1 lane 0  MMA issuer: 4 K=16 steps x 3 tcgen05.mma per stage,
@@ -31,6 +32,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 #include "gemm_tc.h"
@@ -133,48 +135,6 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
       : "memory");
 }
 
-// Cluster forms: the A tile is loaded once per CTA pair and multicast into
-// both CTAs' shared memory; each CTA's MMA completion frees the stage in both.
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap *map,
-                                               uint32_t bar, int c0, int c1, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%3, %4}], [%2], %5;" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "h"(mask)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster"
-      ".b64 [%0], %1;" ::"r"(bar),
-      "h"(mask)
-      : "memory");
-}
-
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-__device__ __forceinline__ uint32_t cluster_id_x() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-  return r;
-}
-
-__device__ __forceinline__ uint32_t n_clusters_x() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-  return r;
-}
-
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
-               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   uint32_t r[32];
   asm volatile(
@@ -201,8 +161,8 @@ struct GroupedParams {
   CUtensorMap b_hi[kGemmMaxGroups], b_lo[kGemmMaxGroups];
   int row0[kGemmMaxGroups], M[kGemmMaxGroups];
   float scale[kGemmMaxGroups];
-  int pair_start[kGemmMaxGroups + 1];  // CTA-pair work items per group (prefix)
-  int n_groups, tiles_np, N, K;         // tiles_np: column-tile pairs per row tile
+  int tile_start[kGemmMaxGroups + 1];  // work items (tiles) per group (prefix)
+  int n_groups, tiles_n, N, K;          // tiles_n: column tiles per row tile
   float *V;
   int ldv;
   DeviceStatus *status;
@@ -228,15 +188,14 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
   auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + 2 + b); };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_pairs = p.pair_start[p.n_groups];
+  const int n_tiles = p.tile_start[p.n_groups];
   const int kblocks = (p.K + BK - 1) / BK;
-  const int rank = (int)cluster_ctarank();  // 0 or 1 within the CTA pair
-  const int cid = (int)cluster_id_x(), ncl = (int)n_clusters_x();
+  const int cid = (int)blockIdx.x, ncl = (int)gridDim.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(full_bar(s), 1);
-      mbar_init(empty_bar(s), 2);  // both CTAs' MMAs must have read the stage
+      mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(accf_bar(b), 1);
@@ -256,23 +215,22 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  // the peer's multicasts and arrivals may target this CTA from here on
-  cluster_sync_all();
 
-  // work item (a pair of column tiles of one row tile; this CTA takes the
-  // column tile of its rank) -> (group, row of the operand block, first column)
+  // work item (one 128 x 128 tile; consecutive items share a row tile, so the
+  // CTAs running at once read each A tile from L2 rather than DRAM)
+  // -> (group, row of the operand block, first column)
   auto locate = [&](int t, int &g, int &mrow, int &n0) {
     g = 0;
-    while (g + 1 < p.n_groups && t >= p.pair_start[g + 1]) g++;
-    const int lt = t - p.pair_start[g];
-    mrow = (lt / p.tiles_np) * BM;
-    n0 = (2 * (lt % p.tiles_np) + rank) * BN;
+    while (g + 1 < p.n_groups && t >= p.tile_start[g + 1]) g++;
+    const int lt = t - p.tile_start[g];
+    mrow = (lt / p.tiles_n) * BM;
+    n0 = (lt % p.tiles_n) * BN;
   };
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer ----------------
     int it = 0;
-    for (int t = cid; t < n_pairs && !*abort_flag; t += ncl) {
+    for (int t = cid; t < n_tiles && !*abort_flag; t += ncl) {
       int g, mrow, n0;
       locate(t, g, mrow, n0);
       const int arow = p.row0[g] + mrow;
@@ -286,19 +244,16 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
         }
         if (*abort_flag) break;
         const uint32_t st = base + s * STAGE_BYTES;
-        // this CTA's B planes, plus one A plane from each CTA of the pair
         mbar_expect_tx(full_bar(s), STAGE_BYTES);
         const int kc = kb * BK;
-        if (rank == 0)
-          tma_load_2d_mc(st, &p.a_hi, full_bar(s), kc, arow, (uint16_t)3);
-        else
-          tma_load_2d_mc(st + A_TILE, &p.a_lo, full_bar(s), kc, arow, (uint16_t)3);
+        tma_load_2d(st, &p.a_hi, full_bar(s), kc, arow);
+        tma_load_2d(st + A_TILE, &p.a_lo, full_bar(s), kc, arow);
         tma_load_2d(st + 2 * A_TILE, &p.b_hi[g], full_bar(s), kc, n0);
         tma_load_2d(st + 2 * A_TILE + B_TILE, &p.b_lo[g], full_bar(s), kc, n0);
       }
     }
-    // drain: every stage this CTA filled has been read by both CTAs (so no
-    // arrival or multicast of this pair is still in flight at exit)
+    // drain: every stage this CTA filled has been read (no MMA completion
+    // arrival is still in flight at exit)
     for (int d = 0; d < STAGES && !*abort_flag; d++, it++) {
       if (!mbar_wait(empty_bar(it % STAGES), (uint32_t)(((it / STAGES) & 1) ^ 1))) {
         set_status(p.status, FPP_ERR_TIMEOUT, 115, d);
@@ -308,7 +263,7 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
     int it = 0, j = 0;
-    for (int t = cid; t < n_pairs; t += ncl, j++) {
+    for (int t = cid; t < n_tiles; t += ncl, j++) {
       const int buf = j & 1;
       const uint32_t acc0 = tmem + (uint32_t)(buf * 2 * BN), acc1 = acc0 + BN;
       if (!mbar_wait(acce_bar(buf), (uint32_t)(((j >> 1) & 1) ^ 1))) {
@@ -346,7 +301,7 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
           mma_f16<2 * BN>(acc0, smem_desc(a_hi + off), smem_desc(b_hi + off), first);
           mma_f16<BN>(acc1, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
         }
-        mma_commit_mc(empty_bar(s), (uint16_t)3);  // frees the stage in both CTAs
+        mma_commit(empty_bar(s));  // frees the stage once these MMAs have read it
       }
       mma_commit(accf_bar(buf));
       if (!ok) break;
@@ -356,7 +311,7 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     int j = 0;
-    for (int t = cid; t < n_pairs; t += ncl, j++) {
+    for (int t = cid; t < n_tiles; t += ncl, j++) {
       const int buf = j & 1;
       bool have = mbar_wait(accf_bar(buf), (uint32_t)((j >> 1) & 1));
       have = __all_sync(0xffffffffu, have) != 0;
@@ -411,7 +366,6 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
                  "r"(TMEM_COLS)
                  : "memory");
   }
-  cluster_sync_all();
 }
 
 // ---------------------------------------------------------------------------
@@ -420,15 +374,17 @@ k_split_gemm_grouped(const __grid_constant__ GroupedParams p) {
 // The tensor-map encoder is a driver entry point; it is resolved through the
 // runtime so that the library does not link libcuda directly.
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // resolved once per process (a function-local static initialises once
+  // even when several host threads get here first together)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
                                          cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+  }();
   return fn;
 }
 
@@ -449,6 +405,32 @@ static int make_map(CUtensorMap *map, const void *ptr, int inner, int rows,
 
 int split_gemm_smem_bytes() { return SMEM_BYTES; }
 
+// The shared-memory attribute and the resident CTA count are properties of a
+// device: set and measured once per device, under a lock (host threads may
+// launch on several devices).
+static int launch_shape(int dev, int *ctas) {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static int cached[kMaxDev] = {0};
+  if (dev < 0 || dev >= kMaxDev) return -1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (cached[dev] == 0) {
+    if (cudaFuncSetAttribute(k_split_gemm_grouped,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SMEM_BYTES) != cudaSuccess)
+      return -1;
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split_gemm_grouped, 192,
+                                                      SMEM_BYTES) != cudaSuccess)
+      return -1;
+    if (per_sm < 1) return -1;
+    cached[dev] = sms * per_sm;
+  }
+  *ctas = cached[dev];
+  return 0;
+}
+
 int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream) {
   if (g.n_groups <= 0 || g.N <= 0) return 0;
   if (g.n_groups > kGemmMaxGroups) return -2;
@@ -461,7 +443,6 @@ int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream) {
       make_map(&p.a_lo, g.a_lo, g.K, g.a_rows, g.lda, BM))
     return -3;
   const int tiles_n = (g.N + BN - 1) / BN;
-  const int tiles_np = (tiles_n + 1) / 2;  // an odd last tile pairs with an empty one
   int tiles = 0;
   for (int k = 0; k < g.n_groups; k++) {
     const GemmGroup &q = g.group[k];
@@ -474,55 +455,29 @@ int launch_split_gemm_grouped(const GroupedGemmArgs &g, cudaStream_t stream) {
     p.row0[k] = q.row0;
     p.M[k] = q.M;
     p.scale[k] = q.out_scale;
-    p.pair_start[k] = tiles;
-    tiles += ((q.M + BM - 1) / BM) * tiles_np;
+    p.tile_start[k] = tiles;
+    tiles += ((q.M + BM - 1) / BM) * tiles_n;
   }
-  p.pair_start[g.n_groups] = tiles;
+  p.tile_start[g.n_groups] = tiles;
   p.n_groups = g.n_groups;
-  p.tiles_np = tiles_np;
+  p.tiles_n = tiles_n;
   p.N = g.N;
   p.K = g.K;
   p.V = g.V;
   p.ldv = g.ldv;
   p.status = g.status;
   if (tiles == 0) return 0;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(k_split_gemm_grouped,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             SMEM_BYTES) != cudaSuccess)
-      return -1;
-    attr = true;
-  }
-  int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return -1;
-  // CTA pairs (clusters of two), one CTA per SM, no more pairs than can be
-  // resident at once (the two SMs of a pair must share a GPC)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  int ctas = 0;
+  if (launch_shape(dev, &ctas) != 0) return -1;
+  // one persistent CTA per SM (the shared-memory ring admits one per SM)
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.blockDim = dim3(192, 1, 1);
   cfg.dynamicSmemBytes = SMEM_BYTES;
   cfg.stream = stream;
-  cudaLaunchAttribute attrs[1];
-  attrs[0].id = cudaLaunchAttributeClusterDimension;
-  attrs[0].val.clusterDim.x = 2;
-  attrs[0].val.clusterDim.y = 1;
-  attrs[0].val.clusterDim.z = 1;
-  cfg.attrs = attrs;
-  cfg.numAttrs = 1;
-  static int resident = 0;
-  if (resident == 0) {
-    cfg.gridDim = dim3(sms & ~1, 1, 1);
-    int nc = 0;
-    if (cudaOccupancyMaxActiveClusters(&nc, k_split_gemm_grouped, &cfg) != cudaSuccess ||
-        nc <= 0)
-      nc = sms / 2;
-    resident = nc < sms / 2 ? nc : sms / 2;
-  }
-  const int pairs = tiles < resident ? tiles : resident;
-  cfg.gridDim = dim3(2 * pairs, 1, 1);
+  cfg.gridDim = dim3(tiles < ctas ? tiles : ctas, 1, 1);
   if (cudaLaunchKernelEx(&cfg, k_split_gemm_grouped, p) != cudaSuccess) return -1;
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

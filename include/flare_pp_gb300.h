@@ -153,9 +153,9 @@ int fpp_b2_compute(const fpp_b2 *b2, fpp_structure *s, double *descriptors,
 
 /* B2 descriptors with no device allocation (no counterpart in the reference).
  * For callers that may not allocate device memory when they need descriptors:
- * an MD engine whose memory pool owns the GPU, code running while a stream is
- * captured into a CUDA graph, a loop with a fixed memory budget.  All pointers
- * are device memory supplied by the caller:
+ * an MD engine whose memory pool owns the GPU (nothing may be cudaMalloc'd
+ * behind its back), or a loop with a fixed memory budget decided up front.
+ * All pointers are device memory supplied by the caller:
  *   species      n_atoms, in [0, n_species)
  *   offsets      n_atoms + 1 CSR offsets into the pair arrays
  *   rel          n_pairs x 4 doubles (r, x, y, z of r_ij = x_j - x_i), 32-byte
@@ -166,10 +166,11 @@ int fpp_b2_compute(const fpp_b2 *b2, fpp_structure *s, double *descriptors,
  * kernel's scratch lives in fixed device arrays of this library (8 MiB, held
  * by every GPU that loads it until the process exits), which limits a call to
  * n_atoms * n_species * N * (lmax+1)^2 <= 2^20 (and n_atoms <= 65536);
- * larger calls return FPP_ERR_CAPACITY.  The first call on a device resolves
- * the arrays' addresses and uploads constant tables: make it before any
- * stream capture.  Calls share the scratch: two calls that overlap on the GPU
- * (different streams, or different threads) race. */
+ * larger calls return FPP_ERR_CAPACITY.  The first call on a device does a
+ * one-time set-up (it resolves the arrays' addresses, uploads constant tables
+ * and synchronizes the stream): make it before any stream capture.  Calls
+ * share the scratch, which keeps the last call's contents: two calls that
+ * overlap on the GPU (different streams, or different threads) race. */
 int fpp_b2_descriptors_noalloc(const fpp_b2 *b2, int32_t n_atoms,
                                const int32_t *species, const int32_t *offsets,
                                const double *rel, const int32_t *nbr_species,
