@@ -147,6 +147,48 @@ def lammps_arrays(cell, sp, pos, rc):
             np.array(nbrs), np.array(owner))
 
 
+def seeded_beta(seed, n_species, n_d, power=2):
+    """Mapped coefficients for pinning the pair-style math: per species a
+    dense symmetric n_d x n_d matrix (power 2) or an n_d vector (power 1) of
+    seeded normal entries scaled by 1/n_d."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_species):
+        if power == 1:
+            out.append(rng.normal(size=n_d) / n_d)
+        else:
+            a = rng.normal(size=(n_d, n_d)) / n_d
+            out.append(0.5 * (a + a.T))
+    return out
+
+
+# Pair-style cases pinned to the reference's own lammps_descriptor.cpp
+# (tests/golden/make_golden.py records them): name -> (structure builder
+# arguments, n_species, N, lmax, cutoff matrix, power, beta seed).
+BETA_CASES = {
+    "fcc108_n8l3": (("fcc", 101, 5), 1, 8, 3, [[5.0]], 2, 7001),
+    "fcc108_n8l3_p1": (("fcc", 101, 5), 1, 8, 3, [[5.0]], 1, 7002),
+    "bcc250_n10l4_mixed_cut": (("bcc", (5, 5, 5), 202), 2, 10, 4,
+                               [[5.5, 5.0], [5.0, 5.2]], 2, 7003),
+    "bcc432_n12l4": (("bcc", (6, 6, 6), 303), 2, 12, 4, [[5.5, 5.5], [5.5, 5.5]], 2, 7004),
+}
+
+
+def beta_case(name):
+    """(cell, species, positions, settings, beta list, power) of a pinned
+    pair-style case."""
+    geo, ns, N, lmax, cut, power, seed = BETA_CASES[name]
+    if geo[0] == "fcc":
+        cell, sp, pos = synth.fcc_al_108(geo[1], geo[2])
+    else:
+        cell, sp, pos = synth.bcc_alloy(geo[1], geo[2])
+    cut = np.asarray(cut, dtype=float)
+    st = settings(ns, N, lmax, float(cut.max()), cutoffs=cut)
+    from oracle.b2 import n_descriptors
+    beta = seeded_beta(seed, ns, n_descriptors(ns, N, lmax), power)
+    return cell, np.asarray(sp), np.asarray(pos), st, beta, power
+
+
 def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
     """Two-species sparse set (10 environments per species of a 54-atom BCC
     alloy frame, per-pair cutoffs) and the inverse Cholesky factor of its

@@ -9,8 +9,20 @@ descriptors/wigner3j.cpp compiled where they lie) and evaluates:
     quadratic and cosine cutoffs (cutoffs.cpp:44-73), N = 12,
   * compute_coeffs (descriptors/wigner3j.cpp:5), the Wigner 3j tables of
     B3, for lmax = 0..4 (nonzero entries as index/value pairs).
-Writes tests/golden/l0_golden.npz.  Run from the repository root:
+Writes tests/golden/l0_golden.npz.
+
+Then the pair style's per-atom math: lammps_plugins/lammps_descriptor.cpp
+(single_bond_multiple_cutoffs, B2_descriptor, compute_energy_and_u),
+compiled unmodified against a small Eigen stand-in, driven by the per-atom
+loop of pair_flare.cpp:95-180 (ref_pair_flare in oracle/ref/ref_shim.cpp)
+over LAMMPS-shaped arrays with ghost atoms, on the seeded cases of
+tests/fixtures.BETA_CASES: per-atom energies, forces folded onto the owning
+atoms, the virial, and the single-bond values, B2 values, u and E_i of the
+first listed atoms.  Writes tests/golden/beta_form_golden.npz.
+
+Run from the repository root:
     python tests/golden/make_golden.py [/path/to/reference]
+(default: $FLARE_PP_REFERENCE, else /root/reference)
 """
 import ctypes
 import os
@@ -20,9 +32,64 @@ import sys
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+N_REC = 6
 
 
-def main(ref_root="/root/reference"):
+def beta_form_golden(lib):
+    from tests import fixtures
+    from oracle.b2 import n_descriptors
+    D = ctypes.POINTER(ctypes.c_double)
+    I = ctypes.POINTER(ctypes.c_int)
+    lib.ref_pair_flare.restype = ctypes.c_int
+    out = {}
+    for name in fixtures.BETA_CASES:
+        cell, sp, pos, st, beta, power = fixtures.beta_case(name)
+        ns, N, lmax = st["n_species"], st["N"], st["lmax"]
+        cut = np.ascontiguousarray(st["cutoffs"], dtype=np.float64)
+        x, types, ilist, numneigh, nbrs, owner = fixtures.lammps_arrays(
+            cell, sp, pos, float(cut.max()))
+        nall, noa = len(x), len(sp)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        ilist = np.ascontiguousarray(ilist, dtype=np.int32)
+        numneigh = np.ascontiguousarray(numneigh, dtype=np.int32)
+        off = np.zeros(noa + 1, dtype=np.int32)
+        off[1:] = np.cumsum(numneigh)
+        nbrs = np.ascontiguousarray(nbrs, dtype=np.int32)
+        B = np.ascontiguousarray(np.stack(beta), dtype=np.float64)
+        n_rad = ns * N
+        nb, nd = n_rad * (lmax + 1) ** 2, n_descriptors(ns, N, lmax)
+        f = np.zeros((nall, 3))
+        eat = np.zeros(nall)
+        vir = np.zeros(6)
+        rsb, rb2, ru, re = (np.zeros((N_REC, nb)), np.zeros((N_REC, nd)),
+                            np.zeros((N_REC, nb)), np.zeros(N_REC))
+        rc = lib.ref_pair_flare(
+            nall, x.ctypes.data_as(D), types.ctypes.data_as(I), noa, ilist.ctypes.data_as(I),
+            numneigh.ctypes.data_as(I), off.ctypes.data_as(I), nbrs.ctypes.data_as(I),
+            ns, N, lmax, ctypes.c_double(st["r1"]), cut.ctypes.data_as(D),
+            st["cutoff_function"].encode(), power, B.ctypes.data_as(D), f.ctypes.data_as(D),
+            eat.ctypes.data_as(D), vir.ctypes.data_as(D), N_REC, rsb.ctypes.data_as(D),
+            rb2.ctypes.data_as(D), ru.ctypes.data_as(D), re.ctypes.data_as(D))
+        assert rc == 0, name
+        F = np.zeros((noa, 3))
+        np.add.at(F, owner, f)
+        out[f"{name}/atom_energies"] = eat[:noa]
+        out[f"{name}/forces"] = F
+        out[f"{name}/virial"] = vir
+        out[f"{name}/rec_single_bond"] = rsb
+        out[f"{name}/rec_b2"] = rb2
+        out[f"{name}/rec_u"] = ru
+        out[f"{name}/rec_energy"] = re
+        print(f"{name}: {noa} atoms, {nall - noa} ghosts, E = {eat[:noa].sum():.12g}")
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "beta_form_golden.npz"), **out)
+    print("wrote tests/golden/beta_form_golden.npz")
+
+
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("FLARE_PP_REFERENCE", "/root/reference")
     subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root],
                    check=True)
     lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libflare_ref.so"))
@@ -86,6 +153,7 @@ def main(ref_root="/root/reference"):
         out[f"w3j_{lmax}_val"] = tab[nz]
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "l0_golden.npz"), **out)
     print("wrote tests/golden/l0_golden.npz")
+    beta_form_golden(lib)
 
 
 if __name__ == "__main__":
