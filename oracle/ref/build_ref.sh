@@ -1,10 +1,13 @@
 #!/bin/sh
-# Build oracle/_ref/libflare_ref.so from the reference's own L0 math sources
-# (radial.cpp, cutoffs.cpp, y_grad.cpp, descriptors/wigner3j.cpp) and its
-# per-atom pair-style math (lammps_plugins/lammps_descriptor.cpp), compiled
-# where they lie in the reference tree, plus oracle/ref/ref_shim.cpp.  Only the
-# small Eigen stand-in in oracle/ref/stub is added; no reference file is copied
-# or modified.
+# Build oracle/_ref/libflare_ref.so from the reference's own sources, compiled
+# where they lie in the reference tree: the L0 math (radial.cpp, cutoffs.cpp,
+# y_grad.cpp, descriptors/wigner3j.cpp), Structure (structure.cpp), B2 and
+# DescriptorValues (descriptors/b2.cpp, descriptor.cpp), the
+# NormalizedDotProduct kernel (kernels/kernel.cpp, normalized_dot_product.cpp)
+# and the pair style's per-atom math (lammps_plugins/lammps_descriptor.cpp),
+# plus oracle/ref/ref_shim*.cpp.  Only the small Eigen and nlohmann_json
+# stand-ins in oracle/ref/stub are added; no reference file is copied or
+# modified.
 # Usage: oracle/ref/build_ref.sh [reference_root]
 #        (default: $FLARE_PP_REFERENCE, else /root/reference)
 set -e
@@ -18,8 +21,11 @@ if [ ! -f "$SRC/radial.cpp" ]; then
 fi
 mkdir -p "$OUT"
 g++ -O2 -std=c++17 -fPIC -shared -ffp-contract=off \
-  -I"$HERE/stub" -I"$SRC" -I"$SRC/descriptors" -I"$REF/lammps_plugins" \
+  -I"$HERE/stub" -I"$SRC" -I"$SRC/descriptors" -I"$SRC/kernels" -I"$SRC/bffs" \
+  -I"$REF/lammps_plugins" \
   "$SRC/radial.cpp" "$SRC/cutoffs.cpp" "$SRC/y_grad.cpp" \
   "$SRC/descriptors/wigner3j.cpp" "$REF/lammps_plugins/lammps_descriptor.cpp" \
-  "$HERE/ref_shim.cpp" -o "$OUT/libflare_ref.so"
+  "$SRC/structure.cpp" "$SRC/descriptors/descriptor.cpp" "$SRC/descriptors/b2.cpp" \
+  "$SRC/kernels/kernel.cpp" "$SRC/kernels/normalized_dot_product.cpp" \
+  "$HERE/ref_shim.cpp" "$HERE/ref_shim_struc.cpp" -o "$OUT/libflare_ref.so"
 echo "built $OUT/libflare_ref.so"

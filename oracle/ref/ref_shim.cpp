@@ -159,9 +159,8 @@ int ref_pair_flare(int nall, const double *x, const int *type, int inum, const i
       if (dx * dx + dy * dy + dz * dz < rc * rc) {
         double fr[3];
         for (int a = 0; a < 3; a++) {
-          const double *row = sbd.row_ptr(3 * n_count + a);
           double acc = 0;
-          for (int k = 0; k < n_bond; k++) acc += row[k] * u(k);
+          for (int k = 0; k < n_bond; k++) acc += sbd(3 * n_count + a, k) * u(k);
           fr[a] = acc;
         }
         for (int a = 0; a < 3; a++) {

@@ -189,6 +189,36 @@ def beta_case(name):
     return cell, np.asarray(sp), np.asarray(pos), st, beta, power
 
 
+# Structure / B2 / kernel cases pinned to the reference's own structure.cpp,
+# b2.cpp and normalized_dot_product.cpp (tests/golden/make_golden.py records
+# them): name -> (cell, species, positions, cutoff, B2 settings
+# (n_species, N, lmax), cutoff matrix).
+def struc_cases():
+    rng = np.random.default_rng(31)
+    out = {}
+    cell, sp, pos = synth.fcc_al_108(101, 5)
+    out["fcc108"] = (cell, np.asarray(sp), pos, 5.0, (1, 8, 3), [[5.0]])
+    tri = np.array([[5.0, 0.3, 0.1], [-0.4, 4.6, 0.2], [0.3, 0.5, 4.9]])
+    out["triclinic_sweep2"] = (tri, rng.integers(0, 2, 9), rng.uniform(-3, 8, size=(9, 3)),
+                               6.5, (2, 4, 2), [[6.5, 5.9], [5.9, 6.2]])
+    out["single_atom"] = (np.eye(3) * 3.1, np.array([0]), np.array([[0.2, 0.3, 0.4]]), 5.0,
+                          (1, 3, 2), [[5.0]])
+    # a sheared cell whose determinant is exactly 420 in floating point (the
+    # kernels' stress columns divide by the volume; see the neighbor-list test)
+    cell = np.array([[8.0, 0.5, 0.0], [0.0, 7.0, 0.25], [0.0, 0.0, 7.5]])
+    out["two_species_20"] = (cell, rng.integers(0, 2, size=20), rng.uniform(0, 7, size=(20, 3)),
+                             4.2, (2, 5, 3), [[4.2, 3.6], [3.6, 4.0]])
+    cell, sp, pos = synth.bcc_alloy((3, 3, 3), 7)
+    out["bcc54"] = (cell, np.asarray(sp), pos, 4.2, (2, 5, 3), [[4.2, 3.6], [3.6, 4.0]])
+    return out
+
+
+# Sparse sets of the kernel cases: (structure case, clusters per species).
+KERNEL_SPARSE = [("two_species_20", [[0, 2, 4], [1, 3]]), ("bcc54", [[1, 5], [0, 2, 7]])]
+KERNEL_STRUCS = ("two_species_20", "bcc54")
+KERNEL_HYPS = [(1.7, 1.0), (1.7, 2.0)]
+
+
 def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
     """Two-species sparse set (10 environments per species of a 54-atom BCC
     alloy frame, per-pair cutoffs) and the inverse Cholesky factor of its

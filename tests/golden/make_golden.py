@@ -88,6 +88,115 @@ def beta_form_golden(lib):
     print("wrote tests/golden/beta_form_golden.npz")
 
 
+def _proj(m, seed=4242):
+    """A seeded random projection of a wide matrix (a check of every entry
+    without storing them all)."""
+    r = np.random.default_rng(seed).normal(size=(m.shape[1], 4))
+    return m @ r
+
+
+def struc_kernel_golden(lib):
+    from tests import fixtures
+    D = ctypes.POINTER(ctypes.c_double)
+    I = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    lib.ref_b2_new.restype = vp
+    lib.ref_b2_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, D, ctypes.c_char_p]
+    lib.ref_structure_new.restype = vp
+    lib.ref_structure_new.argtypes = [D, I, D, ctypes.c_int, ctypes.c_double, vp]
+    for fn in ("ref_structure_dbl", "ref_structure_int"):
+        getattr(lib, fn).argtypes = [vp, ctypes.c_char_p, ctypes.c_void_p]
+    for fn in ("ref_dv_dbl", "ref_dv_int"):
+        getattr(lib, fn).argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_cluster_new.restype = vp
+    lib.ref_cluster_add.argtypes = [vp, vp, I, I]
+    lib.ref_kernel.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, vp, vp,
+                               ctypes.c_void_p, I, I]
+    lib.ref_structure_free.argtypes = [vp]
+    lib.ref_b2_free.argtypes = [vp]
+    lib.ref_cluster_free.argtypes = [vp]
+
+    def dbl(fn, h, field, *extra):
+        n = fn(h, field.encode(), *extra, None)
+        assert n >= 0, field
+        out = np.zeros(n)
+        fn(h, field.encode(), *extra, out.ctypes.data)
+        return out
+
+    def ints(fn, h, field, *extra):
+        n = fn(h, field.encode(), *extra, None)
+        assert n >= 0, field
+        out = np.zeros(n, dtype=np.int32)
+        fn(h, field.encode(), *extra, out.ctypes.data)
+        return out
+
+    out = {}
+    handles = {}
+    cases = fixtures.struc_cases()
+    for name, (cell, sp, pos, rc, (ns, N, lmax), cut) in cases.items():
+        cut = np.ascontiguousarray(cut, dtype=np.float64)
+        b2 = lib.ref_b2_new(ns, N, lmax, 0.0, float(rc), cut.ctypes.data_as(D), b"quadratic")
+        c = np.ascontiguousarray(cell, dtype=np.float64)
+        spi = np.ascontiguousarray(sp, dtype=np.int32)
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        h = lib.ref_structure_new(c.ctypes.data_as(D), spi.ctypes.data_as(I),
+                                  p.ctypes.data_as(D), len(sp), float(rc), b2)
+        handles[name] = (h, b2)
+        k = f"struc/{name}/"
+        for f in ("neighbor_count", "cumulative_neighbor_count", "structure_indices",
+                  "neighbor_species"):
+            out[k + f] = ints(lib.ref_structure_int, h, f)
+        out[k + "relative_positions"] = dbl(lib.ref_structure_dbl, h,
+                                            "relative_positions").reshape(-1, 4)
+        out[k + "wrapped_positions"] = dbl(lib.ref_structure_dbl, h,
+                                           "wrapped_positions").reshape(-1, 3)
+        for f in ("volume", "sweep"):
+            out[k + f] = dbl(lib.ref_structure_dbl, h, f)
+        nd = int(ints(lib.ref_dv_int, h, "n_descriptors", 0)[0])
+        for s_ in range(ns):
+            kd = f"dv/{name}/{s_}/"
+            out[kd + "descriptors"] = dbl(lib.ref_dv_dbl, h, "descriptors", s_).reshape(-1, nd)
+            fd = dbl(lib.ref_dv_dbl, h, "descriptor_force_dervs", s_).reshape(-1, nd)
+            out[kd + "force_dervs_rows"] = fd[:48]
+            out[kd + "force_dervs_proj"] = _proj(fd) if len(fd) else np.zeros((0, 4))
+            out[kd + "neighbor_coordinates"] = dbl(lib.ref_dv_dbl, h, "neighbor_coordinates",
+                                                   s_).reshape(-1, 3)
+            for f in ("descriptor_norms", "descriptor_force_dots", "cutoff_values"):
+                out[kd + f] = dbl(lib.ref_dv_dbl, h, f, s_)
+            for f in ("neighbor_counts", "cumulative_neighbor_counts", "atom_indices",
+                      "neighbor_indices"):
+                out[kd + f] = ints(lib.ref_dv_int, h, f, s_)
+    # kernels on a sparse set drawn from two structures
+    ns, nd = 2, int(ints(lib.ref_dv_int, handles["bcc54"][0], "n_descriptors", 0)[0])
+    cd = lib.ref_cluster_new(ns, nd)
+    for name, cl in fixtures.KERNEL_SPARSE:
+        counts = np.array([len(x) for x in cl], dtype=np.int32)
+        flat = np.array([a for x in cl for a in x], dtype=np.int32)
+        assert lib.ref_cluster_add(cd, handles[name][0], counts.ctypes.data_as(I),
+                                   flat.ctypes.data_as(I)) == 0
+    a_, b_ = (handles[n][0] for n in fixtures.KERNEL_STRUCS)
+    for sig, pw in fixtures.KERNEL_HYPS:
+        for what, x, y in (("envs_envs", cd, cd), ("envs_struc", cd, b_),
+                           ("struc_struc", a_, b_), ("self_kernel_struc", b_, None)):
+            r, cc = ctypes.c_int(), ctypes.c_int()
+            n = lib.ref_kernel(what.encode(), sig, pw, x, y, None, ctypes.byref(r),
+                               ctypes.byref(cc))
+            if n == -2:      # the reference throws (power < 2, zero dot product)
+                out[f"kernel/{what}/{sig}/{pw}/throws"] = np.array(1)
+                continue
+            m = np.zeros(n)
+            lib.ref_kernel(what.encode(), sig, pw, x, y, m.ctypes.data, ctypes.byref(r),
+                           ctypes.byref(cc))
+            out[f"kernel/{what}/{sig}/{pw}"] = m.reshape(r.value, cc.value)
+    lib.ref_cluster_free(cd)
+    for h, b2 in handles.values():
+        lib.ref_structure_free(h)
+        lib.ref_b2_free(b2)
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "struc_kernel_golden.npz"), **out)
+    print("wrote tests/golden/struc_kernel_golden.npz")
+
+
 def main(ref_root=None):
     ref_root = ref_root or os.environ.get("FLARE_PP_REFERENCE", "/root/reference")
     subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root],
@@ -154,6 +263,7 @@ def main(ref_root=None):
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "l0_golden.npz"), **out)
     print("wrote tests/golden/l0_golden.npz")
     beta_form_golden(lib)
+    struc_kernel_golden(lib)
 
 
 if __name__ == "__main__":
