@@ -12,6 +12,11 @@ Writer: the layout of SparseGP::write_mapping_coefficients
     <cutoff function>
     <n_species^2 cutoffs>
     <beta of species 0, five per line> then each further species on a new line
+
+The reader also takes the older layout that files written before the power
+line and the per-species-pair cutoffs existed use (the reference's own
+lammps_plugins/test_compute/Si.txt and beta.txt): no power line (power 2),
+and one cutoff on its own line for every species pair.
 """
 import time
 
@@ -45,17 +50,24 @@ def write_potential(filename, beta, power, n_species, n_max, l_max, cutoffs,
 def read_potential(filename):
     with open(filename) as f:
         lines = f.read().splitlines()
-    power = int(lines[1].split()[0])
+    try:
+        power = int(lines[1].split()[0])
+        legacy = False
+    except ValueError:      # older layout: no power line, one cutoff
+        power = 2
+        legacy = True
+        lines = lines[:1] + ["2"] + lines[1:]
     radial = lines[2].split()[0]
     ns, n_max, l_max, beta_size = (int(v) for v in lines[3].split()[:4])
     cutoff_function = lines[4].split()[0]
     vals = []
     rest = lines[5:]
     k = 0
-    while len(vals) < ns * ns:
+    n_cut = 1 if legacy else ns * ns
+    while len(vals) < n_cut:
         vals += [float(v) for v in rest[k].split()]
         k += 1
-    cutoffs = np.array(vals[:ns * ns])
+    cutoffs = np.full(ns * ns, vals[0]) if legacy else np.array(vals[:ns * ns])
     nums = []
     for line in rest[k:]:
         nums += [float(v) for v in line.split()]
@@ -71,7 +83,7 @@ def read_potential(filename):
     beta = np.array(nums[:beta_size * ns]).reshape(ns, beta_size)
     return dict(power=power, radial=radial, n_species=ns, n_max=n_max,
                 l_max=l_max, beta_size=beta_size, cutoff_function=cutoff_function,
-                cutoffs=cutoffs, beta=beta)
+                cutoffs=cutoffs, beta=beta, legacy=legacy)
 
 
 # ---------------------------------------------------------------------------
