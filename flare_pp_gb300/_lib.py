@@ -57,6 +57,7 @@ SIGNATURES = {
     "fpp_envs_envs": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_envs_struc": (_c_int, [_vp, _vp, _vp, _vp]),
     "fpp_local_uncertainties": (_c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
+    "fpp_predict_energy_uncertainty": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fpp_kuf_batched": (_c_int, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i64, _vp]),
     "fpp_struc_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp, _vp]),
     "fpp_self_kernel_struc": (_c_int, [_vp, _dbl, _dbl, _vp, _vp, _vp]),
@@ -70,6 +71,12 @@ SIGNATURES = {
     "fpp_model_set_L_inv": (_c_int, [_vp, _i32, _vp]),
     "fpp_likelihood_gradient_stable": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp,
                                                 _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
+    "fpp_model_set_max_memory": (_c_int, [_vp, _dbl]),
+    "fpp_model_kuf_tiles": (_c_int, [_vp, _P(_i32), _P(_i32)]),
+    "fpp_model_pair_batches": (_c_int, [_vp, _P(_i32)]),
+    "fpp_likelihood_gradient_stable_kernels": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp,
+                                                        _vp, _vp, _vp, _i32, _vp, _vp, _i32,
+                                                        _vp, _vp, _vp]),
     "fpp_model_compute_varmap": (_c_int, [_vp, _vp, _vp]),
     "fpp_model_set_varmap": (_c_int, [_vp, _vp]),
     "fpp_std_atom_compute": (_c_int, [_vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp,

@@ -465,19 +465,23 @@ def update_matrices_QR(Kuu, Kuf, y, noise_vector, jitter=1e-8, stream=None):
 
 
 class SparseGP:
-    """SparseGP (sparse_gp.h:12-112) for one NormalizedDotProduct kernel over
-    one B2 or B3 descriptor: training solve and prediction on the GPU."""
+    """SparseGP (sparse_gp.h:12-112): NormalizedDotProduct kernels, kernel i
+    over the structures' descriptor i (B2 or B3), training solve and
+    prediction on the GPU.  With several kernels (sparse_gp.h:48-49) the
+    sparse sets are per kernel, Kuu is block diagonal over the kernels and
+    Kuf stacks their rows (sparse_gp.cpp:392-462, 576-610); predictions sum
+    the kernels' contributions (sparse_gp.cpp:612-702)."""
 
     def __init__(self, kernels, energy_noise, force_noise, stress_noise):
         self.kernels = list(kernels)
-        if len(self.kernels) != 1:
-            raise NotImplementedError("one kernel per model")
+        if not self.kernels:
+            raise ValueError("SparseGP needs at least one kernel")
         self.energy_noise = energy_noise
         self.force_noise = force_noise
         self.stress_noise = stress_noise
         self.Kuu_jitter = 1e-8
         self.sparse_descriptors = []
-        self.sparse_indices = [[]]
+        self.sparse_indices = [[] for _ in self.kernels]
         self.training_structures = []
         self.training_atom_indices = []
         self.y = np.zeros(0)
@@ -488,34 +492,49 @@ class SparseGP:
         self.L_inv = None
         self.Sigma = None
         self.Kuu_inverse = None
-        self.b2 = None
-        self._model = None
+        self.b2s = []
+        self._models = []
         self._mapped = False
 
+    # the first kernel's descriptor and device model (the one-kernel names)
+    b2 = property(lambda self: self.b2s[0] if self.b2s else None,
+                  lambda self, v: self._set_b2(v))
+    _model = property(lambda self: self._models[0] if self._models else None)
+
+    def _set_b2(self, v):
+        self.b2s = [] if v is None else [v] + self.b2s[1:]
+
     # ---- training (sparse_gp.cpp:135-610) -------------------------------
-    def _sparse(self, structure):
+    def _sparse(self, structure, i=0):
+        """sparse_gp.cpp:135-183 initialize_sparse_descriptors: one
+        ClusterDescriptor per kernel, over the structure's descriptor i."""
+        if len(structure.descriptors) < len(self.kernels):
+            raise ValueError("the structure has fewer descriptors than the model has kernels")
         if not self.sparse_descriptors:
-            dv = structure.descriptors[0]
-            cd = ClusterDescriptor()
-            cd.initialize_cluster(dv.n_types, dv.n_descriptors)
-            cd.descriptor_calculator = dv.descriptor_calculator
-            self.sparse_descriptors = [cd]
-        return self.sparse_descriptors[0]
+            for dv in structure.descriptors[:len(self.kernels)]:
+                cd = ClusterDescriptor()
+                cd.initialize_cluster(dv.n_types, dv.n_descriptors)
+                cd.descriptor_calculator = dv.descriptor_calculator
+                self.sparse_descriptors.append(cd)
+        return self.sparse_descriptors[i]
 
     def add_specific_environments(self, structure, atoms):
-        """sparse_gp.cpp:135-183."""
-        sd = self._sparse(structure)
-        dv = structure.descriptors[0]
+        """sparse_gp.cpp:135-183: the atoms' environments join every kernel's
+        sparse set."""
         atoms = list(atoms)
-        self.sparse_indices[0].append(atoms)
-        by_type = [[k for k in range(len(dv.atom_indices[t])) for a in atoms
-                    if dv.atom_indices[t][k] == a] for t in range(dv.n_types)]
-        sd.add_clusters_by_type(dv, by_type)
+        for i in range(len(self.kernels)):
+            sd = self._sparse(structure, i)
+            dv = structure.descriptors[i]
+            self.sparse_indices[i].append(atoms)
+            by_type = [[k for k in range(len(dv.atom_indices[t])) for a in atoms
+                        if dv.atom_indices[t][k] == a] for t in range(dv.n_types)]
+            sd.add_clusters_by_type(dv, by_type)
 
     def add_all_environments(self, structure):
         """sparse_gp.cpp:305-331."""
-        self._sparse(structure).add_all_clusters(structure.descriptors[0])
-        self.sparse_indices[0].append(list(range(structure.noa)))
+        for i in range(len(self.kernels)):
+            self._sparse(structure, i).add_all_clusters(structure.descriptors[i])
+            self.sparse_indices[i].append(list(range(structure.noa)))
 
     def add_training_structure(self, structure, atom_indices=(-1,)):
         """sparse_gp.cpp:464-552 (labels energy, forces, stress)."""
@@ -543,9 +562,9 @@ class SparseGP:
         self.training_structures.append(structure)
         self.training_atom_indices.append(atoms)
 
-    def _kuf_columns(self, structure, atoms):
-        k = self.kernels[0]
-        K = k.envs_struc(self.sparse_descriptors[0], structure.descriptors[0])
+    def _kuf_columns(self, structure, atoms, i=0):
+        k = self.kernels[i]
+        K = k.envs_struc(self.sparse_descriptors[i], structure.descriptors[i])
         n = structure.noa
         cols = []
         if len(structure.energy):
@@ -572,6 +591,9 @@ class SparseGP:
             offs.append(len(atoms))
             n_lab += (1 if m & 1 else 0) + (6 if m & 4 else 0)
         model = _Model(sd.descriptor_calculator, k.sigma, k.power, sd)
+        if not hasattr(self, "_kuf_models"):
+            self._kuf_models = []
+        self._kuf_models.append(model)
         Kuf = np.zeros((sd.n_clusters, n_lab))
         hs = (_lib.ctypes.c_void_p * max(1, len(strucs)))(*[s.handle for s in strucs])
         mask_a, offs_a = i32(mask), i32(offs)
@@ -580,25 +602,60 @@ class SparseGP:
                                     ptr(atoms_a), ptr(Kuf), n_lab, _stream(stream)))
         return Kuf
 
+    def _block_sizes(self):
+        return [sd.n_clusters for sd in self.sparse_descriptors]
+
+    def kuf_tiles(self, kernel_index=0):
+        """(sparse environments per pass, threads per block) of the batched
+        Kuf launch of the last update_matrices_QR (the autotuned shape)."""
+        ks, th = _lib.ctypes.c_int32(), _lib.ctypes.c_int32()
+        check(lib().fpp_model_kuf_tiles(self._kuf_models[kernel_index].handle,
+                                        _lib.ctypes.byref(ks), _lib.ctypes.byref(th)))
+        return ks.value, th.value
+
     def update_matrices_QR(self):
-        """sparse_gp.cpp:576-610: Kuu, Kuf and the QR solve on the GPU."""
-        sd = self.sparse_descriptors[0]
-        k = self.kernels[0]
-        self.Kuu = k.envs_envs(sd, sd)
-        self.Kuf = self._kuf_batched(sd, k)
+        """sparse_gp.cpp:576-610: Kuu (block diagonal over the kernels), Kuf
+        (the kernels' rows stacked, sparse_gp.cpp:565-574) and the QR solve,
+        on the GPU."""
+        self._kuf_models = []
+        self.Kuu_kernels = [k.envs_envs(sd, sd)
+                            for k, sd in zip(self.kernels, self.sparse_descriptors)]
+        self.Kuf_kernels = [self._kuf_batched(sd, k)
+                            for k, sd in zip(self.kernels, self.sparse_descriptors)]
+        self._stack_kernels()
         self._solve()
 
+    def _stack_kernels(self):
+        n = sum(self._block_sizes())
+        self.Kuu = np.zeros((n, n))
+        c = 0
+        for K in self.Kuu_kernels:
+            m = K.shape[0]
+            self.Kuu[c:c + m, c:c + m] = K
+            c += m
+        self.Kuf = np.vstack(self.Kuf_kernels)
+
     def _solve(self):
-        sd = self.sparse_descriptors[0]
-        k = self.kernels[0]
         self.alpha, self.R_inv, self.L_inv = update_matrices_QR(
             self.Kuu, self.Kuf, self.y, self.noise_vector, self.Kuu_jitter)
         self.Sigma = self.R_inv @ self.R_inv.T
         self.Kuu_inverse = self.L_inv.T @ self.L_inv
         self.L_diag = np.diag(self.L_inv).copy()
         self.R_inv_diag = np.diag(self.R_inv).copy()
-        self.b2 = sd.descriptor_calculator
-        self._model = _Model(self.b2, k.sigma, k.power, sd, self.alpha, self.R_inv)
+        self._make_models()
+
+    def _make_models(self):
+        """One device model per kernel with its slice of alpha (and, for one
+        kernel, R_inv for the SOR variance on the device)."""
+        self.b2s = [sd.descriptor_calculator for sd in self.sparse_descriptors]
+        self._models = []
+        c = 0
+        one = len(self.kernels) == 1
+        for k, sd, b2 in zip(self.kernels, self.sparse_descriptors, self.b2s):
+            m = sd.n_clusters
+            self._models.append(_Model(b2, k.sigma, k.power, sd, self.alpha[c:c + m],
+                                       self.R_inv if one else None))
+            c += m
         self._mapped = False
 
     # ---- hyperparameters and likelihood (sparse_gp.cpp:704-922, 1105-1140)
@@ -607,13 +664,19 @@ class SparseGP:
         (normalized_dot_product.cpp:581-615), the noise vector rebuilt from the
         new noises, and the QR solve repeated on the GPU."""
         hyps = f64(hyps)
-        k = self.kernels[0]
-        scale = hyps[0] * hyps[0] / (k.sigma * k.sigma)
-        self.Kuu = self.Kuu * scale
-        self.Kuf = self.Kuf * scale
-        k.sigma = float(hyps[0])
-        k.kernel_hyperparameters = np.array([k.sigma])
-        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[1:4])
+        nk = len(self.kernels)
+        if len(hyps) != nk + 3:
+            raise ValueError(f"expected {nk + 3} hyperparameters")
+        if not hasattr(self, "Kuu_kernels"):
+            self.Kuu_kernels, self.Kuf_kernels = [self.Kuu], [self.Kuf]
+        for i, k in enumerate(self.kernels):
+            scale = hyps[i] * hyps[i] / (k.sigma * k.sigma)
+            self.Kuu_kernels[i] = self.Kuu_kernels[i] * scale
+            self.Kuf_kernels[i] = self.Kuf_kernels[i] * scale
+            k.sigma = float(hyps[i])
+            k.kernel_hyperparameters = np.array([k.sigma])
+        self._stack_kernels()
+        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[nk:])
         inv_var = np.array([1 / self.energy_noise ** 2, 1 / self.force_noise ** 2,
                             1 / self.stress_noise ** 2])
         self.noise_vector = inv_var[self.label_kind]
@@ -621,19 +684,22 @@ class SparseGP:
 
     def _likelihood(self, want_gradient, KnK=None, stream=None):
         n, m = self.Kuf.shape
-        out = np.zeros(8)
+        nk = len(self.kernels)
+        out = np.zeros(4 + nk + 3)
         Kuf, Kuu, y = f64(self.Kuf), f64(self.Kuu), f64(self.y)
         kinds = i32(self.label_kind)
         a, S = f64(self.alpha), f64(self.Sigma)
         Ld, Rd = f64(self.L_diag), f64(self.R_inv_diag)
         hyps = f64(self.hyperparameters)
-        check(lib().fpp_likelihood_gradient_stable(
+        offs = i32(np.concatenate([[0], np.cumsum(self._block_sizes())]))
+        check(lib().fpp_likelihood_gradient_stable_kernels(
             n, m, ptr(Kuf), ptr(Kuu), ptr(y), ptr(kinds), ptr(a), ptr(S), ptr(Ld), ptr(Rd),
-            ptr(hyps), 1 if want_gradient else 0, ptr(out), ptr(KnK), _stream(stream)))
+            nk, ptr(offs), ptr(hyps), 1 if want_gradient else 0, ptr(out), ptr(KnK),
+            _stream(stream)))
         (self.log_marginal_likelihood, self.data_fit, self.complexity_penalty,
          self.constant_term) = out[:4]
         if want_gradient:
-            self.likelihood_gradient = out[4:8].copy()
+            self.likelihood_gradient = out[4:].copy()
         return self.log_marginal_likelihood
 
     def compute_likelihood_stable(self, stream=None):
@@ -642,8 +708,8 @@ class SparseGP:
 
     def compute_likelihood_gradient_stable(self, precomputed_KnK=False, stream=None):
         """sparse_gp.cpp:734-862, on the GPU: returns the log marginal
-        likelihood and sets likelihood_gradient (sigma, sigma_e, sigma_f,
-        sigma_s).  The traces it needs come from one GEMM per call, so the
+        likelihood and sets likelihood_gradient (each kernel's sigma, then
+        sigma_e, sigma_f, sigma_s).  The traces it needs come from one GEMM per call, so the
         precomputed and direct forms of the reference give the same numbers."""
         return self._likelihood(True, stream=stream)
 
@@ -658,6 +724,8 @@ class SparseGP:
     def precompute_KnK(self, stream=None):
         """sparse_gp.cpp:864-886: Kuf one_x Kuf^T / sigma^4 for later
         hyperparameter changes."""
+        if len(self.kernels) > 1:
+            raise NotImplementedError("precompute_KnK takes one kernel")
         sig4 = self.kernels[0].sigma ** 4
         KnK = self.compute_KnK(stream=stream)
         self.Kuf_e_noise_Kfu = [KnK[0] / sig4]
@@ -675,42 +743,47 @@ class SparseGP:
         def mat(a):
             return None if a is None else np.asarray(a, dtype=np.float64).tolist()
 
-        k = self.kernels[0]
-        sd = self.sparse_descriptors[0]
-        b2 = self.b2 if self.b2 is not None else sd.descriptor_calculator
-        desc = {"radial_basis": b2.radial_basis, "cutoff_function": b2.cutoff_function,
-                "radial_hyps": list(b2.radial_hyps), "cutoff_hyps": list(b2.cutoff_hyps),
-                "descriptor_settings": list(b2.descriptor_settings),
-                "cutoffs": mat(b2.cutoffs),
-                "descriptor_name": "B3" if isinstance(b2, B3) else "B2"}
-        cd = {"descriptors": [mat(d) for d in sd.descriptors],
-              "descriptor_norms": [mat(n) for n in sd.descriptor_norms],
-              "cutoff_values": [mat(c) for c in sd.cutoff_values],
-              "n_clusters_by_type": [int(v) for v in sd.n_clusters_by_type],
-              "cumulative_type_count": [int(v) for v in sd.cumulative_type_count],
-              "n_descriptors": int(sd.n_descriptors), "n_types": int(sd.n_types),
-              "n_clusters": int(sd.n_clusters)}
-        j = {"hyperparameters": [k.sigma, self.energy_noise, self.force_noise,
-                                 self.stress_noise],
+        def desc_json(b2):
+            return {"radial_basis": b2.radial_basis, "cutoff_function": b2.cutoff_function,
+                    "radial_hyps": list(b2.radial_hyps), "cutoff_hyps": list(b2.cutoff_hyps),
+                    "descriptor_settings": list(b2.descriptor_settings),
+                    "cutoffs": mat(b2.cutoffs),
+                    "descriptor_name": "B3" if isinstance(b2, B3) else "B2"}
+
+        def cd_json(sd):
+            return {"descriptors": [mat(d) for d in sd.descriptors],
+                    "descriptor_norms": [mat(n) for n in sd.descriptor_norms],
+                    "cutoff_values": [mat(c) for c in sd.cutoff_values],
+                    "n_clusters_by_type": [int(v) for v in sd.n_clusters_by_type],
+                    "cumulative_type_count": [int(v) for v in sd.cumulative_type_count],
+                    "n_descriptors": int(sd.n_descriptors), "n_types": int(sd.n_types),
+                    "n_clusters": int(sd.n_clusters)}
+
+        b2s = self.b2s or [sd.descriptor_calculator for sd in self.sparse_descriptors]
+        n_sparse = sum(sd.n_clusters for sd in self.sparse_descriptors)
+        j = {"hyperparameters": [float(h) for h in self.hyperparameters],
              "kernels": [{"kernel_name": "NormalizedDotProduct", "sigma": k.sigma,
                           "sig2": k.sigma * k.sigma, "power": k.power,
-                          "kernel_hyperparameters": [k.sigma]}],
-             "n_kernels": 1, "Kuu_jitter": self.Kuu_jitter,
+                          "kernel_hyperparameters": [k.sigma]} for k in self.kernels],
+             "n_kernels": len(self.kernels), "Kuu_jitter": self.Kuu_jitter,
              "Kuu": mat(getattr(self, "Kuu", None)), "Kuf": mat(getattr(self, "Kuf", None)),
              "Sigma": mat(self.Sigma), "Kuu_inverse": mat(self.Kuu_inverse),
              "R_inv": mat(self.R_inv), "L_inv": mat(self.L_inv), "alpha": mat(self.alpha),
-             "sparse_descriptors": [cd], "noise_vector": mat(self.noise_vector),
-             "y": mat(self.y), "n_sparse": int(sd.n_clusters),
+             "sparse_descriptors": [cd_json(sd) for sd in self.sparse_descriptors],
+             "noise_vector": mat(self.noise_vector),
+             "y": mat(self.y), "n_sparse": int(n_sparse),
              "energy_noise": self.energy_noise, "force_noise": self.force_noise,
              "stress_noise": self.stress_noise,
-             "training_structures": [{"descriptor_calculators": [desc]}]}
+             "training_structures": [{"descriptor_calculators": [desc_json(b)
+                                                                  for b in b2s]}]}
         with open(file_name, "w") as f:
             json.dump(j, f)
 
     @staticmethod
     def from_json(file_name):
         """SparseGP::from_json: a model saved by the reference (or by to_json),
-        loaded for GPU prediction (one NormalizedDotProduct kernel, B2 or B3)."""
+        loaded for GPU prediction (NormalizedDotProduct kernels over B2 or
+        B3 descriptors)."""
         import json
         with open(file_name) as f:
             j = json.load(f)
@@ -720,36 +793,41 @@ class SparseGP:
                 return np.zeros((0, 0)) if shape2 else np.zeros(0)
             return np.asarray(v, dtype=np.float64)
 
-        kj = j["kernels"][0]
-        if kj.get("kernel_name") != "NormalizedDotProduct":
-            raise ValueError(f"unsupported kernel {kj.get('kernel_name')}")
-        dj = j["training_structures"][0]["descriptor_calculators"][0]
-        if dj.get("descriptor_name", "B2") == "B3":
-            b2 = B3(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
-                    dj["cutoff_hyps"], dj["descriptor_settings"])
-        else:
-            b2 = B2(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
-                    dj["cutoff_hyps"], dj["descriptor_settings"],
-                    None if dj.get("cutoffs") is None else np.asarray(dj["cutoffs"]))
-        gp = SparseGP([NormalizedDotProduct(kj["sigma"], kj["power"])],
-                      j.get("energy_noise", 1.0), j.get("force_noise", 1.0),
+        kernels, b2s, cds = [], [], []
+        djs = j["training_structures"][0]["descriptor_calculators"]
+        for i, kj in enumerate(j["kernels"]):
+            if kj.get("kernel_name") != "NormalizedDotProduct":
+                raise ValueError(f"unsupported kernel {kj.get('kernel_name')}")
+            kernels.append(NormalizedDotProduct(kj["sigma"], kj["power"]))
+            dj = djs[i]
+            if dj.get("descriptor_name", "B2") == "B3":
+                b2 = B3(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
+                        dj["cutoff_hyps"], dj["descriptor_settings"])
+            else:
+                b2 = B2(dj["radial_basis"], dj["cutoff_function"], dj["radial_hyps"],
+                        dj["cutoff_hyps"], dj["descriptor_settings"],
+                        None if dj.get("cutoffs") is None else np.asarray(dj["cutoffs"]))
+            b2s.append(b2)
+            sj = j["sparse_descriptors"][i]
+            cd = ClusterDescriptor()
+            nt, nd = int(sj["n_types"]), int(sj["n_descriptors"])
+            cd.initialize_cluster(nt, nd)
+            cd.descriptors = [arr(d, True).reshape(-1, nd) for d in sj["descriptors"]]
+            cd.descriptor_norms = [arr(v) for v in sj["descriptor_norms"]]
+            cd.cutoff_values = [arr(v) for v in sj["cutoff_values"]]
+            cd.n_clusters_by_type = [int(v) for v in sj["n_clusters_by_type"]]
+            cd.cumulative_type_count = [int(v) for v in sj["cumulative_type_count"]]
+            cd.n_clusters = int(sj["n_clusters"])
+            cd.descriptor_calculator = b2
+            cds.append(cd)
+        gp = SparseGP(kernels, j.get("energy_noise", 1.0), j.get("force_noise", 1.0),
                       j.get("stress_noise", 1.0))
-        sj = j["sparse_descriptors"][0]
-        cd = ClusterDescriptor()
-        nt, nd = int(sj["n_types"]), int(sj["n_descriptors"])
-        cd.initialize_cluster(nt, nd)
-        cd.descriptors = [arr(d, True).reshape(-1, nd) for d in sj["descriptors"]]
-        cd.descriptor_norms = [arr(v) for v in sj["descriptor_norms"]]
-        cd.cutoff_values = [arr(v) for v in sj["cutoff_values"]]
-        cd.n_clusters_by_type = [int(v) for v in sj["n_clusters_by_type"]]
-        cd.cumulative_type_count = [int(v) for v in sj["cumulative_type_count"]]
-        cd.n_clusters = int(sj["n_clusters"])
-        cd.descriptor_calculator = b2
         gp.Kuu_jitter = j.get("Kuu_jitter", gp.Kuu_jitter)
         R_inv = arr(j.get("R_inv"), True)
         L_inv = arr(j.get("L_inv"), True)
-        gp.set_model(b2, cd, arr(j["alpha"]), R_inv if R_inv.size else None,
-                     L_inv if L_inv.size else None)
+        one = len(kernels) == 1
+        gp.set_model(b2s[0] if one else b2s, cds[0] if one else cds, arr(j["alpha"]),
+                     R_inv if R_inv.size else None, L_inv if L_inv.size else None)
         for key in ("Sigma", "Kuu_inverse"):
             v = arr(j.get(key), True)
             setattr(gp, key, v if v.size else None)
@@ -758,35 +836,63 @@ class SparseGP:
         return gp
 
     def set_model(self, b2, sparse_descriptors, alpha, R_inv=None, L_inv=None):
-        """Load a trained model: the sparse ClusterDescriptor, alpha and
-        optionally R_inv and L_inv (the outputs of update_matrices_QR)."""
-        self.b2 = b2
-        self.sparse_descriptors = [sparse_descriptors]
+        """Load a trained model: the sparse ClusterDescriptor(s), alpha and
+        optionally R_inv and L_inv (the outputs of update_matrices_QR).  With
+        several kernels, b2 and sparse_descriptors are lists (one per kernel,
+        in kernel order) and alpha, R_inv, L_inv cover the stacked sets."""
+        multi = isinstance(sparse_descriptors, (list, tuple))
+        sds = list(sparse_descriptors) if multi else [sparse_descriptors]
+        b2s = list(b2) if multi else [b2]
+        if len(sds) != len(self.kernels) or len(b2s) != len(self.kernels):
+            raise ValueError("one descriptor and sparse set per kernel")
+        for cd, d in zip(sds, b2s):
+            cd.descriptor_calculator = d
+        self.sparse_descriptors = sds
         self.alpha = f64(alpha)
         self.R_inv = None if R_inv is None else f64(R_inv)
         self.L_inv = None if L_inv is None else f64(L_inv)
-        k = self.kernels[0]
-        self._model = _Model(b2, k.sigma, k.power, sparse_descriptors, self.alpha,
-                             self.R_inv)
-        self._mapped = False
+        self._make_models()
 
     def _ensure_mapped(self, stream=None):
         if not self._mapped:
-            self.mapping_coefficients = self._model.compute_beta(
-                self.kernels[0].power, stream)
+            self.mapping_coefficients_kernels = [
+                m.compute_beta(k.power, stream) for m, k in zip(self._models, self.kernels)]
+            self.mapping_coefficients = self.mapping_coefficients_kernels[0]
             self._mapped = True
 
+    def _descriptors_of(self, structure):
+        if len(structure.descriptors) < len(self.kernels):
+            if not structure.descriptor_calculators:
+                structure.descriptor_calculators = list(self.b2s)
+            structure.compute_descriptors()
+        return structure.descriptors
+
+    def _kernel_mat(self, structure, stream=None):
+        """The stacked envs_struc blocks of the kernels (sparse_gp.cpp:617-626)."""
+        dvs = self._descriptors_of(structure)
+        return np.vstack([k.envs_struc(sd, dvs[i], stream=stream) for i, (k, sd) in
+                          enumerate(zip(self.kernels, self.sparse_descriptors))])
+
     def predict_mean(self, structure, stream=None):
-        """sparse_gp.cpp:612-628 -> structure.mean_efs."""
-        out = np.zeros(1 + 3 * structure.noa + 6)
-        check(lib().fpp_predict(self._model.handle, structure.handle, ptr(out), None,
-                                _stream(stream)))
-        structure.mean_efs = out
+        """sparse_gp.cpp:612-628 -> structure.mean_efs (the kernels' sum)."""
+        total = np.zeros(1 + 3 * structure.noa + 6)
+        out = np.zeros_like(total)
+        for m in self._models:
+            check(lib().fpp_predict(m.handle, structure.handle, ptr(out), None,
+                                    _stream(stream)))
+            total += out
+        structure.mean_efs = total
 
     def predict_SOR(self, structure, stream=None):
         """sparse_gp.cpp:630-649 -> structure.mean_efs, structure.variance_efs."""
         if self.R_inv is None:
             raise ValueError("predict_SOR needs R_inv")
+        if len(self.kernels) > 1:
+            K = self._kernel_mat(structure, stream)
+            structure.mean_efs = K.T @ self.alpha
+            v = K.T @ self.R_inv
+            structure.variance_efs = np.einsum("ij,ij->i", v, v)
+            return
         out = np.zeros(1 + 3 * structure.noa + 6)
         var = np.zeros_like(out)
         check(lib().fpp_predict(self._model.handle, structure.handle, ptr(out),
@@ -797,34 +903,54 @@ class SparseGP:
     def predict_DTC(self, structure, stream=None):
         """sparse_gp.cpp:651-680 -> structure.mean_efs, structure.variance_efs:
         variance = K_self - diag(K^T Kuu^-1 K) + diag(K^T Sigma K), with K the
-        environment/structure kernel and K_self the structure self kernel,
-        both from the GPU (the trained model's Kuu^-1 and Sigma)."""
+        environment/structure kernel and K_self the structure self kernel
+        (summed over the kernels), both from the GPU (the trained model's
+        Kuu^-1 and Sigma)."""
         if self.Sigma is None or self.Kuu_inverse is None:
             raise ValueError("predict_DTC needs a model trained with update_matrices_QR")
-        k = self.kernels[0]
-        b2 = self._model.b2
-        if not structure.descriptors:
-            if not structure.descriptor_calculators:
-                structure.descriptor_calculators = [b2]
-            structure.compute_descriptors()
-        dv = structure.descriptors[0]
-        K = k.envs_struc(self.sparse_descriptors[0], dv, stream=stream)
+        dvs = self._descriptors_of(structure)
+        K = self._kernel_mat(structure, stream)
         structure.mean_efs = K.T @ self.alpha
-        k_self = k.self_kernel_struc(dv, stream=stream)
+        k_self = sum(k.self_kernel_struc(dvs[i], stream=stream)
+                     for i, k in enumerate(self.kernels))
         q_self = np.einsum("ij,ij->j", K, self.Kuu_inverse @ K)
         v_sor = np.einsum("ij,ij->j", K, self.Sigma @ K)
         structure.variance_efs = k_self - q_self + v_sor
 
     def compute_cluster_uncertainties(self, structure, stream=None):
         """sparse_gp.cpp:93-133: per kernel, the energy variance of every
-        cluster (species by species, atoms in structure order), from the GPU."""
+        cluster (species by species, atoms in structure order) from that
+        kernel's block of L_inv, on the GPU."""
         if self.L_inv is None:
             raise ValueError("compute_cluster_uncertainties needs L_inv")
-        L = f64(self.L_inv)
-        v = np.zeros(structure.noa)
-        check(lib().fpp_local_uncertainties(self._model.handle, structure.handle, ptr(L),
-                                            L.shape[0], ptr(v), _stream(stream)))
-        return [v]
+        out = []
+        for i, m in enumerate(self._models):
+            L = self._L_inv_block(i)
+            v = np.zeros(structure.noa)
+            check(lib().fpp_local_uncertainties(m.handle, structure.handle, ptr(L),
+                                                L.shape[0], ptr(v), _stream(stream)))
+            out.append(v)
+        return out
+
+    def predict_energy_uncertainty(self, structure, local=True, stream=None):
+        """At MD sizes: the energy and energy variance of predict_SOR
+        (sparse_gp.cpp:630-649: mean_efs[0], variance_efs[0]) and, with
+        local, the per-atom variances of compute_cluster_uncertainties
+        (sparse_gp.cpp:93-133) in structure atom order; only the energy
+        column of the kernel matrix is formed.  Returns (energy, variance,
+        local variances or None).  One kernel."""
+        if len(self.kernels) > 1:
+            raise NotImplementedError("predict_energy_uncertainty takes one kernel")
+        if self.R_inv is None or (local and self.L_inv is None):
+            raise ValueError("predict_energy_uncertainty needs R_inv (and L_inv)")
+        if local and not getattr(self._model, "_L_inv_set", False):
+            self._model.set_L_inv(self.L_inv)
+            self._model._L_inv_set = True
+        e, v = np.zeros(1), np.zeros(1)
+        lv = np.zeros(structure.noa) if local else None
+        check(lib().fpp_predict_energy_uncertainty(self._model.handle, structure.handle,
+                                                   ptr(e), ptr(v), ptr(lv), _stream(stream)))
+        return e[0], v[0], lv
 
     def predict_local_uncertainties(self, structure, stream=None):
         """sparse_gp.cpp:682-702: mean_efs and local_uncertainties."""
@@ -834,21 +960,26 @@ class SparseGP:
     # ---- coefficient files (sparse_gp.cpp:1142-1404) ----------------------
     @property
     def hyperparameters(self):
-        k = self.kernels[0]
-        return np.array([k.sigma, self.energy_noise, self.force_noise, self.stress_noise])
+        """sparse_gp.cpp:1105-1140 order: every kernel's sigma, then the
+        energy, force and stress noises."""
+        return np.array([k.sigma for k in self.kernels] +
+                        [self.energy_noise, self.force_noise, self.stress_noise])
 
-    def _file_header(self):
-        ns, N, lmax = self.b2.descriptor_settings
-        return dict(n_species=ns, n_max=N, l_max=lmax, cutoffs=self.b2.cutoffs,
-                    cutoff_function=self.b2.cutoff_function, radial=self.b2.radial_basis)
+    def _file_header(self, kernel_index=0):
+        b2 = self.b2s[kernel_index]
+        ns, N, lmax = b2.descriptor_settings
+        return dict(n_species=ns, n_max=N, l_max=lmax, cutoffs=b2.cutoffs,
+                    cutoff_function=b2.cutoff_function, radial=b2.radial_basis)
 
     def write_mapping_coefficients(self, file_name, contributor, kernel_index=0,
                                    stream=None):
-        """SparseGP::write_mapping_coefficients (sparse_gp.cpp:1142-1206)."""
+        """SparseGP::write_mapping_coefficients (sparse_gp.cpp:1142-1206):
+        the mapped coefficients of kernel kernel_index."""
         from .potential import write_potential
         self._ensure_mapped(stream)
-        write_potential(file_name, self.mapping_coefficients, self.kernels[0].power,
-                        contributor=contributor, **self._file_header())
+        write_potential(file_name, self.mapping_coefficients_kernels[kernel_index],
+                        self.kernels[kernel_index].power, contributor=contributor,
+                        **self._file_header(kernel_index))
 
     def write_varmap_coefficients(self, file_name, contributor, kernel_index=0,
                                   stream=None):
@@ -857,24 +988,36 @@ class SparseGP:
         from .potential import write_varmap
         if self.L_inv is None:
             raise ValueError("write_varmap_coefficients needs L_inv")
-        self._model.set_L_inv(self.L_inv)
-        self.varmap_coeffs = self._model.compute_varmap(stream)
-        write_varmap(file_name, self.varmap_coeffs, self.hyperparameters,
-                     contributor=contributor, **self._file_header())
+        m = self._models[kernel_index]
+        m.set_L_inv(self._L_inv_block(kernel_index))
+        self.varmap_coeffs = m.compute_varmap(stream)
+        write_varmap(file_name, self.varmap_coeffs, self._kernel_hyps(kernel_index),
+                     contributor=contributor, **self._file_header(kernel_index))
 
-    def write_L_inverse(self, file_name, contributor):
+    def write_L_inverse(self, file_name, contributor, kernel_index=0):
         """SparseGP::write_L_inverse (sparse_gp.cpp:1283-1344)."""
         from .potential import write_L_inverse
         if self.L_inv is None:
             raise ValueError("write_L_inverse needs L_inv")
-        write_L_inverse(file_name, self.L_inv, self.kernels[0].power,
-                        self.hyperparameters, contributor=contributor,
-                        **self._file_header())
+        write_L_inverse(file_name, self._L_inv_block(kernel_index),
+                        self.kernels[kernel_index].power, self._kernel_hyps(kernel_index),
+                        contributor=contributor, **self._file_header(kernel_index))
 
-    def write_sparse_descriptors(self, file_name, contributor):
+    def _L_inv_block(self, i):
+        """The block of L_inv that belongs to kernel i (Kuu is block diagonal
+        over the kernels, so L_inv is too)."""
+        c = sum(self._block_sizes()[:i])
+        m = self._block_sizes()[i]
+        return np.ascontiguousarray(self.L_inv[c:c + m, c:c + m])
+
+    def _kernel_hyps(self, i):
+        return np.array([self.kernels[i].sigma, self.energy_noise, self.force_noise,
+                         self.stress_noise])
+
+    def write_sparse_descriptors(self, file_name, contributor, kernel_index=0):
         """SparseGP::write_sparse_descriptors (sparse_gp.cpp:1346-1404)."""
         from .potential import write_sparse_descriptors
-        sd = self.sparse_descriptors[0]
+        sd = self.sparse_descriptors[kernel_index]
         write_sparse_descriptors(file_name, sd.descriptors, sd.descriptor_norms,
                                  contributor=contributor)
 
@@ -883,22 +1026,28 @@ class SparseGP:
         """Energy, forces and stress through the mapped coefficients (the pair
         style's evaluation) on the periodic structure."""
         self._ensure_mapped(stream)
+        E, F, S = 0.0, np.zeros((structure.noa, 3)), np.zeros(6)
+        AE = np.zeros(structure.noa) if atom_energies else None
         e = np.zeros(1)
         f = np.zeros((structure.noa, 3))
         s = np.zeros(6)
         ae = np.zeros(structure.noa) if atom_energies else None
-        check(lib().fpp_predict_mapped(self._model.handle, structure.handle,
-                                       PRECISIONS[precision], ptr(e), ptr(f), ptr(s),
-                                       ptr(ae), 0, _stream(stream)))
-        return (e[0], f, s, ae) if atom_energies else (e[0], f, s)
+        for m in self._models:      # the kernels' contributions add
+            check(lib().fpp_predict_mapped(m.handle, structure.handle,
+                                           PRECISIONS[precision], ptr(e), ptr(f), ptr(s),
+                                           ptr(ae), 0, _stream(stream)))
+            E, F, S = E + e[0], F + f, S + s
+            if atom_energies:
+                AE = AE + ae
+        return (E, F, S, AE) if atom_energies else (E, F, S)
 
     def center_mixed_on(self, structure, stream=None):
         """Centre the mixed-precision mapped form on this structure's mean
         environment per species (lowers its energy error on structures far
         from the sparse set's mean; see fpp_model_center_on)."""
         self._ensure_mapped(stream)
-        check(lib().fpp_model_center_on(self._model.handle, structure.handle,
-                                        _stream(stream)))
+        for m in self._models:
+            check(lib().fpp_model_center_on(m.handle, structure.handle, _stream(stream)))
 
 
 class PairFLARE:
@@ -928,6 +1077,17 @@ class PairFLARE:
         self.b2 = b2
         self.model = _Model(b2, 1.0, pot["power"], envs)
         self.model.set_beta(pot["power"], pot["beta"])
+
+    def set_max_memory(self, bytes_):
+        """The Kokkos pair style's MAXMEM (bytes; 0 = no cap): the atoms are
+        evaluated in batches that fit (pair_flare_kokkos.cpp:145-177)."""
+        check(lib().fpp_model_set_max_memory(self.model.handle, float(bytes_)))
+
+    @property
+    def last_batches(self):
+        n = _lib.ctypes.c_int32()
+        check(lib().fpp_model_pair_batches(self.model.handle, _lib.ctypes.byref(n)))
+        return n.value
 
     def compute(self, x, type_, ilist, numneigh, neighbors, nlocal=None,
                 precision=None, eatom=False, stream=None):

@@ -1402,6 +1402,232 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
   }
 }
 
+// ---------------------------------------------------------------------------
+// Kuf of a batch of training structures by the adjoint route (FP64), the
+// envs_struc columns of normalized_dot_product.cpp:115-210 without the stored
+// descriptor derivatives.  One persistent launch: each block takes work items
+// (structure, atom i) and, for the sparse environments k of the atom's
+// species in passes of KS:
+//   z_k = dhat_k . phat_i, the energy column += sig^2 z_k^power;
+//   w_k = dk/dp_i = sig^2 power z_k^(power-1) (dhat_k - z_k phat_i) / |p_i|;
+//   u_k = dk/dc_i through the B2 contraction (u[n1,lm] = sum_n2 (W+W^T) c);
+//   per pair (i, j) the bases g, dg, Y, dY are recomputed once and
+//   f = dk/dr_ij = u_k . dc_i/dr_ij goes to the columns of the labels:
+//   F_i += f, F_j -= f, stress(a <= b) -= f_a r_b / V.
+// Contributions to other atoms' columns are FP64 atomic adds (the order of
+// those additions varies between runs, at the level of FP64 rounding).
+// ---------------------------------------------------------------------------
+struct KufLayout {
+  size_t ph, c, w, u, zz, aa, acc, pg, py, prel, ints, total;
+};
+
+__host__ __device__ inline KufLayout kuf_layout(const B2Args &a, int ks) {
+  const size_t nd = a.n_d, sb = (size_t)a.n_species * a.N * a.H;
+  KufLayout L;
+  size_t o = 0;
+  L.ph = o; o += nd;
+  L.c = o; o += sb;
+  L.w = o; o += (size_t)ks * nd;
+  L.u = o; o += (size_t)ks * sb;
+  L.zz = o; o += ks;
+  L.aa = o; o += ks;
+  L.acc = o; o += (size_t)ks * 9;
+  L.pg = o; o += 32 * 2 * (size_t)a.N;
+  L.py = o; o += 32 * 4 * (size_t)a.H;
+  L.prel = o; o += 32 * 4;
+  L.ints = o; o += (3 * 32 + 1) / 2 + 1;   // pj, psj, pkeep as ints
+  L.total = o * sizeof(double);
+  return L;
+}
+
+__device__ __forceinline__ double kuf_pow(double z, double p) {
+  if (p == 2.0) return z * z;
+  if (p == 1.0) return z;
+  return pow(z, p);
+}
+
+__global__ void __launch_bounds__(256)
+k_kuf_adjoint(const KufArgs k, int ks, int n_items, int item0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *sm = reinterpret_cast<double *>(smem_raw);
+  const B2Args &a = k.a;
+  const KufLayout L = kuf_layout(a, ks);
+  double *ph = sm + L.ph, *c = sm + L.c, *w = sm + L.w, *u = sm + L.u;
+  double *zz = sm + L.zz, *aa = sm + L.aa, *acc = sm + L.acc;
+  double *pg = sm + L.pg, *py = sm + L.py, *prel = sm + L.prel;
+  int *pj = reinterpret_cast<int *>(sm + L.ints), *psj = pj + 32, *pkeep = psj + 32;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
+  const int N = a.N, H = a.H, NS = a.n_species, nd = a.n_d, L1 = a.lmax + 1;
+  const int nr = NS * N, sb = nr * H;
+  for (int it = item0 + blockIdx.x; it < item0 + n_items; it += gridDim.x) {
+    const int2 item = k.items[it];
+    const KufStruc S = k.strucs[item.x];
+    const int i = item.y;
+    const int si = S.species[i];
+    const double nrm = S.norm64[i];
+    if (nrm < 1e-8) continue;  // empty environment: no energy, no forces
+    const KufSpecies SP = k.sp[si];
+    if (SP.n_sparse == 0) continue;
+    const int row = S.row_of_atom[i];
+    __syncthreads();  // the previous item's shared memory is free
+    for (int d = tid; d < nd; d += nth) ph[d] = S.phat64[(size_t)row * k.ldp + d];
+    for (int q = tid; q < sb; q += nth) c[q] = S.c64[(size_t)i * sb + q];
+    const int beg = S.offset[i], end = S.offset[i + 1];
+    const int col_i = S.force_col[i];
+    __syncthreads();
+    for (int k0 = 0; k0 < SP.n_sparse; k0 += ks) {
+      const int kc = min(ks, SP.n_sparse - k0);
+      // z_k = dhat_k . phat_i (a warp per k)
+      for (int kk = warp; kk < kc; kk += nwarp) {
+        const double *dk = SP.dhat + (size_t)(k0 + kk) * nd;
+        double v = 0.0;
+        for (int d = lane; d < nd; d += 32) v = fma(dk[d], ph[d], v);
+        v = warp_sum(v);
+        if (lane == 0) zz[kk] = v;
+      }
+      __syncthreads();
+      for (int kk = tid; kk < kc; kk += nth) {
+        const bool live = SP.norms[k0 + kk] >= 1e-8;
+        const double z = zz[kk];
+        if (live && S.col_e >= 0)
+          atomicAdd(k.kuf + (size_t)(SP.row0 + k0 + kk) * k.n_labels + S.col_e,
+                    k.sig2 * kuf_pow(z, k.power));
+        aa[kk] = live ? k.sig2 * k.power * kuf_pow(z, k.power - 1.0) / nrm : 0.0;
+        for (int q = 0; q < 9; q++) acc[kk * 9 + q] = 0.0;
+      }
+      __syncthreads();
+      // w_k = a_k (dhat_k - z_k phat_i)
+      for (int idx = tid; idx < kc * nd; idx += nth) {
+        const int kk = idx / nd, d = idx - kk * nd;
+        w[idx] = aa[kk] * (SP.dhat[(size_t)(k0 + kk) * nd + d] - zz[kk] * ph[d]);
+      }
+      __syncthreads();
+      // u_k[n1, lm] = sum_n2 w_k[(n1, n2), l] c[n2, lm] (the diagonal twice)
+      for (int idx = tid; idx < kc * sb; idx += nth) {
+        const int kk = idx / sb, rem = idx - kk * sb;
+        const int n1 = rem / H, lm = rem - n1 * H;
+        int l = 0;
+        while ((l + 1) * (l + 1) <= lm) l++;
+        const double *wk = w + (size_t)kk * nd;
+        double v = 0.0;
+        for (int n2 = 0; n2 < nr; n2++) {
+          const int lo = n1 < n2 ? n1 : n2, hi = n1 < n2 ? n2 : n1;
+          const int q = lo * nr - lo * (lo - 1) / 2 + (hi - lo);
+          const double f = n1 == n2 ? 2.0 : 1.0;
+          v = fma(f * wk[q * L1 + l], c[n2 * H + lm], v);
+        }
+        u[idx] = v;
+      }
+      __syncthreads();
+      for (int w0 = beg; w0 < end; w0 += 32) {
+        const int np = min(32, end - w0);
+        // stage the bases of up to 32 pairs (a thread per pair)
+        if (tid < np) {
+          const int p = w0 + tid;
+          const dvec4 rd = S.rel[p];
+          const int sj = S.nbr_s[p];
+          const double rcut = a.cutoffs[si * NS + sj];
+          const bool keep = rd.x <= rcut;  // the B2 filter (b2.cpp:277)
+          pj[tid] = S.nbr_j[p];
+          psj[tid] = sj;
+          pkeep[tid] = keep ? 1 : 0;
+          prel[4 * tid + 0] = rd.x;
+          prel[4 * tid + 1] = rd.y;
+          prel[4 * tid + 2] = rd.z;
+          prel[4 * tid + 3] = rd.w;
+          if (keep) {
+            radial_basis<double>(rd.x, a.r1, rcut, N, a.cutoff_kind, pg + tid * 2 * N,
+                                 pg + tid * 2 * N + N, 1);
+            real_harmonics<double>(rd.y, rd.z, rd.w, a.lmax, py + tid * 4 * H,
+                                   py + tid * 4 * H + H, 1);
+          }
+        }
+        __syncthreads();
+        // f for (sparse k, pair): a warp per k, a lane per pair
+        for (int kk = warp; kk < kc; kk += nwarp) {
+          double f[3] = {0.0, 0.0, 0.0};
+          if (lane < np && pkeep[lane]) {
+            const double *g = pg + lane * 2 * N, *dg = g + N;
+            const double *Y = py + lane * 4 * H, *dY = Y + H;
+            const double *ur = u + (size_t)kk * sb + (size_t)psj[lane] * N * H;
+            double fr = 0.0;
+            for (int lm = 0; lm < H; lm++) {
+              double A = 0.0, B = 0.0;
+              for (int n = 0; n < N; n++) {
+                const double uv = ur[n * H + lm];
+                A = fma(uv, g[n], A);
+                B = fma(uv, dg[n], B);
+              }
+              fr = fma(B, Y[lm], fr);
+              f[0] = fma(A, dY[3 * lm + 0], f[0]);
+              f[1] = fma(A, dY[3 * lm + 1], f[1]);
+              f[2] = fma(A, dY[3 * lm + 2], f[2]);
+            }
+            const double r = prel[4 * lane];
+            f[0] = fma(fr, prel[4 * lane + 1] / r, f[0]);
+            f[1] = fma(fr, prel[4 * lane + 2] / r, f[1]);
+            f[2] = fma(fr, prel[4 * lane + 3] / r, f[2]);
+            const int cj = S.force_col[pj[lane]];
+            double *krow = k.kuf + (size_t)(SP.row0 + k0 + kk) * k.n_labels;
+            if (cj >= 0) {
+              atomicAdd(krow + cj + 0, -f[0]);
+              atomicAdd(krow + cj + 1, -f[1]);
+              atomicAdd(krow + cj + 2, -f[2]);
+            }
+          }
+          // own force column and the stress, summed over the warp's pairs
+          const double rx = lane < np ? prel[4 * lane + 1] : 0.0;
+          const double ry = lane < np ? prel[4 * lane + 2] : 0.0;
+          const double rz = lane < np ? prel[4 * lane + 3] : 0.0;
+          double t[9] = {f[0], f[1], f[2], f[0] * rx, f[0] * ry, f[0] * rz,
+                         f[1] * ry, f[1] * rz, f[2] * rz};
+#pragma unroll
+          for (int q = 0; q < 9; q++) t[q] = warp_sum(t[q]);
+          if (lane == 0)
+            for (int q = 0; q < 9; q++) acc[kk * 9 + q] += t[q];
+        }
+        __syncthreads();
+      }
+      // the atom's own force column and the stress columns
+      for (int kk = tid; kk < kc; kk += nth) {
+        double *krow = k.kuf + (size_t)(SP.row0 + k0 + kk) * k.n_labels;
+        if (col_i >= 0)
+          for (int q = 0; q < 3; q++) atomicAdd(krow + col_i + q, acc[kk * 9 + q]);
+        if (S.col_s >= 0)
+          for (int q = 0; q < 6; q++)
+            atomicAdd(krow + S.col_s + q, -acc[kk * 9 + 3 + q] * S.vol_inv);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+size_t kuf_adjoint_smem(const B2Args &a, int ks, int threads) {
+  if (threads < 64 || threads > 256 || (threads & 31)) return 0;
+  const size_t b = kuf_layout(a, ks).total;
+  return b <= 227 * 1024 ? b : 0;
+}
+
+int launch_kuf_adjoint(const KufArgs &k, int ks, int threads, int n_items, int item0,
+                       cudaStream_t stream) {
+  if (n_items <= 0) return 0;
+  const size_t smem = kuf_adjoint_smem(k.a, ks, threads);
+  if (smem == 0) return -1;
+  if (cudaFuncSetAttribute(k_kuf_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_kuf_adjoint, threads, smem) !=
+          cudaSuccess)
+    return -1;
+  const int grid = std::min(n_items, sms * std::max(per_sm, 1));
+  k_kuf_adjoint<<<grid, threads, smem, stream>>>(k, ks, n_items, item0);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // F_i = sum over pairs of i (f_ij - f_ji); each block also reduces its atoms'
 // energies and virials (sum f_ij (x) r_ij) into one partial row (fixed tree
 // order, so the result is deterministic).  128 threads per block.

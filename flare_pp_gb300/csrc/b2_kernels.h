@@ -100,6 +100,41 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                       double *reduce_out, bool gather, T *u_buf, long long n_pairs,
                       const int *nbr_i, cudaStream_t stream);
 
+// Kuf by the adjoint route (FP64): one persistent launch over work items
+// (structure, atom) of a batch of training structures.
+struct KufStruc {
+  const double *c64;        // noa x sb single-bond coefficients, atom order
+  const double *phat64;     // normalised B2 rows (species-sorted), stride ldp
+  const double *norm64;     // noa
+  const int *row_of_atom, *species, *offset, *nbr_j, *nbr_s;
+  const dvec4 *rel;         // (r, x, y, z) of r_ij = x_j - x_i
+  const int *force_col;     // noa: column of the atom's x force label, -1 none
+  long long col_e, col_s;   // energy and first stress column, -1 none
+  double vol_inv;
+};
+struct KufSpecies {
+  const double *dhat;       // n_sparse x n_d normalised sparse descriptors
+  const double *norms;      // n_sparse
+  int n_sparse, row0;       // rows of this species in Kuf
+};
+struct KufArgs {
+  B2Args a;
+  const KufStruc *strucs;
+  const int2 *items;        // (structure, atom)
+  int n_items;
+  KufSpecies sp[kMaxSpecies];
+  const int *pair_tab;
+  double sig2, power;
+  int ldp;
+  double *kuf;              // n_sparse_total x n_labels, row-major (added to)
+  long long n_labels;
+};
+// ks sparse environments per pass and threads per block (the tile shape);
+// shared-memory bytes the shape needs (0 if it does not fit).
+size_t kuf_adjoint_smem(const B2Args &a, int ks, int threads);
+int launch_kuf_adjoint(const KufArgs &k, int ks, int threads, int n_items, int item0,
+                       cudaStream_t stream);
+
 int launch_b2_dp(const B2Args &a, int npl, const int *plist, const int *nbr_i,
                  const int *nbr_s, const dvec4 *rel, const int *species,
                  const int *pair_tab, const double *c_in, const double *p_in,

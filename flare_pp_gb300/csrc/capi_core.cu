@@ -49,7 +49,7 @@ int DevBuf::reserve(size_t n) {
   return FPP_OK;
 }
 
-static int ensure_tables(cudaStream_t stream) {
+int ensure_tables(cudaStream_t stream) {
   // the harmonic normalisation and B3 coupling tables live in constant memory
   // of this module; upload them once per device (under a lock: host threads
   // may make their first call on a device at the same time)

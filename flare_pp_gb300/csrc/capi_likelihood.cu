@@ -1,24 +1,27 @@
 // C ABI: the log marginal likelihood of the sparse GP and its gradient in the
-// hyperparameters (sigma, sigma_e, sigma_f, sigma_s) for one
-// NormalizedDotProduct kernel, FP64 on the GPU:
+// hyperparameters (sigma of each NormalizedDotProduct kernel, sigma_e,
+// sigma_f, sigma_s), FP64 on the GPU:
 //   SparseGP::compute_likelihood_stable (sparse_gp.cpp:704-732),
 //   SparseGP::compute_likelihood_gradient_stable (sparse_gp.cpp:734-862),
 //   SparseGP::compute_KnK (sparse_gp.cpp:888-922).
 //
-// With Lambda = diag(noise_vector), r = y - Kuf^T alpha and the kernel's
-// dKuu/dsigma = 2 Kuu / sigma, dKuf/dsigma = 2 Kuf / sigma
-// (normalized_dot_product.cpp:581-615):
+// With Lambda = diag(noise_vector), r = y - Kuf^T alpha and, for kernel i
+// (rows [o_i, o_i + n_i) of Kuu and Kuf; Kuu is block diagonal over the
+// kernels), dKuu/dsigma_i = 2 Kuu_i / sigma_i and dKuf/dsigma_i = 2 Kuf_i /
+// sigma_i on kernel i's rows and 0 elsewhere (normalized_dot_product.cpp:
+// 581-615):
 //   data_fit   = -1/2 y . (Lambda r)
 //   complexity = 1/2 (log det Lambda - 2 sum log|L_inv_ii| + 2 sum log|R_inv_ii|)
-//   d/dsigma   = 1/2 tr(Kuu^-1 dKuu) - 1/2 tr(Pi Sigma)
+//   d/dsigma_i = 1/2 tr(Kuu^-1 dKuu) - 1/2 tr(Pi Sigma)
 //                + (dKuf^T alpha) . (Lambda r) - 1/2 alpha . (dKuu alpha),
 //                Pi = dKuf Lambda Kuf^T + (its transpose) + dKuu
 //   d/dsigma_x = -n_x / sigma_x + tr(KnK_x Sigma) / sigma_x^3
 //                + r . (one_x r) / sigma_x^3,   KnK_x = Kuf one_x Kuf^T.
 // The traces tr(KnK_x Sigma) are sums over the labels of kind x of
 // k_l . (Sigma k_l) (k_l = column l of Kuf): one GEMM B = Sigma Kuf replaces
-// the three n x n products of the reference; tr(Kuu^-1 dKuu) is formed as in
-// the reference, by an LU solve of Kuu against dKuu.
+// the three n x n products of the reference, and its row blocks give the
+// per-kernel traces; tr(Kuu^-1 dKuu) is formed as in the reference, by an LU
+// solve of Kuu (against Kuu, then the diagonal of each kernel's block).
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
@@ -50,7 +53,11 @@ namespace {
                                     " status " + std::to_string((int)_s));   \
   } while (0)
 
-constexpr int kLkBlocks = 256, kLkThreads = 256, kLkSums = 9;
+constexpr int kLkBlocks = 256, kLkThreads = 256, kLkMaxKernels = 8;
+// per-block partial sums: 0 y Lambda r, 1-3 r^2 of kind e, f, s, 4-6
+// k_l . (Sigma k_l) of kind e, f, s (all rows), then per kernel i:
+// 7 + 4 i: Ka_i Lambda r, 8 + 4 i .. 10 + 4 i: the traces on kernel i's rows
+constexpr int kLkSums = 7 + 4 * kLkMaxKernels;
 
 __device__ __forceinline__ double block_sum(double v, double *sm) {
 #pragma unroll
@@ -69,12 +76,12 @@ __device__ __forceinline__ double block_sum(double v, double *sm) {
 }
 
 // Per-block partial sums over the labels (fixed order: the host adds the
-// blocks in index order):
-//   0: y Lambda r     1: Ka Lambda r     2-4: r^2 of kind e, f, s
-//   5-7: k_l . (Sigma k_l) of kind e, f, s  (B = Sigma Kuf, when given)
-//   8: unused
-__global__ void k_label_sums(int n, int m, const double *__restrict__ y,
-                             const double *__restrict__ Ka, const int *__restrict__ kind,
+// blocks in index order), laid out as kLkSums above.  Ka is the full
+// Kuf^T alpha, Kak[i] = Kuf_i^T alpha_i (kernel i's rows); B = Sigma Kuf
+// (when given).
+__global__ void k_label_sums(int n, int m, int nk, const int *__restrict__ koff,
+                             const double *__restrict__ y, const double *__restrict__ Ka,
+                             const double *__restrict__ Kak, const int *__restrict__ kind,
                              const double *__restrict__ inv_var,
                              const double *__restrict__ Kuf, const double *__restrict__ B,
                              double *__restrict__ partial) {
@@ -87,18 +94,26 @@ __global__ void k_label_sums(int n, int m, const double *__restrict__ y,
     const double nv = inv_var[t];
     const double r = y[l] - Ka[l];
     acc[0] = fma(y[l], nv * r, acc[0]);
-    acc[1] = fma(Ka[l], nv * r, acc[1]);
     const double r2 = r * r;
-    acc[2] += t == 0 ? r2 : 0.0;
-    acc[3] += t == 1 ? r2 : 0.0;
-    acc[4] += t == 2 ? r2 : 0.0;
-    if (B) {
-      // column l of the row-major n x m matrices
-      double q = 0.0;
-      for (int i = 0; i < n; i++) q = fma(Kuf[(size_t)i * m + l], B[(size_t)i * m + l], q);
-      acc[5] += t == 0 ? q : 0.0;
-      acc[6] += t == 1 ? q : 0.0;
-      acc[7] += t == 2 ? q : 0.0;
+    acc[1] += t == 0 ? r2 : 0.0;
+    acc[2] += t == 1 ? r2 : 0.0;
+    acc[3] += t == 2 ? r2 : 0.0;
+#pragma unroll
+    for (int i = 0; i < kLkMaxKernels; i++) {
+      if (i >= nk) break;
+      acc[7 + 4 * i] = fma(Kak[(size_t)i * m + l], nv * r, acc[7 + 4 * i]);
+      if (B) {
+        // column l of the row-major n x m matrices, kernel i's rows
+        double q = 0.0;
+        for (int row = koff[i]; row < koff[i + 1]; row++)
+          q = fma(Kuf[(size_t)row * m + l], B[(size_t)row * m + l], q);
+        acc[8 + 4 * i] += t == 0 ? q : 0.0;
+        acc[9 + 4 * i] += t == 1 ? q : 0.0;
+        acc[10 + 4 * i] += t == 2 ? q : 0.0;
+        acc[4] += t == 0 ? q : 0.0;
+        acc[5] += t == 1 ? q : 0.0;
+        acc[6] += t == 2 ? q : 0.0;
+      }
     }
   }
   for (int k = 0; k < kLkSums; k++) {
@@ -107,14 +122,18 @@ __global__ void k_label_sums(int n, int m, const double *__restrict__ y,
   }
 }
 
-// sum of A .* C (n x n) per block: tr(A C) for a symmetric C
-__global__ void k_frob(long long nn, const double *__restrict__ A, const double *__restrict__ C,
-                       double *__restrict__ partial) {
+// sum of A .* C over the square block [o, o + len) of n x n matrices, per
+// grid block: tr(A_b C_b) for a symmetric C
+__global__ void k_frob(int n, int o, int len, const double *__restrict__ A,
+                       const double *__restrict__ C, double *__restrict__ partial) {
   __shared__ double sm[32];
   double acc = 0.0;
+  const long long nn = (long long)len * len;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nn;
-       k += (long long)gridDim.x * blockDim.x)
-    acc = fma(A[k], C[k], acc);
+       k += (long long)gridDim.x * blockDim.x) {
+    const size_t idx = (size_t)(o + k / len) * n + (o + k % len);
+    acc = fma(A[idx], C[idx], acc);
+  }
   const double s = block_sum(acc, sm);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
@@ -128,10 +147,10 @@ __global__ void k_mask_kind(int n, int m, const double *__restrict__ Kuf,
   out[k] = kind[l] == t ? Kuf[k] : 0.0;
 }
 
-__global__ void k_diag_sum(int n, const double *__restrict__ X, double *out) {
+__global__ void k_diag_sum(int n, int o, int len, const double *__restrict__ X, double *out) {
   __shared__ double sm[32];
   double acc = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += X[(size_t)i * n + i];
+  for (int i = o + threadIdx.x; i < o + len; i += blockDim.x) acc += X[(size_t)i * n + i];
   const double s = block_sum(acc, sm);
   if (threadIdx.x == 0) out[0] = s;
 }
@@ -147,19 +166,26 @@ int upload(DevBuf &b, const void *h, size_t bytes, cudaStream_t st) {
 
 using namespace fpp;
 
-extern "C" int fpp_likelihood_gradient_stable(
-    int32_t n, int32_t m, const double *Kuf, const double *Kuu, const double *y,
-    const int32_t *label_kind, const double *alpha, const double *Sigma,
-    const double *L_diag, const double *R_inv_diag, const double *hyps,
-    int32_t want_gradient, double *out, double *KnK, void *stream) {
+namespace {
+
+int likelihood_core(int32_t n, int32_t m, const double *Kuf, const double *Kuu,
+                    const double *y, const int32_t *label_kind, const double *alpha,
+                    const double *Sigma, const double *L_diag, const double *R_inv_diag,
+                    int32_t nk, const int32_t *koff, const double *hyps,
+                    int32_t want_gradient, double *out, double *KnK, cudaStream_t st) {
   if (n <= 0 || m < 0) return fail(FPP_ERR_INVALID, "bad sizes");
+  if (nk < 1 || nk > kLkMaxKernels) return fail(FPP_ERR_INVALID, "1 to 8 kernels");
+  if (!koff || koff[0] != 0 || koff[nk] != n)
+    return fail(FPP_ERR_INVALID, "kernel row offsets must run from 0 to n");
+  for (int i = 0; i < nk; i++)
+    if (koff[i + 1] < koff[i]) return fail(FPP_ERR_INVALID, "kernel row offsets decrease");
   if (!Kuf && m > 0) return fail(FPP_ERR_INVALID, "null Kuf");
   if (!y && m > 0) return fail(FPP_ERR_INVALID, "null y");
   if (!label_kind && m > 0) return fail(FPP_ERR_INVALID, "null label kinds");
   if (!alpha || !L_diag || !R_inv_diag || !hyps || !out)
     return fail(FPP_ERR_INVALID, "null argument");
   if (want_gradient && (!Kuu || !Sigma)) return fail(FPP_ERR_INVALID, "null Kuu / Sigma");
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < nk + 3; k++)
     if (!std::isfinite(hyps[k]) || hyps[k] == 0.0)
       return fail(FPP_ERR_NUMERIC, "hyperparameters must be finite and non-zero");
   long long cnt[3] = {0, 0, 0};
@@ -168,9 +194,7 @@ extern "C" int fpp_likelihood_gradient_stable(
       return fail(FPP_ERR_INVALID, "label kind outside 0..2");
     cnt[label_kind[l]]++;
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  const double sig = hyps[0];
-  const double noise[3] = {hyps[1], hyps[2], hyps[3]};
+  const double noise[3] = {hyps[nk], hyps[nk + 1], hyps[nk + 2]};
   const double inv_var[3] = {1.0 / (noise[0] * noise[0]), 1.0 / (noise[1] * noise[1]),
                              1.0 / (noise[2] * noise[2])};
   cublasHandle_t h;
@@ -182,17 +206,33 @@ extern "C" int fpp_likelihood_gradient_stable(
   cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH);
   FPP_CUBLAS_LK(cublasSetStream(h, st));
   const double one = 1.0, zero = 0.0;
-  DevBuf dKuf, dy, dkind, dalpha, dKa, dnv, dpart, dB, dSig, dKuu, dX, dLU, dwork, dpiv, dinfo,
-      dtmp, dfro;
+  DevBuf dKuf, dy, dkind, dalpha, dKa, dKak, dkoff, dnv, dpart, dB, dSig, dKuu, dX, dLU, dwork,
+      dpiv, dinfo, dtmp, dfro;
   FPP_TRY(upload(dKuf, Kuf, sizeof(double) * (size_t)n * m, st));
   FPP_TRY(upload(dy, y, sizeof(double) * (size_t)m, st));
   FPP_TRY(upload(dkind, label_kind, sizeof(int) * (size_t)m, st));
   FPP_TRY(upload(dalpha, alpha, sizeof(double) * n, st));
   FPP_TRY(upload(dnv, inv_var, sizeof(inv_var), st));
+  FPP_TRY(upload(dkoff, koff, sizeof(int32_t) * (nk + 1), st));
   FPP_TRY(dKa.reserve(sizeof(double) * std::max(m, 1)));
-  // Ka = Kuf^T alpha (Kuf row-major n x m is column-major m x n)
-  if (m) FPP_CUBLAS_LK(cublasDgemv(h, CUBLAS_OP_N, m, n, &one, dKuf.as<double>(), m,
-                                   dalpha.as<double>(), 1, &zero, dKa.as<double>(), 1));
+  FPP_TRY(dKak.reserve(sizeof(double) * (size_t)nk * std::max(m, 1)));
+  // Ka = Kuf^T alpha (Kuf row-major n x m is column-major m x n), and per
+  // kernel Ka_i = Kuf_i^T alpha_i from its rows
+  if (m) {
+    FPP_CUBLAS_LK(cublasDgemv(h, CUBLAS_OP_N, m, n, &one, dKuf.as<double>(), m,
+                              dalpha.as<double>(), 1, &zero, dKa.as<double>(), 1));
+    for (int i = 0; i < nk; i++) {
+      const int ni = koff[i + 1] - koff[i];
+      if (ni == 0) {
+        FPP_CUDA(cudaMemsetAsync(dKak.as<double>() + (size_t)i * m, 0, sizeof(double) * m, st));
+        continue;
+      }
+      FPP_CUBLAS_LK(cublasDgemv(h, CUBLAS_OP_N, m, ni, &one,
+                                dKuf.as<double>() + (size_t)koff[i] * m, m,
+                                dalpha.as<double>() + koff[i], 1, &zero,
+                                dKak.as<double>() + (size_t)i * m, 1));
+    }
+  }
   const double *Bp = nullptr;
   if (want_gradient) {
     FPP_TRY(upload(dSig, Sigma, sizeof(double) * (size_t)n * n, st));
@@ -208,26 +248,31 @@ extern "C" int fpp_likelihood_gradient_stable(
   FPP_TRY(dpart.reserve(sizeof(double) * kLkBlocks * kLkSums));
   FPP_CUDA(cudaMemsetAsync(dpart.ptr, 0, sizeof(double) * kLkBlocks * kLkSums, st));
   if (m) {
-    k_label_sums<<<kLkBlocks, kLkThreads, 0, st>>>(n, m, dy.as<double>(), dKa.as<double>(),
-                                                   dkind.as<int>(), dnv.as<double>(),
-                                                   dKuf.as<double>(), Bp, dpart.as<double>());
+    k_label_sums<<<kLkBlocks, kLkThreads, 0, st>>>(
+        n, m, nk, dkoff.as<int>(), dy.as<double>(), dKa.as<double>(), dKak.as<double>(),
+        dkind.as<int>(), dnv.as<double>(), dKuf.as<double>(), Bp, dpart.as<double>());
     FPP_CUDA(cudaGetLastError());
   }
-  double tr_kuu_sigma = 0.0, tr_kinv = 0.0, a_kuu_a = 0.0;
-  std::vector<double> fro(kLkBlocks, 0.0);
+  std::vector<double> tr_kuu_sigma(nk, 0.0), tr_kinv(nk, 0.0), a_kuu_a(nk, 0.0);
   if (want_gradient) {
     const long long nn = (long long)n * n;
-    FPP_TRY(dfro.reserve(sizeof(double) * kLkBlocks));
-    k_frob<<<kLkBlocks, kLkThreads, 0, st>>>(nn, dKuu.as<double>(), dSig.as<double>(),
-                                             dfro.as<double>());
-    FPP_CUDA(cudaGetLastError());
-    // alpha . (Kuu alpha)
-    FPP_TRY(dtmp.reserve(sizeof(double) * (n + 1)));
-    FPP_CUBLAS_LK(cublasDgemv(h, CUBLAS_OP_N, n, n, &one, dKuu.as<double>(), n,
-                              dalpha.as<double>(), 1, &zero, dtmp.as<double>(), 1));
+    FPP_TRY(dfro.reserve(sizeof(double) * kLkBlocks * nk));
+    FPP_TRY(dtmp.reserve(sizeof(double) * (n + nk)));
     cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST);
-    FPP_CUBLAS_LK(cublasDdot(h, n, dtmp.as<double>(), 1, dalpha.as<double>(), 1, &a_kuu_a));
-    // tr(Kuu^-1 dKuu): LU of Kuu, solved against dKuu = 2 Kuu / sigma
+    for (int i = 0; i < nk; i++) {
+      const int o = koff[i], ni = koff[i + 1] - koff[i];
+      if (ni == 0) continue;
+      k_frob<<<kLkBlocks, kLkThreads, 0, st>>>(n, o, ni, dKuu.as<double>(), dSig.as<double>(),
+                                               dfro.as<double>() + (size_t)i * kLkBlocks);
+      FPP_CUDA(cudaGetLastError());
+      // alpha_i . (Kuu_i alpha_i)
+      FPP_CUBLAS_LK(cublasDgemv(h, CUBLAS_OP_N, ni, ni, &one, dKuu.as<double>() + (size_t)o * n + o,
+                                n, dalpha.as<double>() + o, 1, &zero, dtmp.as<double>(), 1));
+      FPP_CUBLAS_LK(cublasDdot(h, ni, dtmp.as<double>(), 1, dalpha.as<double>() + o, 1,
+                               &a_kuu_a[i]));
+    }
+    // tr(Kuu^-1 dKuu_i): LU of Kuu solved against Kuu, then each kernel's
+    // diagonal block scaled by 2 / sigma_i
     cusolverDnHandle_t sh;
     if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS)
       return fail(FPP_ERR_CUDA, "cusolverDnCreate failed");
@@ -240,8 +285,6 @@ extern "C" int fpp_likelihood_gradient_stable(
     FPP_TRY(dX.reserve(sizeof(double) * nn));
     FPP_CUDA(cudaMemcpyAsync(dLU.ptr, dKuu.ptr, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
     FPP_CUDA(cudaMemcpyAsync(dX.ptr, dKuu.ptr, sizeof(double) * nn, cudaMemcpyDeviceToDevice, st));
-    const double gscale = 2.0 / sig;
-    FPP_CUBLAS_LK(cublasDscal(h, (int)nn, &gscale, dX.as<double>(), 1));
     int lwork = 0;
     FPP_CUSOLVER_LK(cusolverDnDgetrf_bufferSize(sh, n, n, dLU.as<double>(), n, &lwork));
     FPP_TRY(dwork.reserve(sizeof(double) * std::max(lwork, 1)));
@@ -252,17 +295,27 @@ extern "C" int fpp_likelihood_gradient_stable(
     // Kuu is symmetric: its row-major and column-major forms agree
     FPP_CUSOLVER_LK(cusolverDnDgetrs(sh, CUBLAS_OP_N, n, n, dLU.as<double>(), n, dpiv.as<int>(),
                                      dX.as<double>(), n, dinfo.as<int>() + 1));
-    k_diag_sum<<<1, 256, 0, st>>>(n, dX.as<double>(), dtmp.as<double>() + n);
-    FPP_CUDA(cudaGetLastError());
+    for (int i = 0; i < nk; i++) {
+      k_diag_sum<<<1, 256, 0, st>>>(n, koff[i], koff[i + 1] - koff[i], dX.as<double>(),
+                                    dtmp.as<double>() + n + i);
+      FPP_CUDA(cudaGetLastError());
+    }
     int info[2] = {0, 0};
+    std::vector<double> fro((size_t)kLkBlocks * nk, 0.0);
     FPP_CUDA(cudaMemcpyAsync(info, dinfo.ptr, sizeof(info), cudaMemcpyDeviceToHost, st));
-    FPP_CUDA(cudaMemcpyAsync(&tr_kinv, dtmp.as<double>() + n, sizeof(double),
+    FPP_CUDA(cudaMemcpyAsync(tr_kinv.data(), dtmp.as<double>() + n, sizeof(double) * nk,
                              cudaMemcpyDeviceToHost, st));
-    FPP_CUDA(cudaMemcpyAsync(fro.data(), dfro.ptr, sizeof(double) * kLkBlocks,
+    FPP_CUDA(cudaMemcpyAsync(fro.data(), dfro.ptr, sizeof(double) * fro.size(),
                              cudaMemcpyDeviceToHost, st));
     FPP_CUDA(cudaStreamSynchronize(st));
     if (info[0] != 0) return fail(FPP_ERR_NUMERIC, "Kuu is singular (LU)");
-    for (int b = 0; b < kLkBlocks; b++) tr_kuu_sigma += fro[b];
+    for (int i = 0; i < nk; i++) {
+      if (koff[i + 1] == koff[i]) {
+        tr_kinv[i] = 0.0;
+        continue;
+      }
+      for (int b = 0; b < kLkBlocks; b++) tr_kuu_sigma[i] += fro[(size_t)i * kLkBlocks + b];
+    }
   }
   if (KnK && m) {
     // Kuf one_x Kuf^T for x = e, f, s (row-major n x n)
@@ -312,16 +365,42 @@ extern "C" int fpp_likelihood_gradient_stable(
   out[2] = complexity;
   out[3] = constant;
   if (want_gradient) {
-    double tx = 0.0;
-    for (int t = 0; t < 3; t++) tx += S[5 + t] * inv_var[t];
-    const double tr_pi_sigma = 2.0 * (2.0 / sig) * tx + (2.0 / sig) * tr_kuu_sigma;
-    const double cg = 0.5 * tr_kinv - 0.5 * tr_pi_sigma;
-    const double dg = (2.0 / sig) * S[1] - 0.5 * (2.0 / sig) * a_kuu_a;
-    out[4] = cg + dg;
+    for (int i = 0; i < nk; i++) {
+      const double g = 2.0 / hyps[i];
+      double tx = 0.0;
+      for (int t = 0; t < 3; t++) tx += S[8 + 4 * i + t] * inv_var[t];
+      const double tr_pi_sigma = 2.0 * g * tx + g * tr_kuu_sigma[i];
+      const double cg = 0.5 * g * tr_kinv[i] - 0.5 * tr_pi_sigma;
+      const double dg = g * S[7 + 4 * i] - 0.5 * g * a_kuu_a[i];
+      out[4 + i] = cg + dg;
+    }
     for (int t = 0; t < 3; t++) {
       const double s3 = noise[t] * noise[t] * noise[t];
-      out[5 + t] = (-(double)cnt[t] / noise[t] + S[5 + t] / s3) + S[2 + t] / s3;
+      out[4 + nk + t] = (-(double)cnt[t] / noise[t] + S[4 + t] / s3) + S[1 + t] / s3;
     }
   }
   return FPP_OK;
+}
+
+}  // namespace
+
+extern "C" int fpp_likelihood_gradient_stable(
+    int32_t n, int32_t m, const double *Kuf, const double *Kuu, const double *y,
+    const int32_t *label_kind, const double *alpha, const double *Sigma,
+    const double *L_diag, const double *R_inv_diag, const double *hyps,
+    int32_t want_gradient, double *out, double *KnK, void *stream) {
+  const int32_t koff[2] = {0, n};
+  return likelihood_core(n, m, Kuf, Kuu, y, label_kind, alpha, Sigma, L_diag, R_inv_diag, 1,
+                         koff, hyps, want_gradient, out, KnK, (cudaStream_t)stream);
+}
+
+extern "C" int fpp_likelihood_gradient_stable_kernels(
+    int32_t n, int32_t m, const double *Kuf, const double *Kuu, const double *y,
+    const int32_t *label_kind, const double *alpha, const double *Sigma,
+    const double *L_diag, const double *R_inv_diag, int32_t n_kernels,
+    const int32_t *kernel_offsets, const double *hyps, int32_t want_gradient, double *out,
+    double *KnK, void *stream) {
+  return likelihood_core(n, m, Kuf, Kuu, y, label_kind, alpha, Sigma, L_diag, R_inv_diag,
+                         n_kernels, kernel_offsets, hyps, want_gradient, out, KnK,
+                         (cudaStream_t)stream);
 }

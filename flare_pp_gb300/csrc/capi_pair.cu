@@ -135,6 +135,9 @@ int lammps_load(fpp_model *m, int32_t nlocal, int32_t nall, const double *x,
       if (neighbors[p] < 0 || neighbors[p] >= nall)
         return fail(FPP_ERR_INVALID, "neighbor index outside 0..nall-1");
   }
+  // a pair style may be the process's first caller: no structure has
+  // uploaded the kernels' constant tables yet
+  FPP_TRY(ensure_tables(st));
   if (!m->lammps) m->lammps = new fpp_lammps_ws();
   fpp_lammps_ws &w = *m->lammps;
   fpp_structure *s = &w.s;
@@ -187,6 +190,37 @@ int lammps_load(fpp_model *m, int32_t nlocal, int32_t nall, const double *x,
 
 using namespace fpp;
 
+namespace fpp {
+
+// Device bytes the pair style needs per listed atom with max_neigh
+// neighbors (the buffers of mapped_core and of the pair list), the
+// estimate that sizes the atom batches under a memory cap.
+static double pair_bytes_per_atom(const fpp_model *m, int max_neigh, int precision) {
+  const double sb = (double)m->args.n_species * m->args.N * m->args.H;
+  const double ldp = (double)((m->n_d + 63) / 64 * 64);
+  double per = 4.0 * (2 * sb + 2 * ldp) + 2.0 * 2 * ldp  // c, u, V, w; split operand
+               + 8.0 * 8;                                // norms, energies, rows
+  if (precision == FPP_PREC_FP64) per += 8.0 * (2 * sb + 3 * ldp);
+  // per neighbor: FP64 and FP32 geometry, indices, pair forces, the list
+  per += (double)max_neigh * (32 + 16 + 4 * 4 + 16 + 4 + (precision == FPP_PREC_FP64 ? 16 : 0));
+  return per;
+}
+
+}  // namespace fpp
+
+extern "C" int fpp_model_set_max_memory(fpp_model *m, double bytes) {
+  if (!m) return fail(FPP_ERR_INVALID, "null model");
+  if (!(bytes >= 0)) return fail(FPP_ERR_INVALID, "bytes must be >= 0");
+  m->max_memory = bytes;
+  return FPP_OK;
+}
+
+extern "C" int fpp_model_pair_batches(const fpp_model *m, int32_t *n_batches) {
+  if (!m || !n_batches) return fail(FPP_ERR_INVALID, "null argument");
+  *n_batches = m->last_pair_batches;
+  return FPP_OK;
+}
+
 extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                                 const double *x, const int32_t *type, int32_t inum,
                                 const int32_t *ilist, const int32_t *numneigh,
@@ -201,47 +235,88 @@ extern "C" int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
     return fail(FPP_ERR_INVALID, "mapped coefficients not set");
   if (precision != FPP_PREC_FP64 && precision != FPP_PREC_MIXED)
     return fail(FPP_ERR_INVALID, "bad precision");
+  if (inum < 0 || (inum > 0 && (!ilist || !numneigh)))
+    return fail(FPP_ERR_INVALID, "bad ilist / numneigh");
   cudaStream_t st = (cudaStream_t)stream;
-  FPP_TRY(lammps_load(m, nlocal, nall, x, type, inum, ilist, numneigh, neighbors, st));
-  fpp_lammps_ws &w = *m->lammps;
-  fpp_structure *s = &w.s;
-  StructureState &S = s->st;
-  const int np = (int)S.n_pairs;
-  FPP_TRY(w.d_f.reserve(sizeof(double) * 3 * std::max(nall, 1)));
-  FPP_TRY(w.d_vir.reserve(sizeof(double) * 8));
-  FPP_TRY(w.d_e.reserve(sizeof(double) * 8));
-  if (nall) FPP_CUDA(cudaMemsetAsync(w.d_f.ptr, 0, sizeof(double) * 3 * nall, st));
-  FPP_CUDA(cudaMemsetAsync(w.d_vir.ptr, 0, sizeof(double) * 8, st));
-  // same kernels as fpp_predict_mapped, with the pair style's strict filter
-  FPP_TRY(mapped_core(m, s, precision, st, /*strict=*/1));
-  if (np) {
-    if (precision == FPP_PREC_FP64)
-      k_pair_scatter<double><<<(np + 127) / 128, 128, 0, st>>>(
-          np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
-          S.pair_f.as<double>(), w.d_f.as<double>(), w.d_vir.as<double>());
-    else
-      k_pair_scatter<float><<<(np + 127) / 128, 128, 0, st>>>(
-          np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(), S.nbr_rel.as<dvec4>(),
-          S.pair_f.as<float>(), w.d_f.as<double>(), w.d_vir.as<double>());
+  // Atom batches under the memory cap (pair_flare_kokkos.cpp:145-177): the
+  // cap less the mapped coefficients, over the bytes per atom; as many
+  // batches as needed, sizes differing by at most one atom, the first ones
+  // the larger.  No cap (0): one batch.
+  int n_batches = 1;
+  if (m->max_memory > 0 && inum > 0) {
+    int max_neigh = 0;
+    for (int ii = 0; ii < inum; ii++) max_neigh = std::max(max_neigh, (int)numneigh[ii]);
+    const double beta_mem = (double)m->n_species * m->n_d * m->n_d * 8.0;
+    const double avail = m->max_memory - beta_mem;
+    const double per = pair_bytes_per_atom(m, max_neigh, precision);
+    const long long fit = avail > 0 ? (long long)(avail / per) : 0;
+    if (fit < 1) return fail(FPP_ERR_CAPACITY, "Not enough memory for even a single atom!");
+    const int approx = (int)std::min<long long>(fit, inum);
+    n_batches = (inum + approx - 1) / approx;
+  }
+  const int base = inum / n_batches;
+  int remainder = inum - n_batches * base;
+  std::vector<long long> nb_off(inum + 1, 0);
+  for (int ii = 0; ii < inum; ii++) nb_off[ii + 1] = nb_off[ii] + numneigh[ii];
+  std::vector<double> hf(3 * (size_t)nall, 0.0);
+  double vir_total[6] = {0, 0, 0, 0, 0, 0}, e_total = 0;
+  std::vector<double> he;
+  int start = 0;
+  for (int b = 0; b < n_batches; b++) {
+    const int bs = base + (remainder-- > 0 ? 1 : 0);
+    const int32_t *nbrs_b = neighbors ? neighbors + nb_off[start] : nullptr;
+    FPP_TRY(lammps_load(m, nlocal, nall, x, type, bs, ilist + start, numneigh + start, nbrs_b,
+                        st));
+    fpp_lammps_ws &w = *m->lammps;
+    fpp_structure *s = &w.s;
+    StructureState &S = s->st;
+    const int np = (int)S.n_pairs;
+    FPP_TRY(w.d_f.reserve(sizeof(double) * 3 * std::max(nall, 1)));
+    FPP_TRY(w.d_vir.reserve(sizeof(double) * 8));
+    FPP_TRY(w.d_e.reserve(sizeof(double) * 8));
+    if (nall) FPP_CUDA(cudaMemsetAsync(w.d_f.ptr, 0, sizeof(double) * 3 * nall, st));
+    FPP_CUDA(cudaMemsetAsync(w.d_vir.ptr, 0, sizeof(double) * 8, st));
+    // same kernels as fpp_predict_mapped, with the pair style's strict filter
+    FPP_TRY(mapped_core(m, s, precision, st, /*strict=*/1));
+    if (np) {
+      if (precision == FPP_PREC_FP64)
+        k_pair_scatter<double><<<(np + 127) / 128, 128, 0, st>>>(
+            np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(),
+            S.nbr_rel.as<dvec4>(), S.pair_f.as<double>(), w.d_f.as<double>(),
+            w.d_vir.as<double>());
+      else
+        k_pair_scatter<float><<<(np + 127) / 128, 128, 0, st>>>(
+            np, w.d_ilist.as<int>(), S.nbr_i.as<int>(), w.d_nbrs.as<int>(),
+            S.nbr_rel.as<dvec4>(), S.pair_f.as<float>(), w.d_f.as<double>(),
+            w.d_vir.as<double>());
+      FPP_CUDA(cudaGetLastError());
+    }
+    if (bs) k_energy_sum<<<1, 256, 0, st>>>(bs, S.atom_e.as<double>(), w.d_e.as<double>());
     FPP_CUDA(cudaGetLastError());
+    std::vector<double> bf(3 * (size_t)nall);
+    he.assign(bs, 0.0);
+    double vir[6] = {0, 0, 0, 0, 0, 0}, etot = 0;
+    FPP_CUDA(cudaStreamSynchronize(st));
+    FPP_TRY(check_status(S, st, "pair compute"));
+    if (nall)
+      FPP_CUDA(cudaMemcpy(bf.data(), w.d_f.ptr, sizeof(double) * 3 * nall,
+                          cudaMemcpyDeviceToHost));
+    if (bs) {
+      FPP_CUDA(cudaMemcpy(he.data(), S.atom_e.ptr, sizeof(double) * bs, cudaMemcpyDeviceToHost));
+      FPP_CUDA(cudaMemcpy(&etot, w.d_e.ptr, sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    FPP_CUDA(cudaMemcpy(vir, w.d_vir.ptr, sizeof(vir), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < bf.size(); k++) hf[k] += bf[k];
+    e_total += etot;
+    for (int k = 0; k < 6; k++) vir_total[k] += vir[k];
+    if (eatom)
+      for (int ii = 0; ii < bs; ii++) eatom[ilist[start + ii]] += he[ii];
+    start += bs;
   }
-  if (inum) k_energy_sum<<<1, 256, 0, st>>>(inum, S.atom_e.as<double>(), w.d_e.as<double>());
-  FPP_CUDA(cudaGetLastError());
-  std::vector<double> hf(3 * (size_t)nall), he(inum);
-  double vir[6] = {0, 0, 0, 0, 0, 0}, etot = 0;
-  FPP_CUDA(cudaStreamSynchronize(st));
-  FPP_TRY(check_status(S, st, "pair compute"));
-  if (nall) FPP_CUDA(cudaMemcpy(hf.data(), w.d_f.ptr, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost));
-  if (inum) {
-    FPP_CUDA(cudaMemcpy(he.data(), S.atom_e.ptr, sizeof(double) * inum, cudaMemcpyDeviceToHost));
-    FPP_CUDA(cudaMemcpy(&etot, w.d_e.ptr, sizeof(double), cudaMemcpyDeviceToHost));
-  }
-  FPP_CUDA(cudaMemcpy(vir, w.d_vir.ptr, sizeof(vir), cudaMemcpyDeviceToHost));
   for (size_t k = 0; k < hf.size(); k++) f[k] += hf[k];
-  if (eng_vdwl) *eng_vdwl += etot;
+  if (eng_vdwl) *eng_vdwl += e_total;
   if (virial)
-    for (int k = 0; k < 6; k++) virial[k] += vir[k];
-  if (eatom)
-    for (int ii = 0; ii < inum; ii++) eatom[ilist[ii]] += he[ii];
+    for (int k = 0; k < 6; k++) virial[k] += vir_total[k];
+  m->last_pair_batches = n_batches;
   return FPP_OK;
 }

@@ -3,9 +3,15 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -126,6 +132,102 @@ int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want
                                 S.norm64.as<double>(), S.phat64.as<double>(),
                                 nullptr, nullptr, ldp, nullptr, st) != 0)
     return fail(FPP_ERR_CUDA, "B2 forward (FP64) launch failed");
+  return FPP_OK;
+}
+
+// Tile shape of the adjoint Kuf kernel (sparse environments per pass,
+// threads per block), chosen by timing the candidates that fit in shared
+// memory on a prefix of the work list (CUDA events on the stream) and cached
+// per device and descriptor shape: in this process, and in a text file
+// ($FPP_TUNE_CACHE, else $HOME/.cache/flare_pp_gb300/tiles.txt; one line
+// "key ks threads" per shape) so that later processes skip the timing.
+static std::string kuf_tune_path() {
+  if (const char *p = std::getenv("FPP_TUNE_CACHE")) return p;
+  if (const char *h = std::getenv("HOME")) return std::string(h) + "/.cache/flare_pp_gb300/tiles.txt";
+  return std::string();
+}
+
+static std::string kuf_tune_key(const B2Args &a) {
+  int dev = 0;
+  cudaDeviceProp prop;
+  std::string name = "gpu";
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess)
+    name = prop.name;
+  for (char &ch : name)
+    if (ch == ' ') ch = '_';
+  return "kuf_adjoint:" + name + ":ns" + std::to_string(a.n_species) + ":N" +
+         std::to_string(a.N) + ":l" + std::to_string(a.lmax);
+}
+
+int kuf_tiles(fpp_model *m, const KufArgs &ka, int n_items, cudaStream_t st, int *ks,
+              int *threads) {
+  (void)m;
+  static std::mutex mu;
+  static std::map<std::string, std::pair<int, int>> memo;
+  const std::string key = kuf_tune_key(ka.a);
+  std::lock_guard<std::mutex> lock(mu);
+  auto hit = memo.find(key);
+  if (hit == memo.end()) {
+    const std::string path = kuf_tune_path();
+    if (!path.empty()) {
+      std::ifstream in(path);
+      std::string k2;
+      int a2, b2;
+      while (in >> k2 >> a2 >> b2)
+        if (k2 == key && kuf_adjoint_smem(ka.a, a2, b2) > 0) memo[key] = {a2, b2};
+    }
+    hit = memo.find(key);
+  }
+  if (hit != memo.end()) {
+    *ks = hit->second.first;
+    *threads = hit->second.second;
+    return FPP_OK;
+  }
+  const int sample = std::min(n_items, 2048);
+  cudaEvent_t e0, e1;
+  FPP_CUDA(cudaEventCreate(&e0));
+  FPP_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bks = 0, bth = 0;
+  for (int t : {128, 256})
+    for (int c : {2, 4, 8, 16}) {
+      if (kuf_adjoint_smem(ka.a, c, t) == 0) continue;
+      // once to warm, once timed
+      if (launch_kuf_adjoint(ka, c, t, sample, 0, st) != 0) continue;
+      FPP_CUDA(cudaEventRecord(e0, st));
+      if (launch_kuf_adjoint(ka, c, t, sample, 0, st) != 0) continue;
+      FPP_CUDA(cudaEventRecord(e1, st));
+      FPP_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      FPP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        bks = c;
+        bth = t;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (bks == 0) return fail(FPP_ERR_UNSUPPORTED, "no Kuf tile shape fits in shared memory");
+  memo[key] = {bks, bth};
+  const std::string path = kuf_tune_path();
+  if (!path.empty()) {
+    const size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) {
+      // best effort: create the directory chain
+      std::string dir = path.substr(0, slash), cur;
+      size_t pos = 0;
+      while ((pos = dir.find('/', pos + 1)) != std::string::npos) {
+        cur = dir.substr(0, pos);
+        mkdir(cur.c_str(), 0755);
+      }
+      mkdir(dir.c_str(), 0755);
+    }
+    std::ofstream out(path, std::ios::app);
+    if (out) out << key << " " << bks << " " << bth << "\n";
+  }
+  *ks = bks;
+  *threads = bth;
   return FPP_OK;
 }
 
@@ -574,18 +676,18 @@ static int set_center(fpp_model *m, const std::vector<std::vector<double>> &pbar
   FPP_TRY(m->g32.reserve(sizeof(float) * gv.size()));
   FPP_CUDA(cudaMemcpy(m->pbar32.ptr, pb.data(), sizeof(float) * pb.size(), cudaMemcpyHostToDevice));
   FPP_CUDA(cudaMemcpy(m->g32.ptr, gv.data(), sizeof(float) * gv.size(), cudaMemcpyHostToDevice));
-  m->needs_center = false;
   return FPP_OK;
 }
 
-// pbar from the sparse set: the normalised mean of its unit descriptors.
+// pbar from the sparse set: the normalised mean of its unit descriptors (a
+// species without sparse environments keeps a zero centre).  The mixed form
+// replaces it, species by species, with the mean of the first structure it
+// evaluates that contains the species.
 static int center_from_sparse(fpp_model *m) {
   const int nd = m->n_d;
   std::vector<std::vector<double>> pbar(m->n_species, std::vector<double>(nd, 0.0));
-  bool all = true;
   for (int s = 0; s < m->n_species; s++) {
     auto &sp = m->sp[s];
-    if (sp.n_sparse == 0) all = false;
     for (int k = 0; k < sp.n_sparse; k++) {
       if (sp.norms[k] < 1e-8) continue;
       for (int d = 0; d < nd; d++) pbar[s][d] += sp.desc[(size_t)k * nd + d] / sp.norms[k];
@@ -597,13 +699,28 @@ static int center_from_sparse(fpp_model *m) {
       for (double &v : pbar[s]) v /= n;
   }
   FPP_TRY(set_center(m, pbar));
-  m->needs_center = !all;  // species without sparse environments: calibrate later
+  m->centred.assign(m->n_species, 0);
   return FPP_OK;
 }
 
+// Column sums of the FP64 normalised descriptor rows of one species block:
+// thread per column, rows split over blockIdx.y, fixed-order partial sums
+// per (column, row chunk) combined on the host in chunk order.
+__global__ void k_column_sums(const double *__restrict__ rows, int n_rows, int ldp, int nd,
+                              int chunk, double *__restrict__ partial) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd) return;
+  const int r0 = blockIdx.y * chunk;
+  const int r1 = min(n_rows, r0 + chunk);
+  double acc = 0;
+  for (int r = r0; r < r1; r++) acc += rows[(size_t)r * ldp + d];
+  partial[(size_t)blockIdx.y * nd + d] = acc;
+}
+
 // pbar from a structure: the normalised mean of its atoms' unit descriptors
-// (FP64 forward pass), for species the sparse set does not cover, or (with
-// every_species) for every species that has atoms in the structure.
+// (FP64 forward pass, column sums on the device), for the species with atoms
+// in s that are not yet centred on a structure, or (with every_species) for
+// every species with atoms in s.
 static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st,
                                  bool every_species = false) {
   StructureState &S = s->st;
@@ -612,30 +729,39 @@ static int center_from_structure(fpp_model *m, fpp_structure *s, cudaStream_t st
   a.noa = S.noa;
   a.strict = 0;
   FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
-  FPP_CUDA(cudaStreamSynchronize(st));
+  if ((int)m->centred.size() != m->n_species) m->centred.assign(m->n_species, 0);
   std::vector<std::vector<double>> pbar(m->n_species, std::vector<double>(nd, 0.0));
   std::vector<float> old((size_t)m->n_species * nd, 0.f);
   if (m->pbar32.ptr)
     FPP_CUDA(cudaMemcpy(old.data(), m->pbar32.ptr, sizeof(float) * old.size(),
                         cudaMemcpyDeviceToHost));
+  constexpr int kChunks = 64;
+  DevBuf partial;
+  FPP_TRY(partial.reserve(sizeof(double) * (size_t)kChunks * nd));
+  std::vector<double> host((size_t)kChunks * nd);
   for (int sp = 0; sp < m->n_species; sp++) {
-    double n0 = 0;
+    for (int d = 0; d < nd; d++) pbar[sp][d] = old[(size_t)sp * nd + d];
+    if (s->n_rows[sp] == 0 || (m->centred[sp] && !every_species)) continue;
+    const int chunk = ceil_div(s->n_rows[sp], kChunks);
+    const int nchunks = ceil_div(s->n_rows[sp], chunk);
+    k_column_sums<<<dim3(ceil_div(nd, 128), nchunks), 128, 0, st>>>(
+        S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp, s->n_rows[sp], ldp, nd, chunk,
+        partial.as<double>());
+    FPP_CUDA(cudaGetLastError());
+    FPP_CUDA(cudaMemcpyAsync(host.data(), partial.ptr, sizeof(double) * (size_t)nchunks * nd,
+                             cudaMemcpyDeviceToHost, st));
+    FPP_CUDA(cudaStreamSynchronize(st));
     for (int d = 0; d < nd; d++) {
-      pbar[sp][d] = old[(size_t)sp * nd + d];
-      n0 += pbar[sp][d] * pbar[sp][d];
+      double v = 0;
+      for (int c = 0; c < nchunks; c++) v += host[(size_t)c * nd + d];
+      pbar[sp][d] = v;
     }
-    if (s->n_rows[sp] == 0 || (n0 > 0 && !every_species)) continue;
-    for (int d = 0; d < nd; d++) pbar[sp][d] = 0.0;
-    std::vector<double> rows((size_t)s->n_rows[sp] * ldp);
-    FPP_CUDA(cudaMemcpy(rows.data(), S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp,
-                        sizeof(double) * rows.size(), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < s->n_rows[sp]; i++)
-      for (int d = 0; d < nd; d++) pbar[sp][d] += rows[(size_t)i * ldp + d];
     double n = 0;
     for (double v : pbar[sp]) n += v * v;
     n = std::sqrt(n);
     if (n > 0)
       for (double &v : pbar[sp]) v /= n;
+    m->centred[sp] = 1;
   }
   return set_center(m, pbar);
 }
@@ -695,7 +821,13 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
                                   S.u.as<double>(), S.n_pairs, S.nbr_i.as<int>(), st) != 0)
       return fail(FPP_ERR_CUDA, "adjoint (FP64) launch failed");
   } else {
-    if (m->needs_center) FPP_TRY(center_from_structure(m, s, st));
+    // centre every species of s that is not yet centred on a structure
+    FPP_TRY(ensure_layout(s, a.n_species, st));
+    if ((int)m->centred.size() != m->n_species) m->centred.assign(m->n_species, 0);
+    bool recentre = false;
+    for (int sp = 0; sp < m->n_species; sp++)
+      if (s->n_rows[sp] > 0 && !m->centred[sp]) recentre = true;
+    if (recentre) FPP_TRY(center_from_structure(m, s, st));
     FPP_TRY(forward32(s, a, m->pair_tab.as<int>(), m->pbar32.as<float>(), st));
     S.mark(3, st);
     if (m->beta_power == 2) {
@@ -882,16 +1014,12 @@ __global__ void k_copy_cols(int rows, int ncols, const double *__restrict__ src,
 }
 }  // namespace fpp
 
-extern "C" {
-
-int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures, int32_t n_structures,
-                    const int32_t *label_mask, const int32_t *atom_offsets,
-                    const int32_t *atoms, double *kuf, int64_t n_labels, void *stream) {
-  if (!m || (n_structures > 0 && (!structures || !label_mask)) || !kuf)
-    return fail(FPP_ERR_INVALID, "null argument");
-  if (n_structures < 0 || n_labels < 0) return fail(FPP_ERR_INVALID, "negative count");
-  cudaStream_t st = (cudaStream_t)stream;
-  // label columns of each structure: [E] [F of the listed atoms] [S]
+// B3 models: envs_struc of each structure through its stored descriptor
+// derivatives (the reference's route), copied column by column into Kuf.
+static int kuf_stored_derivatives(fpp_model *m, fpp_structure *const *structures,
+                                  int32_t n_structures, const int32_t *label_mask,
+                                  const int32_t *atom_offsets, const int32_t *atoms,
+                                  double *kuf, int64_t n_labels, cudaStream_t st) {
   std::vector<std::vector<int>> cols(n_structures);
   int64_t total = 0;
   for (int k = 0; k < n_structures; k++) {
@@ -941,6 +1069,137 @@ int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures, int32_t n_st
   if (nst && n_labels)
     FPP_CUDA(cudaMemcpy(kuf, dK.ptr, sizeof(double) * (size_t)nst * n_labels,
                         cudaMemcpyDeviceToHost));
+  return FPP_OK;
+}
+
+extern "C" {
+
+int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures, int32_t n_structures,
+                    const int32_t *label_mask, const int32_t *atom_offsets,
+                    const int32_t *atoms, double *kuf, int64_t n_labels, void *stream) {
+  if (!m || (n_structures > 0 && (!structures || !label_mask)) || !kuf)
+    return fail(FPP_ERR_INVALID, "null argument");
+  if (n_structures < 0 || n_labels < 0) return fail(FPP_ERR_INVALID, "negative count");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (m->args.kind != kB2)
+    return kuf_stored_derivatives(m, structures, n_structures, label_mask, atom_offsets,
+                                  atoms, kuf, n_labels, st);
+  // label columns of each structure, stacked: [E] [F of the listed atoms] [S]
+  std::vector<KufStruc> hs(n_structures);
+  std::vector<int> fcol_off(n_structures + 1, 0);
+  for (int k = 0; k < n_structures; k++) {
+    if (!structures[k]) return fail(FPP_ERR_INVALID, "null structure");
+    fcol_off[k + 1] = fcol_off[k] + structures[k]->st.noa;
+  }
+  std::vector<int> fcol(std::max(fcol_off[n_structures], 1), -1);
+  int64_t col = 0;
+  for (int k = 0; k < n_structures; k++) {
+    fpp_structure *s = structures[k];
+    const int noa = s->st.noa;
+    KufStruc &q = hs[k];
+    q.col_e = (label_mask[k] & 1) ? col++ : -1;
+    if (label_mask[k] & 2) {
+      const int b = atom_offsets ? atom_offsets[k] : 0;
+      const int e = atom_offsets ? atom_offsets[k + 1] : noa;
+      for (int t = b; t < e; t++) {
+        const int a = atom_offsets ? atoms[t] : t;
+        if (a < 0 || a >= noa) return fail(FPP_ERR_INVALID, "force atom index out of range");
+        fcol[fcol_off[k] + a] = (int)col;
+        col += 3;
+      }
+    }
+    q.col_s = (label_mask[k] & 4) ? col : -1;
+    if (label_mask[k] & 4) col += 6;
+  }
+  if (col != n_labels)
+    return fail(FPP_ERR_INVALID, "n_labels (" + std::to_string(n_labels) +
+                                     ") differs from the labels of the structures (" +
+                                     std::to_string(col) + ")");
+  const int nst = m->n_sparse_total;
+  if (nst == 0 || n_labels == 0) {
+    std::fill(kuf, kuf + (size_t)nst * n_labels, 0.0);
+    return FPP_OK;
+  }
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  // FP64 descriptors of every structure, queued without synchronization
+  // (each structure keeps its own workspace), and the work list
+  DevBuf dK, dfcol, dstruc, ditems;
+  FPP_TRY(dK.reserve(sizeof(double) * (size_t)nst * n_labels));
+  FPP_CUDA(cudaMemsetAsync(dK.ptr, 0, sizeof(double) * (size_t)nst * n_labels, st));
+  FPP_TRY(dfcol.reserve(sizeof(int) * fcol.size()));
+  FPP_CUDA(cudaMemcpyAsync(dfcol.ptr, fcol.data(), sizeof(int) * fcol.size(),
+                           cudaMemcpyHostToDevice, st));
+  std::vector<int2> items;
+  for (int k = 0; k < n_structures; k++) {
+    fpp_structure *s = structures[k];
+    FPP_TRY(model_check(m, s));
+    if (!(label_mask[k] & 7)) continue;
+    StructureState &S = s->st;
+    B2Args a = m->args;
+    a.noa = S.noa;
+    FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+    KufStruc &q = hs[k];
+    q.c64 = S.c64.as<double>();
+    q.phat64 = S.phat64.as<double>();
+    q.norm64 = S.norm64.as<double>();
+    q.row_of_atom = s->row_of_atom.as<int>();
+    q.species = S.species.as<int>();
+    q.offset = S.nbr_offset.as<int>();
+    q.nbr_j = S.nbr_j.as<int>();
+    q.nbr_s = S.nbr_s.as<int>();
+    q.rel = S.nbr_rel.as<dvec4>();
+    q.force_col = dfcol.as<int>() + fcol_off[k];
+    q.vol_inv = 1.0 / S.ci.volume;
+    for (int i = 0; i < S.noa; i++) items.push_back(make_int2(k, i));
+  }
+  if (items.empty()) {
+    FPP_CUDA(cudaMemcpy(kuf, dK.ptr, sizeof(double) * (size_t)nst * n_labels,
+                        cudaMemcpyDeviceToHost));
+    return FPP_OK;
+  }
+  FPP_TRY(dstruc.reserve(sizeof(KufStruc) * hs.size()));
+  FPP_CUDA(cudaMemcpyAsync(dstruc.ptr, hs.data(), sizeof(KufStruc) * hs.size(),
+                           cudaMemcpyHostToDevice, st));
+  FPP_TRY(ditems.reserve(sizeof(int2) * items.size()));
+  FPP_CUDA(cudaMemcpyAsync(ditems.ptr, items.data(), sizeof(int2) * items.size(),
+                           cudaMemcpyHostToDevice, st));
+  KufArgs ka;
+  std::memset(&ka, 0, sizeof(ka));
+  ka.a = m->args;
+  ka.strucs = dstruc.as<KufStruc>();
+  ka.items = ditems.as<int2>();
+  ka.n_items = (int)items.size();
+  for (int s = 0; s < m->n_species; s++) {
+    ka.sp[s].dhat = m->sp[s].d_dhat.as<double>();
+    ka.sp[s].norms = m->sp[s].d_norms.as<double>();
+    ka.sp[s].n_sparse = m->sp[s].n_sparse;
+    ka.sp[s].row0 = m->sp[s].sparse_offset;
+  }
+  ka.pair_tab = m->pair_tab.as<int>();
+  ka.sig2 = m->sigma * m->sigma;
+  ka.power = m->power;
+  ka.ldp = round_up(m->n_d, 64);
+  ka.kuf = dK.as<double>();
+  ka.n_labels = n_labels;
+  // tile shape: the cached choice for this device and descriptor, else the
+  // autotuner's (timed on a prefix of the work list, then Kuf is cleared)
+  int ks = 0, threads = 0;
+  FPP_TRY(kuf_tiles(m, ka, (int)items.size(), st, &ks, &threads));
+  FPP_CUDA(cudaMemsetAsync(dK.ptr, 0, sizeof(double) * (size_t)nst * n_labels, st));
+  if (launch_kuf_adjoint(ka, ks, threads, (int)items.size(), 0, st) != 0)
+    return fail(FPP_ERR_CUDA, "Kuf (adjoint) launch failed");
+  m->kuf_ks = ks;
+  m->kuf_threads = threads;
+  FPP_CUDA(cudaMemcpyAsync(kuf, dK.ptr, sizeof(double) * (size_t)nst * n_labels,
+                           cudaMemcpyDeviceToHost, st));
+  FPP_CUDA(cudaStreamSynchronize(st));
+  return FPP_OK;
+}
+
+int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads) {
+  if (!m || !ks || !threads) return fail(FPP_ERR_INVALID, "null argument");
+  *ks = m->kuf_ks;
+  *threads = m->kuf_threads;
   return FPP_OK;
 }
 
@@ -1040,6 +1299,144 @@ int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
       const int row = s->row_off[sp] + r;
       variances[out++] = (hn[row] >= 1e-8 ? sig2 : 0.0) - hq[row];
     }
+  return FPP_OK;
+}
+
+int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energy,
+                                   double *energy_variance, double *local_variances,
+                                   void *stream) {
+  FPP_TRY(model_check(m, s));
+  if (!energy && !energy_variance && !local_variances)
+    return fail(FPP_ERR_INVALID, "no output requested");
+  if (energy_variance && !m->has_R_inv)
+    return fail(FPP_ERR_INVALID, "R_inv not set (fpp_model_set_R_inv)");
+  if (local_variances && !m->has_L_inv)
+    return fail(FPP_ERR_INVALID, "L_inv not set (fpp_model_set_L_inv)");
+  cudaStream_t st = (cudaStream_t)stream;
+  StructureState &S = s->st;
+  const int noa = S.noa, nd = m->n_d, ldp = round_up(nd, 64), n = m->n_sparse_total;
+  if (noa == 0) {
+    if (energy) *energy = 0;
+    if (energy_variance) *energy_variance = 0;
+    return FPP_OK;
+  }
+  FPP_TRY(upload_pair_tab(m->pair_tab, m->pair_tab_host, st));
+  B2Args a = m->args;
+  a.noa = noa;
+  FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
+  const int R = s->total_rows;
+  cublasHandle_t h;
+  FPP_TRY(get_cublas(m, st, &h));
+  const double one = 1.0, zero = 0.0;
+  DevBuf rown, K, kE, ones, al, y, Q, q;
+  FPP_TRY(rown.reserve(sizeof(double) * std::max(1, R)));
+  FPP_CUDA(cudaMemsetAsync(rown.ptr, 0, sizeof(double) * R, st));
+  if (launch_gather_rows(noa, s->row_of_atom.as<int>(), S.norm64.as<double>(),
+                         rown.as<double>(), st) != 0)
+    return fail(FPP_ERR_CUDA, "gather launch failed");
+  // per species block: K_s[c][k] = k(atom c, sparse k) (column-major S_s x
+  // n_rows_s, at the block's row offset times S_s); only the energy column of
+  // the kernel matrix is needed, so no force or stress columns are formed
+  std::vector<size_t> koff(m->n_species + 1, 0);
+  for (int sp = 0; sp < m->n_species; sp++)
+    koff[sp + 1] = koff[sp] + (size_t)m->sp[sp].n_sparse * std::max(s->n_rows[sp], 0);
+  FPP_TRY(K.reserve(sizeof(double) * std::max<size_t>(1, koff[m->n_species])));
+  FPP_TRY(kE.reserve(sizeof(double) * std::max(1, n)));
+  FPP_CUDA(cudaMemsetAsync(kE.ptr, 0, sizeof(double) * std::max(1, n), st));
+  int max_rows = 1;
+  for (int sp = 0; sp < m->n_species; sp++) max_rows = std::max(max_rows, s->n_rows[sp]);
+  FPP_TRY(ones.reserve(sizeof(double) * max_rows));
+  {
+    std::vector<double> o(max_rows, 1.0);
+    FPP_CUDA(cudaMemcpyAsync(ones.ptr, o.data(), sizeof(double) * max_rows,
+                             cudaMemcpyHostToDevice, st));
+    FPP_CUDA(cudaStreamSynchronize(st));
+  }
+  for (int sp = 0; sp < m->n_species; sp++) {
+    const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
+    if (Ss == 0 || nsa == 0) continue;
+    double *C = K.as<double>() + koff[sp];
+    const double *Ph = S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp;
+    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one,
+                           m->sp[sp].d_dhat.as<double>(), nd, Ph, ldp, &zero, C, Ss));
+    if (launch_envs_block(nsa, Ss, C, Ss, rown.as<double>() + s->row_off[sp],
+                          m->sp[sp].d_norms.as<double>(), m->sigma * m->sigma, m->power, C,
+                          Ss, st) != 0)
+      return fail(FPP_ERR_CUDA, "kernel block launch failed");
+    // k_E = sum over the species' atoms of k(atom, sparse)
+    FPP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, Ss, nsa, &one, C, Ss, ones.as<double>(), 1, &zero,
+                           kE.as<double>() + m->sp[sp].sparse_offset, 1));
+  }
+  double e_mean = 0, e_var = 0;
+  if (energy) {
+    std::vector<double> h_al(std::max(n, 1), 0.0);
+    for (auto &x : m->sp)
+      for (int k = 0; k < x.n_sparse; k++) h_al[x.sparse_offset + k] = x.alpha[k];
+    FPP_TRY(al.reserve(sizeof(double) * h_al.size()));
+    FPP_CUDA(cudaMemcpyAsync(al.ptr, h_al.data(), sizeof(double) * h_al.size(),
+                             cudaMemcpyHostToDevice, st));
+    FPP_CUBLAS(cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST));
+    FPP_CUBLAS(cublasDdot(h, n, kE.as<double>(), 1, al.as<double>(), 1, &e_mean));
+  }
+  if (energy_variance) {
+    // variance_efs[0] = |R_inv^T k_E|^2 (R_inv row-major: column-major R_inv^T)
+    FPP_TRY(y.reserve(sizeof(double) * std::max(1, n)));
+    FPP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, n, n, &one, m->R_inv.as<double>(), n,
+                           kE.as<double>(), 1, &zero, y.as<double>(), 1));
+    FPP_CUBLAS(cublasDdot(h, n, y.as<double>(), 1, y.as<double>(), 1, &e_var));
+  }
+  if (local_variances) {
+    // q_c = |L_inv k_c|^2, species block by species block when L_inv is
+    // block diagonal, else against the whole L_inv
+    FPP_TRY(q.reserve(sizeof(double) * std::max(1, R)));
+    FPP_CUDA(cudaMemsetAsync(q.ptr, 0, sizeof(double) * std::max(1, R), st));
+    if (m->L_inv_species_blocks) {
+      FPP_TRY(Q.reserve(sizeof(double) * std::max<size_t>(1, koff[m->n_species])));
+      for (int sp = 0; sp < m->n_species; sp++) {
+        const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp], off = m->sp[sp].sparse_offset;
+        if (Ss == 0 || nsa == 0) continue;
+        const double *Lb = m->L_inv.as<double>() + (size_t)off * n + off;
+        FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, Ss, &one, Lb, n,
+                               K.as<double>() + koff[sp], Ss, &zero, Q.as<double>() + koff[sp],
+                               Ss));
+        if (launch_row_sq(nsa, Ss, Q.as<double>() + koff[sp], Ss,
+                          q.as<double>() + s->row_off[sp], st) != 0)
+          return fail(FPP_ERR_CUDA, "row-norm launch failed");
+      }
+    } else {
+      DevBuf Kf;
+      FPP_TRY(Kf.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
+      FPP_CUDA(cudaMemsetAsync(Kf.ptr, 0, sizeof(double) * (size_t)R * n, st));
+      for (int sp = 0; sp < m->n_species; sp++) {
+        const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
+        if (Ss == 0 || nsa == 0) continue;
+        FPP_CUDA(cudaMemcpy2DAsync(Kf.as<double>() + (size_t)s->row_off[sp] * n +
+                                       m->sp[sp].sparse_offset,
+                                   sizeof(double) * n, K.as<double>() + koff[sp],
+                                   sizeof(double) * Ss, sizeof(double) * Ss, nsa,
+                                   cudaMemcpyDeviceToDevice, st));
+      }
+      FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
+      FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, n, R, n, &one, m->L_inv.as<double>(),
+                             n, Kf.as<double>(), n, &zero, Q.as<double>(), n));
+      if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
+        return fail(FPP_ERR_CUDA, "row-norm launch failed");
+    }
+    std::vector<double> hq(R), hn(R);
+    FPP_CUDA(cudaStreamSynchronize(st));
+    FPP_CUDA(cudaMemcpy(hq.data(), q.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
+    FPP_CUDA(cudaMemcpy(hn.data(), rown.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
+    const double sig2 = m->sigma * m->sigma;
+    std::vector<int> cnt(m->n_species, 0);
+    for (int i = 0; i < noa; i++) {
+      const int sp = S.species_host[i];
+      const int row = s->row_off[sp] + cnt[sp]++;
+      local_variances[i] = (hn[row] >= 1e-8 ? sig2 : 0.0) - hq[row];
+    }
+  }
+  FPP_CUDA(cudaStreamSynchronize(st));
+  if (energy) *energy = e_mean;
+  if (energy_variance) *energy_variance = e_var;
   return FPP_OK;
 }
 

@@ -57,10 +57,12 @@ struct fpp_model {
   std::vector<Species> sp;
   int beta_power = 0;                   // 0: no mapped coefficients yet
   // centre of the mixed-precision operand (per species): pbar, beta pbar,
-  // pbar^T beta pbar; calibrated on the first structure when no sparse set
+  // pbar^T beta pbar; per species, whether pbar is already the mean of a
+  // structure's environments (the mixed form centres each species on the
+  // first structure it evaluates that contains the species)
   fpp::DevBuf pbar32, g32;
   std::vector<double> c0;
-  bool needs_center = true;
+  std::vector<char> centred;
   fpp::DevBuf beta1;                    // double[n_species * n_d] (power 1)
   int n_sparse_total = 0;
   fpp::DevBuf R_inv;                    // double[n * n]
@@ -69,13 +71,21 @@ struct fpp_model {
   // triangle) and the variance map (per species n_d x n_d, row-major)
   fpp::DevBuf L_inv;
   bool has_L_inv = false;
+  bool L_inv_species_blocks = false;    // L_inv is zero across species blocks
   fpp::DevBuf varmap;
   bool has_varmap = false;
   fpp_lammps_ws *lammps = nullptr;      // LAMMPS-array workspace
+  double max_memory = 0;                // pair style's device-memory cap (0: none)
+  int kuf_ks = 0, kuf_threads = 0;      // tile shape of the last batched Kuf
+  int last_pair_batches = 0;            // atom batches of the last pair compute
   void *cublas = nullptr;               // cublasHandle_t
 };
 
 namespace fpp {
+// constant-memory tables of the descriptor kernels (harmonic normalisations,
+// B3 couplings), uploaded once per device before the first kernel that reads
+// them
+int ensure_tables(cudaStream_t stream);
 int prepare_structure(fpp_structure *s, cudaStream_t stream);
 int ensure_layout(fpp_structure *s, int n_species, cudaStream_t stream);
 int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
@@ -92,4 +102,8 @@ int upload_pair_tab(DevBuf &buf, const std::vector<int> &tab, cudaStream_t st);
 // when want_p.
 int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want_p,
               cudaStream_t st);
+// tile shape of the batched Kuf kernel (autotuned, cached per device and
+// descriptor shape)
+int kuf_tiles(fpp_model *m, const KufArgs &ka, int n_items, cudaStream_t st, int *ks,
+              int *threads);
 }  // namespace fpp

@@ -98,6 +98,21 @@ int fpp_model_set_L_inv(fpp_model *m, int32_t n, const double *L_inv) {
     FPP_CUDA(cudaMemcpy(m->L_inv.ptr, L_inv, sizeof(double) * (size_t)n * n,
                         cudaMemcpyHostToDevice));
   m->has_L_inv = true;
+  // Kuu of one NormalizedDotProduct kernel is zero between species, so its
+  // Cholesky factor and that factor's inverse are block diagonal; the
+  // uncertainty products then run species block by species block
+  bool blocks = true;
+  for (int a = 0; a < m->n_species && blocks; a++) {
+    const auto &sa = m->sp[a];
+    for (int i = sa.sparse_offset; i < sa.sparse_offset + sa.n_sparse && blocks; i++)
+      for (int j = 0; j < n; j++)
+        if ((j < sa.sparse_offset || j >= sa.sparse_offset + sa.n_sparse) &&
+            L_inv[(size_t)i * n + j] != 0.0) {
+          blocks = false;
+          break;
+        }
+  }
+  m->L_inv_species_blocks = blocks;
   return FPP_OK;
 }
 

@@ -168,25 +168,29 @@ def fit_site_energy_model(b2, frames, n_sparse_per_species, sigma=2.0, power=2,
     kern = NormalizedDotProduct(sigma, power)
     Kuu = kern.envs_envs(sparse, sparse)
     Kuf = kern.envs_envs(sparse, train)
-    alpha, _, _ = update_matrices_QR(Kuu, Kuf, y, np.full(len(y), 1 / noise ** 2))
-    return dict(sparse=sparse, alpha=alpha, sigma=sigma, power=power,
-                n_train=train.n_clusters)
+    alpha, R_inv, L_inv = update_matrices_QR(Kuu, Kuf, y, np.full(len(y), 1 / noise ** 2))
+    return dict(sparse=sparse, alpha=alpha, R_inv=R_inv, L_inv=L_inv, sigma=sigma,
+                power=power, n_train=train.n_clusters)
 
 
-def bcc_alloy_32k_model(seed=303, n_sparse=2000, device="cuda"):
+def bcc_alloy_32k_recipe(seed=303, n_sparse=2000, reps=(32, 32, 16)):
     """The 32,768-atom two-species BCC workload (32x32x16 cells, a=3.0 A,
-    rattle 0.08 A, rc 5.5 A, chebyshev N=12, lmax=4, quadratic cutoff) and a
-    model with n_sparse environments per species drawn from four
-    16x8x8-cell frames of the same alloy (seeds seed+1..seed+4)."""
-    from .api import B2, NormalizedDotProduct, SparseGP
-    b2 = B2("chebyshev", "quadratic", [0.0, 5.5], [], [2, 12, 4])
+    rattle 0.08 A, rc 5.5 A, chebyshev N=12, lmax=4, quadratic cutoff) and
+    the recipe of its model: n_sparse environments per species drawn from
+    four 16x8x8-cell frames of the same alloy (seeds seed+1..seed+4), weights
+    fitted to Lennard-Jones site energies (sigma 2, power 2).  numpy only.
+    reps sets the evaluated frame's cells (the same model for any size)."""
     frames = [bcc_alloy((16, 8, 8), seed + k) for k in range(1, 5)]
-    fit = fit_site_energy_model(b2, frames, n_sparse, sigma=2.0, power=2, seed=seed,
-                                device=device)
-    gp = SparseGP([NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
-    gp.set_model(b2, fit["sparse"], fit["alpha"])
-    cell, sp, pos = bcc_alloy((32, 32, 16), seed)
-    return dict(b2=b2, gp=gp, cell=cell, species=sp, positions=pos, fit=fit)
+    cell, sp, pos = bcc_alloy(tuple(reps), seed)
+    return dict(kind="B2", descriptor=("chebyshev", "quadratic", [0.0, 5.5], [], [2, 12, 4]),
+                frames=frames, n_sparse=n_sparse, seed=seed, sigma=2.0, power=2,
+                cell=cell, species=sp, positions=pos)
+
+
+def bcc_alloy_16k_recipe(seed=303, n_sparse=2000):
+    """The 32k workload's model on a 16,384-atom frame (32x16x16 cells): the
+    small case for hardware-counter captures of the same kernels."""
+    return bcc_alloy_32k_recipe(seed, n_sparse, reps=(32, 16, 16))
 
 
 def fcc_al(reps, seed, rattle=0.05, a=4.05):
@@ -195,18 +199,37 @@ def fcc_al(reps, seed, rattle=0.05, a=4.05):
     return rattled(FCC_BASIS, a, reps, rattle, rng)
 
 
-def fcc_al_b3_1m_model(seed=505, n_sparse=500, reps=(64, 64, 64), device="cuda"):
+def fcc_al_b3_1m_recipe(seed=505, n_sparse=500, reps=(64, 64, 64)):
     """The B3 workload: FCC Al, a = 4.05 A, 64^3 conventional cells
     (1,048,576 atoms), rattle 0.05 A, rc 5.0 A, chebyshev N=6, lmax=3,
     quadratic cutoff, with n_sparse environments drawn from four 6x6x6-cell
     frames (seeds seed+1..seed+4) and weights fitted to Lennard-Jones site
-    energies."""
-    from .api import B3, NormalizedDotProduct, SparseGP
-    b3 = B3("chebyshev", "quadratic", [0.0, 5.0], [], [1, 6, 3])
+    energies.  numpy only."""
     frames = [fcc_al((6, 6, 6), seed + k) for k in range(1, 5)]
-    fit = fit_site_energy_model(b3, frames, n_sparse, sigma=2.0, power=2, seed=seed,
-                                device=device)
-    gp = SparseGP([NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
-    gp.set_model(b3, fit["sparse"], fit["alpha"])
     cell, sp, pos = fcc_al(reps, seed)
-    return dict(b2=b3, gp=gp, cell=cell, species=sp, positions=pos, fit=fit)
+    return dict(kind="B3", descriptor=("chebyshev", "quadratic", [0.0, 5.0], [], [1, 6, 3]),
+                frames=frames, n_sparse=n_sparse, seed=seed, sigma=2.0, power=2,
+                cell=cell, species=sp, positions=pos)
+
+
+def model_from_recipe(r, device="cuda"):
+    """The GPU model of a workload recipe (descriptors, kernels and the QR
+    solve in the library, FP64)."""
+    from .api import B2, B3, NormalizedDotProduct, SparseGP
+    desc = (B3 if r["kind"] == "B3" else B2)(*r["descriptor"])
+    fit = fit_site_energy_model(desc, r["frames"], r["n_sparse"], sigma=r["sigma"],
+                                power=r["power"], seed=r["seed"], device=device)
+    gp = SparseGP([NormalizedDotProduct(r["sigma"], r["power"])], 0.001, 0.05, 0.006)
+    gp.set_model(desc, fit["sparse"], fit["alpha"], fit["R_inv"], fit["L_inv"])
+    return dict(b2=desc, gp=gp, cell=r["cell"], species=r["species"],
+                positions=r["positions"], fit=fit)
+
+
+def bcc_alloy_32k_model(seed=303, n_sparse=2000, device="cuda"):
+    """bcc_alloy_32k_recipe with its model built in the library."""
+    return model_from_recipe(bcc_alloy_32k_recipe(seed, n_sparse), device)
+
+
+def fcc_al_b3_1m_model(seed=505, n_sparse=500, reps=(64, 64, 64), device="cuda"):
+    """fcc_al_b3_1m_recipe with its model built in the library."""
+    return model_from_recipe(fcc_al_b3_1m_recipe(seed, n_sparse, reps), device)

@@ -239,19 +239,44 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs,
 int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
                             int32_t n, double *variances, void *stream);
 
+/* The energy of SparseGP::predict_SOR (sparse_gp.cpp:630-649) at MD sizes:
+ * energy = k_E . alpha and energy_variance = |R_inv^T k_E|^2, the first
+ * entries of mean_efs and variance_efs, with k_E[k] = sum over atoms i of
+ * k(sparse k, atom i); and, with local_variances != NULL, the per-atom
+ * variances of SparseGP::compute_cluster_uncertainties (sparse_gp.cpp:
+ * 93-133), k(i, i) - |L_inv k(sparse, i)|^2, in structure atom order.  Only
+ * the energy column of the kernel matrix is formed (no force or stress
+ * columns), FP64 on the GPU; when L_inv is zero across species blocks (one
+ * NormalizedDotProduct kernel) the L_inv products run block by block.
+ * Requires fpp_model_set_R_inv for energy_variance and fpp_model_set_L_inv
+ * for local_variances.  Outputs are host pointers; NULL skips one. */
+int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energy,
+                                   double *energy_variance, double *local_variances,
+                                   void *stream);
+
 /* SparseGP::update_Kuf / stack_Kuf for a batch of training structures
  * (sparse_gp.cpp:392-462, 464-552, 565-574): the sparse-environment columns
  * of each structure's labels, [E] [F of the listed atoms] [S], stacked in
  * structure order into kuf (host, n_sparse_total x n_labels, row-major),
- * FP64 on the GPU with one device-resident Kuf and one copy out.
+ * FP64 on the GPU.  The columns are the envs_struc values of
+ * normalized_dot_product.cpp:115-210, formed by the adjoint route (no
+ * stored descriptor derivatives): one persistent launch over the (structure,
+ * atom) work list of the whole batch, no synchronization per structure; the
+ * kernel's tile shape (sparse environments per pass, threads per block) is
+ * autotuned once per device and descriptor shape and cached in the file
+ * $FPP_TUNE_CACHE (else $HOME/.cache/flare_pp_gb300/tiles.txt).  Additions
+ * into other atoms' columns are FP64 atomics, so results vary between runs
+ * at the level of FP64 rounding.  B2 models only.
  * label_mask[k]: bit 0 energy, bit 1 forces, bit 2 stress of structure k;
  * atom_offsets (n_structures + 1) and atoms list the force atoms of each
  * structure (the reference's atom_indices; NULL: every atom).  n_labels must
  * equal the total label count (FPP_ERR_INVALID otherwise). */
 int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures,
                     int32_t n_structures, const int32_t *label_mask,
-                    const int32_t *atom_offsets, const int32_t *atoms, double *kuf,
-                    int64_t n_labels, void *stream);
+                    const int32_t *atom_offsets, const int32_t *atoms,
+                    double *kuf, int64_t n_labels, void *stream);
+/* The tile shape the last fpp_kuf_batched call on m used. */
+int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads);
 
 /* NormalizedDotProduct::struc_struc (normalized_dot_product.cpp:212-444):
  * the full energy/force/stress covariance of two structures, FP64, from the
@@ -284,8 +309,13 @@ int fpp_self_kernel_struc(const fpp_b2 *descriptor, double sigma, double power,
  * c0 = pbar.g in FP64).  The tensor cores accumulate beta delta in FP32 with
  * truncation, so the energy error grows with |delta| |beta delta|: it is
  * smallest when pbar is the mean environment of the structures predicted.
- * The centre defaults to the mean of the sparse set (or, for species without
- * sparse environments, of the first structure predicted). */
+ * So each species is centred on the first structure the mixed form evaluates
+ * that contains it (the normalised mean of that structure's unit descriptors,
+ * from an FP64 forward pass; a one-time cost that synchronizes the stream);
+ * later structures reuse that centre.  fpp_model_compute_beta /
+ * fpp_model_set_beta reset it; fpp_model_center_on sets it explicitly.
+ * The centre is a numerical device: results equal the FP64 form's to within
+ * the mixed form's error whatever it is. */
 int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
                        double *energy, double *forces, double *stress,
                        double *atom_energies, int outputs_on_device,
@@ -294,7 +324,7 @@ int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
 /* Recentre the mixed form on a structure: pbar of every species with atoms in
  * s becomes the normalised mean of their unit descriptors (FP64 forward pass,
  * synchronizes the stream).  Deterministic: later predictions depend only on
- * the model and the structure it was centred on.  No reference counterpart
+ * the model and the structures it was centred on.  No reference counterpart
  * (pair_flare.cpp evaluates in FP64 throughout). */
 int fpp_model_center_on(fpp_model *m, fpp_structure *s, void *stream);
 
@@ -330,10 +360,20 @@ int fpp_pair_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                      const int32_t *neighbors, int precision, double *f,
                      double *eng_vdwl, double *virial, double *eatom,
                      void *stream);
+/* Device-memory cap of the pair style (the MAXMEM of the Kokkos pair style,
+ * pair_flare_kokkos.cpp:145-177 and :741): fpp_pair_compute then evaluates
+ * the listed atoms in batches sized so that the mapped coefficients and the
+ * per-atom buffers fit in `bytes` (the batches' sizes differ by at most one
+ * atom, the first ones the larger); FPP_ERR_CAPACITY ("Not enough memory for
+ * even a single atom!") if one atom does not fit.  0 (the default): one
+ * batch.  fpp_model_pair_batches reports the batch count of the last call. */
+int fpp_model_set_max_memory(fpp_model *m, double bytes);
+int fpp_model_pair_batches(const fpp_model *m, int32_t *n_batches);
 
 /* ------------------------------------------------------------------------
  * Training side: the log marginal likelihood and its hyperparameter gradient
- * for one NormalizedDotProduct kernel, FP64 on the GPU.
+ * for one NormalizedDotProduct kernel (and, below, for several), FP64 on the
+ * GPU.
  * SparseGP::compute_likelihood_stable (sparse_gp.cpp:704-732) and, with
  * want_gradient, compute_likelihood_gradient_stable (sparse_gp.cpp:734-862).
  * Host inputs: Kuf n x m (row-major), Kuu n x n (the kernel matrix without
@@ -354,6 +394,19 @@ int fpp_likelihood_gradient_stable(int32_t n, int32_t m, const double *Kuf,
                                    const double *R_inv_diag, const double *hyps,
                                    int32_t want_gradient, double *out, double *KnK,
                                    void *stream);
+/* The same for a SparseGP with several NormalizedDotProduct kernels
+ * (sparse_gp.h:48-49): kernel i owns rows [kernel_offsets[i],
+ * kernel_offsets[i+1]) of Kuu (block diagonal) and Kuf, n_kernels <= 8;
+ * hyps = sigma_0 .. sigma_{n_kernels-1}, sigma_e, sigma_f, sigma_s (the
+ * order of SparseGP::set_hyperparameters, sparse_gp.cpp:1105-1140); out has
+ * 4 + n_kernels + 3 entries: the four likelihood terms, then d/d hyps in
+ * the same order. */
+int fpp_likelihood_gradient_stable_kernels(
+    int32_t n, int32_t m, const double *Kuf, const double *Kuu, const double *y,
+    const int32_t *label_kind, const double *alpha, const double *Sigma,
+    const double *L_diag, const double *R_inv_diag, int32_t n_kernels,
+    const int32_t *kernel_offsets, const double *hyps, int32_t want_gradient, double *out,
+    double *KnK, void *stream);
 
 /* ------------------------------------------------------------------------
  * ComputeFlareStdAtom (lammps_plugins/compute_flare_std_atom.cpp): the

@@ -477,6 +477,84 @@ int oracle_beta_form(int noa, const double *cell, const int *species, const doub
 }
 
 /*
+ * B2 descriptors of every atom (the values of B2::compute_struc,
+ * src/flare_pp/descriptors/b2.cpp:181-242 and :244-399, without the stored
+ * derivatives), in atom order: p (noa x n_d, the n1 <= n2, l order of
+ * b2.cpp:205-218) and |p|.  Same neighbors, filter and bases as
+ * oracle_beta_form.  Returns 0, -1 (allocation) or -2 (more than 4096
+ * neighbors).
+ */
+int oracle_b2_descriptors(int noa, const double *cell, const int *species, const double *pos,
+                          int n_species, int N, int lmax, double r1, const double *cutoffs,
+                          int n_threads, double *p_out, double *norms) {
+  init_tables();
+  double cmax = 0;
+  for (int k = 0; k < n_species * n_species; k++)
+    if (cutoffs[k] > cmax) cmax = cutoffs[k];
+  Geo G;
+  if (geo_init(&G, noa, cell, pos, cmax)) return -1;
+  const int H = (lmax + 1) * (lmax + 1), nr = n_species * N, sb = nr * H;
+  const int L1 = lmax + 1, nd = nr * (nr + 1) / 2 * L1;
+  const int cap = 4096;
+  int err = 0;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel
+  {
+    int *js = (int *)malloc(sizeof(int) * cap);
+    double *rel = (double *)malloc(sizeof(double) * 4 * cap);
+    double *b = (double *)malloc(sizeof(double) * (2 * N + 4 * H));
+    double *c = (double *)malloc(sizeof(double) * sb);
+    int lerr = (!js || !rel || !b || !c) ? -1 : 0;
+#pragma omp for schedule(dynamic, 16)
+    for (int i = 0; i < noa; i++) {
+      if (lerr) continue;
+      int si = species[i];
+      int nn = neighbors_of(&G, i, cap, js, rel);
+      if (nn > cap) {
+        lerr = -2;
+        continue;
+      }
+      memset(c, 0, sizeof(double) * sb);
+      for (int q = 0; q < nn; q++) {
+        int sj = species[js[q]];
+        double rc = cutoffs[si * n_species + sj];
+        double r = rel[4 * q + 3];
+        if (!(r <= rc)) continue;
+        radial(r, r1, rc, N, b, b + N);
+        harmonics(rel[4 * q], rel[4 * q + 1], rel[4 * q + 2], lmax, b + 2 * N, b + 2 * N + H);
+        for (int n = 0; n < N; n++)
+          for (int lm = 0; lm < H; lm++) c[(sj * N + n) * H + lm] += b[n] * b[2 * N + lm];
+      }
+      double *p = p_out + (size_t)i * nd;
+      int d = 0;
+      double nsq = 0;
+      for (int n1 = 0; n1 < nr; n1++)
+        for (int n2 = n1; n2 < nr; n2++)
+          for (int l = 0; l < L1; l++, d++) {
+            double v = 0;
+            for (int m = 0; m < 2 * l + 1; m++)
+              v += c[n1 * H + l * l + m] * c[n2 * H + l * l + m];
+            p[d] = v;
+            nsq += v * v;
+          }
+      norms[i] = sqrt(nsq);
+    }
+#pragma omp critical
+    {
+      if (lerr) err = lerr;
+    }
+    free(js);
+    free(rel);
+    free(b);
+    free(c);
+  }
+  geo_free(&G);
+  return err;
+}
+
+/*
  * B3 (src/flare_pp/descriptors/b3.cpp:134-382) in the same per-atom form:
  * complex single bond from the real one (c[l,+m] = (-1)^m (R + iS)/sqrt2,
  * c[l,-m] = (R - iS)/sqrt2 with R = c_real[l,m], S = c_real[l,-m]), the

@@ -20,6 +20,8 @@ def lib():
         _lib.oracle_b3_beta_form.restype = ctypes.c_int
         _lib.oracle_b3_beta_form.argtypes = [ci, vp, vp, vp, ci, ci, ci, cd, cd, vp, ci,
                                              vp, ci, ci, vp, vp, vp, vp]
+        _lib.oracle_b2_descriptors.restype = ctypes.c_int
+        _lib.oracle_b2_descriptors.argtypes = [ci, vp, vp, vp, ci, ci, ci, cd, vp, ci, vp, vp]
         _lib.oracle_max_threads.restype = ctypes.c_int
     return _lib
 
@@ -55,6 +57,26 @@ def beta_form(cell, species, positions, settings, beta, power=2, atoms=None,
     if rc != 0:
         raise RuntimeError(f"oracle_beta_form failed ({rc})")
     return dict(energy=e.value, forces=F, stress=S, atom_energies=ae)
+
+
+def b2_descriptors(cell, species, positions, settings, n_threads=0):
+    """B2 descriptors p (noa x n_d) and norms of every atom, FP64."""
+    from .b2 import n_descriptors
+    cell = np.ascontiguousarray(cell, dtype=np.float64)
+    sp = np.ascontiguousarray(species, dtype=np.int32)
+    pos = np.ascontiguousarray(positions, dtype=np.float64)
+    cut = np.ascontiguousarray(settings["cutoffs"], dtype=np.float64)
+    ns, N, lmax = settings["n_species"], settings["N"], settings["lmax"]
+    noa = len(sp)
+    p = np.zeros((noa, n_descriptors(ns, N, lmax)))
+    nrm = np.zeros(noa)
+    P = lambda a: a.ctypes.data
+    rc = lib().oracle_b2_descriptors(noa, P(cell), P(sp), P(pos), ns, N, lmax,
+                                     ctypes.c_double(settings["r1"]), P(cut), n_threads,
+                                     P(p), P(nrm))
+    if rc != 0:
+        raise RuntimeError(f"oracle_b2_descriptors failed ({rc})")
+    return p, nrm
 
 
 def max_threads():

@@ -147,22 +147,31 @@ class SparseGP:
     # ---- likelihood (sparse_gp.cpp:704-992, 1105-1140) -------------------
     @property
     def hyperparameters(self):
-        return np.array([self.kernels[0].sigma, self.energy_noise, self.force_noise,
-                         self.stress_noise])
+        return np.array([k.sigma for k in self.kernels]
+                        + [self.energy_noise, self.force_noise, self.stress_noise])
+
+    def _kernel_blocks(self):
+        """Row ranges of each kernel's sparse set in Kuu and Kuf."""
+        out, o = [], 0
+        for sd in self.sparse_descriptors:
+            out.append((o, o + sd.n_clusters))
+            o += sd.n_clusters
+        return out
 
     def set_hyperparameters(self, hyps):
-        """sparse_gp.cpp:1105-1140 for one NormalizedDotProduct kernel: Kuu and
-        Kuf rescaled by (sigma_new / sigma)^2 (Kuu_grad / Kuf_grad [0],
-        normalized_dot_product.cpp:581-615), the noise vector rebuilt, and
-        the QR solve repeated."""
-        k = self.kernels[0]
-        scale = hyps[0] * hyps[0] / k.sig2
-        self.Kuu_mat = self.Kuu_mat * scale
-        self.Kuf_mat = self.Kuf_mat * scale
-        k.sigma = float(hyps[0])
-        k.sig2 = k.sigma * k.sigma
-        k.kernel_hyperparameters = np.array([k.sigma])
-        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[1:4])
+        """sparse_gp.cpp:1105-1140 for NormalizedDotProduct kernels: each
+        kernel's Kuu block and Kuf rows rescaled by (sigma_new / sigma)^2
+        (Kuu_grad / Kuf_grad [0], normalized_dot_product.cpp:581-615), the
+        noise vector rebuilt, and the QR solve repeated."""
+        nk = len(self.kernels)
+        for k, (a, b), h in zip(self.kernels, self._kernel_blocks(), hyps[:nk]):
+            scale = h * h / k.sig2
+            self.Kuu_mat[a:b, a:b] *= scale
+            self.Kuf_mat[a:b, :] *= scale
+            k.sigma = float(h)
+            k.sig2 = k.sigma * k.sigma
+            k.kernel_hyperparameters = np.array([k.sigma])
+        self.energy_noise, self.force_noise, self.stress_noise = (float(v) for v in hyps[nk:nk + 3])
         one = [self.label_kind == t for t in range(3)]
         self.noise_vector = (one[0] / self.energy_noise ** 2 + one[1] / self.force_noise ** 2
                              + one[2] / self.stress_noise ** 2)
@@ -196,12 +205,12 @@ class SparseGP:
         return self.log_marginal_likelihood
 
     def compute_likelihood_gradient_stable(self):
-        """sparse_gp.cpp:734-862 (the form without precomputed KnK) for one
-        NormalizedDotProduct kernel: dKuu/dsigma = 2 Kuu / sigma and
-        dKuf/dsigma = 2 Kuf / sigma (normalized_dot_product.cpp:581-615).
-        Sets likelihood_gradient (sigma, sigma_e, sigma_f, sigma_s) and
-        returns the log marginal likelihood."""
-        sig = self.kernels[0].sigma
+        """sparse_gp.cpp:734-862 (the form without precomputed KnK) for
+        NormalizedDotProduct kernels: dKuu/dsigma = 2 Kuu / sigma and
+        dKuf/dsigma = 2 Kuf / sigma (normalized_dot_product.cpp:581-615),
+        each kernel's gradient masked to its own block of Kuu and rows of
+        Kuf (:775-829).  Sets likelihood_gradient (sigma per kernel, sigma_e,
+        sigma_f, sigma_s) and returns the log marginal likelihood."""
         Kuf, Kuu, S, a, y = self.Kuf_mat, self.Kuu_mat, self.Sigma, self.alpha, self.y
         nv = self.noise_vector
         r = y - Kuf.T @ a
@@ -215,21 +224,28 @@ class SparseGP:
         self.complexity_penalty = 0.5 * (noise_det + kuu_inv_det + sigma_inv_det)
         self.log_marginal_likelihood = (self.complexity_penalty + self.data_fit
                                         + self.constant_term)
-        grad = np.zeros(4)
-        Kuu_grad = Kuu * (2 / sig)
-        Kuf_grad = Kuf * (2 / sig)
-        dKnK = Kuf_grad @ (nv[:, None] * Kuf.T)
-        Pi = dKnK + dKnK.T + Kuu_grad
-        cg = 0.5 * np.trace(np.linalg.inv(Kuu) @ Kuu_grad) - 0.5 * np.trace(Pi @ S)
-        dK_alpha = Kuf_grad.T @ a
-        dg = dK_alpha @ (nv * r) - 0.5 * a @ Kuu_grad @ a
-        grad[0] = cg + dg
+        nk = len(self.kernels)
+        grad = np.zeros(nk + 3)
+        for i, (k, (a0, a1)) in enumerate(zip(self.kernels, self._kernel_blocks())):
+            sig = k.sigma
+            Kuu_grad = np.zeros_like(Kuu)
+            Kuu_grad[a0:a1, a0:a1] = Kuu[a0:a1, a0:a1] * (2 / sig)
+            Kuf_grad = np.zeros_like(Kuf)
+            Kuf_grad[a0:a1] = Kuf[a0:a1] * (2 / sig)
+            dKnK = Kuf_grad @ (nv[:, None] * Kuf.T)
+            Pi = dKnK + dKnK.T + Kuu_grad
+            Kuu_i = Kuu[a0:a1, a0:a1]
+            cg = (0.5 * np.trace(np.linalg.inv(Kuu_i) @ Kuu_grad[a0:a1, a0:a1])
+                  - 0.5 * np.trace(Pi @ S))
+            dK_alpha = Kuf_grad.T @ a
+            dg = dK_alpha @ (nv * r) - 0.5 * a @ Kuu_grad @ a
+            grad[i] = cg + dg
         for t in range(3):
             KnK = Kuf @ (one[t][:, None] * Kuf.T)
             s3 = noises[t] ** 3
             cg = -one[t].sum() / noises[t] + np.trace(KnK @ S) / s3
             dg = (r @ (one[t] * r)) / s3
-            grad[1 + t] = cg + dg
+            grad[nk + t] = cg + dg
         self.likelihood_gradient = grad
         return self.log_marginal_likelihood
 

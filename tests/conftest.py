@@ -10,6 +10,10 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # the Kuf autotuner's cache stays inside the test session
+    import tempfile
+    os.environ.setdefault("FPP_TUNE_CACHE",
+                          os.path.join(tempfile.mkdtemp(prefix="fpp_tune_"), "tiles.txt"))
 
 
 @pytest.fixture(scope="session")

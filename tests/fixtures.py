@@ -219,6 +219,49 @@ KERNEL_STRUCS = ("two_species_20", "bcc54")
 KERNEL_HYPS = [(1.7, 1.0), (1.7, 2.0)]
 
 
+def build_pair_harness(out_dir):
+    """Compile tests/cpp/pair_harness.cpp with the C++ pair-style core
+    (flare_pp_gb300/lammps/pair_flare_gb300.cpp), linked against
+    libflare_pp_gb300.so.  Returns the executable's path."""
+    import os
+    import subprocess
+    from flare_pp_gb300 import build
+    lib = build.build()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(lib)
+    exe = os.path.join(str(out_dir), "pair_harness")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror",
+                    "-I", os.path.join(root, "include"),
+                    "-I", os.path.join(root, "flare_pp_gb300", "lammps"),
+                    os.path.join(root, "tests", "cpp", "pair_harness.cpp"),
+                    os.path.join(root, "flare_pp_gb300", "lammps", "pair_flare_gb300.cpp"),
+                    "-L", libdir, "-lflare_pp_gb300", f"-Wl,-rpath,{libdir}", "-o", exe],
+                   check=True)
+    return exe
+
+
+def write_case(fn, x, types, ilist, numneigh, nbrs):
+    """A LAMMPS-shaped case file for the pair harness (local atoms first,
+    numneigh and the neighbor lists in ilist order = atom order)."""
+    nlocal = len(numneigh)
+    with open(fn, "w") as f:
+        f.write(f"{nlocal} {len(x) - nlocal} {len(ilist)}\n")
+        for r in x:
+            f.write(f"{r[0]:.17g} {r[1]:.17g} {r[2]:.17g}\n")
+        f.write(" ".join(str(int(t)) for t in types) + "\n")
+        f.write(" ".join(str(int(i)) for i in ilist) + "\n")
+        f.write(" ".join(str(int(n)) for n in numneigh) + "\n")
+        f.write(" ".join(str(int(j)) for j in nbrs) + "\n")
+
+
+def read_harness_output(fn, nall):
+    with open(fn) as f:
+        e = float(f.readline().split()[0])
+        vir = np.array([float(v) for v in f.readline().split()])
+        rows = np.array([[float(v) for v in f.readline().split()] for _ in range(nall)])
+    return e, vir, rows[:, :3], rows[:, 3]
+
+
 def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
     """Two-species sparse set (10 environments per species of a 54-atom BCC
     alloy frame, per-pair cutoffs) and the inverse Cholesky factor of its
@@ -245,18 +288,25 @@ def std_atom_model(power, sigma=1.5, seed=606, n_per_species=10):
                 settings=settings(2, 4, 2, rc, cut))
 
 
-def likelihood_model(seed=808, sigma=2.0, noises=(1.0, 2.0, 3.0), power=2):
+def likelihood_model(seed=808, sigma=2.0, noises=(1.0, 2.0, 3.0), power=2,
+                     second_kernel=None):
     """Two-species model for the likelihood tests: three 16-atom BCC alloy
     frames (a = 3.6 A) rattled by 0.2 A (E, F, S labels from Lennard-Jones;
     the second frame labels the forces of three atoms only) and 5 sparse
-    environments per frame, so that Kuu is well conditioned."""
+    environments per frame, so that Kuu is well conditioned.  second_kernel
+    = (sigma, [N, lmax]) adds a second NormalizedDotProduct kernel over a
+    second B2 descriptor."""
     rc = 4.0
     b2 = OB2("chebyshev", "quadratic", [0, rc], [], [2, 4, 2])
-    gp = OSGP([ONDP(sigma, power)], *noises)
+    kernels, descs = [ONDP(sigma, power)], [b2]
+    if second_kernel is not None:
+        kernels.append(ONDP(second_kernel[0], power))
+        descs.append(OB2("chebyshev", "quadratic", [0, rc], [], [2] + list(second_kernel[1])))
+    gp = OSGP(kernels, *noises)
     frames = []
     for k in range(3):
         cell, sp, pos = synth.bcc_alloy((2, 2, 2), seed + k, sigma=0.2, a=3.6)
-        s = OStructure(cell, sp, pos, rc, [b2])
+        s = OStructure(cell, sp, pos, rc, descs)
         e, f, st, _ = synth.lennard_jones(cell, pos)
         s.energy = np.array([e])
         s.forces = f.reshape(-1)

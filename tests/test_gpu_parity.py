@@ -202,6 +202,57 @@ def test_mapped_config2_mixed_gates(gpu_lib, c2):
     assert err_f < F_GATE
 
 
+@pytest.fixture(scope="module")
+def c3s():
+    """The shape of the 32k-atom workload at 2000 atoms: two-species BCC
+    alloy (10 x 10 x 10 cells, a = 3.0 A, 0.08 A rattle), chebyshev N = 12,
+    lmax = 4, rc = 5.5 A, 600 sparse environments per species fitted to
+    Lennard-Jones site energies.  These settings run the library's compiled
+    N = 12, lmax = 4, two-species kernels (the headline's).  The reference
+    values come from the C oracle (oracle/c/flare_oracle.c), whose pair-style
+    math is pinned to the reference's lammps_descriptor.cpp."""
+    from oracle import cfast
+    rc = 5.5
+    ob = OB2("chebyshev", "quadratic", [0, rc], [], [2, 12, 4])
+    ob.store_dervs = False
+    frames = [synth.bcc_alloy((8, 8, 8), 303 + 10 * k) for k in range(1, 3)]
+    fit = fixtures.site_energy_model(ob, frames, 600, sigma=2.0, power=2)
+    ggp, gb2 = fixtures.to_gpu_model((2, 12, 4, rc), fit["sparse"], fit["alpha"], 2.0, 2)
+    cell, sp, pos = synth.bcc_alloy((10, 10, 10), 303)
+    st = fixtures.settings(2, 12, 4, rc)
+    beta = ONDP(2.0, 2).compute_map_coeff_pow2(fit["sparse"], fit["alpha"])
+    B = opred.unpack_beta(beta, ob_n(ob))
+    ref = cfast.beta_form(cell, sp, pos, st, B)
+    gs = fg.Structure(cell, sp, pos, rc)
+    return dict(ggp=ggp, gs=gs, ref=ref, noa=len(sp), cell=cell, sp=sp, pos=pos)
+
+
+def test_mapped_headline_shape_fp64_vs_oracle(gpu_lib, c3s):
+    e, f, s, ae = c3s["ggp"].predict_mapped(c3s["gs"], "fp64", atom_energies=True)
+    ref = c3s["ref"]
+    assert abs(e - ref["energy"]) < 1e-9 * np.abs(ref["atom_energies"]).sum()
+    np.testing.assert_allclose(ae, ref["atom_energies"], rtol=0,
+                               atol=1e-9 * np.abs(ref["atom_energies"]).max())
+    np.testing.assert_allclose(f, ref["forces"], rtol=0, atol=1e-9 * np.abs(ref["forces"]).max())
+    np.testing.assert_allclose(s, ref["stress"], rtol=0, atol=1e-9 * np.abs(ref["stress"]).max())
+
+
+def test_mapped_headline_shape_mixed_gates_vs_oracle(gpu_lib, c3s):
+    """Mixed form (FP32 descriptors, split-fp16 tcgen05 contraction) within the
+    gates against the FP64 oracle: 1e-6 eV/atom, 1e-4 eV/A."""
+    e, f, s, ae = c3s["ggp"].predict_mapped(c3s["gs"], "mixed", atom_energies=True)
+    ref = c3s["ref"]
+    n = c3s["noa"]
+    err_e = abs(e - ref["energy"]) / n
+    err_f = np.abs(f - ref["forces"]).max()
+    err_s = np.abs(s - ref["stress"]).max()
+    print(f"mixed N=12 lmax=4 at 2000 atoms: energy err/atom {err_e:.3e}, max force err "
+          f"{err_f:.3e}, stress err {err_s:.3e}")
+    assert err_e < E_GATE
+    assert err_f < F_GATE
+    assert err_s < 1e-5
+
+
 def test_pair_compute_matches_mapped(gpu_lib, c1, tmp_path):
     from flare_pp_gb300.potential import write_potential
     m, ggp = c1["m"], c1["ggp"]
@@ -305,3 +356,71 @@ def test_training_solve_matches_oracle(gpu_lib):
     np.testing.assert_allclose(gs.mean_efs, os_.mean_efs, rtol=0, atol=1e-6)
     np.testing.assert_allclose(gs.variance_efs[1:], os_.variance_efs[1:], rtol=1e-4,
                                atol=1e-8)
+
+
+def test_cpp_pair_style_core_matches_oracle(gpu_lib, c3s, tmp_path):
+    """The C++ pair-style core (flare_pp_gb300/lammps/pair_flare_gb300.cpp),
+    linked with -lflare_pp_gb300 and driven by a LAMMPS-shaped harness
+    (double** x / f, 1-based types, full neighbor list with ghost atoms),
+    against the FP64 oracle: FP64 to 1e-9, mixed within the gates."""
+    from flare_pp_gb300.potential import write_potential
+    exe = fixtures.build_pair_harness(tmp_path)
+    ggp = c3s["ggp"]
+    ggp._ensure_mapped()
+    pot = tmp_path / "alloy.txt"
+    write_potential(pot, ggp.mapping_coefficients, 2, 2, 12, 4, np.full((2, 2), 5.5))
+    gs = c3s["gs"]
+    cell, sp, pos = c3s["cell"], c3s["sp"], c3s["pos"]
+    x, t, il, nn, nb, owner = fixtures.lammps_arrays(cell, sp, pos, 5.5)
+    case = tmp_path / "case.txt"
+    fixtures.write_case(case, x, t, il, nn, nb)
+    ref = c3s["ref"]
+    V = abs(np.linalg.det(cell))
+    n = gs.noa
+    for prec in ("fp64", "mixed"):
+        out = tmp_path / f"out_{prec}.txt"
+        import subprocess
+        subprocess.run([exe, str(pot), str(case), str(out), prec], check=True)
+        e, vir, f, ea = fixtures.read_harness_output(out, len(x))
+        F = np.zeros((n, 3))
+        np.add.at(F, owner, f)
+        st = ref["stress"]
+        vir_ref = V * st[[0, 3, 5, 1, 2, 4]]
+        if prec == "fp64":
+            assert abs(e - ref["energy"]) < 1e-9 * np.abs(ref["atom_energies"]).sum()
+            np.testing.assert_allclose(F, ref["forces"], rtol=0,
+                                       atol=1e-9 * np.abs(ref["forces"]).max())
+            np.testing.assert_allclose(vir, vir_ref, rtol=0, atol=1e-9 * np.abs(vir_ref).max())
+        else:
+            assert abs(e - ref["energy"]) / n < E_GATE
+            assert np.abs(F - ref["forces"]).max() < F_GATE
+        assert abs(ea[:n].sum() - e) < 1e-9 * max(1.0, abs(e))
+
+
+def test_pair_compute_memory_batches(gpu_lib, c3s, tmp_path):
+    """Under a device-memory cap (the Kokkos pair style's MAXMEM) the pair
+    style evaluates the atoms in batches; the results equal the one-batch
+    call (up to the order of the force scatter's additions)."""
+    from flare_pp_gb300.potential import write_potential
+    ggp = c3s["ggp"]
+    ggp._ensure_mapped()
+    pot = tmp_path / "alloy.txt"
+    write_potential(pot, ggp.mapping_coefficients, 2, 2, 12, 4, np.full((2, 2), 5.5))
+    pair = fg.PairFLARE(str(pot))
+    x, t, il, nn, nb, owner = fixtures.lammps_arrays(c3s["cell"], c3s["sp"], c3s["pos"], 5.5)
+    beta_mem = 2 * 1500 * 1500 * 8.0
+    for prec in ("fp64", "mixed"):
+        pair.set_max_memory(0)
+        f1, e1, v1, a1 = pair.compute(x, t, il, nn, nb, precision=prec, eatom=True)
+        assert pair.last_batches == 1
+        pair.set_max_memory(beta_mem + 25e6)
+        f2, e2, v2, a2 = pair.compute(x, t, il, nn, nb, precision=prec, eatom=True)
+        assert pair.last_batches >= 2
+        assert abs(e2 - e1) <= 1e-12 * np.abs(a1).sum()
+        np.testing.assert_allclose(a2, a1, rtol=0, atol=1e-12 * np.abs(a1).max())
+        np.testing.assert_allclose(f2, f1, rtol=0, atol=1e-11 * np.abs(f1).max())
+        np.testing.assert_allclose(v2, v1, rtol=0, atol=1e-11 * np.abs(v1).max())
+    pair.set_max_memory(1.0)
+    from flare_pp_gb300._lib import FlareGpuError
+    with pytest.raises(FlareGpuError):
+        pair.compute(x, t, il, nn, nb, precision="fp64")

@@ -176,12 +176,14 @@ def test_batched_kuf_full_size(gpu_lib):
     """The batched-Kuf workload at full size: 256 strained (+-3 %), rattled
     (0.1 A) two-species FCC cells of 32-512 atoms (69,380 atoms, 209,932 E/F/S
     labels), N = 8, lmax = 3, rc 5.0, 1000 sparse environments.  Kuf is
-    assembled in one device-resident pass and the QR solve runs on the GPU.
-    Checked (a) column by column against the oracle's envs_struc
-    (normalized_dot_product.cpp:115-210) for the three smallest structures,
-    with the same sparse set, and (b) through the normal equations of the
-    solve, (Kuu + jitter I + Kuf Lambda Kuf^T) alpha = Kuf Lambda y, which hold
-    whatever the size."""
+    assembled by one persistent adjoint launch over all structures' atoms
+    (autotuned tiles) and the QR solve runs on the GPU.  Checked (a) column
+    by column against the oracle's envs_struc (normalized_dot_product.cpp:
+    115-210) for six structures (the three smallest and three drawn at
+    random), with the same sparse set, (b) through the normal equations of
+    the solve, (Kuu + jitter I + Kuf Lambda Kuf^T) alpha = Kuf Lambda y, and
+    (c) alpha against the oracle's QR solve (sparse_gp.cpp:576-610, numpy /
+    scipy on the host) of the same Kuu, Kuf, y and noise."""
     from flare_pp_gb300 import synth
     from oracle.b2 import ClusterDescriptor as OCD
     rc = 5.0
@@ -203,7 +205,12 @@ def test_batched_kuf_full_size(gpu_lib):
         atoms = sorted(allc[p][1] for p in pick if allc[p][0] == k)
         if atoms:
             gp.add_specific_environments(strucs[k], atoms)
+    import time
+    t0 = time.perf_counter()
     gp.update_matrices_QR()
+    print(f"full-size training (Kuu, Kuf of 256 structures, GPU QR): "
+          f"{time.perf_counter() - t0:.2f} s, Kuf tiles {gp.kuf_tiles()}")
+    assert all(v > 0 for v in gp.kuf_tiles())
     n_lab = sum(1 + 3 * len(sp) + 6 for _, sp, _ in cells)
     assert gp.Kuf.shape == (1000, n_lab) and len(gp.y) == n_lab
     # (a) three structures against the oracle, same sparse set
@@ -217,7 +224,9 @@ def test_batched_kuf_full_size(gpu_lib):
     osd.n_clusters = sd.n_clusters
     ob = OB2("chebyshev", "quadratic", [0, rc], [], [2, 8, 3])
     offs = np.concatenate([[0], np.cumsum([1 + 3 * len(sp) + 6 for _, sp, _ in cells])])
-    for k in np.argsort([len(sp) for _, sp, _ in cells], kind="stable")[:3]:
+    pick6 = list(np.argsort([len(sp) for _, sp, _ in cells], kind="stable")[:3])
+    pick6 += list(np.random.default_rng(7).choice(256, 3, replace=False))
+    for k in pick6:
         cell, sp, pos = cells[k]
         os_ = OStructure(cell, sp, pos, rc, [ob])
         ref = ONDP(2.0, 2).envs_struc(osd, os_.descriptors[0])
@@ -229,3 +238,12 @@ def test_batched_kuf_full_size(gpu_lib):
     Aa = gp.Kuu @ a + gp.Kuu_jitter * a + gp.Kuf @ (nv * (gp.Kuf.T @ a))
     a_norm = np.sum(nv * np.einsum("ij,ij->j", gp.Kuf, gp.Kuf)) + np.linalg.norm(gp.Kuu)
     assert np.linalg.norm(Aa - b) <= 1e-10 * a_norm * np.linalg.norm(a)
+    # (c) alpha against the oracle's QR solve of the same system
+    import scipy.linalg as sla
+    n = gp.Kuu.shape[0]
+    L = np.linalg.cholesky(gp.Kuu + gp.Kuu_jitter * np.eye(n))
+    sq = np.sqrt(nv)
+    A = np.vstack([sq[:, None] * gp.Kuf.T, L.T])
+    Q, R = np.linalg.qr(A, mode="reduced")
+    a_ref = sla.solve_triangular(R, Q.T @ np.concatenate([sq * gp.y, np.zeros(n)]))
+    np.testing.assert_allclose(gp.alpha, a_ref, rtol=0, atol=1e-6 * np.abs(a_ref).max())

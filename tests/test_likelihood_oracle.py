@@ -42,3 +42,25 @@ def test_gradient_matches_finite_differences(lm):
         fd = (vals[0] - vals[1]) / (2 * pert)
         assert abs(fd - g[i]) < 1e-5 * abs(g[i]) + 1e-4, (i, fd, g[i])
     gp.set_hyperparameters(h)
+
+
+def test_two_kernel_gradient_matches_finite_differences():
+    """Two kernels (sparse_gp.cpp:775-829 masks each kernel's gradient to its
+    own Kuu block and Kuf rows): all five components against central
+    differences."""
+    gp = fixtures.likelihood_model(second_kernel=(1.5, [3, 3]))["gp"]
+    h = gp.hyperparameters.copy()
+    assert len(h) == 5
+    gp.compute_likelihood_gradient_stable()
+    g = gp.likelihood_gradient.copy()
+    pert = 1e-6
+    for i in range(5):
+        vals = []
+        for sgn in (1, -1):
+            hh = h.copy()
+            hh[i] += sgn * pert
+            gp.set_hyperparameters(hh)
+            vals.append(gp.compute_likelihood_stable())
+        fd = (vals[0] - vals[1]) / (2 * pert)
+        assert abs(fd - g[i]) < 1e-5 * abs(g[i]) + 1e-4, (i, fd, g[i])
+    gp.set_hyperparameters(h)
