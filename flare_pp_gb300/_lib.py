@@ -48,6 +48,7 @@ SIGNATURES = {
     "fpp_b2_pair_count": (_c_int, [_vp, _vp, _P(_i64), _vp]),
     "fpp_b2_compute": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fpp_b2_descriptors_noalloc": (_c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fpp_dgemm_nt": (_c_int, [_i32, _i32, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _vp]),
     "fpp_model_create": (_c_int, [_vp, _dbl, _dbl, _P(_vp)]),
     "fpp_model_destroy": (_c_int, [_vp]),
     "fpp_model_set_sparse": (_c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
@@ -72,7 +73,7 @@ SIGNATURES = {
     "fpp_likelihood_gradient_stable": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp,
                                                 _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "fpp_model_set_max_memory": (_c_int, [_vp, _dbl]),
-    "fpp_model_kuf_tiles": (_c_int, [_vp, _P(_i32), _P(_i32)]),
+    "fpp_model_kuf_tiles": (_c_int, [_vp, _P(_i32), _P(_i32), _P(ctypes.c_float), _P(_i64)]),
     "fpp_model_pair_batches": (_c_int, [_vp, _P(_i32)]),
     "fpp_likelihood_gradient_stable_kernels": (_c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp,
                                                         _vp, _vp, _vp, _i32, _vp, _vp, _i32,

@@ -608,10 +608,18 @@ class SparseGP:
     def kuf_tiles(self, kernel_index=0):
         """(sparse environments per pass, threads per block) of the batched
         Kuf launch of the last update_matrices_QR (the autotuned shape)."""
-        ks, th = _lib.ctypes.c_int32(), _lib.ctypes.c_int32()
-        check(lib().fpp_model_kuf_tiles(self._kuf_models[kernel_index].handle,
-                                        _lib.ctypes.byref(ks), _lib.ctypes.byref(th)))
-        return ks.value, th.value
+        return self.kuf_launch(kernel_index)[:2]
+
+    def kuf_launch(self, kernel_index=0):
+        """(sparse environments per pass, threads per block, kernel ms, work
+        items) of the batched Kuf launch of the last update_matrices_QR: the
+        autotuned tile shape, the CUDA-event time of the Kuf kernel alone and
+        its (structure, atom) work items."""
+        C = _lib.ctypes
+        ks, th, ms, n = C.c_int32(), C.c_int32(), C.c_float(), C.c_int64()
+        check(lib().fpp_model_kuf_tiles(self._kuf_models[kernel_index].handle, C.byref(ks),
+                                        C.byref(th), C.byref(ms), C.byref(n)))
+        return ks.value, th.value, ms.value, n.value
 
     def update_matrices_QR(self):
         """sparse_gp.cpp:576-610: Kuu (block diagonal over the kernels), Kuf

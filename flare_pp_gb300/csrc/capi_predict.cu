@@ -938,9 +938,6 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
   }
   std::vector<int> local(noa, 0), cnt(m->n_species, 0);
   for (int i = 0; i < noa; i++) local[i] = cnt[S.species_host[i]]++;
-  cublasHandle_t h;
-  FPP_TRY(get_cublas(m, st, &h));
-  const double one = 1.0, zero = 0.0;
   for (int sp = 0; sp < m->n_species; sp++) {
     const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
     if (Ss == 0) continue;
@@ -960,9 +957,8 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
     FPP_TRY(d_ndm.reserve(sizeof(double) * (size_t)Ss * nsa));
     const double *Dh = m->sp[sp].d_dhat.as<double>();
     const double *Ph = phat + (size_t)s->row_off[sp] * ldp;
-    // ndm[k][i] = dhat_k . phat_i  (row-major S x n_s)
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, nsa, Ss, nd, &one, Ph, ldp, Dh, nd,
-                           &zero, d_ndm.as<double>(), nsa));
+    // ndm[k][i] = dhat_k . phat_i  (row-major S x n_s), tensor cores, FP64-accurate
+    FPP_TRY(ozaki_dgemm_nt(Ss, nsa, nd, Dh, nd, Ph, ldp, d_ndm.as<double>(), nsa, m->oz, st));
     const double *anorm = rown.as<double>() + s->row_off[sp];
     if (launch_envs_energy(Ss, nsa, d_ndm.as<double>(), nsa, m->sp[sp].d_norms.as<double>(),
                            anorm, sig2, m->power, Kb, n_out, st) != 0)
@@ -983,9 +979,9 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
                      S.c64.as<double>(), S.p64.as<double>(), d_dp.as<double>(), nd,
                      d_sfd.as<double>(), st) != 0)
       return fail(FPP_ERR_CUDA, "stored-derivative kernel launch failed");
-    // fd[k][r] = dhat_k . dp_r  (row-major S x 3nq)
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, 3 * nq, Ss, nd, &one,
-                           d_dp.as<double>(), nd, Dh, nd, &zero, d_fd.as<double>(), 3 * nq));
+    // fd[k][r] = dhat_k . dp_r  (row-major S x 3nq), tensor cores, FP64-accurate
+    FPP_TRY(ozaki_dgemm_nt(Ss, 3 * nq, nd, Dh, nd, d_dp.as<double>(), nd, d_fd.as<double>(),
+                           3 * nq, m->oz, st));
     if (launch_envs_fkv(Ss, nq, d_fd.as<double>(), 3 * nq, d_ndm.as<double>(), nsa,
                         d_qatom.as<int>(), d_sfd.as<double>(),
                         m->sp[sp].d_norms.as<double>(), anorm, sig2, m->power, st) != 0 ||
@@ -997,7 +993,7 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
       return fail(FPP_ERR_CUDA, "envs assembly launch failed");
     FPP_CUDA(cudaStreamSynchronize(st));  // scratch buffers are freed at scope exit
   }
-  return FPP_OK;
+  return ozaki_check_status(m->oz, st);
 }
 
 }  // extern "C"
@@ -1186,20 +1182,38 @@ int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures, int32_t n_st
   int ks = 0, threads = 0;
   FPP_TRY(kuf_tiles(m, ka, (int)items.size(), st, &ks, &threads));
   FPP_CUDA(cudaMemsetAsync(dK.ptr, 0, sizeof(double) * (size_t)nst * n_labels, st));
+  struct Events {  // released on every return path
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Events() {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } ev;
+  FPP_CUDA(cudaEventCreate(&ev.e0));
+  FPP_CUDA(cudaEventCreate(&ev.e1));
+  FPP_CUDA(cudaEventRecord(ev.e0, st));
   if (launch_kuf_adjoint(ka, ks, threads, (int)items.size(), 0, st) != 0)
     return fail(FPP_ERR_CUDA, "Kuf (adjoint) launch failed");
+  FPP_CUDA(cudaEventRecord(ev.e1, st));
   m->kuf_ks = ks;
   m->kuf_threads = threads;
+  m->kuf_items = (long long)items.size();
   FPP_CUDA(cudaMemcpyAsync(kuf, dK.ptr, sizeof(double) * (size_t)nst * n_labels,
                            cudaMemcpyDeviceToHost, st));
   FPP_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  FPP_CUDA(cudaEventElapsedTime(&ms, ev.e0, ev.e1));
+  m->kuf_ms = ms;
   return FPP_OK;
 }
 
-int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads) {
+int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads, float *kernel_ms,
+                        int64_t *n_items) {
   if (!m || !ks || !threads) return fail(FPP_ERR_INVALID, "null argument");
   *ks = m->kuf_ks;
   *threads = m->kuf_threads;
+  if (kernel_ms) *kernel_ms = m->kuf_ms;
+  if (n_items) *n_items = m->kuf_items;
   return FPP_OK;
 }
 
@@ -1261,17 +1275,14 @@ int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
     return fail(FPP_ERR_CUDA, "gather launch failed");
   FPP_TRY(K.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
   FPP_CUDA(cudaMemsetAsync(K.ptr, 0, sizeof(double) * (size_t)R * n, st));
-  cublasHandle_t h;
-  FPP_TRY(get_cublas(m, st, &h));
-  const double one = 1.0, zero = 0.0;
   // K[cluster][k] = k(cluster, sparse k): block-diagonal in the species
   for (int sp = 0; sp < m->n_species; sp++) {
     const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
     if (Ss == 0 || nsa == 0) continue;
     double *C = K.as<double>() + (size_t)s->row_off[sp] * n + m->sp[sp].sparse_offset;
     const double *Ph = S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp;
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one,
-                           m->sp[sp].d_dhat.as<double>(), nd, Ph, ldp, &zero, C, n));
+    FPP_TRY(ozaki_dgemm_nt(nsa, Ss, nd, Ph, ldp, m->sp[sp].d_dhat.as<double>(), nd, C, n,
+                           m->oz, st));
     if (launch_envs_block(nsa, Ss, C, n, rown.as<double>() + s->row_off[sp],
                           m->sp[sp].d_norms.as<double>(), m->sigma * m->sigma, m->power, C,
                           n, st) != 0)
@@ -1282,13 +1293,13 @@ int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
   FPP_CUDA(cudaMemcpyAsync(Ld.ptr, L_inv, sizeof(double) * (size_t)n * n,
                            cudaMemcpyHostToDevice, st));
   FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
-  FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, n, R, n, &one, Ld.as<double>(), n,
-                         K.as<double>(), n, &zero, Q.as<double>(), n));
+  FPP_TRY(ozaki_dgemm_nt(R, n, n, K.as<double>(), n, Ld.as<double>(), n, Q.as<double>(), n,
+                         m->oz, st));
   FPP_TRY(q.reserve(sizeof(double) * std::max(1, R)));
   if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
     return fail(FPP_ERR_CUDA, "row-norm launch failed");
   std::vector<double> hq(R), hn(R);
-  FPP_CUDA(cudaStreamSynchronize(st));
+  FPP_TRY(ozaki_check_status(m->oz, st));
   FPP_CUDA(cudaMemcpy(hq.data(), q.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
   FPP_CUDA(cudaMemcpy(hn.data(), rown.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
   // clusters in species order, atoms in structure order within a species
@@ -1357,8 +1368,9 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
     if (Ss == 0 || nsa == 0) continue;
     double *C = K.as<double>() + koff[sp];
     const double *Ph = S.phat64.as<double>() + (size_t)s->row_off[sp] * ldp;
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one,
-                           m->sp[sp].d_dhat.as<double>(), nd, Ph, ldp, &zero, C, Ss));
+    // z[c][k] = phat_c . dhat_k on the tensor cores, FP64-accurate
+    FPP_TRY(ozaki_dgemm_nt(nsa, Ss, nd, Ph, ldp, m->sp[sp].d_dhat.as<double>(), nd, C, Ss,
+                           m->oz, st));
     if (launch_envs_block(nsa, Ss, C, Ss, rown.as<double>() + s->row_off[sp],
                           m->sp[sp].d_norms.as<double>(), m->sigma * m->sigma, m->power, C,
                           Ss, st) != 0)
@@ -1367,6 +1379,7 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
     FPP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, Ss, nsa, &one, C, Ss, ones.as<double>(), 1, &zero,
                            kE.as<double>() + m->sp[sp].sparse_offset, 1));
   }
+  FPP_TRY(ozaki_check_status(m->oz, st));
   double e_mean = 0, e_var = 0;
   if (energy) {
     std::vector<double> h_al(std::max(n, 1), 0.0);
@@ -1396,9 +1409,9 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
         const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp], off = m->sp[sp].sparse_offset;
         if (Ss == 0 || nsa == 0) continue;
         const double *Lb = m->L_inv.as<double>() + (size_t)off * n + off;
-        FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, Ss, &one, Lb, n,
-                               K.as<double>() + koff[sp], Ss, &zero, Q.as<double>() + koff[sp],
-                               Ss));
+        // Q[c][i] = sum_k K[c][k] L_inv[i][k] on the tensor cores
+        FPP_TRY(ozaki_dgemm_nt(nsa, Ss, Ss, K.as<double>() + koff[sp], Ss, Lb, n,
+                               Q.as<double>() + koff[sp], Ss, m->oz, st));
         if (launch_row_sq(nsa, Ss, Q.as<double>() + koff[sp], Ss,
                           q.as<double>() + s->row_off[sp], st) != 0)
           return fail(FPP_ERR_CUDA, "row-norm launch failed");
@@ -1417,13 +1430,13 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
                                    cudaMemcpyDeviceToDevice, st));
       }
       FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
-      FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, n, R, n, &one, m->L_inv.as<double>(),
-                             n, Kf.as<double>(), n, &zero, Q.as<double>(), n));
+      FPP_TRY(ozaki_dgemm_nt(R, n, n, Kf.as<double>(), n, m->L_inv.as<double>(), n,
+                             Q.as<double>(), n, m->oz, st));
       if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
         return fail(FPP_ERR_CUDA, "row-norm launch failed");
     }
     std::vector<double> hq(R), hn(R);
-    FPP_CUDA(cudaStreamSynchronize(st));
+    FPP_TRY(ozaki_check_status(m->oz, st));
     FPP_CUDA(cudaMemcpy(hq.data(), q.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
     FPP_CUDA(cudaMemcpy(hn.data(), rown.ptr, sizeof(double) * R, cudaMemcpyDeviceToHost));
     const double sig2 = m->sigma * m->sigma;

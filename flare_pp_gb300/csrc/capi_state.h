@@ -77,7 +77,10 @@ struct fpp_model {
   fpp_lammps_ws *lammps = nullptr;      // LAMMPS-array workspace
   double max_memory = 0;                // pair style's device-memory cap (0: none)
   int kuf_ks = 0, kuf_threads = 0;      // tile shape of the last batched Kuf
+  float kuf_ms = 0.f;                   // its Kuf kernel's CUDA-event time
+  long long kuf_items = 0;              // (structure, atom) work items of it
   int last_pair_batches = 0;            // atom batches of the last pair compute
+  fpp::OzakiWork oz;                    // kernel-form GEMM workspace
   void *cublas = nullptr;               // cublasHandle_t
 };
 
@@ -106,4 +109,11 @@ int forward64(fpp_structure *s, const B2Args &a0, const int *pair_tab, bool want
 // descriptor shape)
 int kuf_tiles(fpp_model *m, const KufArgs &ka, int n_items, cudaStream_t st, int *ks,
               int *threads);
+// FP64-accurate C = A B^T (row-major, device memory) on the tensor cores by
+// exact fp16 digit planes (gemm_ozaki.cu); w holds the planes between calls.
+// Queued on st; ozaki_check_status synchronizes st and reports a bounded
+// wait that ran out.
+int ozaki_dgemm_nt(int M, int N, int K, const double *A, long long lda, const double *B,
+                   long long ldb, double *C, long long ldc, OzakiWork &w, cudaStream_t st);
+int ozaki_check_status(OzakiWork &w, cudaStream_t st);
 }  // namespace fpp

@@ -42,6 +42,12 @@ struct DevBuf {
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Workspace of the FP64-accurate tensor-core GEMM (digit planes and row
+// powers of two of both operands, status word), kept between calls.
+struct OzakiWork {
+  DevBuf a, b, pa, pb, status;
+};
+
 // Cell quantities of Structure (structure.cpp:15-35), computed on the host
 // with the oracle's operation order and no contraction.
 struct CellInfo {

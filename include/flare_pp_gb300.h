@@ -275,8 +275,12 @@ int fpp_kuf_batched(fpp_model *m, fpp_structure *const *structures,
                     int32_t n_structures, const int32_t *label_mask,
                     const int32_t *atom_offsets, const int32_t *atoms,
                     double *kuf, int64_t n_labels, void *stream);
-/* The tile shape the last fpp_kuf_batched call on m used. */
-int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads);
+/* The tile shape the last fpp_kuf_batched call on m used (sparse
+ * environments per pass, threads per block), and (each may be NULL) the
+ * CUDA-event time of its Kuf kernel in ms and its (structure, atom) work
+ * items.  No counterpart in the reference (an instrumentation call). */
+int fpp_model_kuf_tiles(const fpp_model *m, int32_t *ks, int32_t *threads,
+                        float *kernel_ms, int64_t *n_items);
 
 /* NormalizedDotProduct::struc_struc (normalized_dot_product.cpp:212-444):
  * the full energy/force/stress covariance of two structures, FP64, from the
@@ -439,6 +443,21 @@ int fpp_std_atom_compute(fpp_model *m, int32_t nlocal, int32_t nall,
                          const int32_t *ilist, const int32_t *numneigh,
                          const int32_t *neighbors, int32_t use_map,
                          double *stds, void *stream);
+
+/* FP64-accurate C = A B^T on the fp16 tensor cores: row-major A (M x K, row
+ * stride lda), B (N x K, ldb), C (M x N, ldc).  Each row of A and of B is cut
+ * into 11 exact 5-bit digit planes relative to its largest entry; the level
+ * sums of the digit products are exact in the FP32 accumulators and are added
+ * in FP64, so every product keeps ~55 bits of each operand relative to its
+ * row's largest entry (the error bound of an FP64 GEMM, with |a_ik| |b_jk|
+ * replaced by max_k |a_ik| max_k |b_jk|).  The kernel-form GEMMs of
+ * envs_struc / predict_SOR (normalized_dot_product.cpp:140-143,
+ * sparse_gp.cpp:630-649) run on it.  Entries must be finite.  on_device: A,
+ * B, C are device pointers (queued on stream, then synchronized), else host
+ * arrays. */
+int fpp_dgemm_nt(int32_t M, int32_t N, int32_t K, const double *A, int64_t lda,
+                 const double *B, int64_t ldb, double *C, int64_t ldc, int32_t on_device,
+                 void *stream);
 
 #ifdef __cplusplus
 }
