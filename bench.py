@@ -354,7 +354,8 @@ def run_ours(args):
             times.append(time.perf_counter() - t0)
         variance = {"ms": round(1e3 * float(np.median(times)), 2),
                     "what": "SOR energy variance and per-atom (L_inv) variances of all "
-                            "atoms, FP64 (cuBLAS DGEMM), host outputs",
+                            "atoms, FP64-accurate (kernel and L_inv products on the "
+                            "tensor cores by exact fp16 digit planes), host outputs",
                     "energy_variance": vv, "local_variance_max": float(lv.max())}
         if rank == 0 and not args.no_cpu:
             variance["errors_vs_oracle"] = variance_check(w, disp[0], ev, vv, lv)

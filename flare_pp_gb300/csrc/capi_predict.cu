@@ -1496,12 +1496,19 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
     FPP_CUDA(cudaMemcpyAsync(alpha.ptr, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st));
     FPP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, n_out, nst, &one, K.as<double>(), n_out,
                            alpha.as<double>(), 1, &zero, mean.as<double>(), 1));
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, nst, n_out, nst, &one,
-                           m->R_inv.as<double>(), nst, K.as<double>(), n_out, &zero,
-                           V.as<double>(), nst));
+    // V[o][i] = sum_k K[k][o] R_inv[k][i] (predict_SOR's R_inv^T K, row o per
+    // label) on the tensor cores, FP64-accurate: operands K^T and R_inv^T
+    DevBuf KT, RT;
+    FPP_TRY(KT.reserve(sizeof(double) * (size_t)n_out * std::max(nst, 1)));
+    FPP_TRY(RT.reserve(sizeof(double) * (size_t)std::max(nst, 1) * std::max(nst, 1)));
+    if (launch_transpose(nst, n_out, K.as<double>(), n_out, KT.as<double>(), nst, st) != 0 ||
+        launch_transpose(nst, nst, m->R_inv.as<double>(), nst, RT.as<double>(), nst, st) != 0)
+      return fail(FPP_ERR_CUDA, "transpose launch failed");
+    FPP_TRY(ozaki_dgemm_nt(n_out, nst, nst, KT.as<double>(), nst, RT.as<double>(), nst,
+                           V.as<double>(), nst, m->oz, st));
     if (launch_row_sq(n_out, nst, V.as<double>(), nst, var.as<double>(), st) != 0)
       return fail(FPP_ERR_CUDA, "variance launch failed");
-    FPP_CUDA(cudaStreamSynchronize(st));
+    FPP_TRY(ozaki_check_status(m->oz, st));
     FPP_CUDA(cudaMemcpy(mean_efs, mean.ptr, sizeof(double) * n_out, cudaMemcpyDeviceToHost));
     FPP_CUDA(cudaMemcpy(variance_efs, var.ptr, sizeof(double) * n_out, cudaMemcpyDeviceToHost));
     return FPP_OK;
@@ -1512,7 +1519,7 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
   a.noa = noa;
   FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
   double *phat = S.phat64.as<double>();
-  DevBuf rown, E, zc, Z, G;
+  DevBuf rown, E, zc, Z, G, DT;
   FPP_TRY(rown.reserve(sizeof(double) * std::max(1, s->total_rows)));
   FPP_TRY(E.reserve(sizeof(double) * std::max(1, s->total_rows)));
   FPP_TRY(zc.reserve(sizeof(double) * std::max(1, s->total_rows)));
@@ -1530,22 +1537,26 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
     const size_t r0 = s->row_off[sp];
     FPP_TRY(Z.reserve(sizeof(double) * (size_t)nsa * Ss));
     const double *Dh = m->sp[sp].d_dhat.as<double>();
-    // Z[i][k] = phat_i . dhat_k
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, Ss, nsa, nd, &one, Dh, nd,
-                           phat + r0 * ldp, ldp, &zero, Z.as<double>(), Ss));
+    // Z[i][k] = phat_i . dhat_k (tensor cores, FP64-accurate)
+    FPP_TRY(ozaki_dgemm_nt(nsa, Ss, nd, phat + r0 * ldp, ldp, Dh, nd, Z.as<double>(), Ss,
+                           m->oz, st));
     if (launch_kernel_c(nsa, Ss, Z.as<double>(), Ss, m->sp[sp].d_alpha.as<double>(),
                         rown.as<double>() + r0, m->sigma * m->sigma, m->power,
                         E.as<double>() + r0, zc.as<double>() + r0, st) != 0)
       return fail(FPP_ERR_CUDA, "kernel-form launch failed");
-    // G[i][d] = sum_k C[i][k] dhat_k[d]
-    FPP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nd, nsa, Ss, &one, Dh, nd,
-                           Z.as<double>(), Ss, &zero, G.as<double>() + r0 * ldp, ldp));
+    // G[i][d] = sum_k C[i][k] dhat_k[d] = (C Dhat^T^T): B operand Dhat^T (nd x S)
+    FPP_TRY(DT.reserve(sizeof(double) * (size_t)nd * Ss));
+    if (launch_transpose(Ss, nd, Dh, nd, DT.as<double>(), Ss, st) != 0)
+      return fail(FPP_ERR_CUDA, "transpose launch failed");
+    FPP_TRY(ozaki_dgemm_nt(nsa, nd, Ss, Z.as<double>(), Ss, DT.as<double>(), Ss,
+                           G.as<double>() + r0 * ldp, ldp, m->oz, st));
     if (launch_kernel_w(nsa, nd, G.as<double>() + r0 * ldp, ldp, phat + r0 * ldp, ldp,
                         zc.as<double>() + r0, rown.as<double>() + r0,
                         S.w64.as<double>() + r0 * ldp, ldp, st) != 0)
       return fail(FPP_ERR_CUDA, "kernel-form launch failed");
     FPP_CUDA(cudaStreamSynchronize(st));  // Z is reused by the next species
   }
+  FPP_TRY(ozaki_check_status(m->oz, st));
   AdjArgs g;
   std::memset(&g, 0, sizeof(g));
   g.mode = kWGiven;

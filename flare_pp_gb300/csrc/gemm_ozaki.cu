@@ -16,16 +16,17 @@
 // which keeps about 55 bits of every operand relative to its row's largest
 // entry (the pairs of levels 11 and above, dropped, weigh below 2^-55 of it).
 //
-// Kernel layout (one persistent CTA per SM, 192 threads):
+// Kernel layout (one persistent CTA per SM, 320 threads):
 //   warp 0 lane 0  TMA producer: 128B-swizzled 128 x 64 tiles of the A and B
 //                  digit planes into a 6-stage ring
 //   warp 1 lane 0  MMA issuer: per unit (tile, level, K chunk) the pairs of
-//                  the level into one 128-column TMEM accumulator; two
-//                  accumulators alternate between units
-//   warps 2-5      epilogue: tcgen05.ld of their 32 TMEM lanes, C += level *
-//                  2^(-5 (L + 2)) in FP64 (read-modify-write of the tile,
-//                  which stays in L2 between levels), the row and column
-//                  powers of two applied after the last level
+//                  the level into one 128-column TMEM accumulator; four
+//                  accumulators rotate between units
+//   warps 2-9      epilogue: two warps per TMEM lane quarter, each owning 64
+//                  columns of its 32 rows: tcgen05.ld, then the level times
+//                  2^(-5 (L + 2)) added to FP64 sums held in registers for the
+//                  whole tile; after the last level the row and column powers
+//                  of two are applied and the tile is stored once
 // Every wait is bounded; a wait that runs out records FPP_ERR_TIMEOUT in the
 // status word and the CTA skips to its exit.
 #include <cuda.h>
@@ -46,7 +47,10 @@ namespace {
 constexpr int OBM = 128, OBN = 128, OBK = kTmaBoxK, OSTAGES = 6;
 constexpr int OA_TILE = OBM * OBK * 2, OB_TILE = OBN * OBK * 2;
 constexpr int OSTAGE_BYTES = OA_TILE + OB_TILE;
-constexpr int OTMEM_COLS = 2 * OBN;
+constexpr int OACC = 4;                 // TMEM accumulators (units in flight)
+constexpr int OTMEM_COLS = OACC * OBN;
+constexpr int OEPI = 8;                 // epilogue warps
+constexpr int OTHREADS = 32 * (2 + OEPI);
 constexpr int OSMEM_BYTES = OSTAGES * OSTAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int kChunkBlocks = kOzakiChunkK / OBK;
 static_assert(kOzakiChunkK % OBK == 0, "K chunks are whole TMA boxes");
@@ -65,19 +69,20 @@ struct OzakiParams {
   DeviceStatus *status;
 };
 
-__global__ void __launch_bounds__(192, 1) k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
+__global__ void __launch_bounds__(OTHREADS, 1)
+k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   unsigned char *gbase = smem_raw + (base - raw);
   const uint32_t bars = base + OSTAGES * OSTAGE_BYTES;
   uint64_t *bar_ptr = reinterpret_cast<uint64_t *>(gbase + OSTAGES * OSTAGE_BYTES);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_ptr + 2 * OSTAGES + 4);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_ptr + 2 * OSTAGES + 2 * OACC);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   auto full_bar = [&](int s) { return bars + 8u * s; };
   auto empty_bar = [&](int s) { return bars + 8u * (OSTAGES + s); };
   auto accf_bar = [&](int b) { return bars + 8u * (2 * OSTAGES + b); };
-  auto acce_bar = [&](int b) { return bars + 8u * (2 * OSTAGES + 2 + b); };
+  auto acce_bar = [&](int b) { return bars + 8u * (2 * OSTAGES + OACC + b); };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cid = (int)blockIdx.x, ncta = (int)gridDim.x;
@@ -87,9 +92,9 @@ __global__ void __launch_bounds__(192, 1) k_ozaki_gemm(const __grid_constant__ O
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
     }
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < OACC; b++) {
       mbar_init(accf_bar(b), 1);
-      mbar_init(acce_bar(b), 4);
+      mbar_init(acce_bar(b), OEPI);
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -151,9 +156,9 @@ __global__ void __launch_bounds__(192, 1) k_ozaki_gemm(const __grid_constant__ O
     for (int t = cid; t < p.n_tiles && !stop; t += ncta)
       for (int L = 0; L < kOzakiDigits && !stop; L++)
         for (int c = 0; c < p.n_chunks && !stop; c++, j++) {
-          const int buf = j & 1;
+          const int buf = j % OACC;
           const uint32_t acc = tmem + (uint32_t)(buf * OBN);
-          if (!mbar_wait(acce_bar(buf), (uint32_t)(((j >> 1) & 1) ^ 1))) {
+          if (!mbar_wait(acce_bar(buf), (uint32_t)(((j / OACC) & 1) ^ 1))) {
             set_status(p.status, FPP_ERR_TIMEOUT, 212, t);
             *abort_flag = 1;
           }
@@ -189,22 +194,23 @@ __global__ void __launch_bounds__(192, 1) k_ozaki_gemm(const __grid_constant__ O
         }
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int q = warp & 3;                 // TMEM lane quarter this warp may access
+    const int half = (warp - 2) / 4;        // which 64 columns of the tile
     const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     int j = 0;
     bool stop = false;
     for (int t = cid; t < p.n_tiles && !stop; t += ncta) {
-      const int mrow = (t / p.tiles_n) * OBM, n0 = (t % p.tiles_n) * OBN;
+      const int mrow = (t / p.tiles_n) * OBM, n0 = (t % p.tiles_n) * OBN + half * 64;
       const int r = mrow + q * 32 + lane;
-      const bool row_ok = r < p.M;
-      const double pr = row_ok ? p.pa[r] : 0.0;
-      double *crow = p.C + (size_t)(row_ok ? r : 0) * p.ldc;
+      double acc[64];
+#pragma unroll
+      for (int i = 0; i < 64; i++) acc[i] = 0.0;
       for (int L = 0; L < kOzakiDigits && !stop; L++) {
         // 2^(-5 (L + 2)), exact
         const double sL = __longlong_as_double((long long)(1023 - 5 * (L + 2)) << 52);
         for (int c = 0; c < p.n_chunks; c++, j++) {
-          const int buf = j & 1;
-          bool have = mbar_wait(accf_bar(buf), (uint32_t)((j >> 1) & 1));
+          const int buf = j % OACC;
+          bool have = mbar_wait(accf_bar(buf), (uint32_t)((j / OACC) & 1));
           have = __all_sync(0xffffffffu, have) != 0;
           if (!have) {
             if (lane == 0) set_status(p.status, FPP_ERR_TIMEOUT, 214, t);
@@ -217,31 +223,25 @@ __global__ void __launch_bounds__(192, 1) k_ozaki_gemm(const __grid_constant__ O
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const bool first = (L == 0 && c == 0);
-          const bool last = (L == kOzakiDigits - 1 && c == p.n_chunks - 1);
-          const uint32_t acc = tmem + (uint32_t)(buf * OBN) + lane_base;
-#pragma unroll 1
-          for (int cc = 0; cc < OBN; cc += 32) {
-            float v[32];
-            tmem_ld32(acc + cc, v);
-            if (row_ok) {
+          const uint32_t tm = tmem + (uint32_t)(buf * OBN + half * 64) + lane_base;
+          float v[32];
+          tmem_ld32(tm, v);
 #pragma unroll
-              for (int i = 0; i < 32; i++) {
-                const int col = n0 + cc + i;
-                if (col < p.N) {
-                  double x = (double)v[i] * sL;
-                  if (!first) x += crow[col];
-                  if (last) x = x * pr * p.pb[col];
-                  crow[col] = x;
-                }
-              }
-            }
-          }
+          for (int i = 0; i < 32; i++) acc[i] = fma((double)v[i], sL, acc[i]);
+          tmem_ld32(tm + 32, v);
+#pragma unroll
+          for (int i = 0; i < 32; i++) acc[32 + i] = fma((double)v[i], sL, acc[32 + i]);
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
           if (lane == 0) mbar_arrive(acce_bar(buf));
         }
       }
+      if (stop || r >= p.M) continue;
+      const double pr = p.pa[r];
+      double *crow = p.C + (size_t)r * p.ldc + n0;
+#pragma unroll
+      for (int i = 0; i < 64; i++)
+        if (n0 + i < p.N) crow[i] = acc[i] * pr * p.pb[n0 + i];
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -304,7 +304,7 @@ static int ozaki_launch_shape(int dev, int *ctas) {
       return -1;
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ozaki_gemm, 192,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ozaki_gemm, OTHREADS,
                                                       OSMEM_BYTES) != cudaSuccess)
       return -1;
     if (per_sm < 1) return -1;
@@ -364,7 +364,7 @@ int launch_ozaki_gemm(int M, int N, int K, const __half *a_planes, const double 
   if (cudaGetDevice(&dev) != cudaSuccess || ozaki_launch_shape(dev, &ctas) != 0) return -1;
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
-  cfg.blockDim = dim3(192, 1, 1);
+  cfg.blockDim = dim3(OTHREADS, 1, 1);
   cfg.dynamicSmemBytes = OSMEM_BYTES;
   cfg.stream = stream;
   cfg.gridDim = dim3(p.n_tiles < ctas ? p.n_tiles : ctas, 1, 1);

@@ -281,4 +281,28 @@ int launch_row_sq(int rows, int cols, const double *V, int ldv, double *out,
   return LAUNCH_OK;
 }
 
+// 32 x 32 tiles through shared memory (the extra column avoids bank conflicts)
+__global__ void k_transpose(int rows, int cols, const double *__restrict__ src, int lds,
+                            double *__restrict__ dst, int ldd) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[k][threadIdx.x] = src[(size_t)r * lds + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(size_t)c * ldd + r] = tile[threadIdx.x][k];
+  }
+}
+
+int launch_transpose(int rows, int cols, const double *src, int lds, double *dst, int ldd,
+                     cudaStream_t st) {
+  if (rows <= 0 || cols <= 0) return 0;
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  k_transpose<<<grid, block, 0, st>>>(rows, cols, src, lds, dst, ldd);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace fpp

@@ -30,4 +30,7 @@ int launch_envs_block(int S1, int S2, const double *Z, int ldz, const double *n1
                       cudaStream_t st);
 int launch_row_sq(int rows, int cols, const double *V, int ldv, double *out,
                   cudaStream_t st);
+// dst[c][r] = src[r][c] for r < rows, c < cols (row-major, leading dims)
+int launch_transpose(int rows, int cols, const double *src, int lds, double *dst, int ldd,
+                     cudaStream_t st);
 }  // namespace fpp
