@@ -85,6 +85,21 @@ class Structure(_Handle):
                 self.handle, ptr(self.positions), 0, _stream(stream)))
         self._nb = None
 
+    def set_skin(self, skin, stream=None):
+        """Keep the neighbor list between set_positions calls while no atom
+        has moved more than skin / 2 (fpp_structure_set_skin); 0 restores a
+        rebuild at every call."""
+        check(lib().fpp_structure_set_skin(self.handle, float(skin), _stream(stream)))
+        self._nb = None
+
+    def neighbor_stats(self):
+        """(builds, reuses, list cutoff) of the neighbor list since creation."""
+        C = _lib.ctypes
+        b, r, c = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().fpp_structure_neighbor_stats(self.handle, C.byref(b), C.byref(r),
+                                                 C.byref(c)))
+        return b.value, r.value, c.value
+
     def compute_descriptors(self):
         self.descriptors = [d.compute_struc(self)
                             for d in self.descriptor_calculators]

@@ -74,7 +74,8 @@ int ensure_tables(cudaStream_t stream) {
 int prepare_structure(fpp_structure *s, cudaStream_t stream) {
   FPP_TRY(ensure_tables(stream));
   s->st.mark(0, stream);
-  int rc = build_neighbors(s->st, stream);
+  bool reused = false;
+  int rc = update_neighbors(s->st, stream, &reused);
   s->st.mark(1, stream);
   s->st.ev_nb = s->st.profile;
   return rc;
@@ -105,6 +106,7 @@ int fpp_structure_create(const double *cell, const int32_t *species,
   auto *s = new fpp_structure();
   StructureState &st = s->st;
   st.noa = noa;
+  st.base_cutoff = cutoff;
   int rc = make_cell_info(cell, cutoff, &st.ci);
   if (rc != FPP_OK) {
     delete s;
@@ -154,6 +156,28 @@ int fpp_structure_set_positions(fpp_structure *s, const double *positions,
                              cs));
   s->version++;
   FPP_TRY(prepare_structure(s, cs));
+  return FPP_OK;
+}
+
+int fpp_structure_set_skin(fpp_structure *s, double skin, void *stream) {
+  if (!s) return fail(FPP_ERR_INVALID, "null structure");
+  if (!(skin >= 0) || !std::isfinite(skin)) return fail(FPP_ERR_INVALID, "skin must be >= 0");
+  StructureState &st = s->st;
+  CellInfo ci;
+  FPP_TRY(make_cell_info(st.ci.cell, st.base_cutoff + skin, &ci));
+  st.ci = ci;
+  st.skin = skin;
+  st.have_build = false;
+  s->version++;
+  return prepare_structure(s, (cudaStream_t)stream);
+}
+
+int fpp_structure_neighbor_stats(const fpp_structure *s, int64_t *builds, int64_t *reuses,
+                                 double *list_cutoff) {
+  if (!s) return fail(FPP_ERR_INVALID, "null structure");
+  if (builds) *builds = s->st.n_builds;
+  if (reuses) *reuses = s->st.n_reuses;
+  if (list_cutoff) *list_cutoff = s->st.ci.cutoff;
   return FPP_OK;
 }
 

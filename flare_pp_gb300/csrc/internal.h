@@ -115,6 +115,14 @@ struct StructureState {
   DevBuf nbr_rev;        // int32[n_pairs]  index of the reverse pair
   DevBuf scan_tmp;       // CUB scratch
   DevBuf status;         // DeviceStatus
+  // neighbor reuse within a skin (fpp_structure_set_skin): the list is built
+  // at base_cutoff + skin; while no atom has moved more than skin / 2 since
+  // that build, new positions only refresh the pair geometry
+  double base_cutoff = 0, skin = 0;
+  bool have_build = false;
+  DevBuf pos_build, wrapped_build;       // positions and wrapped positions at the build
+  DevBuf disp_max;                       // uint64: bits of max |x - x_build|^2
+  long long n_builds = 0, n_reuses = 0;
   // descriptor / prediction workspace (sized by the callers)
   DevBuf c64, p64, norm64;            // FP64 single-bond, B2, norms
   DevBuf phat64;                      // FP64 normalised B2 rows (species-sorted)
@@ -145,6 +153,9 @@ struct StructureState {
 };
 
 int build_neighbors(StructureState &st, cudaStream_t stream);
+// build_neighbors, or (skin > 0, no atom moved more than skin / 2 since the
+// last build) a refresh of the pair geometry of the existing list
+int update_neighbors(StructureState &st, cudaStream_t stream, bool *reused);
 // the FP64 pair table for the callers that return or consume FP64 geometry
 int ensure_rel64(StructureState &st, cudaStream_t stream);
 // exact-distance geometry of the structure's neighbor list (geom.cuh)

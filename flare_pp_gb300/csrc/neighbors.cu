@@ -25,6 +25,7 @@
 // filled on demand (ensure_rel64) for the callers that return or consume FP64
 // geometry.
 #include <cub/cub.cuh>
+#include <algorithm>
 #include <cstring>
 
 #include <cmath>
@@ -946,6 +947,133 @@ int ensure_rel64(StructureState &st, cudaStream_t stream) {
       st.nbr_i.as<int>(), st.nbr_rel.as<dvec4>());
   FPP_CUDA(cudaGetLastError());
   st.rel64_valid = true;
+  return FPP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbor reuse within a skin.  The list was built at cutoff + skin from the
+// positions x_b (wrapped w_b); for new positions x with max |x - x_b| <= skin/2
+// every pair within the cutoff is still in it.  The pair keys (j, shift) stay
+// valid when the positions are not re-wrapped, so the wrapped positions become
+// w = w_b + (x - x_b) and every pair vector is recomputed from them with the
+// build's float-float image formula; the FP64 table follows on demand
+// (ensure_rel64, the reference's image formula on w).
+// ---------------------------------------------------------------------------
+__global__ void k_max_disp2(int noa, const double *__restrict__ pos,
+                            const double *__restrict__ pos_b,
+                            unsigned long long *__restrict__ out) {
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < noa; i += gridDim.x * blockDim.x) {
+    const double dx = pos[3 * i] - pos_b[3 * i], dy = pos[3 * i + 1] - pos_b[3 * i + 1],
+                 dz = pos[3 * i + 2] - pos_b[3 * i + 2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    m = (d2 > m || d2 != d2) ? d2 : m;  // a NaN propagates (forces a rebuild)
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (v > m || v != v) ? v : m;
+  }
+  // non-negative doubles (and NaN) order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_refresh_wrapped(int noa, const double *__restrict__ pos,
+                                  const double *__restrict__ pos_b,
+                                  const dvec4 *__restrict__ wp_b, dvec4 *__restrict__ wp,
+                                  float4 *__restrict__ wp32, float4 *__restrict__ wp_lo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= noa) return;
+  const dvec4 b = wp_b[i];
+  const double w[3] = {dadd(b.x, dsub(pos[3 * i], pos_b[3 * i])),
+                       dadd(b.y, dsub(pos[3 * i + 1], pos_b[3 * i + 1])),
+                       dadd(b.z, dsub(pos[3 * i + 2], pos_b[3 * i + 2]))};
+  wp[i] = dvec4{w[0], w[1], w[2], 0.0};
+  const float4 h = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+  wp32[i] = h;
+  wp_lo[i] = make_float4((float)(w[0] - (double)h.x), (float)(w[1] - (double)h.y),
+                         (float)(w[2] - (double)h.z), 0.f);
+}
+
+// The canonical half of the pairs (key above (i, centre shift)) computes its
+// float-float vector and writes it, negated, to its reverse pair as well, as
+// the build does.
+__global__ void k_refresh_rel32(long long n_pairs, CellDev cd, const float4 *__restrict__ wp32,
+                                const float4 *__restrict__ wp_lo,
+                                const long long *__restrict__ keys,
+                                const int *__restrict__ nbr_i, const int *__restrict__ rev,
+                                float4 *__restrict__ rel32) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_pairs) return;
+  const int i = nbr_i[p];
+  const long long key = keys[p];
+  const long long thr = ((long long)i << kKeyBits) |
+                        ((cd.sweep * cd.ns + cd.sweep) * cd.ns + cd.sweep);
+  if (key <= thr) return;
+  const int j = (int)(key >> kKeyBits);
+  int s1, s2, s3;
+  decode_shift((int)(key & kKeyMask), cd.ns, cd.sweep, s1, s2, s3);
+  ff im[3], r2;
+  image_ff(wp32[i], wp_lo[i], wp32[j], wp_lo[j], cd.cff, s1, s2, s3, im, r2);
+  const float4 v = make_float4(im[0].hi + im[0].lo, im[1].hi + im[1].lo, im[2].hi + im[2].lo,
+                               ff_sqrt_f(r2));
+  rel32[p] = v;
+  const int q = rev[p];
+  if (q >= 0) rel32[q] = make_float4(-v.x, -v.y, -v.z, v.w);
+}
+
+// New positions (already in st.positions): refresh the geometry of the list
+// when no atom has moved more than skin / 2 since its build, else rebuild.
+// Sets *reused.
+int update_neighbors(StructureState &st, cudaStream_t stream, bool *reused) {
+  *reused = false;
+  const int noa = st.noa;
+  if (st.skin > 0 && st.have_build && noa > 0) {
+    FPP_TRY(st.disp_max.reserve(sizeof(unsigned long long)));
+    FPP_CUDA(cudaMemsetAsync(st.disp_max.ptr, 0, sizeof(unsigned long long), stream));
+    const int tb = 256, blocks = std::min(ceil_div(noa, tb), 4 * 152);
+    k_max_disp2<<<blocks, tb, 0, stream>>>(noa, st.positions.as<double>(),
+                                            st.pos_build.as<double>(),
+                                            st.disp_max.as<unsigned long long>());
+    FPP_CUDA(cudaGetLastError());
+    unsigned long long bits = 0;
+    FPP_CUDA(cudaMemcpyAsync(&bits, st.disp_max.ptr, sizeof(bits), cudaMemcpyDeviceToHost,
+                             stream));
+    FPP_CUDA(cudaStreamSynchronize(stream));
+    double d2;
+    std::memcpy(&d2, &bits, sizeof(d2));
+    if (d2 == d2 && 4.0 * d2 <= st.skin * st.skin) {
+      const CellDev cd = make_dev(st.ci);
+      k_refresh_wrapped<<<ceil_div(noa, tb), tb, 0, stream>>>(
+          noa, st.positions.as<double>(), st.pos_build.as<double>(),
+          st.wrapped_build.as<dvec4>(), st.wrapped.as<dvec4>(), st.wrapped32.as<float4>(),
+          st.wrapped_lo.as<float4>());
+      FPP_CUDA(cudaGetLastError());
+      if (st.n_pairs > 0) {
+        k_refresh_rel32<<<(int)((st.n_pairs + tb - 1) / tb), tb, 0, stream>>>(
+            st.n_pairs, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(),
+            st.nbr_key.as<long long>(), st.nbr_i.as<int>(), st.nbr_rev.as<int>(),
+            st.nbr_rel32.as<float4>());
+        FPP_CUDA(cudaGetLastError());
+      }
+      st.rel64_valid = false;
+      st.n_reuses++;
+      *reused = true;
+      return FPP_OK;
+    }
+  }
+  FPP_TRY(build_neighbors(st, stream));
+  st.n_builds++;
+  st.have_build = false;
+  if (st.skin > 0 && noa > 0) {
+    FPP_TRY(st.pos_build.reserve(sizeof(double) * 3 * noa));
+    FPP_TRY(st.wrapped_build.reserve(sizeof(dvec4) * noa));
+    FPP_CUDA(cudaMemcpyAsync(st.pos_build.ptr, st.positions.ptr, sizeof(double) * 3 * noa,
+                             cudaMemcpyDeviceToDevice, stream));
+    FPP_CUDA(cudaMemcpyAsync(st.wrapped_build.ptr, st.wrapped.ptr, sizeof(dvec4) * noa,
+                             cudaMemcpyDeviceToDevice, stream));
+    st.have_build = true;
+  }
   return FPP_OK;
 }
 

@@ -76,6 +76,22 @@ int fpp_structure_create(const double *cell, const int32_t *species,
  * pointer (noa*3 doubles). */
 int fpp_structure_set_positions(fpp_structure *s, const double *positions,
                                 int positions_on_device, void *stream);
+/* Neighbor reuse within a skin, as a molecular-dynamics engine keeps its
+ * lists (the reference's pair style receives such lists from LAMMPS: neighbor
+ * skin with neigh_modify check yes): the list is built at cutoff + skin, and
+ * fpp_structure_set_positions then refreshes only the pair vectors while no
+ * atom has moved more than skin / 2 since the last build (it rebuilds
+ * otherwise).  Descriptors filter pairs by their own cutoffs, so predictions
+ * equal those of a list at the cutoff up to FP64 rounding of the refreshed
+ * vectors; the neighbor attributes then include the pairs in the skin, and the
+ * wrapped positions are not re-wrapped between builds.  skin = 0 (the
+ * default) restores the reference's semantics.  Rebuilds the list now.  No
+ * counterpart in the reference's Structure. */
+int fpp_structure_set_skin(fpp_structure *s, double skin, void *stream);
+/* Neighbor builds and reuses since creation, and the list's cutoff (cutoff +
+ * skin); each pointer may be NULL. */
+int fpp_structure_neighbor_stats(const fpp_structure *s, int64_t *builds, int64_t *reuses,
+                                 double *list_cutoff);
 int fpp_structure_destroy(fpp_structure *s);
 /* noa, total neighbors, sweep, volume. */
 int fpp_structure_info(const fpp_structure *s, int32_t *noa,
