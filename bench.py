@@ -362,7 +362,7 @@ def run_ours(args):
     kuf = None
     if rank == 0 and world == 1 and not args.no_kuf:
         try:
-            kuf = kuf_batch_leg()
+            kuf = kuf_batch_leg(args.kuf_structures)
         except Exception as e:      # recorded, never fatal to the headline line
             kuf = {"error": f"{type(e).__name__}: {e}"}
     line = {
@@ -395,7 +395,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def kuf_batch_leg():
+def kuf_batch_leg(n_structures=256):
     """Training-side Kuf of the batched workload: 256 strained, rattled
     two-species FCC cells of 32-512 atoms (seed 404), N = 8, lmax = 3,
     rc 5.0, 1000 sparse environments drawn at random (seed 404), E, F and S
@@ -410,7 +410,7 @@ def kuf_batch_leg():
     import flare_pp_gb300 as fg
     from flare_pp_gb300 import synth
     rc = 5.0
-    cells = synth.fcc_batch(n_structures=256, seed=404, lo=32, hi=512)
+    cells = synth.fcc_batch(n_structures=n_structures, seed=404, lo=32, hi=512)
     gb = fg.B2("chebyshev", "quadratic", [0, rc], [], [2, 8, 3])
     gb.store_dervs = False
     gp = fg.SparseGP([fg.NormalizedDotProduct(2.0, 2)], 0.001, 0.05, 0.006)
@@ -422,7 +422,7 @@ def kuf_batch_leg():
         strucs.append(s)
     rng = np.random.default_rng(404)
     allc = [(k, a) for k, (_, sp, _) in enumerate(cells) for a in range(len(sp))]
-    pick = rng.choice(len(allc), 1000, replace=False)
+    pick = rng.choice(len(allc), min(1000, len(allc)), replace=False)
     for k in range(len(cells)):
         atoms = sorted(allc[p][1] for p in pick if allc[p][0] == k)
         if atoms:
@@ -450,8 +450,8 @@ def kuf_batch_leg():
         flop += float(np.sum(m * (4 * nd + 2 * nr * nr * H + cnt * (4 * N * H + 8 * H))))
     n_labels = Kuf.shape[1]
     achieved = flop / (ms / 1e3) / 1e12
-    return {"workload": "fcc_batch_256 (256 FCC two-species cells of 32-512 atoms, "
-                        "N=8 lmax=3 rc 5.0, 1000 sparse)",
+    return {"workload": f"fcc_batch_{n_structures} ({n_structures} FCC two-species cells "
+                        f"of 32-512 atoms, N=8 lmax=3 rc 5.0, {len(pick)} sparse)",
             "n_atoms": int(sum(len(sp) for _, sp, _ in cells)), "n_labels": int(n_labels),
             "work_items": int(items), "tiles": {"ks": ks, "threads": th},
             "tile_source": "autotuner (cached per device and descriptor shape)",
@@ -662,6 +662,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-kuf", action="store_true",
                     help="skip the batched-Kuf (training) leg")
+    ap.add_argument("--kuf-structures", type=int, default=256,
+                    help="structures of the batched-Kuf leg (256: the full workload)")
     ap.add_argument("--workload", default="bcc_alloy_32k", choices=sorted(WORKLOADS))
     ap.add_argument("--measure-peaks", action="store_true",
                     help="print the FP64 and TF32 matmul peaks and exit")

@@ -1,5 +1,5 @@
 // extern "C" entry points over the reference's Structure (structure.cpp),
-// B2 (descriptors/b2.cpp, descriptors/descriptor.cpp) and
+// B2 and B3 (descriptors/b2.cpp, descriptors/b3.cpp, descriptors/descriptor.cpp) and
 // NormalizedDotProduct (kernels/normalized_dot_product.cpp), compiled
 // unmodified from the reference tree by oracle/ref/build_ref.sh against the
 // Eigen and nlohmann_json stand-ins in oracle/ref/stub.  Used only to record
@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "b2.h"
+#include "b3.h"
 #include "descriptor.h"
 #include "normalized_dot_product.h"
 #include "structure.h"
@@ -38,7 +39,6 @@ template <typename V> int copy_int(const V &v, int *out) {
 }
 
 struct RefStructure {
-  B2 *b2 = nullptr;
   Structure *s = nullptr;
 };
 
@@ -46,6 +46,7 @@ struct RefStructure {
 
 extern "C" {
 
+// Descriptor handles are Descriptor pointers (ref_structure_new takes either).
 // B2(radial_basis = "chebyshev", cutoff_function, radial_hyps = {r1, rc},
 //    cutoff_hyps = {}, descriptor_settings = {ns, N, lmax}, cutoffs) (b2.h:34-46).
 void *ref_b2_new(int ns, int N, int lmax, double r1, double rc, const double *cutoffs,
@@ -53,17 +54,29 @@ void *ref_b2_new(int ns, int N, int lmax, double r1, double rc, const double *cu
   Eigen::MatrixXd cut(ns, ns);
   for (int a = 0; a < ns; a++)
     for (int b = 0; b < ns; b++) cut(a, b) = cutoffs[a * ns + b];
-  return new B2("chebyshev", cutoff_name, std::vector<double>{r1, rc}, std::vector<double>{},
-                std::vector<int>{ns, N, lmax}, cut);
+  Descriptor *d = new B2("chebyshev", cutoff_name, std::vector<double>{r1, rc},
+                         std::vector<double>{}, std::vector<int>{ns, N, lmax}, cut);
+  return d;
 }
 
-void ref_b2_free(void *b2) { delete static_cast<B2 *>(b2); }
+void ref_b2_free(void *b2) { delete static_cast<B2 *>(static_cast<Descriptor *>(b2)); }
 
-// Structure(cell, species, positions, cutoff, {b2}) (structure.h:92-97):
-// neighbors (structure.cpp:52-118) and, with a descriptor, its values.
+// B3(radial_basis = "chebyshev", cutoff_function, radial_hyps = {r1, rc},
+//    cutoff_hyps = {}, descriptor_settings = {ns, N, lmax}) (b3.h:27-30).
+void *ref_b3_new(int ns, int N, int lmax, double r1, double rc, const char *cutoff_name) {
+  Descriptor *d = new B3("chebyshev", cutoff_name, std::vector<double>{r1, rc},
+                         std::vector<double>{}, std::vector<int>{ns, N, lmax});
+  return d;
+}
+
+void ref_b3_free(void *b3) { delete static_cast<B3 *>(static_cast<Descriptor *>(b3)); }
+
+// Structure(cell, species, positions, cutoff, {descriptor}) (structure.h:92-97):
+// neighbors (structure.cpp:52-118) and, with a descriptor (a handle of
+// ref_b2_new or ref_b3_new), its values.
 // cell: 3 x 3 row-major, rows are the lattice vectors; positions noa x 3.
 void *ref_structure_new(const double *cell, const int *species, const double *pos, int noa,
-                        double cutoff, void *b2) {
+                        double cutoff, void *desc) {
   Eigen::MatrixXd c(3, 3), p(noa, 3);
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) c(i, j) = cell[3 * i + j];
@@ -71,9 +84,8 @@ void *ref_structure_new(const double *cell, const int *species, const double *po
     for (int j = 0; j < 3; j++) p(i, j) = pos[3 * i + j];
   std::vector<int> sp(species, species + noa);
   std::vector<Descriptor *> calc;
-  if (b2) calc.push_back(static_cast<B2 *>(b2));
+  if (desc) calc.push_back(static_cast<Descriptor *>(desc));
   auto *r = new RefStructure;
-  r->b2 = static_cast<B2 *>(b2);
   r->s = new Structure(c, sp, p, cutoff, calc);
   return r;
 }

@@ -213,6 +213,29 @@ def struc_cases():
     return out
 
 
+def b3_cases():
+    """B3 cases pinned to the reference's b3.cpp: (cell, species, positions,
+    cutoff, (n_species, N, lmax)); B3 uses one cutoff for every species pair
+    (b3.cpp:258)."""
+    base = struc_cases()
+    out = {}
+    cell, sp, pos, _, _, _ = base["fcc108"]
+    out["fcc108_n4l3"] = (cell, sp, pos, 5.0, (1, 4, 3))
+    cell, sp, pos, _, _, _ = base["two_species_20"]
+    out["two_species_20_n3l2"] = (cell, sp, pos, 4.2, (2, 3, 2))
+    cell, sp, pos, _, _, _ = base["triclinic_sweep2"]
+    out["triclinic_n2l3"] = (cell, sp, pos, 6.0, (2, 2, 3))
+    cell, sp, pos, _, _, _ = base["bcc54"]
+    out["bcc54_n2l4"] = (cell, sp, pos, 4.2, (2, 2, 4))
+    return out
+
+
+# B3 kernel cases: a sparse set from two B3 structures, and the two structures
+B3_KERNEL_SPARSE = [("two_species_20_n3l2", [[0, 2], [1, 3, 5]]),
+                    ("two_species_20_n3l2", [[4], [7]])]
+B3_KERNEL_STRUCS = ("two_species_20_n3l2", "two_species_20_n3l2")
+
+
 # Sparse sets of the kernel cases: (structure case, clusters per species).
 KERNEL_SPARSE = [("two_species_20", [[0, 2, 4], [1, 3]]), ("bcc54", [[1, 5], [0, 2, 7]])]
 KERNEL_STRUCS = ("two_species_20", "bcc54")

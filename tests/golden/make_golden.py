@@ -197,6 +197,94 @@ def struc_kernel_golden(lib):
     print("wrote tests/golden/struc_kernel_golden.npz")
 
 
+def b3_golden(lib):
+    """DescriptorValues of the reference's B3 (descriptors/b3.cpp) on the
+    tests.fixtures.b3_cases structures, and the NormalizedDotProduct kernels
+    on B3 descriptors, into tests/golden/b3_golden.npz."""
+    from tests import fixtures
+    D = ctypes.POINTER(ctypes.c_double)
+    I = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    lib.ref_b3_new.restype = vp
+    lib.ref_b3_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_char_p]
+    lib.ref_b3_free.argtypes = [vp]
+    lib.ref_structure_new.restype = vp
+    lib.ref_structure_new.argtypes = [D, I, D, ctypes.c_int, ctypes.c_double, vp]
+    lib.ref_structure_free.argtypes = [vp]
+    for fn in ("ref_dv_dbl", "ref_dv_int"):
+        getattr(lib, fn).argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_cluster_new.restype = vp
+    lib.ref_cluster_add.argtypes = [vp, vp, I, I]
+    lib.ref_cluster_free.argtypes = [vp]
+    lib.ref_kernel.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, vp, vp,
+                               ctypes.c_void_p, I, I]
+
+    def dbl(h, field, s_):
+        n = lib.ref_dv_dbl(h, field.encode(), s_, None)
+        assert n >= 0, field
+        out = np.zeros(n)
+        lib.ref_dv_dbl(h, field.encode(), s_, out.ctypes.data)
+        return out
+
+    def ints(h, field, s_):
+        n = lib.ref_dv_int(h, field.encode(), s_, None)
+        assert n >= 0, field
+        out = np.zeros(n, dtype=np.int32)
+        lib.ref_dv_int(h, field.encode(), s_, out.ctypes.data)
+        return out
+
+    out, handles = {}, {}
+    for name, (cell, sp, pos, rc, (ns, N, lmax)) in fixtures.b3_cases().items():
+        b3 = lib.ref_b3_new(ns, N, lmax, 0.0, float(rc), b"quadratic")
+        c = np.ascontiguousarray(cell, dtype=np.float64)
+        spi = np.ascontiguousarray(sp, dtype=np.int32)
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        h = lib.ref_structure_new(c.ctypes.data_as(D), spi.ctypes.data_as(I),
+                                  p.ctypes.data_as(D), len(sp), float(rc), b3)
+        handles[name] = (h, b3)
+        nd = int(ints(h, "n_descriptors", 0)[0])
+        for s_ in range(ns):
+            kd = f"dv/{name}/{s_}/"
+            out[kd + "descriptors"] = dbl(h, "descriptors", s_).reshape(-1, nd)
+            fd = dbl(h, "descriptor_force_dervs", s_).reshape(-1, nd)
+            out[kd + "force_dervs_rows"] = fd[:48]
+            out[kd + "force_dervs_proj"] = _proj(fd) if len(fd) else np.zeros((0, 4))
+            for f in ("descriptor_norms", "descriptor_force_dots", "cutoff_values"):
+                out[kd + f] = dbl(h, f, s_)
+            for f in ("neighbor_counts", "cumulative_neighbor_counts", "atom_indices",
+                      "neighbor_indices"):
+                out[kd + f] = ints(h, f, s_)
+    name0 = fixtures.B3_KERNEL_SPARSE[0][0]
+    nd = int(ints(handles[name0][0], "n_descriptors", 0)[0])
+    cd = lib.ref_cluster_new(2, nd)
+    for name, cl in fixtures.B3_KERNEL_SPARSE:
+        counts = np.array([len(x) for x in cl], dtype=np.int32)
+        flat = np.array([a for x in cl for a in x], dtype=np.int32)
+        assert lib.ref_cluster_add(cd, handles[name][0], counts.ctypes.data_as(I),
+                                   flat.ctypes.data_as(I)) == 0
+    a_, b_ = (handles[n][0] for n in fixtures.B3_KERNEL_STRUCS)
+    for sig, pw in fixtures.KERNEL_HYPS:
+        for what, x, y in (("envs_envs", cd, cd), ("envs_struc", cd, b_),
+                           ("struc_struc", a_, b_), ("self_kernel_struc", b_, None)):
+            r, cc = ctypes.c_int(), ctypes.c_int()
+            n = lib.ref_kernel(what.encode(), sig, pw, x, y, None, ctypes.byref(r),
+                               ctypes.byref(cc))
+            if n == -2:
+                out[f"kernel/{what}/{sig}/{pw}/throws"] = np.array(1)
+                continue
+            m = np.zeros(n)
+            lib.ref_kernel(what.encode(), sig, pw, x, y, m.ctypes.data, ctypes.byref(r),
+                           ctypes.byref(cc))
+            out[f"kernel/{what}/{sig}/{pw}"] = m.reshape(r.value, cc.value)
+    lib.ref_cluster_free(cd)
+    for h, b3 in handles.values():
+        lib.ref_structure_free(h)
+        lib.ref_b3_free(b3)
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "b3_golden.npz"), **out)
+    print("wrote tests/golden/b3_golden.npz")
+
+
 def main(ref_root=None):
     ref_root = ref_root or os.environ.get("FLARE_PP_REFERENCE", "/root/reference")
     subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root],
@@ -264,6 +352,7 @@ def main(ref_root=None):
     print("wrote tests/golden/l0_golden.npz")
     beta_form_golden(lib)
     struc_kernel_golden(lib)
+    b3_golden(lib)
 
 
 if __name__ == "__main__":
