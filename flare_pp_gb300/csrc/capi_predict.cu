@@ -1,4 +1,5 @@
 // C ABI: descriptors, model, predictions.
+#include <cub/cub.cuh>
 #include <cublas_v2.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -920,40 +921,43 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
   FPP_TRY(K.reserve(sizeof(double) * (size_t)std::max(1, m->n_sparse_total) * n_out));
   FPP_CUDA(cudaMemsetAsync(K.ptr, 0, sizeof(double) * (size_t)m->n_sparse_total * n_out, st));
   // row-ordered atom norms
-  DevBuf rown;
+  DevBuf &rown = m->es_rown;
   FPP_TRY(rown.reserve(sizeof(double) * std::max(1, s->total_rows)));
   FPP_CUDA(cudaMemsetAsync(rown.ptr, 0, sizeof(double) * s->total_rows, st));
   if (launch_gather_rows(noa, s->row_of_atom.as<int>(), S.norm64.as<double>(),
                          rown.as<double>(), st) != 0)
     return fail(FPP_ERR_CUDA, "gather launch failed");
-  // neighbor data on the host to form the per-species descriptor pair lists
-  std::vector<int> off(noa + 1, 0), nbr_i(S.n_pairs), nbr_s(S.n_pairs);
-  std::vector<dvec4> rel(S.n_pairs);
-  FPP_CUDA(cudaStreamSynchronize(st));
-  if (noa) FPP_CUDA(cudaMemcpy(off.data(), S.nbr_offset.ptr, sizeof(int) * (noa + 1), cudaMemcpyDeviceToHost));
-  if (S.n_pairs) {
-    FPP_CUDA(cudaMemcpy(nbr_i.data(), S.nbr_i.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
-    FPP_CUDA(cudaMemcpy(nbr_s.data(), S.nbr_s.ptr, sizeof(int) * S.n_pairs, cudaMemcpyDeviceToHost));
-    FPP_CUDA(cudaMemcpy(rel.data(), S.nbr_rel.ptr, sizeof(dvec4) * S.n_pairs, cudaMemcpyDeviceToHost));
-  }
-  std::vector<int> local(noa, 0), cnt(m->n_species, 0);
-  for (int i = 0; i < noa; i++) local[i] = cnt[S.species_host[i]]++;
+  // per species: the descriptor pairs (central atom of the species, within
+  // the pair's cutoff, b2.cpp:277) selected on the device in pair order
+  const long long np = S.n_pairs;
+  FPP_TRY(m->es_flags.reserve(sizeof(int) * (size_t)(np + 1)));
+  FPP_TRY(m->es_pos.reserve(sizeof(int) * (size_t)(np + 1)));
+  FPP_TRY(m->es_dmap.reserve(sizeof(int) * (size_t)std::max<long long>(np, 1)));
+  size_t scan_bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, m->es_flags.as<int>(), m->es_pos.as<int>(),
+                                (int)(np + 1), st);
+  FPP_TRY(m->es_scan.reserve(std::max<size_t>(scan_bytes, 16)));
   for (int sp = 0; sp < m->n_species; sp++) {
     const int Ss = m->sp[sp].n_sparse, nsa = s->n_rows[sp];
     if (Ss == 0) continue;
     double *Kb = K.as<double>() + (size_t)m->sp[sp].sparse_offset * n_out;
     if (nsa == 0) continue;
-    std::vector<int> plist, qatom, dmap(std::max<int64_t>(S.n_pairs, 1), -1);
-    for (int64_t p = 0; p < S.n_pairs; p++) {
-      const int i = nbr_i[p];
-      if (S.species_host[i] != sp) continue;
-      if (!(rel[p].x <= a.cutoffs[sp * a.n_species + nbr_s[p]])) continue;
-      dmap[p] = (int)plist.size();
-      plist.push_back((int)p);
-      qatom.push_back(local[i]);
+    CutRow cut;
+    for (int t = 0; t < kSelMaxSpecies; t++)
+      cut.c[t] = t < a.n_species ? a.cutoffs[sp * a.n_species + t] : 0.0;
+    int nq = 0;
+    if (np > 0) {
+      if (launch_pair_flags(np, S.nbr_i.as<int>(), S.nbr_s.as<int>(), S.nbr_rel.as<dvec4>(),
+                            S.species.as<int>(), sp, cut, m->es_flags.as<int>(), st) != 0)
+        return fail(FPP_ERR_CUDA, "pair selection launch failed");
+      size_t tb = m->es_scan.bytes;
+      FPP_CUDA(cub::DeviceScan::ExclusiveSum(m->es_scan.ptr, tb, m->es_flags.as<int>(),
+                                             m->es_pos.as<int>(), (int)(np + 1), st));
+      FPP_CUDA(cudaMemcpyAsync(&nq, m->es_pos.as<int>() + np, sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+      FPP_CUDA(cudaStreamSynchronize(st));
     }
-    const int nq = (int)plist.size();
-    DevBuf d_ndm;
+    DevBuf &d_ndm = m->es_ndm;
     FPP_TRY(d_ndm.reserve(sizeof(double) * (size_t)Ss * nsa));
     const double *Dh = m->sp[sp].d_dhat.as<double>();
     const double *Ph = phat + (size_t)s->row_off[sp] * ldp;
@@ -963,35 +967,37 @@ static int envs_struc_device(fpp_model *m, fpp_structure *s, cudaStream_t st, De
     if (launch_envs_energy(Ss, nsa, d_ndm.as<double>(), nsa, m->sp[sp].d_norms.as<double>(),
                            anorm, sig2, m->power, Kb, n_out, st) != 0)
       return fail(FPP_ERR_CUDA, "envs energy launch failed");
-    if (nq == 0) continue;
-    DevBuf d_plist, d_qatom, d_dmap, d_dp, d_sfd, d_fd;
-    FPP_TRY(d_plist.reserve(sizeof(int) * nq));
-    FPP_TRY(d_qatom.reserve(sizeof(int) * nq));
-    FPP_TRY(d_dmap.reserve(sizeof(int) * dmap.size()));
-    FPP_TRY(d_dp.reserve(sizeof(double) * 3 * (size_t)nq * nd));
-    FPP_TRY(d_sfd.reserve(sizeof(double) * 3 * nq));
-    FPP_TRY(d_fd.reserve(sizeof(double) * 3 * (size_t)nq * Ss));
-    FPP_CUDA(cudaMemcpyAsync(d_plist.ptr, plist.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
-    FPP_CUDA(cudaMemcpyAsync(d_qatom.ptr, qatom.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
-    FPP_CUDA(cudaMemcpyAsync(d_dmap.ptr, dmap.data(), sizeof(int) * dmap.size(), cudaMemcpyHostToDevice, st));
-    if (launch_b2_dp(a, nq, d_plist.as<int>(), S.nbr_i.as<int>(), S.nbr_s.as<int>(),
+    if (nq == 0) {
+      FPP_CUDA(cudaStreamSynchronize(st));  // ndm is reused by the next species
+      continue;
+    }
+    FPP_TRY(m->es_plist.reserve(sizeof(int) * nq));
+    FPP_TRY(m->es_qatom.reserve(sizeof(int) * nq));
+    FPP_TRY(m->es_dp.reserve(sizeof(double) * 3 * (size_t)nq * nd));
+    FPP_TRY(m->es_sfd.reserve(sizeof(double) * 3 * nq));
+    FPP_TRY(m->es_fd.reserve(sizeof(double) * 3 * (size_t)nq * Ss));
+    int *d_plist = m->es_plist.as<int>(), *d_qatom = m->es_qatom.as<int>(),
+        *d_dmap = m->es_dmap.as<int>();
+    double *d_dp = m->es_dp.as<double>(), *d_sfd = m->es_sfd.as<double>(),
+           *d_fd = m->es_fd.as<double>();
+    if (launch_pair_scatter(np, m->es_flags.as<int>(), m->es_pos.as<int>(), S.nbr_i.as<int>(),
+                            s->row_of_atom.as<int>(), s->row_off[sp], d_plist, d_qatom, d_dmap,
+                            st) != 0)
+      return fail(FPP_ERR_CUDA, "pair selection launch failed");
+    if (launch_b2_dp(a, nq, d_plist, S.nbr_i.as<int>(), S.nbr_s.as<int>(),
                      S.nbr_rel.as<dvec4>(), S.species.as<int>(), m->pair_tab.as<int>(),
-                     S.c64.as<double>(), S.p64.as<double>(), d_dp.as<double>(), nd,
-                     d_sfd.as<double>(), st) != 0)
+                     S.c64.as<double>(), S.p64.as<double>(), d_dp, nd, d_sfd, st) != 0)
       return fail(FPP_ERR_CUDA, "stored-derivative kernel launch failed");
     // fd[k][r] = dhat_k . dp_r  (row-major S x 3nq), tensor cores, FP64-accurate
-    FPP_TRY(ozaki_dgemm_nt(Ss, 3 * nq, nd, Dh, nd, d_dp.as<double>(), nd, d_fd.as<double>(),
-                           3 * nq, m->oz, st));
-    if (launch_envs_fkv(Ss, nq, d_fd.as<double>(), 3 * nq, d_ndm.as<double>(), nsa,
-                        d_qatom.as<int>(), d_sfd.as<double>(),
+    FPP_TRY(ozaki_dgemm_nt(Ss, 3 * nq, nd, Dh, nd, d_dp, nd, d_fd, 3 * nq, m->oz, st));
+    if (launch_envs_fkv(Ss, nq, d_fd, 3 * nq, d_ndm.as<double>(), nsa, d_qatom, d_sfd,
                         m->sp[sp].d_norms.as<double>(), anorm, sig2, m->power, st) != 0 ||
-        launch_envs_force(Ss, noa, d_fd.as<double>(), 3 * nq, S.nbr_offset.as<int>(),
-                          S.nbr_rev.as<int>(), d_dmap.as<int>(), Kb, n_out, st) != 0 ||
-        launch_envs_stress(Ss, nq, d_fd.as<double>(), 3 * nq, d_plist.as<int>(),
-                           S.nbr_rel.as<dvec4>(), 1.0 / S.ci.volume, noa, Kb, n_out,
-                           st) != 0)
+        launch_envs_force(Ss, noa, d_fd, 3 * nq, S.nbr_offset.as<int>(), S.nbr_rev.as<int>(),
+                          d_dmap, Kb, n_out, st) != 0 ||
+        launch_envs_stress(Ss, nq, d_fd, 3 * nq, d_plist, S.nbr_rel.as<dvec4>(),
+                           1.0 / S.ci.volume, noa, Kb, n_out, st) != 0)
       return fail(FPP_ERR_CUDA, "envs assembly launch failed");
-    FPP_CUDA(cudaStreamSynchronize(st));  // scratch buffers are freed at scope exit
+    FPP_CUDA(cudaStreamSynchronize(st));  // the workspace is reused by the next species
   }
   return ozaki_check_status(m->oz, st);
 }

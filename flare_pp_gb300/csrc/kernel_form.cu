@@ -305,4 +305,53 @@ int launch_transpose(int rows, int cols, const double *src, int lds, double *dst
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+__global__ void k_pair_flags(long long n, const int *__restrict__ nbr_i,
+                             const int *__restrict__ nbr_s, const dvec4 *__restrict__ rel,
+                             const int *__restrict__ species, int sp, CutRow cut,
+                             int *__restrict__ flags) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > n) return;
+  if (p == n) {
+    flags[n] = 0;
+    return;
+  }
+  flags[p] = (species[nbr_i[p]] == sp && rel[p].x <= cut.c[nbr_s[p]]) ? 1 : 0;
+}
+
+__global__ void k_pair_scatter(long long n, const int *__restrict__ flags,
+                               const int *__restrict__ pos, const int *__restrict__ nbr_i,
+                               const int *__restrict__ row_of_atom, int row0,
+                               int *__restrict__ plist, int *__restrict__ qatom,
+                               int *__restrict__ dmap) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (flags[p]) {
+    const int q = pos[p];
+    plist[q] = (int)p;
+    qatom[q] = row_of_atom[nbr_i[p]] - row0;
+    dmap[p] = q;
+  } else {
+    dmap[p] = -1;
+  }
+}
+
+int launch_pair_flags(long long n_pairs, const int *nbr_i, const int *nbr_s, const dvec4 *rel,
+                      const int *species, int sp, CutRow cut, int *flags, cudaStream_t st) {
+  const int tb = 256;
+  k_pair_flags<<<(int)((n_pairs + 1 + tb - 1) / tb), tb, 0, st>>>(n_pairs, nbr_i, nbr_s, rel,
+                                                                  species, sp, cut, flags);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_pair_scatter(long long n_pairs, const int *flags, const int *pos, const int *nbr_i,
+                        const int *row_of_atom, int row0, int *plist, int *qatom, int *dmap,
+                        cudaStream_t st) {
+  if (n_pairs <= 0) return 0;
+  const int tb = 256;
+  k_pair_scatter<<<(int)((n_pairs + tb - 1) / tb), tb, 0, st>>>(n_pairs, flags, pos, nbr_i,
+                                                                row_of_atom, row0, plist,
+                                                                qatom, dmap);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace fpp

@@ -30,6 +30,20 @@ int launch_envs_block(int S1, int S2, const double *Z, int ldz, const double *n1
                       cudaStream_t st);
 int launch_row_sq(int rows, int cols, const double *V, int ldv, double *out,
                   cudaStream_t st);
+// The descriptor pairs of one species: flags[p] = 1 when pair p's central
+// atom has species sp and r <= cut[neighbor species] (b2.cpp:277), flags[n]
+// = 0; then, from the exclusive scan pos of flags, plist[pos[p]] = p,
+// qatom[pos[p]] = the central atom's row within its species block, dmap[p]
+// = pos[p] or -1.
+constexpr int kSelMaxSpecies = 8;
+struct CutRow {
+  double c[kSelMaxSpecies];
+};
+int launch_pair_flags(long long n_pairs, const int *nbr_i, const int *nbr_s, const dvec4 *rel,
+                      const int *species, int sp, CutRow cut, int *flags, cudaStream_t st);
+int launch_pair_scatter(long long n_pairs, const int *flags, const int *pos, const int *nbr_i,
+                        const int *row_of_atom, int row0, int *plist, int *qatom, int *dmap,
+                        cudaStream_t st);
 // dst[c][r] = src[r][c] for r < rows, c < cols (row-major, leading dims)
 int launch_transpose(int rows, int cols, const double *src, int lds, double *dst, int ldd,
                      cudaStream_t st);
