@@ -236,6 +236,30 @@ B3_KERNEL_SPARSE = [("two_species_20_n3l2", [[0, 2], [1, 3, 5]]),
 B3_KERNEL_STRUCS = ("two_species_20_n3l2", "two_species_20_n3l2")
 
 
+def sgp_scenario(two_kernels=False, power=2.0):
+    """The sparse-GP case pinned to the reference's sparse_gp.cpp: three
+    16-atom BCC alloy frames (a = 3.6 A, rattled 0.2 A, Lennard-Jones E/F/S
+    labels; frame 1 trains on the forces of atoms 0, 3, 5), 5 sparse
+    environments per frame, noises (1, 2, 3), a held-out frame; one B2 kernel
+    (sigma 2, power 2) or B2 + B3 (sigma 2 and 1.5).  Returns the frames as
+    (cell, species, positions, energy, forces, stress), the training atom
+    lists, the sparse atoms per frame, the held-out frame, rc and the
+    descriptor / kernel settings."""
+    rc = 4.0
+    frames = []
+    for k in range(3):
+        cell, sp, pos = synth.bcc_alloy((2, 2, 2), 808 + k, sigma=0.2, a=3.6)
+        e, f, st, _ = synth.lennard_jones(cell, pos)
+        frames.append((cell, sp, pos, np.array([e]), f.reshape(-1), st))
+    train_atoms = [None, [0, 3, 5], None]
+    sparse_atoms = [[(3 * k + 5 * j) % 16 for j in range(5)] for k in range(3)]
+    test = synth.bcc_alloy((2, 2, 2), 900, sigma=0.2, a=3.6)
+    descs = [("B2", (2, 4, 2))] + ([("B3", (2, 2, 2))] if two_kernels else [])
+    hyps = [(2.0, power)] + ([(1.5, power)] if two_kernels else [])
+    return dict(rc=rc, frames=frames, train_atoms=train_atoms, sparse_atoms=sparse_atoms,
+                test=test, descs=descs, hyps=hyps, noises=(1.0, 2.0, 3.0))
+
+
 # Sparse sets of the kernel cases: (structure case, clusters per species).
 KERNEL_SPARSE = [("two_species_20", [[0, 2, 4], [1, 3]]), ("bcc54", [[1, 5], [0, 2, 7]])]
 KERNEL_STRUCS = ("two_species_20", "bcc54")

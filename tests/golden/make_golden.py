@@ -285,6 +285,151 @@ def b3_golden(lib):
     print("wrote tests/golden/b3_golden.npz")
 
 
+def sgp_golden(lib):
+    """The reference's SparseGP (bffs/sparse_gp.cpp) on tests.fixtures.
+    sgp_scenario, one kernel and two (B2 + B3): Kuu, Kuf, y, noise vector,
+    alpha, R_inv, L_inv, the stable likelihood and its gradient, the same after
+    set_hyperparameters, predict_mean / SOR / DTC and the cluster
+    uncertainties of the held-out frame, into tests/golden/sgp_golden.npz."""
+    from tests import fixtures
+    D = ctypes.POINTER(ctypes.c_double)
+    I = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    lib.ref_b2_new.restype = vp
+    lib.ref_b2_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, D, ctypes.c_char_p]
+    lib.ref_b3_new.restype = vp
+    lib.ref_b3_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_char_p]
+    lib.ref_b2_free.argtypes = [vp]
+    lib.ref_b3_free.argtypes = [vp]
+    lib.ref_sgp_structure_new.restype = vp
+    lib.ref_sgp_structure_new.argtypes = [D, I, D, ctypes.c_int, ctypes.c_double,
+                                          ctypes.POINTER(vp), ctypes.c_int]
+    lib.ref_sgp_structure_free.argtypes = [vp]
+    lib.ref_sgp_structure_set_labels.argtypes = [vp, D, ctypes.c_int, D, ctypes.c_int, D,
+                                                 ctypes.c_int]
+    lib.ref_sgp_structure_get.argtypes = [vp, ctypes.c_char_p, ctypes.c_void_p]
+    lib.ref_sgp_new.restype = vp
+    lib.ref_sgp_new.argtypes = [ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_double]
+    lib.ref_sgp_free.argtypes = [vp]
+    lib.ref_sgp_add_training_structure.argtypes = [vp, vp, I, ctypes.c_int]
+    lib.ref_sgp_add_specific_environments.argtypes = [vp, vp, I, ctypes.c_int]
+    lib.ref_sgp_update_matrices_QR.argtypes = [vp]
+    lib.ref_sgp_set_hyperparameters.argtypes = [vp, D, ctypes.c_int]
+    lib.ref_sgp_compute_likelihood_stable.argtypes = [vp]
+    lib.ref_sgp_compute_likelihood_gradient_stable.argtypes = [vp]
+    lib.ref_sgp_compute_likelihood_gradient_stable.restype = ctypes.c_double
+    lib.ref_sgp_predict.argtypes = [vp, ctypes.c_char_p, vp]
+    lib.ref_sgp_cluster_uncertainties.argtypes = [vp, vp, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_sgp_get.argtypes = [vp, ctypes.c_char_p, ctypes.c_void_p, I, I]
+    for fn in ("ref_sgp_mapping_coefficients", "ref_sgp_varmap_coefficients"):
+        getattr(lib, fn).argtypes = [vp, ctypes.c_int, ctypes.c_void_p, I, I]
+
+    def coeffs(fn, gp, ki):
+        r, c = ctypes.c_int(), ctypes.c_int()
+        n = fn(gp, ki, None, ctypes.byref(r), ctypes.byref(c))
+        assert n >= 0
+        out = np.zeros(n)
+        fn(gp, ki, out.ctypes.data, None, None)
+        return out.reshape(r.value, c.value)
+
+    def arr(x, t=np.float64):
+        return np.ascontiguousarray(x, dtype=t)
+
+    def get(h, f):
+        r, c = ctypes.c_int(), ctypes.c_int()
+        n = lib.ref_sgp_get(h, f.encode(), None, ctypes.byref(r), ctypes.byref(c))
+        assert n >= 0, f
+        out = np.zeros(n)
+        lib.ref_sgp_get(h, f.encode(), out.ctypes.data, None, None)
+        return out.reshape(r.value, c.value)
+
+    def sget(s, f):
+        n = lib.ref_sgp_structure_get(s, f.encode(), None)
+        out = np.zeros(n)
+        lib.ref_sgp_structure_get(s, f.encode(), out.ctypes.data)
+        return out
+
+    out = {}
+    for tag, two, power in (("one", False, 2.0), ("two", True, 2.0), ("pow1", False, 1.0)):
+        sc = fixtures.sgp_scenario(two, power)
+        rc = sc["rc"]
+        descs = []
+        for kind, (ns, N, lmax) in sc["descs"]:
+            if kind == "B2":
+                cut = arr(np.full((ns, ns), rc))
+                descs.append(lib.ref_b2_new(ns, N, lmax, 0.0, rc, cut.ctypes.data_as(D),
+                                            b"quadratic"))
+            else:
+                descs.append(lib.ref_b3_new(ns, N, lmax, 0.0, rc, b"quadratic"))
+        dv = (vp * len(descs))(*descs)
+
+        def structure(cell, sp, pos):
+            c, s_, p = arr(cell), arr(sp, np.int32), arr(pos)
+            return lib.ref_sgp_structure_new(c.ctypes.data_as(D), s_.ctypes.data_as(I),
+                                             p.ctypes.data_as(D), len(sp), rc, dv, len(descs))
+        sig = arr([h[0] for h in sc["hyps"]])
+        pw = arr([h[1] for h in sc["hyps"]])
+        gp = lib.ref_sgp_new(len(descs), sig.ctypes.data_as(D), pw.ctypes.data_as(D),
+                             *sc["noises"])
+        strucs = []
+        for (cell, sp, pos, e, f, st), atoms in zip(sc["frames"], sc["train_atoms"]):
+            s = structure(cell, sp, pos)
+            e, f, st = arr(e), arr(f), arr(st)
+            lib.ref_sgp_structure_set_labels(s, e.ctypes.data_as(D), len(e),
+                                             f.ctypes.data_as(D), len(f),
+                                             st.ctypes.data_as(D), len(st))
+            a = arr(atoms if atoms is not None else [0], np.int32)
+            lib.ref_sgp_add_training_structure(gp, s, a.ctypes.data_as(I),
+                                               -1 if atoms is None else len(atoms))
+            strucs.append(s)
+        for s, atoms in zip(strucs, sc["sparse_atoms"]):
+            a = arr(atoms, np.int32)
+            lib.ref_sgp_add_specific_environments(gp, s, a.ctypes.data_as(I), len(atoms))
+        lib.ref_sgp_update_matrices_QR(gp)
+        k = f"{tag}/"
+        for f in ("Kuu", "Kuf", "y", "noise_vector", "alpha", "R_inv", "L_inv",
+                  "hyperparameters"):
+            out[k + f] = get(gp, f)
+        lib.ref_sgp_compute_likelihood_stable(gp)
+        for f in ("log_marginal_likelihood", "data_fit", "complexity_penalty"):
+            out[k + "stable/" + f] = get(gp, f)
+        out[k + "grad/value"] = np.array(lib.ref_sgp_compute_likelihood_gradient_stable(gp))
+        out[k + "grad/likelihood_gradient"] = get(gp, "likelihood_gradient")
+        test = structure(*sc["test"])
+        for what in ("mean", "SOR", "DTC"):
+            assert lib.ref_sgp_predict(gp, what.encode(), test) == 0
+            out[k + f"predict/{what}/mean_efs"] = sget(test, "mean_efs")
+            if what != "mean":
+                out[k + f"predict/{what}/variance_efs"] = sget(test, "variance_efs")
+        for ki in range(len(descs)):
+            n = lib.ref_sgp_cluster_uncertainties(gp, test, ki, None)
+            u = np.zeros(n)
+            lib.ref_sgp_cluster_uncertainties(gp, test, ki, u.ctypes.data)
+            out[k + f"cluster_uncertainties/{ki}"] = u
+            out[k + f"mapping/{ki}"] = coeffs(lib.ref_sgp_mapping_coefficients, gp, ki)
+            if power == 1.0:
+                out[k + f"varmap/{ki}"] = coeffs(lib.ref_sgp_varmap_coefficients, gp, ki)
+        # new hyperparameters: each kernel's sigma and the noises changed
+        h2 = arr([s_ * 1.25 for s_ in sig] + [1.3, 1.7, 2.6])
+        lib.ref_sgp_set_hyperparameters(gp, h2.ctypes.data_as(D), len(h2))
+        out[k + "set_hyps/hyps"] = h2
+        out[k + "set_hyps/alpha"] = get(gp, "alpha")
+        out[k + "set_hyps/grad/value"] = np.array(
+            lib.ref_sgp_compute_likelihood_gradient_stable(gp))
+        out[k + "set_hyps/grad/likelihood_gradient"] = get(gp, "likelihood_gradient")
+        lib.ref_sgp_structure_free(test)
+        for s in strucs:
+            lib.ref_sgp_structure_free(s)
+        lib.ref_sgp_free(gp)
+        for (kind, _), d in zip(sc["descs"], descs):
+            (lib.ref_b2_free if kind == "B2" else lib.ref_b3_free)(d)
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "sgp_golden.npz"), **out)
+    print("wrote tests/golden/sgp_golden.npz")
+
+
 def main(ref_root=None):
     ref_root = ref_root or os.environ.get("FLARE_PP_REFERENCE", "/root/reference")
     subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), ref_root],
@@ -353,6 +498,7 @@ def main(ref_root=None):
     beta_form_golden(lib)
     struc_kernel_golden(lib)
     b3_golden(lib)
+    sgp_golden(lib)
 
 
 if __name__ == "__main__":
