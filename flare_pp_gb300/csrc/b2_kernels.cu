@@ -1418,7 +1418,7 @@ k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ r
 // those additions varies between runs, at the level of FP64 rounding).
 // ---------------------------------------------------------------------------
 struct KufLayout {
-  size_t ph, c, w, u, zz, aa, acc, pg, py, prel, ints, total;
+  size_t ph, c, w, u, zz, aa, acc, pg, py, prel, prh, ints, total;
 };
 
 __host__ __device__ inline KufLayout kuf_layout(const B2Args &a, int ks) {
@@ -1435,6 +1435,7 @@ __host__ __device__ inline KufLayout kuf_layout(const B2Args &a, int ks) {
   L.pg = o; o += 32 * 2 * (size_t)a.N;
   L.py = o; o += 32 * 4 * (size_t)a.H;
   L.prel = o; o += 32 * 4;
+  L.prh = o; o += 32 * 3;                    // unit vectors r / |r| of the window
   L.ints = o; o += (3 * 32 + 1) / 2 + 1;   // pj, psj, pkeep as ints
   L.total = o * sizeof(double);
   return L;
@@ -1454,7 +1455,7 @@ k_kuf_adjoint(const KufArgs k, int ks, int n_items, int item0) {
   const KufLayout L = kuf_layout(a, ks);
   double *ph = sm + L.ph, *c = sm + L.c, *w = sm + L.w, *u = sm + L.u;
   double *zz = sm + L.zz, *aa = sm + L.aa, *acc = sm + L.acc;
-  double *pg = sm + L.pg, *py = sm + L.py, *prel = sm + L.prel;
+  double *pg = sm + L.pg, *py = sm + L.py, *prel = sm + L.prel, *prh = sm + L.prh;
   int *pj = reinterpret_cast<int *>(sm + L.ints), *psj = pj + 32, *pkeep = psj + 32;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
@@ -1536,11 +1537,18 @@ k_kuf_adjoint(const KufArgs k, int ks, int n_items, int item0) {
           prel[4 * tid + 1] = rd.y;
           prel[4 * tid + 2] = rd.z;
           prel[4 * tid + 3] = rd.w;
+          // the unit vector once per pair (FP64 divisions are costly here)
+          const double ir = keep ? 1.0 / rd.x : 0.0;
+          prh[3 * tid + 0] = rd.y * ir;
+          prh[3 * tid + 1] = rd.z * ir;
+          prh[3 * tid + 2] = rd.w * ir;
+          // bases lane-fastest (stride 32): the warp's lanes read one
+          // coefficient of 32 different pairs from 32 consecutive doubles,
+          // free of shared-memory bank conflicts
           if (keep) {
-            radial_basis<double>(rd.x, a.r1, rcut, N, a.cutoff_kind, pg + tid * 2 * N,
-                                 pg + tid * 2 * N + N, 1);
-            real_harmonics<double>(rd.y, rd.z, rd.w, a.lmax, py + tid * 4 * H,
-                                   py + tid * 4 * H + H, 1);
+            radial_basis<double>(rd.x, a.r1, rcut, N, a.cutoff_kind, pg + tid,
+                                 pg + 32 * N + tid, 32);
+            real_harmonics<double>(rd.y, rd.z, rd.w, a.lmax, py + tid, py + 32 * H + tid, 32);
           }
         }
         __syncthreads();
@@ -1548,26 +1556,25 @@ k_kuf_adjoint(const KufArgs k, int ks, int n_items, int item0) {
         for (int kk = warp; kk < kc; kk += nwarp) {
           double f[3] = {0.0, 0.0, 0.0};
           if (lane < np && pkeep[lane]) {
-            const double *g = pg + lane * 2 * N, *dg = g + N;
-            const double *Y = py + lane * 4 * H, *dY = Y + H;
+            const double *g = pg + lane, *dg = pg + 32 * N + lane;      // stride 32
+            const double *Y = py + lane, *dY = py + 32 * H + lane;      // stride 32
             const double *ur = u + (size_t)kk * sb + (size_t)psj[lane] * N * H;
             double fr = 0.0;
             for (int lm = 0; lm < H; lm++) {
               double A = 0.0, B = 0.0;
               for (int n = 0; n < N; n++) {
                 const double uv = ur[n * H + lm];
-                A = fma(uv, g[n], A);
-                B = fma(uv, dg[n], B);
+                A = fma(uv, g[32 * n], A);
+                B = fma(uv, dg[32 * n], B);
               }
-              fr = fma(B, Y[lm], fr);
-              f[0] = fma(A, dY[3 * lm + 0], f[0]);
-              f[1] = fma(A, dY[3 * lm + 1], f[1]);
-              f[2] = fma(A, dY[3 * lm + 2], f[2]);
+              fr = fma(B, Y[32 * lm], fr);
+              f[0] = fma(A, dY[32 * (3 * lm + 0)], f[0]);
+              f[1] = fma(A, dY[32 * (3 * lm + 1)], f[1]);
+              f[2] = fma(A, dY[32 * (3 * lm + 2)], f[2]);
             }
-            const double r = prel[4 * lane];
-            f[0] = fma(fr, prel[4 * lane + 1] / r, f[0]);
-            f[1] = fma(fr, prel[4 * lane + 2] / r, f[1]);
-            f[2] = fma(fr, prel[4 * lane + 3] / r, f[2]);
+            f[0] = fma(fr, prh[3 * lane + 0], f[0]);
+            f[1] = fma(fr, prh[3 * lane + 1], f[1]);
+            f[2] = fma(fr, prh[3 * lane + 2], f[2]);
             const int cj = S.force_col[pj[lane]];
             double *krow = k.kuf + (size_t)(SP.row0 + k0 + kk) * k.n_labels;
             if (cj >= 0) {
