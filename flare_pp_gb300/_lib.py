@@ -50,6 +50,7 @@ SIGNATURES = {
     "fpp_b2_descriptors_noalloc": (_c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fpp_structure_set_skin": (_c_int, [_vp, _dbl, _vp]),
     "fpp_structure_neighbor_stats": (_c_int, [_vp, _P(_i64), _P(_i64), _P(_dbl)]),
+    "fpp_predict_mapped_batched": (_c_int, [_vp, _vp, _i32, _c_int, _vp, _vp, _vp, _vp]),
     "fpp_dgemm_nt": (_c_int, [_i32, _i32, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _vp]),
     "fpp_model_create": (_c_int, [_vp, _dbl, _dbl, _P(_vp)]),
     "fpp_model_destroy": (_c_int, [_vp]),

@@ -1064,6 +1064,24 @@ class SparseGP:
                 AE = AE + ae
         return (E, F, S, AE) if atom_energies else (E, F, S)
 
+    def predict_mapped_batched(self, structures, precision="mixed", stream=None):
+        """Energies (n,), forces (a list of (noa_k, 3)) and stresses (n, 6) of
+        a batch of structures of any sizes in one pass of the mapped form
+        (fpp_predict_mapped_batched: the structures' atoms packed into one
+        launch per stage)."""
+        self._ensure_mapped(stream)
+        n = len(structures)
+        counts = [s.noa for s in structures]
+        hs = (_lib.ctypes.c_void_p * max(1, n))(*[s.handle for s in structures])
+        E, F, S = np.zeros(n), np.zeros((sum(counts), 3)), np.zeros((n, 6))
+        e, f, st = np.zeros(n), np.zeros((sum(counts), 3)), np.zeros((n, 6))
+        for m in self._models:      # the kernels' contributions add
+            check(lib().fpp_predict_mapped_batched(m.handle, hs, n, PRECISIONS[precision],
+                                                   ptr(e), ptr(f), ptr(st), _stream(stream)))
+            E, F, S = E + e, F + f, S + st
+        offs = np.concatenate([[0], np.cumsum(counts)])
+        return E, [F[offs[k]:offs[k + 1]] for k in range(n)], S
+
     def center_mixed_on(self, structure, stream=None):
         """Centre the mixed-precision mapped form on this structure's mean
         environment per species (lowers its energy error on structures far

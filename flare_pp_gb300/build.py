@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libflare_pp_gb300.so")
 SOURCES = ["neighbors.cu", "b2_kernels.cu", "gemm_tc.cu", "kernel_form.cu",
            "capi_core.cu", "capi_predict.cu", "capi_pair.cu", "capi_solve.cu",
            "capi_noalloc.cu", "capi_struc.cu", "capi_std.cu",
-           "capi_likelihood.cu", "gemm_ozaki.cu", "capi_gemm.cu"]
+           "capi_likelihood.cu", "gemm_ozaki.cu", "capi_gemm.cu", "capi_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

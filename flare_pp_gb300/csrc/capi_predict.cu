@@ -457,7 +457,10 @@ int fpp_model_create(const fpp_b2 *b2, double sigma, double power, fpp_model **o
 
 int fpp_model_destroy(fpp_model *m) {
   if (m && m->cublas) cublasDestroy((cublasHandle_t)m->cublas);
-  if (m) delete m->lammps;
+  if (m) {
+    delete m->lammps;
+    delete m->batch;
+  }
   delete m;
   return FPP_OK;
 }

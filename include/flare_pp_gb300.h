@@ -340,6 +340,19 @@ int fpp_predict_mapped(fpp_model *m, fpp_structure *s, int precision,
                        double *energy, double *forces, double *stress,
                        double *atom_energies, int outputs_on_device,
                        void *stream);
+/* The mapped form of fpp_predict_mapped for a batch of structures of any
+ * sizes in one pass (the batched prediction that pair_flare / SparseGP
+ * callers otherwise loop over): the structures' atoms and neighbor lists are
+ * packed into one structure, so the forward pass, the contraction and the
+ * adjoint each run as one launch over all atoms; each structure's energy and
+ * virial are then summed over its own atoms and pairs.  energies: n_structures
+ * doubles; forces: 3 x (total atoms), the structures' atoms in order;
+ * stresses: 6 x n_structures (xx xy xz yy yz zz); host memory, each may be
+ * NULL.  Same precisions and results as fpp_predict_mapped per structure (up
+ * to the order of the sums).  Synchronizes the stream. */
+int fpp_predict_mapped_batched(fpp_model *m, fpp_structure *const *structures,
+                               int32_t n_structures, int precision, double *energies,
+                               double *forces, double *stresses, void *stream);
 
 /* Recentre the mixed form on a structure: pbar of every species with atoms in
  * s becomes the normalised mean of their unit descriptors (FP64 forward pass,

@@ -1,0 +1,77 @@
+"""fpp_predict_mapped_batched: a batch of uneven structures (a few to a few
+hundred atoms, two species, strained and rattled FCC cells) predicted in one
+pass of the mapped form equals the structure-by-structure prediction (FP64:
+to FP64 rounding; mixed: to the mixed form's own reproducibility), and the
+FP64 energies, forces and stresses equal the oracle's beta form."""
+import time
+
+import numpy as np
+import pytest
+
+import flare_pp_gb300 as fg
+from flare_pp_gb300 import synth
+from oracle import predict as opred
+from oracle.b2 import B2 as OB2
+from oracle.geometry import Structure as OStructure
+from oracle.kernel import NormalizedDotProduct as ONDP
+from tests import fixtures
+
+pytestmark = pytest.mark.gpu
+
+RC = 5.0
+
+
+@pytest.fixture(scope="module")
+def setup():
+    ob = OB2("chebyshev", "quadratic", [0, RC], [], [2, 6, 3])
+    frames = [synth.bcc_alloy((5, 5, 5), 950 + k, a=3.4) for k in range(2)]
+    fit = fixtures.site_energy_model(ob, frames, 60, sigma=2.0, power=2, seed=6)
+    gp, gb = fixtures.to_gpu_model((2, 6, 3, RC), fit["sparse"], fit["alpha"], 2.0, 2)
+    cells = synth.fcc_batch(n_structures=24, seed=808, lo=4, hi=256)
+    strucs = [fg.Structure(c, sp, p, RC) for c, sp, p in cells]
+    return dict(gp=gp, fit=fit, cells=cells, strucs=strucs)
+
+
+@pytest.mark.parametrize("precision,tol_e,tol_f", [("fp64", 1e-12, 1e-11),
+                                                   ("mixed", 1e-7, 1e-5)])
+def test_batched_equals_per_structure(gpu_lib, setup, precision, tol_e, tol_f):
+    gp, strucs = setup["gp"], setup["strucs"]
+    E, F, S = gp.predict_mapped_batched(strucs, precision)
+    for k, s in enumerate(strucs):
+        e, f, st = gp.predict_mapped(s, precision)
+        assert abs(E[k] - e) <= tol_e * max(1.0, abs(e)), (k, E[k], e)
+        np.testing.assert_allclose(F[k], f, rtol=0, atol=tol_f * max(1.0, np.abs(f).max()))
+        np.testing.assert_allclose(S[k], st, rtol=0, atol=tol_f * max(1e-3, np.abs(st).max()))
+
+
+def test_batched_fp64_matches_oracle(gpu_lib, setup):
+    gp, fit, cells, strucs = setup["gp"], setup["fit"], setup["cells"], setup["strucs"]
+    E, F, S = gp.predict_mapped_batched(strucs, "fp64")
+    st = fixtures.settings(2, 6, 3, RC)
+    B = opred.unpack_beta(ONDP(2.0, 2).compute_map_coeff_pow2(fit["sparse"], fit["alpha"]),
+                          fit["sparse"].n_descriptors)
+    for k in (0, 7, 23):
+        cell, sp, pos = cells[k]
+        ref = opred.beta_form(OStructure(cell, sp, pos, RC), st, B)
+        assert abs(E[k] - ref["energy"]) <= 1e-10 * max(1.0, abs(ref["energy"]))
+        np.testing.assert_allclose(F[k], ref["forces"], rtol=0,
+                                   atol=1e-9 * max(1.0, np.abs(ref["forces"]).max()))
+        np.testing.assert_allclose(S[k], ref["stress"], rtol=0,
+                                   atol=1e-9 * max(1e-3, np.abs(ref["stress"]).max()))
+
+
+def test_batched_timing(gpu_lib, setup):
+    gp, strucs = setup["gp"], setup["strucs"]
+    gp.predict_mapped_batched(strucs, "mixed")
+    t0 = time.perf_counter()
+    for _ in range(5):
+        gp.predict_mapped_batched(strucs, "mixed")
+    tb = (time.perf_counter() - t0) / 5
+    t0 = time.perf_counter()
+    for _ in range(5):
+        for s in strucs:
+            gp.predict_mapped(s, "mixed")
+    ts = (time.perf_counter() - t0) / 5
+    n = sum(s.noa for s in strucs)
+    print(f"batched mapped prediction of {len(strucs)} structures ({n} atoms): "
+          f"{1e3 * tb:.2f} ms batched, {1e3 * ts:.2f} ms one by one")
