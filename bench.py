@@ -367,6 +367,31 @@ def run_ours(args):
                        "vs_fp64_dgemm_rate": round(kf_tf / 1.10, 2)}
         res_kf = (float(mean[0]), mean[1:1 + 3 * noa].reshape(-1, 3).copy(),
                   mean[1 + 3 * noa:].copy(), None)
+    # ---- batched prediction: 256 uneven structures in one pass ----
+    batched = None
+    if rank == 0 and world == 1 and SETTINGS["kind"] == "B2" and not args.no_kuf:
+        from flare_pp_gb300 import Structure
+        from flare_pp_gb300 import synth as _synth
+        cells = _synth.fcc_batch(n_structures=256, seed=404, lo=32, hi=512)
+        strucs = [Structure(c, sp, p, SETTINGS["rcut"]) for c, sp, p in cells]
+        n_b = sum(s.noa for s in strucs)
+        gp.predict_mapped_batched(strucs, "mixed")    # warm (workspaces)
+        times = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            gp.predict_mapped_batched(strucs, "mixed")
+            times.append(time.perf_counter() - t0)
+        tb = float(np.median(times))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in strucs:
+            gp.predict_mapped(s, "mixed")
+        t1 = time.perf_counter() - t0
+        batched = {"what": "mapped E/F/S (mixed) of 256 FCC two-species cells of 32-512 "
+                           "atoms in one pass (fpp_predict_mapped_batched), host outputs",
+                   "structures": len(strucs), "atoms": int(n_b), "ms": round(1e3 * tb, 2),
+                   "atoms_per_s": round(n_b / tb, 1), "one_by_one_ms": round(1e3 * t1, 2)}
     cpu, err_oracle = None, None
     if rank == 0 and not args.no_cpu:
         forms = {"mixed": resmx, "fp64_gpu": res64}
@@ -417,6 +442,7 @@ def run_ours(args):
         "errors_vs_fp64_gpu": err_fp64,
         "variance": variance,
         "kernel_form": kernel_form,
+        "batched_prediction": batched,
         "kuf_batched": kuf,
         "gpu_launches": int(K * launches_per_step(SETTINGS["n_species"])),
         "clocks": clk,

@@ -19,31 +19,37 @@
 
 namespace fpp {
 
-__global__ void k_batch_pairs(long long np, int atom_off, long long pair_off,
-                              const int *__restrict__ nbr_i, const int *__restrict__ nbr_j,
-                              const int *__restrict__ nbr_s, const int *__restrict__ rev,
-                              const dvec4 *__restrict__ rel, const float4 *__restrict__ rel32,
-                              int *__restrict__ o_i, int *__restrict__ o_j,
-                              int *__restrict__ o_s, int *__restrict__ o_rev,
-                              dvec4 *__restrict__ o_rel, float4 *__restrict__ o_rel32) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  const long long q = pair_off + p;
-  o_i[q] = nbr_i[p] + atom_off;
-  o_j[q] = nbr_j[p] + atom_off;
-  o_s[q] = nbr_s[p];
-  o_rev[q] = rev[p] >= 0 ? (int)(rev[p] + pair_off) : -1;
-  o_rel[q] = rel[p];
-  o_rel32[q] = rel32[p];
-}
+// One structure's neighbor data and its place in the packed structure.
+struct BatchSrc {
+  const int *nbr_i, *nbr_j, *nbr_s, *rev, *offset, *species;
+  const dvec4 *rel;
+  const float4 *rel32;
+  int noa, atom_off;
+  long long np, pair_off;
+};
 
-__global__ void k_batch_atoms(int noa, int atom_off, int pair_off, const int *__restrict__ offset,
-                              const int *__restrict__ species, int *__restrict__ o_offset,
-                              int *__restrict__ o_species) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= noa) return;
-  o_offset[atom_off + i] = offset[i] + pair_off;
-  o_species[atom_off + i] = species[i];
+// blockIdx.y = structure; its pairs (shifted by its atom and pair offsets)
+// and atoms are copied into the packed arrays.
+__global__ void k_batch_pack(const BatchSrc *__restrict__ src, int *__restrict__ o_i,
+                             int *__restrict__ o_j, int *__restrict__ o_s,
+                             int *__restrict__ o_rev, dvec4 *__restrict__ o_rel,
+                             float4 *__restrict__ o_rel32, int *__restrict__ o_offset,
+                             int *__restrict__ o_species) {
+  const BatchSrc b = src[blockIdx.y];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < b.np; p += stride) {
+    const long long q = b.pair_off + p;
+    o_i[q] = b.nbr_i[p] + b.atom_off;
+    o_j[q] = b.nbr_j[p] + b.atom_off;
+    o_s[q] = b.nbr_s[p];
+    o_rev[q] = b.rev[p] >= 0 ? (int)(b.rev[p] + b.pair_off) : -1;
+    o_rel[q] = b.rel[p];
+    o_rel32[q] = b.rel32[p];
+  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < b.noa; i += stride) {
+    o_offset[b.atom_off + i] = b.offset[i] + (int)b.pair_off;
+    o_species[b.atom_off + i] = b.species[i];
+  }
 }
 
 // Per structure (a block each): out[10 s] = sum of its atom energies,
@@ -141,29 +147,41 @@ extern "C" int fpp_predict_mapped_batched(fpp_model *m, fpp_structure *const *st
     FPP_TRY(B.status.reserve(sizeof(DeviceStatus)));
     FPP_CUDA(cudaMemsetAsync(B.status.ptr, 0, sizeof(DeviceStatus), st));
   }
-  const int tb = 256;
+  std::vector<BatchSrc> src(n_structures);
+  long long max_work = 1;
   for (int k = 0; k < n_structures; k++) {
     StructureState &S = structures[k]->st;
-    if (S.noa > 0) {
-      k_batch_atoms<<<ceil_div(S.noa, tb), tb, 0, st>>>(
-          S.noa, aoff[k], (int)poff[k], S.nbr_offset.as<int>(), S.species.as<int>(),
-          B.nbr_offset.as<int>(), B.species.as<int>());
-      FPP_CUDA(cudaGetLastError());
-    }
-    if (S.n_pairs > 0) {
-      k_batch_pairs<<<(unsigned)((S.n_pairs + tb - 1) / tb), tb, 0, st>>>(
-          S.n_pairs, aoff[k], poff[k], S.nbr_i.as<int>(), S.nbr_j.as<int>(), S.nbr_s.as<int>(),
-          S.nbr_rev.as<int>(), S.nbr_rel.as<dvec4>(), S.nbr_rel32.as<float4>(),
-          B.nbr_i.as<int>(), B.nbr_j.as<int>(), B.nbr_s.as<int>(), B.nbr_rev.as<int>(),
-          B.nbr_rel.as<dvec4>(), B.nbr_rel32.as<float4>());
-      FPP_CUDA(cudaGetLastError());
-    }
+    BatchSrc &q = src[k];
+    q.nbr_i = S.nbr_i.as<int>();
+    q.nbr_j = S.nbr_j.as<int>();
+    q.nbr_s = S.nbr_s.as<int>();
+    q.rev = S.nbr_rev.as<int>();
+    q.offset = S.nbr_offset.as<int>();
+    q.species = S.species.as<int>();
+    q.rel = S.nbr_rel.as<dvec4>();
+    q.rel32 = S.nbr_rel32.as<float4>();
+    q.noa = S.noa;
+    q.atom_off = aoff[k];
+    q.np = S.n_pairs;
+    q.pair_off = poff[k];
+    max_work = std::max(max_work, std::max<long long>(S.n_pairs, S.noa));
+  }
+  FPP_TRY(m->batch_src.reserve(sizeof(BatchSrc) * n_structures));
+  FPP_CUDA(cudaMemcpyAsync(m->batch_src.ptr, src.data(), sizeof(BatchSrc) * n_structures,
+                           cudaMemcpyHostToDevice, st));
+  const int tb = 256;
+  const int bx = (int)std::min<long long>((max_work + tb - 1) / tb, 1024);
+  for (int c0 = 0; c0 < n_structures; c0 += 65535) {  // grid y holds 65535 structures
+    const int cy = std::min(65535, n_structures - c0);
+    k_batch_pack<<<dim3(bx, cy), tb, 0, st>>>(
+        m->batch_src.as<BatchSrc>() + c0, B.nbr_i.as<int>(), B.nbr_j.as<int>(),
+        B.nbr_s.as<int>(), B.nbr_rev.as<int>(), B.nbr_rel.as<dvec4>(),
+        B.nbr_rel32.as<float4>(), B.nbr_offset.as<int>(), B.species.as<int>());
+    FPP_CUDA(cudaGetLastError());
   }
   const int P32 = (int)P;
   FPP_CUDA(cudaMemcpyAsync(B.nbr_offset.as<int>() + N, &P32, sizeof(int),
                            cudaMemcpyHostToDevice, st));
-  // the packed structure must be complete before the host value P32 goes
-  FPP_CUDA(cudaStreamSynchronize(st));
   FPP_TRY(mapped_core(m, b, precision, st, 0));
   // per-structure energies and virials
   DevBuf &d_aoff = m->batch_aoff, &d_poff = m->batch_poff, &d_out = m->batch_sums;

@@ -82,7 +82,7 @@ struct fpp_model {
   int last_pair_batches = 0;            // atom batches of the last pair compute
   fpp::OzakiWork oz;                    // kernel-form GEMM workspace
   fpp_structure *batch = nullptr;       // packed structure of a batched prediction
-  fpp::DevBuf batch_aoff, batch_poff, batch_sums;
+  fpp::DevBuf batch_aoff, batch_poff, batch_sums, batch_src;
   // envs_struc workspace (grown on demand, kept between calls)
   fpp::DevBuf es_rown, es_ndm, es_flags, es_pos, es_scan, es_plist, es_qatom, es_dmap,
       es_dp, es_sfd, es_fd;
