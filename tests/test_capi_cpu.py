@@ -123,3 +123,32 @@ def test_std_atom_argument_errors(lib):
     assert lib.fpp_model_set_varmap(m, None) == _lib.FPP_ERR_INVALID
     lib.fpp_model_destroy(m)
     lib.fpp_b2_destroy(h)
+
+
+def test_new_entry_points_reject_bad_arguments(lib):
+    """The tensor-core FP64 GEMM, batched prediction, neighbor skin and Kuf
+    instrumentation entry points report argument errors before device work."""
+    from flare_pp_gb300 import _lib
+    A = np.zeros((4, 8))
+    C = np.zeros((4, 4))
+    # negative sizes, leading dimensions below K / N
+    assert lib.fpp_dgemm_nt(-1, 4, 8, A.ctypes.data, 8, A.ctypes.data, 8, C.ctypes.data, 4,
+                            0, None) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_dgemm_nt(4, 4, 8, A.ctypes.data, 4, A.ctypes.data, 8, C.ctypes.data, 4,
+                            0, None) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_dgemm_nt(4, 4, 8, A.ctypes.data, 8, A.ctypes.data, 8, C.ctypes.data, 2,
+                            0, None) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_dgemm_nt(4, 4, 8, None, 8, A.ctypes.data, 8, C.ctypes.data, 4,
+                            0, None) == _lib.FPP_ERR_INVALID
+    # empty products need no device: M = 0 is a no-op, K = 0 writes zeros
+    assert lib.fpp_dgemm_nt(0, 4, 8, None, 8, None, 8, None, 4, 0, None) == 0
+    C[:] = 7.0
+    assert lib.fpp_dgemm_nt(4, 4, 0, A.ctypes.data, 1, A.ctypes.data, 1, C.ctypes.data, 4,
+                            0, None) == 0
+    assert (C == 0).all()
+    # batched prediction, skin, Kuf statistics
+    assert lib.fpp_predict_mapped_batched(None, None, 1, 0, None, None, None, None) == \
+        _lib.FPP_ERR_INVALID
+    assert lib.fpp_structure_set_skin(None, 0.5, None) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_structure_neighbor_stats(None, None, None, None) == _lib.FPP_ERR_INVALID
+    assert lib.fpp_model_kuf_tiles(None, None, None, None, None) == _lib.FPP_ERR_INVALID

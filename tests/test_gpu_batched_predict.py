@@ -75,3 +75,30 @@ def test_batched_timing(gpu_lib, setup):
     n = sum(s.noa for s in strucs)
     print(f"batched mapped prediction of {len(strucs)} structures ({n} atoms): "
           f"{1e3 * tb:.2f} ms batched, {1e3 * ts:.2f} ms one by one")
+
+
+def test_batched_b3_equals_per_structure(gpu_lib):
+    """A single-species B3 model (N = 4, lmax = 3): the packed batch runs the
+    B3 forward and adjoint kernels unchanged."""
+    from oracle.b3 import B3 as OB3
+    ob = OB3("chebyshev", "quadratic", [0, RC], [], [1, 4, 3])
+    frames = [synth.fcc_al_108(515, k) for k in range(2)]
+    fit = fixtures.site_energy_model(ob, frames, 40, sigma=2.0, power=2, seed=8)
+    gp, _ = fixtures.to_gpu_model((1, 4, 3, RC), fit["sparse"], fit["alpha"], 2.0, 2,
+                                  kind="B3")
+    rng = np.random.default_rng(3)
+    strucs = []
+    for k in range(6):
+        cell, sp, pos = synth.fcc_al_108(516, k)
+        keep = np.sort(rng.choice(len(sp), 20 + 15 * k, replace=False)) if k % 2 else \
+            np.arange(len(sp))
+        strucs.append(fg.Structure(cell, sp[keep], pos[keep], RC))
+    for precision, tol_e, tol_f in (("fp64", 1e-12, 1e-11), ("mixed", 1e-7, 1e-5)):
+        E, F, S = gp.predict_mapped_batched(strucs, precision)
+        for k, s in enumerate(strucs):
+            e, f, st = gp.predict_mapped(s, precision)
+            assert abs(E[k] - e) <= tol_e * max(1.0, abs(e)), (precision, k)
+            np.testing.assert_allclose(F[k], f, rtol=0,
+                                       atol=tol_f * max(1.0, np.abs(f).max()))
+            np.testing.assert_allclose(S[k], st, rtol=0,
+                                       atol=tol_f * max(1e-3, np.abs(st).max()))
