@@ -12,7 +12,8 @@
 namespace fpp {
 
 int ozaki_dgemm_nt(int M, int N, int K, const double *A, long long lda, const double *B,
-                   long long ldb, double *C, long long ldc, OzakiWork &w, cudaStream_t st) {
+                   long long ldb, double *C, long long ldc, OzakiWork &w, cudaStream_t st,
+                   bool b_lower) {
   if (M <= 0 || N <= 0) return FPP_OK;
   if (K <= 0) return fail(FPP_ERR_INVALID, "GEMM with K <= 0");
   const OzakiShape sa = ozaki_shape(M, K), sb = ozaki_shape(N, K);
@@ -29,7 +30,7 @@ int ozaki_dgemm_nt(int M, int N, int K, const double *A, long long lda, const do
     return fail(FPP_ERR_CUDA, "digit-plane split launch failed");
   const int rc = launch_ozaki_gemm(M, N, K, w.a.as<__half>(), w.pa.as<double>(),
                                    w.b.as<__half>(), w.pb.as<double>(), C, ldc,
-                                   w.status.as<DeviceStatus>(), st);
+                                   w.status.as<DeviceStatus>(), st, b_lower);
   if (rc != 0) return fail(FPP_ERR_CUDA, "tensor-core FP64 GEMM launch failed (" +
                                              std::to_string(rc) + ")");
   return FPP_OK;

@@ -513,6 +513,15 @@ int fpp_model_set_R_inv(fpp_model *m, int32_t n, const double *R_inv) {
   FPP_TRY(m->R_inv.reserve(sizeof(double) * std::max(1, n) * std::max(1, n)));
   if (n) FPP_CUDA(cudaMemcpy(m->R_inv.ptr, R_inv, sizeof(double) * n * n, cudaMemcpyHostToDevice));
   m->has_R_inv = true;
+  // upper triangular (the QR solve's): the variance products skip its zeros
+  bool upper = true;
+  for (int i = 1; i < n && upper; i++)
+    for (int j = 0; j < i; j++)
+      if (R_inv[(size_t)i * n + j] != 0.0) {
+        upper = false;
+        break;
+      }
+  m->R_inv_upper = upper;
   return FPP_OK;
 }
 
@@ -1302,8 +1311,15 @@ int fpp_local_uncertainties(fpp_model *m, fpp_structure *s, const double *L_inv,
   FPP_CUDA(cudaMemcpyAsync(Ld.ptr, L_inv, sizeof(double) * (size_t)n * n,
                            cudaMemcpyHostToDevice, st));
   FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
+  bool lower = true;  // a Cholesky factor's inverse: its zeros are skipped
+  for (int i = 0; i < n && lower; i++)
+    for (int j = i + 1; j < n; j++)
+      if (L_inv[(size_t)i * n + j] != 0.0) {
+        lower = false;
+        break;
+      }
   FPP_TRY(ozaki_dgemm_nt(R, n, n, K.as<double>(), n, Ld.as<double>(), n, Q.as<double>(), n,
-                         m->oz, st));
+                         m->oz, st, lower));
   FPP_TRY(q.reserve(sizeof(double) * std::max(1, R)));
   if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
     return fail(FPP_ERR_CUDA, "row-norm launch failed");
@@ -1420,7 +1436,7 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
         const double *Lb = m->L_inv.as<double>() + (size_t)off * n + off;
         // Q[c][i] = sum_k K[c][k] L_inv[i][k] on the tensor cores
         FPP_TRY(ozaki_dgemm_nt(nsa, Ss, Ss, K.as<double>() + koff[sp], Ss, Lb, n,
-                               Q.as<double>() + koff[sp], Ss, m->oz, st));
+                               Q.as<double>() + koff[sp], Ss, m->oz, st, m->L_inv_lower));
         if (launch_row_sq(nsa, Ss, Q.as<double>() + koff[sp], Ss,
                           q.as<double>() + s->row_off[sp], st) != 0)
           return fail(FPP_ERR_CUDA, "row-norm launch failed");
@@ -1440,7 +1456,7 @@ int fpp_predict_energy_uncertainty(fpp_model *m, fpp_structure *s, double *energ
       }
       FPP_TRY(Q.reserve(sizeof(double) * (size_t)std::max(1, R) * std::max(1, n)));
       FPP_TRY(ozaki_dgemm_nt(R, n, n, Kf.as<double>(), n, m->L_inv.as<double>(), n,
-                             Q.as<double>(), n, m->oz, st));
+                             Q.as<double>(), n, m->oz, st, m->L_inv_lower));
       if (launch_row_sq(R, n, Q.as<double>(), n, q.as<double>(), st) != 0)
         return fail(FPP_ERR_CUDA, "row-norm launch failed");
     }
@@ -1514,7 +1530,7 @@ int fpp_predict(fpp_model *m, fpp_structure *s, double *mean_efs, double *varian
         launch_transpose(nst, nst, m->R_inv.as<double>(), nst, RT.as<double>(), nst, st) != 0)
       return fail(FPP_ERR_CUDA, "transpose launch failed");
     FPP_TRY(ozaki_dgemm_nt(n_out, nst, nst, KT.as<double>(), nst, RT.as<double>(), nst,
-                           V.as<double>(), nst, m->oz, st));
+                           V.as<double>(), nst, m->oz, st, m->R_inv_upper));
     if (launch_row_sq(n_out, nst, V.as<double>(), nst, var.as<double>(), st) != 0)
       return fail(FPP_ERR_CUDA, "variance launch failed");
     FPP_TRY(ozaki_check_status(m->oz, st));

@@ -67,11 +67,13 @@ struct fpp_model {
   int n_sparse_total = 0;
   fpp::DevBuf R_inv;                    // double[n * n]
   bool has_R_inv = false;
+  bool R_inv_upper = false;             // R_inv is upper triangular (as from the QR)
   // ComputeFlareStdAtom coefficients: L_inv (n x n, row-major lower
   // triangle) and the variance map (per species n_d x n_d, row-major)
   fpp::DevBuf L_inv;
   bool has_L_inv = false;
   bool L_inv_species_blocks = false;    // L_inv is zero across species blocks
+  bool L_inv_lower = false;             // L_inv is lower triangular
   fpp::DevBuf varmap;
   bool has_varmap = false;
   fpp_lammps_ws *lammps = nullptr;      // LAMMPS-array workspace
@@ -118,7 +120,9 @@ int kuf_tiles(fpp_model *m, const KufArgs &ka, int n_items, cudaStream_t st, int
 // exact fp16 digit planes (gemm_ozaki.cu); w holds the planes between calls.
 // Queued on st; ozaki_check_status synchronizes st and reports a bounded
 // wait that ran out.
+// b_lower: B is lower triangular (the zero blocks are skipped).
 int ozaki_dgemm_nt(int M, int N, int K, const double *A, long long lda, const double *B,
-                   long long ldb, double *C, long long ldc, OzakiWork &w, cudaStream_t st);
+                   long long ldb, double *C, long long ldc, OzakiWork &w, cudaStream_t st,
+                   bool b_lower = false);
 int ozaki_check_status(OzakiWork &w, cudaStream_t st);
 }  // namespace fpp

@@ -113,6 +113,14 @@ int fpp_model_set_L_inv(fpp_model *m, int32_t n, const double *L_inv) {
         }
   }
   m->L_inv_species_blocks = blocks;
+  bool lower = true;
+  for (int i = 0; i < n && lower; i++)
+    for (int j = i + 1; j < n; j++)
+      if (L_inv[(size_t)i * n + j] != 0.0) {
+        lower = false;
+        break;
+      }
+  m->L_inv_lower = lower;
   return FPP_OK;
 }
 

@@ -63,6 +63,7 @@ struct OzakiParams {
   CUtensorMap a, b;          // digit planes: rows s * Mp + m (s * Np + n), inner Kp
   int M, N, Mp, Np;
   int kblocks, n_chunks, tiles_n, n_tiles;
+  int b_lower;               // B lower triangular: tile n0 needs K < n0 + OBN only
   const double *pa, *pb;     // 2^e of each row of A and of B
   double *C;
   long long ldc;
@@ -111,10 +112,15 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  auto chunk_end = [&](int c) {
-    const int e = (c + 1) * kChunkBlocks;
+  // K blocks and chunks of a tile: all of K, or with a lower-triangular B
+  // (row n of B is zero beyond column n) only the blocks below n0 + OBN
+  auto tile_kb = [&](int t) {
+    if (!p.b_lower) return p.kblocks;
+    const int n0 = (t % p.tiles_n) * OBN;
+    const int e = (n0 + OBN + OBK - 1) / OBK;
     return e < p.kblocks ? e : p.kblocks;
   };
+  auto n_chunks_of = [&](int kbt) { return (kbt + kChunkBlocks - 1) / kChunkBlocks; };
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer ----------------
@@ -122,10 +128,12 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
     bool stop = false;
     for (int t = cid; t < p.n_tiles && !stop; t += ncta) {
       const int mrow = (t / p.tiles_n) * OBM, n0 = (t % p.tiles_n) * OBN;
+      const int kbt = tile_kb(t), nch = n_chunks_of(kbt);
       for (int L = 0; L < kOzakiDigits && !stop; L++)
-        for (int c = 0; c < p.n_chunks && !stop; c++)
+        for (int c = 0; c < nch && !stop; c++) {
+          const int kb1 = min((c + 1) * kChunkBlocks, kbt);
           for (int s = 0; s <= L && !stop; s++)
-            for (int kb = c * kChunkBlocks; kb < chunk_end(c); kb++, it++) {
+            for (int kb = c * kChunkBlocks; kb < kb1; kb++, it++) {
               const int st = it % OSTAGES;
               const uint32_t ph = (uint32_t)((it / OSTAGES) & 1);
               if (!mbar_wait(empty_bar(st), ph ^ 1u)) {
@@ -141,6 +149,7 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
               tma_load_2d(sa, &p.a, full_bar(st), kb * OBK, s * p.Mp + mrow);
               tma_load_2d(sa + OA_TILE, &p.b, full_bar(st), kb * OBK, (L - s) * p.Np + n0);
             }
+        }
     }
     // drain: every stage this CTA filled has been read before it exits
     for (int d = 0; d < OSTAGES && !*abort_flag; d++, it++) {
@@ -153,9 +162,11 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
     // ---------------- MMA issuer ----------------
     int it = 0, j = 0;
     bool stop = false;
-    for (int t = cid; t < p.n_tiles && !stop; t += ncta)
+    for (int t = cid; t < p.n_tiles && !stop; t += ncta) {
+      const int kbt = tile_kb(t), nch = n_chunks_of(kbt);
       for (int L = 0; L < kOzakiDigits && !stop; L++)
-        for (int c = 0; c < p.n_chunks && !stop; c++, j++) {
+        for (int c = 0; c < nch && !stop; c++, j++) {
+          const int kb1 = min((c + 1) * kChunkBlocks, kbt);
           const int buf = j % OACC;
           const uint32_t acc = tmem + (uint32_t)(buf * OBN);
           if (!mbar_wait(acce_bar(buf), (uint32_t)(((j / OACC) & 1) ^ 1))) {
@@ -170,7 +181,7 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           bool first = true;
           for (int s = 0; s <= L && !stop; s++)
-            for (int kb = c * kChunkBlocks; kb < chunk_end(c); kb++, it++) {
+            for (int kb = c * kChunkBlocks; kb < kb1; kb++, it++) {
               const int st = it % OSTAGES;
               const uint32_t ph = (uint32_t)((it / OSTAGES) & 1);
               if (!mbar_wait(full_bar(st), ph)) {
@@ -192,6 +203,7 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
             }
           mma_commit(accf_bar(buf));
         }
+    }
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
     const int q = warp & 3;                 // TMEM lane quarter this warp may access
@@ -202,13 +214,14 @@ k_ozaki_gemm(const __grid_constant__ OzakiParams p) {
     for (int t = cid; t < p.n_tiles && !stop; t += ncta) {
       const int mrow = (t / p.tiles_n) * OBM, n0 = (t % p.tiles_n) * OBN + half * 64;
       const int r = mrow + q * 32 + lane;
+      const int nch = n_chunks_of(tile_kb(t));
       double acc[64];
 #pragma unroll
       for (int i = 0; i < 64; i++) acc[i] = 0.0;
       for (int L = 0; L < kOzakiDigits && !stop; L++) {
         // 2^(-5 (L + 2)), exact
         const double sL = __longlong_as_double((long long)(1023 - 5 * (L + 2)) << 52);
-        for (int c = 0; c < p.n_chunks; c++, j++) {
+        for (int c = 0; c < nch; c++, j++) {
           const int buf = j % OACC;
           bool have = mbar_wait(accf_bar(buf), (uint32_t)((j / OACC) & 1));
           have = __all_sync(0xffffffffu, have) != 0;
@@ -336,7 +349,7 @@ int launch_ozaki_split(int rows, int K, const double *X, long long ldx, __half *
 
 int launch_ozaki_gemm(int M, int N, int K, const __half *a_planes, const double *pa,
                       const __half *b_planes, const double *pb, double *C, long long ldc,
-                      DeviceStatus *status, cudaStream_t stream) {
+                      DeviceStatus *status, cudaStream_t stream, bool b_lower) {
   if (M <= 0 || N <= 0) return 0;
   if (K <= 0) return -2;
   const OzakiShape sa = ozaki_shape(M, K), sb = ozaki_shape(N, K);
@@ -353,6 +366,7 @@ int launch_ozaki_gemm(int M, int N, int K, const __half *a_planes, const double 
   p.Np = sb.rows_pad;
   p.kblocks = sa.k_pad / OBK;
   p.n_chunks = (p.kblocks + kChunkBlocks - 1) / kChunkBlocks;
+  p.b_lower = b_lower ? 1 : 0;
   p.tiles_n = (N + OBN - 1) / OBN;
   p.n_tiles = (sa.rows_pad / OBM) * p.tiles_n;
   p.pa = pa;

@@ -29,9 +29,12 @@ int launch_ozaki_split(int rows, int K, const double *X, long long ldx, __half *
                        double *p2, cudaStream_t stream);
 
 // C (M x N, row stride ldc) = A B^T from the digit planes and powers of two
-// of A (M x K) and B (N x K).  C need not be initialised.  0 on success.
+// of A (M x K) and B (N x K).  C need not be initialised.  b_lower: B is
+// lower triangular (B[n][k] = 0 for k > n; an L^-1, or an R^-1 transposed),
+// and the K blocks above each column tile's last row are skipped.  0 on
+// success.
 int launch_ozaki_gemm(int M, int N, int K, const __half *a_planes, const double *pa,
                       const __half *b_planes, const double *pb, double *C, long long ldc,
-                      DeviceStatus *status, cudaStream_t stream);
+                      DeviceStatus *status, cudaStream_t stream, bool b_lower = false);
 
 }  // namespace fpp
