@@ -24,6 +24,7 @@
 #include "b2_kernels.h"
 #include "b3.cuh"
 #include "common.cuh"
+#include "tc_prims.cuh"
 
 namespace fpp {
 
@@ -596,6 +597,95 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
   }
 }
 
+// The mixed power-2 w = dE/dp and energy of one atom from its rows of V and of
+// the split operand (global or shared memory): four consecutive entries per
+// lane, 16-byte (8-byte for the fp16 planes) loads, |p| and E as float-float.
+// Every entry is stored by the lane that read it, so store may overwrite V4
+// in place.
+template <typename T, typename Store>
+__device__ __forceinline__ double w_mixed2(const AdjArgs &g, int si, int nd, float2 nrm32,
+                                           const float4 *V4, const uint2 *H4,
+                                           const uint2 *L4, Store store, int lane) {
+  double e;
+  const bool empty = nrm32.x * nrm32.x < g.empty_thresh_f;
+  const int nq = nd >> 2;
+  const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
+  const float4 *B4 = reinterpret_cast<const float4 *>(g.pbar + (size_t)si * nd);
+  auto deltas = [&](uint2 h, uint2 l, float (&dl)[4]) {
+    const float2 h01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
+    const float2 h23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
+    const float2 l01 = __half22float2(*reinterpret_cast<const __half2 *>(&l.x));
+    const float2 l23 = __half22float2(*reinterpret_cast<const __half2 *>(&l.y));
+    dl[0] = (h01.x + l01.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+    dl[1] = (h01.y + l01.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+    dl[2] = (h23.x + l23.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+    dl[3] = (h23.y + l23.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
+  };
+  // loads of kU iterations are issued before any of them is used (one atom's
+  // rows are a few KB: the loop is latency-bound without this)
+  constexpr int kU = 4;
+  Acc<float> acc;
+  for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
+    uint2 h[kU], l[kU];
+    float4 v[kU], gg[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int q = q0 + 32 * u;
+      if (q < nq) {
+        h[u] = H4[q];
+        l[u] = L4[q];
+        v[u] = V4[q];
+        gg[u] = G4[q];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (q0 + 32 * u < nq) {
+        float dl[4];
+        deltas(h[u], l[u], dl);
+        acc.add((2.0f * gg[u].x + v[u].x) * dl[0]);
+        acc.add((2.0f * gg[u].y + v[u].y) * dl[1]);
+        acc.add((2.0f * gg[u].z + v[u].z) * dl[2]);
+        acc.add((2.0f * gg[u].w + v[u].w) * dl[3]);
+      }
+    }
+  }
+  float hi = acc.s, lo = acc.c;
+  ff_warp_sum(hi, lo);
+  const ff et = ff_add(ff_norm(hi, lo), ff{g.c0_hi[si], g.c0_lo[si]});
+  const float ef = empty ? 0.0f : et.hi + et.lo;
+  const float inv = empty ? 0.0f : 1.0f / nrm32.x;
+  e = empty ? 0.0 : double(et.hi) + double(et.lo);
+  for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
+    uint2 h[kU], l[kU];
+    float4 v[kU], gg[kU], pb[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int q = q0 + 32 * u;
+      if (q < nq) {
+        h[u] = H4[q];
+        l[u] = L4[q];
+        v[u] = V4[q];
+        gg[u] = G4[q];
+        pb[u] = B4[q];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int q = q0 + 32 * u;
+      if (q < nq) {
+        float dl[4];
+        deltas(h[u], l[u], dl);
+        store(4 * q + 0, T(2.0f * ((gg[u].x + v[u].x) - ef * (pb[u].x + dl[0])) * inv));
+        store(4 * q + 1, T(2.0f * ((gg[u].y + v[u].y) - ef * (pb[u].y + dl[1])) * inv));
+        store(4 * q + 2, T(2.0f * ((gg[u].z + v[u].z) - ef * (pb[u].z + dl[2])) * inv));
+        store(4 * q + 3, T(2.0f * ((gg[u].w + v[u].w) - ef * (pb[u].w + dl[3])) * inv));
+      }
+    }
+  }
+  return e;
+}
+
 // w = dE/dp of one atom into w_s[nd] (all lanes), returning the atom energy:
 // from the contraction V (mapped power 2), the beta vector (power 1), or
 // given per operand row (kernel form).
@@ -625,87 +715,12 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
         store(d, T((g.beta1[(size_t)si * nd + d] - e * ph) * inv));
     }
   } else if (g.mode == kWFromV2 && (nd & 3) == 0) {
-    // the mixed power-2 form below, four consecutive entries per lane and
-    // 16-byte (8-byte for the fp16 planes) loads; |p| and E as float-float
-    const bool empty = nrm32.x * nrm32.x < g.empty_thresh_f;
-    const int nq = nd >> 2;
-    const float4 *V4 = reinterpret_cast<const float4 *>(g.V32 + (size_t)row * g.ldv);
-    const float4 *G4 = reinterpret_cast<const float4 *>(g.gvec + (size_t)si * nd);
-    const float4 *B4 = reinterpret_cast<const float4 *>(g.pbar + (size_t)si * nd);
-    const uint2 *H4 = reinterpret_cast<const uint2 *>(g.phat_hi + (size_t)row * g.ldp);
-    const uint2 *L4 = reinterpret_cast<const uint2 *>(g.phat_lo + (size_t)row * g.ldp);
-    auto deltas = [&](uint2 h, uint2 l, float (&dl)[4]) {
-      const float2 h01 = __half22float2(*reinterpret_cast<const __half2 *>(&h.x));
-      const float2 h23 = __half22float2(*reinterpret_cast<const __half2 *>(&h.y));
-      const float2 l01 = __half22float2(*reinterpret_cast<const __half2 *>(&l.x));
-      const float2 l23 = __half22float2(*reinterpret_cast<const __half2 *>(&l.y));
-      dl[0] = (h01.x + l01.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[1] = (h01.y + l01.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[2] = (h23.x + l23.x * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-      dl[3] = (h23.y + l23.y * (1.0f / 2048.0f)) * (1.0f / 8192.0f);
-    };
-    // loads of kU iterations are issued before any of them is used (one atom's
-    // rows are a few KB: the loop is latency-bound without this)
-    constexpr int kU = 4;
-    Acc<float> acc;
-    for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
-      uint2 h[kU], l[kU];
-      float4 v[kU], gg[kU];
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        const int q = q0 + 32 * u;
-        if (q < nq) {
-          h[u] = H4[q];
-          l[u] = L4[q];
-          v[u] = V4[q];
-          gg[u] = G4[q];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        if (q0 + 32 * u < nq) {
-          float dl[4];
-          deltas(h[u], l[u], dl);
-          acc.add((2.0f * gg[u].x + v[u].x) * dl[0]);
-          acc.add((2.0f * gg[u].y + v[u].y) * dl[1]);
-          acc.add((2.0f * gg[u].z + v[u].z) * dl[2]);
-          acc.add((2.0f * gg[u].w + v[u].w) * dl[3]);
-        }
-      }
-    }
-    float hi = acc.s, lo = acc.c;
-    ff_warp_sum(hi, lo);
-    const ff et = ff_add(ff_norm(hi, lo), ff{g.c0_hi[si], g.c0_lo[si]});
-    const float ef = empty ? 0.0f : et.hi + et.lo;
-    const float inv = empty ? 0.0f : 1.0f / nrm32.x;
-    e = empty ? 0.0 : double(et.hi) + double(et.lo);
-    for (int q0 = lane; q0 < nq; q0 += 32 * kU) {
-      uint2 h[kU], l[kU];
-      float4 v[kU], gg[kU], pb[kU];
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        const int q = q0 + 32 * u;
-        if (q < nq) {
-          h[u] = H4[q];
-          l[u] = L4[q];
-          v[u] = V4[q];
-          gg[u] = G4[q];
-          pb[u] = B4[q];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        const int q = q0 + 32 * u;
-        if (q < nq) {
-          float dl[4];
-          deltas(h[u], l[u], dl);
-          store(4 * q + 0, T(2.0f * ((gg[u].x + v[u].x) - ef * (pb[u].x + dl[0])) * inv));
-          store(4 * q + 1, T(2.0f * ((gg[u].y + v[u].y) - ef * (pb[u].y + dl[1])) * inv));
-          store(4 * q + 2, T(2.0f * ((gg[u].z + v[u].z) - ef * (pb[u].z + dl[2])) * inv));
-          store(4 * q + 3, T(2.0f * ((gg[u].w + v[u].w) - ef * (pb[u].w + dl[3])) * inv));
-        }
-      }
-    }
+    // the mixed power-2 form, rows read from global memory
+    e = w_mixed2<T>(g, si, nd, nrm32,
+                    reinterpret_cast<const float4 *>(g.V32 + (size_t)row * g.ldv),
+                    reinterpret_cast<const uint2 *>(g.phat_hi + (size_t)row * g.ldp),
+                    reinterpret_cast<const uint2 *>(g.phat_lo + (size_t)row * g.ldp), store,
+                    lane);
   } else if (g.mode == kWFromV2 || g.mode == kWFromV1) {
     // mixed form on the centred operand delta = phat - pbar (float):
     //   power 2: E = c0 + sum_d (2 g_d + V_d) delta_d,  V = beta delta,
@@ -747,42 +762,14 @@ __device__ __forceinline__ double adjoint_w(const B2Args &a, const AdjArgs &g, i
   return e;
 }
 
-// ---------------------------------------------------------------------------
-// Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
-// u = dE/dc = (W + W^T) c per l, written to global memory.
-// ---------------------------------------------------------------------------
+// u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm] of one atom from its
+// packed w (n1 <= n2, l fastest) and c rows in shared memory; lane owns lm.
 template <typename T, typename SH>
-__global__ void __launch_bounds__(128)
-k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
-        const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
-        const T *__restrict__ c_in, const double *__restrict__ norm_in,
-        double *__restrict__ atom_e, T *__restrict__ u_out) {
-  (void)pair_tab;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nwarps = blockDim.x >> 5;
-  const int atom = blockIdx.x * nwarps + warp;
+__device__ __forceinline__ void b2_u_columns(const B2Args &a, const T *w_s, const T *c_s,
+                                             T *u_row, int lane) {
   const int N = SH::N(a), LMAX = SH::lmax(a), H = (LMAX + 1) * (LMAX + 1), NS = SH::NS(a);
-  const int nd = a.n_d;
-  const int sb = NS * N * H, nr = NS * N;
+  const int nr = NS * N;
   const int L1 = LMAX + 1;
-  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
-  T *w_s = reinterpret_cast<T *>(base);  // [nd]
-  T *c_s = w_s + nd;                     // [sb]
-  if (atom >= a.noa) return;
-  const int si = species[atom];
-  const int row = row_of_atom[atom];
-  // FP32 kernels: the forward stored |p| as a float-float pair
-  const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
-  const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
-                                      : make_float2(0.0f, 0.0f);
-#pragma unroll 4
-  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
-  const double e =
-      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
-  if (lane == 0) atom_e[atom] = e;
-  __syncwarp();
-  // u[n1, lm] = sum_n2 (W + W^T)[n1, n2, l] c[n2, lm]; lane owns lm
   for (int lm0 = 0; lm0 < H; lm0 += 32) {
     const int lm = lm0 + lane;
     if (lm >= H) continue;
@@ -849,7 +836,7 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
           }
       }
 #pragma unroll
-      for (int n1 = 0; n1 < NR; n1++) u_out[(size_t)atom * sb + n1 * H + lm] = acc[n1];
+      for (int n1 = 0; n1 < NR; n1++) u_row[n1 * H + lm] = acc[n1];
     } else {
       for (int n1 = 0; n1 < nr; n1++) {
         T acc = T(0);
@@ -864,10 +851,120 @@ k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
         acc += T(2) * w_s[q * L1 + l] * c_s[n1 * H + lm];
         for (int n2 = n1 + 1; n2 < nr; n2++)
           acc += w_s[(q + n2 - n1) * L1 + l] * c_s[n2 * H + lm];
-        u_out[(size_t)atom * sb + n1 * H + lm] = acc;
+        u_row[n1 * H + lm] = acc;
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint, part 1 (one warp per atom): w = dE/dp and the atom energy, then
+// u = dE/dc = (W + W^T) c per l, written to global memory.
+// ---------------------------------------------------------------------------
+template <typename T, typename SH>
+__global__ void __launch_bounds__(128)
+k_b2_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
+        const int *__restrict__ row_of_atom, const int *__restrict__ pair_tab,
+        const T *__restrict__ c_in, const double *__restrict__ norm_in,
+        double *__restrict__ atom_e, T *__restrict__ u_out) {
+  (void)pair_tab;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int atom = blockIdx.x * nwarps + warp;
+  const int N = SH::N(a), LMAX = SH::lmax(a), H = (LMAX + 1) * (LMAX + 1), NS = SH::NS(a);
+  const int nd = a.n_d;
+  const int sb = NS * N * H;
+  unsigned char *base = smem_raw + a.smem_per_warp_adj * warp;
+  T *w_s = reinterpret_cast<T *>(base);  // [nd]
+  T *c_s = w_s + nd;                     // [sb]
+  if (atom >= a.noa) return;
+  const int si = species[atom];
+  const int row = row_of_atom[atom];
+  // FP32 kernels: the forward stored |p| as a float-float pair
+  const double nrm = sizeof(T) == 8 ? norm_in[atom] : 0.0;
+  const float2 nrm32 = sizeof(T) == 4 ? reinterpret_cast<const float2 *>(norm_in)[atom]
+                                      : make_float2(0.0f, 0.0f);
+#pragma unroll 4
+  for (int k = lane; k < sb; k += 32) c_s[k] = c_in[(size_t)atom * sb + k];
+  const double e =
+      adjoint_w<T>(a, g, si, row, nrm, nrm32, [&](int d, T v) { w_s[d] = v; }, lane);
+  if (lane == 0) atom_e[atom] = e;
+  __syncwarp();
+  b2_u_columns<T, SH>(a, w_s, c_s, u_out + (size_t)atom * sb, lane);
+}
+
+// Per-warp shared memory of the staged adjoint (byte offsets, 16-byte
+// aligned): the atom's V row (overwritten in place by w), the hi and lo rows of
+// its split operand (nd fp16 each, copied rounded up to 16 bytes), its c row,
+// and the mbarrier the copies complete on.
+struct WuStaged {
+  uint32_t hi, lo, c, bar, total, hbytes;
+};
+
+__host__ __device__ inline WuStaged wu_staged_layout(int nd, int sb) {
+  WuStaged L;
+  L.hbytes = ((uint32_t)nd * 2u + 15u) & ~15u;
+  L.hi = (uint32_t)nd * 4u;
+  L.lo = L.hi + L.hbytes;
+  L.c = L.lo + L.hbytes;
+  L.bar = L.c + (uint32_t)sb * 4u;
+  L.total = (L.bar + 8u + 15u) & ~15u;
+  return L;
+}
+
+// The mixed power-2 adjoint, part 1, with the atom's rows staged: one lane
+// starts bulk asynchronous copies of the V row, both split-operand rows and
+// the c row (about 14 KB for n_d = 1500) into the warp's shared memory, all
+// completing on one mbarrier, so every warp keeps its whole row in flight at
+// once; then the same arithmetic as k_b2_wu from shared memory.  The wait is
+// bounded: when it runs out the warp records FPP_ERR_TIMEOUT, waits (bounded)
+// once more for its copies and returns without outputs.
+template <typename SH>
+__global__ void __launch_bounds__(128)
+k_b2_wu_staged(B2Args a, AdjArgs g, const int *__restrict__ species,
+               const int *__restrict__ row_of_atom, const float *__restrict__ c_in,
+               const double *__restrict__ norm_in, double *__restrict__ atom_e,
+               float *__restrict__ u_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int atom = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (atom >= a.noa) return;
+  const int nd = a.n_d;
+  const int sb = SH::kNR * SH::kL1 * SH::kL1;
+  const WuStaged Ly = wu_staged_layout(nd, sb);
+  unsigned char *base = smem_raw + (size_t)Ly.total * warp;
+  float *v_s = reinterpret_cast<float *>(base);
+  const uint32_t bar = smem_u32(base + Ly.bar);
+  const int si = species[atom];
+  const int row = row_of_atom[atom];
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(bar, (uint32_t)nd * 4u + 2u * Ly.hbytes + (uint32_t)sb * 4u);
+    bulk_load(smem_u32(v_s), g.V32 + (size_t)row * g.ldv, (uint32_t)nd * 4u, bar);
+    bulk_load(smem_u32(base + Ly.hi), g.phat_hi + (size_t)row * g.ldp, Ly.hbytes, bar);
+    bulk_load(smem_u32(base + Ly.lo), g.phat_lo + (size_t)row * g.ldp, Ly.hbytes, bar);
+    bulk_load(smem_u32(base + Ly.c), c_in + (size_t)atom * sb, (uint32_t)sb * 4u, bar);
+  }
+  __syncwarp();
+  const float2 nrm32 = reinterpret_cast<const float2 *>(norm_in)[atom];
+  bool ok = mbar_wait(bar, 0);
+  ok = __all_sync(0xffffffffu, ok) != 0;
+  if (!ok) {
+    if (lane == 0) set_status(g.status, FPP_ERR_TIMEOUT, 221, atom);
+    mbar_wait(bar, 0);
+    return;
+  }
+  const double e = w_mixed2<float>(
+      g, si, nd, nrm32, reinterpret_cast<const float4 *>(v_s),
+      reinterpret_cast<const uint2 *>(base + Ly.hi), reinterpret_cast<const uint2 *>(base + Ly.lo),
+      [&](int d, float v) { v_s[d] = v; }, lane);
+  if (lane == 0) atom_e[atom] = e;
+  __syncwarp();
+  b2_u_columns<float, SH>(a, v_s, reinterpret_cast<const float *>(base + Ly.c),
+                          u_out + (size_t)atom * sb, lane);
+  if (lane == 0) mbar_inval(bar);
 }
 
 // ---------------------------------------------------------------------------
@@ -1836,7 +1933,30 @@ int launch_b2_adjoint(B2Args a, const AdjArgs &g, const Neigh &nb,
                                                             u_buf);
   } else {
     const int rc = with_shape<T>(a, [&](auto sh) {
-      auto kern = k_b2_wu<T, decltype(sh)>;
+      using SH = decltype(sh);
+      if constexpr (sizeof(T) == 4 && SH::kNR > 0 && SH::kL1 > 0) {
+        // the mixed power-2 form with every row a whole number of 16-byte
+        // units at 16-byte aligned addresses: the staged kernel
+        const int sb = SH::kNR * SH::kL1 * SH::kL1;
+        auto al16 = [](const void *q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+        if (g.mode == kWFromV2 && !g.phat64 && g.V32 && g.phat_hi && g.phat_lo &&
+            (a.n_d & 3) == 0 && (g.ldv & 3) == 0 && (g.ldp & 7) == 0 &&
+            2 * g.ldp >= (int)wu_staged_layout(a.n_d, sb).hbytes && (sb & 3) == 0 &&
+            al16(g.V32) && al16(g.phat_hi) && al16(g.phat_lo) && al16(c_in)) {
+          const size_t per = wu_staged_layout(a.n_d, sb).total;
+          const int w = warps_per_block(per);
+          if (w == 0) return -1;
+          auto ks = k_b2_wu_staged<SH>;
+          if (cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(per * w)) != cudaSuccess)
+            return -1;
+          ks<<<ceil_div(a.noa, w), 32 * w, per * w, stream>>>(
+              a, g, species, row_of_atom, reinterpret_cast<const float *>(c_in), norm_in,
+              atom_e, reinterpret_cast<float *>(u_buf));
+          return 0;
+        }
+      }
+      auto kern = k_b2_wu<T, SH>;
       if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem) != cudaSuccess)
         return -1;

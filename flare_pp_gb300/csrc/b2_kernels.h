@@ -68,6 +68,7 @@ struct AdjArgs {
   // given dE/dp and energies per operand row (row stride ldp)
   const double *w_given;
   const double *e_given;
+  DeviceStatus *status;  // staged adjoint: where a wait that ran out is recorded
 };
 
 struct Neigh {

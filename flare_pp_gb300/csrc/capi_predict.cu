@@ -804,6 +804,7 @@ int mapped_core(fpp_model *m, fpp_structure *s, int precision, cudaStream_t st,
   g.ldp = ldp;
   g.ldv = ldp;
   g.beta1 = m->beta1.as<double>();
+  g.status = S.status.as<DeviceStatus>();
   S.mark(2, st);
   if (precision == FPP_PREC_FP64) {
     FPP_TRY(forward64(s, a, m->pair_tab.as<int>(), false, st));
