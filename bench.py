@@ -87,18 +87,107 @@ def replica_value(n_atoms, steps, ms_total, world):
     return world * n_atoms * steps / (ms_total / 1e3)
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (the driver's
+    libnvidia-ml, by ctypes) about every millisecond on a host thread, so that
+    even a timed region of a few tens of milliseconds holds many samples.
+    Reads only; the device is matched to the CUDA device by UUID."""
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown",
+               0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, dev):
+        import ctypes
+        import torch
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        props = torch.cuda.get_device_properties(dev)
+        found = False
+        uuid = str(getattr(props, "uuid", ""))
+        if uuid:
+            uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            found = self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(self.h)) == 0
+        if not found and hasattr(props, "pci_bus_id"):
+            bus = "%08x:%02x:%02x.0" % (getattr(props, "pci_domain_id", 0), props.pci_bus_id,
+                                        props.pci_device_id)
+            found = self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(),
+                                                              ctypes.byref(self.h)) == 0
+        if not found:
+            n = ctypes.c_uint()
+            if self.lib.nvmlDeviceGetCount_v2(ctypes.byref(n)) == 0 and n.value == 1:
+                found = self.lib.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(self.h)) == 0
+        if not found:
+            raise OSError("no NVML device matches CUDA device %s" % dev)
+        try:
+            self.reason_fn = self.lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reason_fn = self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx))   # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.samples = []
+        self.stop_flag = False
+
+    def read(self):
+        clk, rs = self.ct.c_uint(), self.ct.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.ct.byref(clk)) != 0:
+            return None
+        self.reason_fn(self.h, self.ct.byref(rs))
+        return float(clk.value), int(rs.value)
+
+    def _run(self):
+        while not self.stop_flag:
+            r = self.read()
+            if r is not None:
+                self.samples.append((time.perf_counter(),) + r)
+            time.sleep(0.001)
+
+    def start(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def stop(self, b, e):
+        self.stop_flag = True
+        self.t.join(timeout=2.0)
+        inside = [x for x in self.samples if b <= x[0] <= e]
+        window = "timed steps (NVML, ~1 ms period)"
+        if not inside and self.samples:
+            inside = [min(self.samples, key=lambda x: min(abs(x[0] - b), abs(x[0] - e)))]
+            window = "adjacent to the timed steps (NVML)"
+        reasons = sorted({nm for _, _, rs in inside for bit, nm in self.REASONS.items()
+                          if rs & bit})
+        self.lib.nvmlShutdown()
+        return {"sm_mhz": float(np.median([c for _, c, _ in inside])) if inside else None,
+                "sm_max_mhz": self.max_mhz, "reasons": reasons, "samples": len(inside),
+                "window": window, "source": "nvml"}
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """Clocks and throttle reasons sampled during the timed region: NVML every
+    ~1 ms where the driver library loads, else nvidia-smi every 100 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, dev=None):
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.nvml = None
+        self.nvml_error = None
+        if dev is not None:
+            try:
+                self.nvml = NvmlClocks(dev)
+            except Exception as ex:  # no driver library or no match: nvidia-smi
+                self.nvml = None
+                self.nvml_error = str(ex)[:120]
 
     def start(self):
+        if self.nvml is not None:
+            self.nvml.start()
+            return
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
@@ -115,7 +204,8 @@ class ClockSampler:
 
     def wait_first(self, limit_s):
         t0 = time.perf_counter()
-        while self.proc is not None and not self.lines and time.perf_counter() - t0 < limit_s:
+        while (self.nvml is None and self.proc is not None and not self.lines
+               and time.perf_counter() - t0 < limit_s):
             time.sleep(0.02)
 
     def mark_begin(self):
@@ -125,6 +215,8 @@ class ClockSampler:
         self.t_end = time.perf_counter()
 
     def stop(self):
+        if self.nvml is not None:
+            return self.nvml.stop(getattr(self, "t_begin", -1e30), getattr(self, "t_end", 1e30))
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -161,7 +253,9 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm), "window": window}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window,
+                "source": "nvidia-smi" + (" (NVML: %s)" % self.nvml_error
+                                          if self.nvml_error else "")}
 
 
 def measured_peaks():
@@ -243,7 +337,7 @@ def run_ours(args):
 
     n_pairs = st.n_neighbors
     # ---- device-resident timing (value) ----
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, dev)
     clocks.start()
     for k in range(W):
         step(k, _lib.FPP_PREC_MIXED)

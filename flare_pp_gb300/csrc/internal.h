@@ -145,9 +145,13 @@ struct StructureState {
   void mark(int k, cudaStream_t s) {
     if (profile && ev[k]) cudaEventRecord(ev[k], s);
   }
+  // recorded after the neighbor readback: the host waits on it, not on the
+  // work queued behind it
+  cudaEvent_t nb_ready = nullptr;
   ~StructureState() {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
+    if (nb_ready) cudaEventDestroy(nb_ready);
     if (rb) cudaFreeHost(rb);
   }
 };

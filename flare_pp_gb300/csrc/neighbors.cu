@@ -479,9 +479,13 @@ __global__ void k_compact_geom(int noa, CellDev cd, const float4 *__restrict__ w
                                long long *__restrict__ keys, int *__restrict__ nbr_i,
                                int *__restrict__ nbr_j, int *__restrict__ nbr_s,
                                float4 *__restrict__ rel32, int *__restrict__ rev,
-                               DeviceStatus *st) {
+                               DeviceStatus *st, long long cap,
+                               const int *__restrict__ flags) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= noa) return;
+  // launched before the host has read the pair total: nothing is written
+  // when the slab overflowed or the pair buffers hold fewer than the total
+  if (flags[0] != 0 || (long long)offset[noa] > cap) return;
   const int lane = threadIdx.x & 31;
   const int beg = offset[i], n = offset[i + 1] - beg;
   const float4 hi_i = wp32[i], lo_i = wp_lo[i];
@@ -800,6 +804,22 @@ __global__ void k_nb_readback(const int *__restrict__ total, const int *__restri
   rb->status[3] = status->pad;
 }
 
+// Pairs the pair buffers hold (0 before the first build; the FP64 table,
+// filled on demand, counts too).
+static long long pair_capacity(const StructureState &st) {
+  if (!st.nbr_key.ptr || !st.nbr_i.ptr || !st.nbr_j.ptr || !st.nbr_s.ptr ||
+      !st.nbr_rel.ptr || !st.nbr_rel32.ptr || !st.nbr_rev.ptr)
+    return 0;
+  size_t c = st.nbr_key.bytes / sizeof(long long);
+  c = std::min(c, st.nbr_rel.bytes / sizeof(dvec4));
+  c = std::min(c, st.nbr_i.bytes / sizeof(int));
+  c = std::min(c, st.nbr_j.bytes / sizeof(int));
+  c = std::min(c, st.nbr_s.bytes / sizeof(int));
+  c = std::min(c, st.nbr_rel32.bytes / sizeof(float4));
+  c = std::min(c, st.nbr_rev.bytes / sizeof(int));
+  return (long long)c;
+}
+
 int build_neighbors(StructureState &st, cudaStream_t stream) {
   const int noa = st.noa;
   CellDev cd = make_dev(st.ci);
@@ -874,7 +894,22 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   k_nb_readback<<<1, 32, 0, stream>>>(st.nbr_offset.as<int>() + noa, st.flags.as<int>(),
                                       st.status.as<DeviceStatus>(), st.rb_dev);
   FPP_CUDA(cudaGetLastError());
-  FPP_CUDA(cudaStreamSynchronize(stream));
+  if (!st.nb_ready) FPP_CUDA(cudaEventCreateWithFlags(&st.nb_ready, cudaEventDisableTiming));
+  FPP_CUDA(cudaEventRecord(st.nb_ready, stream));
+  // the compaction into the pair buffers of an earlier build, queued before
+  // the host waits for the pair total so that the GPU has work meanwhile; it
+  // writes nothing (and is launched again below) when the slab overflowed or
+  // the buffers are too small
+  const long long cap = pair_capacity(st);
+  if (cap > 0) {
+    k_compact_geom<<<grid, block, 0, stream>>>(
+        noa, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.species.as<int>(),
+        st.nbr_offset.as<int>(), st.slab.as<long long>(), st.nbr_key.as<long long>(),
+        st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_s.as<int>(),
+        st.nbr_rel32.as<float4>(), st.nbr_rev.as<int>(), dst, cap, st.flags.as<int>());
+    FPP_CUDA(cudaGetLastError());
+  }
+  FPP_CUDA(cudaEventSynchronize(st.nb_ready));
   FPP_TRY(status_from_readback(st, stream, "neighbor build or an earlier asynchronous call"));
   const bool overflow = st.rb->overflow != 0;
   int total = st.rb->total_pairs;
@@ -895,23 +930,35 @@ int build_neighbors(StructureState &st, cudaStream_t stream) {
   }
   if (total < 0) return fail(FPP_ERR_CAPACITY, "more than 2^31 neighbor pairs");
   st.n_pairs = total;
-  size_t np = (size_t)std::max(total, 1);
-  FPP_TRY(st.nbr_key.reserve(sizeof(long long) * np));
-  FPP_TRY(st.nbr_i.reserve(sizeof(int) * np));
-  FPP_TRY(st.nbr_j.reserve(sizeof(int) * np));
-  FPP_TRY(st.nbr_s.reserve(sizeof(int) * np));
-  FPP_TRY(st.nbr_rel.reserve(sizeof(dvec4) * np));
-  FPP_TRY(st.nbr_rel32.reserve(sizeof(float4) * np));
-  FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
-  st.rb->geom = nb_geom(st);  // the stream is idle here (synchronized above)
+  const bool compacted = !overflow && (long long)total <= cap;
+  // an eighth of headroom, so that a pair total that grows a little from one
+  // build to the next stays within the buffers
+  const size_t np = (size_t)std::max(total, 1) + (size_t)total / 8;
+  if (!compacted) {
+    // the queued compaction (which wrote nothing) may still hold the buffers
+    if (cap > 0) FPP_CUDA(cudaStreamSynchronize(stream));
+    FPP_TRY(st.nbr_key.reserve(sizeof(long long) * np));
+    FPP_TRY(st.nbr_i.reserve(sizeof(int) * np));
+    FPP_TRY(st.nbr_j.reserve(sizeof(int) * np));
+    FPP_TRY(st.nbr_s.reserve(sizeof(int) * np));
+    FPP_TRY(st.nbr_rel.reserve(sizeof(dvec4) * np));
+    FPP_TRY(st.nbr_rel32.reserve(sizeof(float4) * np));
+    FPP_TRY(st.nbr_rev.reserve(sizeof(int) * np));
+  }
+  // read by later kernels through mapped memory; no kernel in flight reads it
+  // (the queued compaction does not)
+  st.rb->geom = nb_geom(st);
   if (total == 0) return FPP_OK;
   if (!overflow) {
-    k_compact_geom<<<grid, block, 0, stream>>>(
-        noa, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.species.as<int>(),
-        st.nbr_offset.as<int>(), st.slab.as<long long>(), st.nbr_key.as<long long>(),
-        st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_s.as<int>(),
-        st.nbr_rel32.as<float4>(), st.nbr_rev.as<int>(), dst);
-    FPP_CUDA(cudaGetLastError());
+    if (!compacted) {
+      k_compact_geom<<<grid, block, 0, stream>>>(
+          noa, cd, st.wrapped32.as<float4>(), st.wrapped_lo.as<float4>(), st.species.as<int>(),
+          st.nbr_offset.as<int>(), st.slab.as<long long>(), st.nbr_key.as<long long>(),
+          st.nbr_i.as<int>(), st.nbr_j.as<int>(), st.nbr_s.as<int>(),
+          st.nbr_rel32.as<float4>(), st.nbr_rev.as<int>(), dst, (long long)total,
+          st.flags.as<int>());
+      FPP_CUDA(cudaGetLastError());
+    }
     return FPP_OK;  // reverse links and mirrored geometry written above
   } else {
     FPP_TRY(st.nbr_key_tmp.reserve(sizeof(long long) * np));
