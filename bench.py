@@ -357,6 +357,12 @@ def run_ours(args):
     torch.cuda.profiler.stop()
     clocks.mark_end()
     clk = clocks.stop()
+    free_b, total_b = torch.cuda.mem_get_info(dev)
+    device_memory = {"used_gb": round((total_b - free_b) / 1e9, 2),
+                     "total_gb": round(total_b / 1e9, 1),
+                     "what": "device memory in use right after the timed steps: library "
+                             "workspaces, model, inputs and torch buffers (other processes "
+                             "on this GPU included)"}
     ms_total = replica_time(ev0.elapsed_time(ev1), world, dev)
     ms_step = ms_total / K
     value = replica_value(noa, K, ms_total, world)
@@ -540,6 +546,7 @@ def run_ours(args):
         "kuf_batched": kuf,
         "gpu_launches": int(K * launches_per_step(SETTINGS["n_species"])),
         "clocks": clk,
+        "device_memory": device_memory,
         "cpu_baseline": cpu,
     }
     if rank == 0:
