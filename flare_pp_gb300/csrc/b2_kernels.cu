@@ -434,7 +434,64 @@ k_b2_forward(B2Args a, const int *__restrict__ offset,
     __syncwarp();
     for (int d = lane; d < nd; d += 32) nacc.add(p_s[d] * p_s[d]);
   }
-  if constexpr (SH::kL1 > 0 && sizeof(T) == 4) {
+  if constexpr (SH::kL1 > 0 && SH::kNR >= 16 && (SH::kNR % 2) == 0 && sizeof(T) == 4) {
+    // shape known, FP32, at least 16 radial channels: 2 x 2 blocks of c rows
+    // (2a, 2a + 1) x (2b, 2b + 1), a <= b, one block per lane, so that four
+    // rows read through 16-byte loads give four pairs (three on the diagonal
+    // blocks); each entry m feeds the chain of its l, every p value the same
+    // chain of fmaf as for one pair at a time
+    constexpr int LL = SH::kL1, HH = LL * LL, H4 = (HH + 3) / 4, NR = SH::kNR;
+    constexpr int NB = NR / 2, NBLK = NB * (NB + 1) / 2;
+    auto l_of = [](int m) { int l = 0; while ((l + 1) * (l + 1) <= m) l++; return l; };
+    auto q_of = [](int n1, int n2) { return n1 * NR - (n1 * (n1 - 1)) / 2 + (n2 - n1); };
+    for (int j = lane; j < NBLK; j += 32) {
+      int ba = 0, rem = j;
+      while (rem >= NB - ba) {
+        rem -= NB - ba;
+        ba++;
+      }
+      const int bb = ba + rem;
+      const float4 *x0 = reinterpret_cast<const float4 *>(c_s + (2 * ba) * HP);
+      const float4 *x1 = reinterpret_cast<const float4 *>(c_s + (2 * ba + 1) * HP);
+      const float4 *y0 = reinterpret_cast<const float4 *>(c_s + (2 * bb) * HP);
+      const float4 *y1 = reinterpret_cast<const float4 *>(c_s + (2 * bb + 1) * HP);
+      float v00[LL], v01[LL], v10[LL], v11[LL];
+#pragma unroll
+      for (int l = 0; l < LL; l++) v00[l] = v01[l] = v10[l] = v11[l] = 0.0f;
+#pragma unroll
+      for (int k = 0; k < H4; k++) {
+        const float4 a0 = x0[k], a1 = x1[k], b0 = y0[k], b1 = y1[k];
+        const float u0[4] = {a0.x, a0.y, a0.z, a0.w}, u1[4] = {a1.x, a1.y, a1.z, a1.w};
+        const float w0[4] = {b0.x, b0.y, b0.z, b0.w}, w1[4] = {b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+          const int m = 4 * k + jj;
+          if (m < HH) {
+            const int l = l_of(m);
+            v00[l] = fmaf(u0[jj], w0[jj], v00[l]);
+            v01[l] = fmaf(u0[jj], w1[jj], v01[l]);
+            v10[l] = fmaf(u1[jj], w0[jj], v10[l]);
+            v11[l] = fmaf(u1[jj], w1[jj], v11[l]);
+          }
+        }
+      }
+      // (2a+1, 2b) is a pair only off the diagonal (n1 <= n2)
+      auto put = [&](const float (&v)[LL], int n1, int n2) {
+        const int q = q_of(n1, n2);
+        float sq = 0.0f;
+#pragma unroll
+        for (int l = 0; l < LL; l++) {
+          p_s[q * LL + l] = v[l];
+          sq = fmaf(v[l], v[l], sq);
+        }
+        nacc.add(sq);
+      };
+      put(v00, 2 * ba, 2 * bb);
+      put(v01, 2 * ba, 2 * bb + 1);
+      if (bb != ba) put(v10, 2 * ba + 1, 2 * bb);
+      put(v11, 2 * ba + 1, 2 * bb + 1);
+    }
+  } else if constexpr (SH::kL1 > 0 && sizeof(T) == 4) {
     // shape known, FP32: the lane's pairs q and q + 32 advance together with
     // paired multiply-adds; the c rows stream through 16-byte loads and each
     // entry m feeds the chain of its l, so every p value is the same chain of
