@@ -1035,7 +1035,9 @@ k_b2_wu_staged(B2Args a, AdjArgs g, const int *__restrict__ species,
 template <typename T>
 __host__ __device__ inline size_t b3_adjoint_smem_per_warp(const B2Args &a, bool fixed = false) {
   const size_t nr = (size_t)a.n_species * a.N;
-  const size_t priv = 6 * (size_t)a.H * 32;
+  // fixed: the private rows of positions 2 and 3 (position 1 is in
+  // registers); otherwise all three
+  const size_t priv = (fixed ? 4 : 6) * (size_t)a.H * 32;
   size_t b;
   if (fixed) {
     // the private rows share memory with the w rows of the first round
@@ -1071,7 +1073,7 @@ k_b3_wu(B2Args a, AdjArgs g, const int *__restrict__ species,
                                          // [3 H][32] private rows
   const int rows_a = a.n_tri < 32 ? a.n_tri : 32;
   if constexpr (LM >= 0) {
-    const size_t priv = 6 * (size_t)H * 32, wa = (size_t)rows_a * a.n_ls;
+    const size_t priv = 4 * (size_t)H * 32, wa = (size_t)rows_a * a.n_ls;
     const size_t wbn = (size_t)(a.n_tri - rows_a) * a.n_ls;
     w_b = w_s + (priv > wa ? priv : wa);
     z = reinterpret_cast<V2<T> *>(w_b + ((wbn + 3) & ~(size_t)3));

@@ -312,15 +312,16 @@ __device__ __forceinline__ void b3_static_for(F &&f) {
   }
 }
 
-// One triangle of the adjoint for lane-private rows p1, p2, p3 (stride 32):
-// the terms of each m1 sum into a register pair before the one update of
-// p1[l1 m1]; the rows of positions 2 and 3 sum in registers over the whole
-// triangle.
-template <int LM, int L1, int L2, int L3, typename T, int NLS>
+// One triangle of the adjoint for the lane's rows: p1 in registers (indexed
+// by lm, every index a compile-time constant), p2 and p3 lane-private rows in
+// shared memory (stride 32).  The terms of each m1 sum into a register pair
+// before the one update of p1[l1 m1]; the rows of positions 2 and 3 sum in
+// registers over the whole triangle before their one update.
+template <int LM, int L1, int L2, int L3, typename T, int NLS, int HH>
 __device__ __forceinline__ void b3_adjoint_triangle(const V2<T> *__restrict__ z1,
                                                     const V2<T> *__restrict__ z2,
                                                     const V2<T> *__restrict__ z3,
-                                                    const T (&wr)[NLS], V2<T> *p1,
+                                                    const T (&wr)[NLS], V2<T> (&p1)[HH],
                                                     V2<T> *p2, V2<T> *p3) {
   constexpr int t = b3_tri_index(LM, L1, L2, L3);
   constexpr int q0 = b3_tri_first(LM, L1, L2, L3);
@@ -350,7 +351,7 @@ __device__ __forceinline__ void b3_adjoint_triangle(const V2<T> *__restrict__ z1
         s3[m3 + L3].y += f * (a.x * b.y + a.y * b.x);
       }
     });
-    V2<T> &d = p1[(L1 * L1 + L1 + m1) * 32];
+    V2<T> &d = p1[L1 * L1 + L1 + m1];
     d.x += s1.x;
     d.y += s1.y;
   });
@@ -421,11 +422,11 @@ __host__ __device__ constexpr int b3_n_triangles(int LM) {
   return t;
 }
 
-template <int LM, typename T, int NLS>
+template <int LM, typename T, int NLS, int HH>
 __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
                                                  const V2<T> *__restrict__ z2,
                                                  const V2<T> *__restrict__ z3,
-                                                 const T (&wr)[NLS], V2<T> *p1,
+                                                 const T (&wr)[NLS], V2<T> (&p1)[HH],
                                                  V2<T> *p2, V2<T> *p3) {
   b3_static_for<0, LM + 1>([&](auto i1) {
     b3_static_for<0, LM + 1>([&](auto i2) {
@@ -433,7 +434,7 @@ __device__ __forceinline__ void b3_adjoint_fixed(const V2<T> *__restrict__ z1,
         constexpr int l1 = decltype(i1)::value, l2 = decltype(i2)::value,
                       l3 = decltype(i3)::value;
         if constexpr (b3_tri_ok(l1, l2, l3))
-          b3_adjoint_triangle<LM, l1, l2, l3, T, NLS>(z1, z2, z3, wr, p1, p2, p3);
+          b3_adjoint_triangle<LM, l1, l2, l3, T, NLS, HH>(z1, z2, z3, wr, p1, p2, p3);
       });
     });
   });
@@ -492,6 +493,43 @@ __device__ __forceinline__ void b3_reduce_private(int r0, int n_tri, int H, int 
   }
 }
 
+// b3_reduce_private for npos positions pos0 .. pos0 + npos - 1 of the
+// triples, their rows at rows[(p * H + lm) * 32 + lane], p < npos.
+template <typename T>
+__device__ __forceinline__ void b3_reduce_rows(int r0, int n_tri, int H, int nr,
+                                               const int *__restrict__ tri,
+                                               const V2<T> *__restrict__ rows, int pos0,
+                                               int npos, V2<T> *__restrict__ u2, int lane) {
+  const int own = r0 + lane < n_tri ? tri[r0 + lane] : -1;
+  const int total = nr * H;
+  for (int k0 = 0; k0 < total; k0 += 32) {
+    const int k = k0 + lane;
+    const bool act = k < total;
+    const int n = act ? k / H : -1;
+    const int lm = act ? k - n * H : 0;
+    V2<T> acc{T(0), T(0)};
+    for (int j0 = 0; j0 < 32; j0++) {
+      const int j = (j0 + lane) & 31;
+      const int tj = __shfl_sync(0xffffffffu, own, j);
+      if (tj < 0) continue;  // no triple in this round's slot j
+      const V2<T> *col = rows + (size_t)lm * 32 + j;
+      for (int p = 0; p < npos; p++) {
+        const int sh = 8 * (pos0 + p);
+        const int np = sh == 16 ? (tj >> 16) : ((tj >> sh) & 0xff);
+        if (np == n) {
+          const V2<T> v = col[(size_t)p * H * 32];
+          acc.x += v.x;
+          acc.y += v.y;
+        }
+      }
+    }
+    if (act) {
+      u2[k].x += acc.x;
+      u2[k].y += acc.y;
+    }
+  }
+}
+
 // The adjoint with every term unrolled for lmax = LM.  Each lane first copies
 // its triple's row of w into registers, so the rows of the first round (wa)
 // may share memory with the private rows; the rows of later rounds (wb, triple
@@ -504,6 +542,7 @@ __device__ __forceinline__ void b3_contract_adjoint_fixed(int n_tri, int H, int 
                                                           V2<T> *priv, V2<T> *__restrict__ u2,
                                                           int lane) {
   constexpr int NLS = b3_n_triangles(LM);
+  constexpr int HH = (LM + 1) * (LM + 1);
   const int H1 = H + 1;
   for (int r0 = 0; r0 < n_tri; r0 += 32) {
     const int r = r0 + lane;
@@ -513,16 +552,23 @@ __device__ __forceinline__ void b3_contract_adjoint_fixed(int n_tri, int H, int 
     const T *wrow = r < 32 ? wa + r * NLS : wb + (r - 32) * NLS;
 #pragma unroll
     for (int t = 0; t < NLS; t++) wr[t] = live ? wrow[t] : T(0);
+    V2<T> p1[HH];  // position 1 in registers, positions 2 and 3 in priv
+#pragma unroll
+    for (int k = 0; k < HH; k++) p1[k] = V2<T>{T(0), T(0)};
     __syncwarp();  // every row is in registers before the private rows are zeroed
-    for (int k = 0; k < 3 * H; k++) priv[k * 32 + lane] = V2<T>{T(0), T(0)};
+    for (int k = 0; k < 2 * H; k++) priv[k * 32 + lane] = V2<T>{T(0), T(0)};
     if (live) {
       const int n1 = tr & 0xff, n2 = (tr >> 8) & 0xff, n3 = tr >> 16;
-      b3_adjoint_fixed<LM, T, NLS>(z + n1 * H1, z + n2 * H1, z + n3 * H1, wr, priv + lane,
-                                   priv + (size_t)H * 32 + lane,
-                                   priv + (size_t)(2 * H) * 32 + lane);
+      b3_adjoint_fixed<LM, T, NLS, HH>(z + n1 * H1, z + n2 * H1, z + n3 * H1, wr, p1,
+                                       priv + lane, priv + (size_t)H * 32 + lane);
     }
     __syncwarp();
-    b3_reduce_private<T>(r0, n_tri, H, nr, tri, priv, u2, lane);
+    b3_reduce_rows<T>(r0, n_tri, H, nr, tri, priv, 1, 2, u2, lane);  // positions 2, 3
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < HH; k++) priv[k * 32 + lane] = p1[k];
+    __syncwarp();
+    b3_reduce_rows<T>(r0, n_tri, H, nr, tri, priv, 0, 1, u2, lane);  // position 1
     __syncwarp();
   }
 }
