@@ -343,12 +343,21 @@ __device__ __forceinline__ void b3_adjoint_triangle(const V2<T> *__restrict__ z1
         constexpr int q = q0 + b3_term_offset(L1, L2, L3, m1, m2);
         const T f = wq * b3_w<T>(q);
         const V2<T> b = z2[L2 * L2 + L2 + m2], c = z3[L3 * L3 + L3 + m3];
-        s1.x += f * (b.x * c.x - b.y * c.y);
-        s1.y += f * (b.x * c.y + b.y * c.x);
-        s2[m2 + L2].x += f * (a.x * c.x - a.y * c.y);
-        s2[m2 + L2].y += f * (a.x * c.y + a.y * c.x);
-        s3[m3 + L3].x += f * (a.x * b.x - a.y * b.y);
-        s3[m3 + L3].y += f * (a.x * b.y + a.y * b.x);
+        // f a and f b once, then each complex product added by multiply-adds
+        const V2<T> fa{f * a.x, f * a.y}, fb{f * b.x, f * b.y};
+        s1.x = fma_t(fb.x, c.x, s1.x);
+        s1.x = fma_t(-fb.y, c.y, s1.x);
+        s1.y = fma_t(fb.x, c.y, s1.y);
+        s1.y = fma_t(fb.y, c.x, s1.y);
+        V2<T> &t2 = s2[m2 + L2], &t3 = s3[m3 + L3];
+        t2.x = fma_t(fa.x, c.x, t2.x);
+        t2.x = fma_t(-fa.y, c.y, t2.x);
+        t2.y = fma_t(fa.x, c.y, t2.y);
+        t2.y = fma_t(fa.y, c.x, t2.y);
+        t3.x = fma_t(fa.x, b.x, t3.x);
+        t3.x = fma_t(-fa.y, b.y, t3.x);
+        t3.y = fma_t(fa.x, b.y, t3.y);
+        t3.y = fma_t(fa.y, b.x, t3.y);
       }
     });
     V2<T> &d = p1[L1 * L1 + L1 + m1];
