@@ -102,3 +102,23 @@ def test_batched_b3_equals_per_structure(gpu_lib):
                                        atol=tol_f * max(1.0, np.abs(f).max()))
             np.testing.assert_allclose(S[k], st, rtol=0,
                                        atol=tol_f * max(1e-3, np.abs(st).max()))
+
+
+def test_batched_edge_structures(gpu_lib, setup):
+    """Empty structures and a single atom whose neighbors are all its own
+    periodic images, packed between ordinary cells: each structure's result
+    equals its own prediction (an empty one: zero energy, no forces)."""
+    gp, strucs = setup["gp"], setup["strucs"]
+    empty = fg.Structure(np.eye(3) * 8.0, np.zeros(0, np.int32), np.zeros((0, 3)), RC)
+    single = fg.Structure(np.eye(3) * 3.0, np.array([1], np.int32),
+                          np.array([[0.3, 0.2, 0.1]]), RC)
+    batch = [empty, strucs[0], single, strucs[5], empty]
+    for precision, tol in (("fp64", 1e-11), ("mixed", 1e-5)):
+        E, F, S = gp.predict_mapped_batched(batch, precision)
+        assert E[0] == 0.0 and E[4] == 0.0
+        assert F[0].shape == (0, 3) and F[4].shape == (0, 3)
+        for k in (1, 2, 3):
+            e, f, st = gp.predict_mapped(batch[k], precision)
+            assert abs(E[k] - e) <= tol * max(1.0, abs(e)), (precision, k, E[k], e)
+            np.testing.assert_allclose(F[k], f, rtol=0, atol=tol * max(1.0, np.abs(f).max()))
+            np.testing.assert_allclose(S[k], st, rtol=0, atol=tol * max(1e-3, np.abs(st).max()))
