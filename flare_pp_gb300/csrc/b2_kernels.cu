@@ -1466,7 +1466,9 @@ __device__ __forceinline__ void ff_group_sum(float &hi, float &lo) {
   }
 }
 
-__global__ void __launch_bounds__(32 * kGatherWarps)
+// four resident blocks per SM (64 registers): the kernel waits on its
+// dependent loads, and 32 warps hide more of that than 24
+__global__ void __launch_bounds__(32 * kGatherWarps, 4)
 k_gather_warp(int noa, const int *__restrict__ offset, const int *__restrict__ rev,
               const float4 *__restrict__ rel32, const float4 *__restrict__ pair_f,
               const double *__restrict__ atom_e, double *__restrict__ forces,
