@@ -502,34 +502,55 @@ __device__ __forceinline__ void b3_reduce_private(int r0, int n_tri, int H, int 
   }
 }
 
-// b3_reduce_private for npos positions pos0 .. pos0 + npos - 1 of the
-// triples, their rows at rows[(p * H + lm) * 32 + lane], p < npos.
+// b3_reduce_private for npos (1 or 2) positions pos0 .. pos0 + npos - 1 of
+// the triples, their rows at rows[(p * H + lm) * 32 + lane], p < npos.  The
+// lanes whose triple holds row n at those positions come from one ballot per
+// position and row value; each output entry then visits just those lanes, in
+// the order lane, lane + 1, ... (mod 32) and position by position within a
+// lane, the order of the full slot scan, so the sums are the same.
 template <typename T>
 __device__ __forceinline__ void b3_reduce_rows(int r0, int n_tri, int H, int nr,
                                                const int *__restrict__ tri,
                                                const V2<T> *__restrict__ rows, int pos0,
                                                int npos, V2<T> *__restrict__ u2, int lane) {
   const int own = r0 + lane < n_tri ? tri[r0 + lane] : -1;
+  // the rows of this lane's triple at the positions summed here (-1: none)
+  const int row0 = own < 0 ? -1 : (own >> (8 * pos0)) & 0xff;
+  const int row1 = (own < 0 || npos < 2) ? -1 : (own >> (8 * (pos0 + 1))) & 0xff;
   const int total = nr * H;
   for (int k0 = 0; k0 < total; k0 += 32) {
     const int k = k0 + lane;
     const bool act = k < total;
     const int n = act ? k / H : -1;
     const int lm = act ? k - n * H : 0;
+    // the contributing lanes for each row value n of this group of outputs
+    unsigned m0 = 0u, m1 = 0u;
+    const int nlo = k0 / H, nhi = min(k0 + 31, total - 1) / H;
+    for (int nn = nlo; nn <= nhi; nn++) {
+      const unsigned b0 = __ballot_sync(0xffffffffu, row0 == nn);
+      const unsigned b1 = __ballot_sync(0xffffffffu, row1 == nn);
+      if (nn == n) {
+        m0 = b0;
+        m1 = b1;
+      }
+    }
     V2<T> acc{T(0), T(0)};
-    for (int j0 = 0; j0 < 32; j0++) {
-      const int j = (j0 + lane) & 31;
-      const int tj = __shfl_sync(0xffffffffu, own, j);
-      if (tj < 0) continue;  // no triple in this round's slot j
+    const unsigned any = m0 | m1;
+    unsigned r = __funnelshift_r(any, any, lane);  // bit b: lane (b + lane) mod 32
+    while (r) {
+      const int b = __ffs(r) - 1;
+      r &= r - 1u;
+      const int j = (b + lane) & 31;
       const V2<T> *col = rows + (size_t)lm * 32 + j;
-      for (int p = 0; p < npos; p++) {
-        const int sh = 8 * (pos0 + p);
-        const int np = sh == 16 ? (tj >> 16) : ((tj >> sh) & 0xff);
-        if (np == n) {
-          const V2<T> v = col[(size_t)p * H * 32];
-          acc.x += v.x;
-          acc.y += v.y;
-        }
+      if ((m0 >> j) & 1u) {
+        const V2<T> v = col[0];
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+      if ((m1 >> j) & 1u) {
+        const V2<T> v = col[(size_t)H * 32];
+        acc.x += v.x;
+        acc.y += v.y;
       }
     }
     if (act) {
