@@ -385,20 +385,26 @@ __device__ __forceinline__ T b3_contract_triangle(const V2<T> *__restrict__ z1,
                                                   const V2<T> *__restrict__ z3) {
   constexpr int q0 = b3_tri_first(LM, L1, L2, L3);
   static_assert(q0 >= 0, "triangle outside the tables");
+  // per m1: S = sum_m2 w_q b c (complex), then Re(a S) once
   T acc = T(0);
   b3_static_for<0, 2 * L1 + 1>([&](auto j1) {
     constexpr int m1 = decltype(j1)::value - L1;
-    const V2<T> a = z1[L1 * L1 + L1 + m1];
+    V2<T> sm{T(0), T(0)};
     b3_static_for<0, 2 * L2 + 1>([&](auto j2) {
       constexpr int m2 = decltype(j2)::value - L2;
       constexpr int m3 = -m1 - m2;
       if constexpr (b3_iabs(m3) <= L3) {
         constexpr int q = q0 + b3_term_offset(L1, L2, L3, m1, m2);
         const V2<T> b = z2[L2 * L2 + L2 + m2], c = z3[L3 * L3 + L3 + m3];
-        const T xr = a.x * b.x - a.y * b.y, xi = a.x * b.y + a.y * b.x;
-        acc += b3_w<T>(q) * (xr * c.x - xi * c.y);
+        const T br = b.x * c.x - b.y * c.y, bi = b.x * c.y + b.y * c.x;
+        const T w = b3_w<T>(q);
+        sm.x = fma_t(w, br, sm.x);
+        sm.y = fma_t(w, bi, sm.y);
       }
     });
+    const V2<T> a = z1[L1 * L1 + L1 + m1];
+    acc = fma_t(a.x, sm.x, acc);
+    acc = fma_t(-a.y, sm.y, acc);
   });
   return acc;
 }
