@@ -88,7 +88,7 @@ def replica_value(n_atoms, steps, ms_total, world):
 
 
 class NvmlClocks:
-    """SM clock and clock-event reasons read through NVML (the driver's
+    """SM clock and clock-event reasons read through NVML (the NVIDIA driver's
     libnvidia-ml, by ctypes) about every millisecond on a host thread, so that
     even a timed region of a few tens of milliseconds holds many samples.
     Reads only; the device is matched to the CUDA device by UUID."""
@@ -166,7 +166,8 @@ class NvmlClocks:
 
 class ClockSampler:
     """Clocks and throttle reasons sampled during the timed region: NVML every
-    ~1 ms where the driver library loads, else nvidia-smi every 100 ms."""
+    ~1 ms where the NVIDIA driver's NVML library loads, else nvidia-smi every
+    100 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
